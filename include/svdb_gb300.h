@@ -1,0 +1,129 @@
+/*
+ * svdb_gb300.h -- batch entry points of libsvdb_gb300.so (additive to the
+ * drop-in vector_database.h / kdtree.h API).
+ *
+ * The reference answers one /compare pair or one /nearest query per HTTP
+ * request.  These calls take whole batches so a server (or a batching
+ * front end) can amortise one kernel launch over many requests.  Each
+ * entry cites the reference code path whose semantics it keeps.
+ *
+ * Conventions: plain pointers and sizes, no CUDA or torch types.  Unless a
+ * name ends in _device, every buffer is HOST memory and the call returns
+ * when the results are in it.  Return value: SVDB_OK or a negative SVDB_E*
+ * code; svdb_last_error() gives a message for the calling thread.
+ */
+#ifndef SVDB_GB300_H
+#define SVDB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "vector_database.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* metrics: the three /compare/<metric> URLs (src/compare_handler.c:152-160) */
+#define SVDB_COSINE 0
+#define SVDB_EUCLIDEAN 1
+#define SVDB_DOT 2
+
+/* search precision */
+#define SVDB_PREC_FP64 0 /* plain FP64 streaming scan of the master copy */
+#define SVDB_PREC_BF16 1 /* BF16 tensor-core screen + certified FP64 re-rank */
+
+/* return codes */
+#define SVDB_OK 0
+#define SVDB_EINVAL (-1)   /* bad argument (NULL pointer, k == 0, dimension mismatch) */
+#define SVDB_ENOMEM (-2)   /* host/device allocation failed or admission refused */
+#define SVDB_ECUDA (-3)    /* a CUDA call failed (message in svdb_last_error) */
+#define SVDB_ETIMEOUT (-4) /* a kernel's bounded wait ran out; the context is still usable */
+#define SVDB_ENODEV (-5)   /* no usable GPU */
+
+/* per-pair status of svdb_compare_batch: the error branches of
+ * compare_handler_callback (src/compare_handler.c:74-195), in its order */
+#define SVDB_CMP_OK 0
+#define SVDB_CMP_OUT_OF_BOUNDS 1  /* "Index out of bounds", 400 (:101-110) */
+#define SVDB_CMP_NOT_FOUND 2      /* "Vector not found", 404 (:116-125) */
+#define SVDB_CMP_DIFF_DIM 3       /* "Vectors have different dimensions", 400 (:127-136) */
+#define SVDB_CMP_SIZE_MISMATCH 4  /* "Vector size mismatch", 400 (:139-147) */
+#define SVDB_CMP_UNKNOWN_METHOD 5 /* "Unknown comparison method", 400 (:161-170) */
+
+typedef struct svdb_search_stats {
+    uint64_t candidates;   /* rows re-ranked in FP64 over the whole batch */
+    uint32_t widened;      /* queries whose shortlist overflowed and were answered by an exact scan */
+    uint32_t kernels;      /* kernel launches issued by the call */
+    double max_err_bound;  /* max over results of the bound on |reported - exact real value| */
+} svdb_search_stats;
+
+/*
+ * GET /compare/<metric>?index1=&index2= for npairs pairs at once
+ * (src/compare_handler.c:74-195).  out[i] is bit-identical to the reference's
+ * float result; status[i] is SVDB_CMP_*.  expected_dim is the server's
+ * db_vector_size (0 skips that check).  metric outside 0..2 gives
+ * SVDB_CMP_UNKNOWN_METHOD for every pair.
+ */
+int svdb_compare_batch(VectorDatabase* db, int metric, const int64_t* index1, const int64_t* index2,
+                       size_t npairs, size_t expected_dim, float* out, int32_t* status);
+
+/*
+ * POST /nearest for nq queries (src/compare_handler.c:403 -> kdtree_nearest,
+ * src/kdtree.c:171-178): out_index[i] is the KD tree's stored index, or -1
+ * for "No nearest neighbor found".  queries is nq x dim, row-major; only the
+ * first kd-dimension coordinates are read.
+ */
+int svdb_nearest_batch(VectorDatabase* db, const double* queries, size_t nq, size_t dim,
+                       int64_t* out_index);
+
+/*
+ * Exact top-k (no reference counterpart: /nearest is top-1 and documents an
+ * unimplemented `number` parameter, README.md:287).  For each of nq queries
+ * (nq x dim, row-major), ids[i*k + j] is the logical index of the j-th
+ * result and dists[i*k + j] its FP64 value (cosine similarity, Euclidean
+ * distance or dot product, the reference's formulas carried in double);
+ * order is best first, ties to the lowest index; missing results are
+ * id -1 / NaN.  Ids are exact for both precisions.  err (optional, nq*k)
+ * receives a bound on |dists - exact real value|.
+ */
+int svdb_search_topk(VectorDatabase* db, const double* queries, size_t nq, size_t dim, size_t k,
+                     int metric, int precision, int64_t* ids, double* dists, double* err,
+                     svdb_search_stats* stats);
+
+/* As svdb_search_topk with queries/ids/dists/err in DEVICE memory; the work
+ * is queued on the database's stream (svdb_stream) and the call returns
+ * without waiting for it.  stats may be NULL. */
+int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim, size_t k,
+                            int metric, int precision, int64_t* d_ids, double* d_dists, double* d_err,
+                            svdb_search_stats* stats);
+
+/* Bulk insert of n rows (n x dim, row-major, copied): the same result as n
+ * vector_db_insert calls, including the KD nodes.  uuids: n*37 bytes or
+ * NULL.  Returns the first new index in *first_index. */
+int svdb_insert_batch(VectorDatabase* db, const double* rows, size_t n, size_t dim, const char* uuids,
+                      size_t* first_index);
+
+/* Reserve device capacity for `rows` rows of dimension `dim` (avoids
+ * regrowth copies).  Refused with SVDB_ENOMEM when free HBM minus the
+ * configured headroom is too small (admission by free memory). */
+int svdb_reserve(VectorDatabase* db, size_t rows, size_t dim);
+
+/* Push pending host-side mutations to the device and rebuild derived
+ * arrays (norms, BF16 shadow, logical index map).  Searches do this
+ * implicitly. */
+int svdb_sync(VectorDatabase* db);
+
+/* The CUDA stream (cudaStream_t) the database's kernels run on. */
+void* svdb_stream(VectorDatabase* db);
+
+/* Block until the database's queued device work is done. */
+int svdb_wait(VectorDatabase* db);
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* svdb_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVDB_GB300_H */

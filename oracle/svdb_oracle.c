@@ -1,0 +1,386 @@
+/*
+ * svdb_oracle.c -- CPU oracle for the similarity path of simple-vector-db.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this file; only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg do, and only as the checker.
+ *
+ * It restates, in plain C, the arithmetic of the reference's hot path:
+ *
+ *   orc_ref_cosine / orc_ref_euclidean / orc_ref_dot
+ *       src/vector_database.c:301-313, :322-333, :342-352 -- FP64 inputs,
+ *       FLOAT accumulators; every "acc += a*b" is a double product and a
+ *       double add rounded back to float.  Must be compiled with
+ *       -ffp-contract=off (the reference ships at -O0, where GCC never
+ *       contracts; at -O2 on aarch64 it would fuse and change the bits).
+ *
+ *   orc_kd_*      src/kdtree.c:15-178 -- the insertion-order KD tree over the
+ *       first `dim` coordinates: split axis depth % dim, "<" goes left
+ *       (:53-59); exact 1-NN with strict "<" replacement (:139) and the
+ *       plane prune (q[cd]-p[cd])^2 < best (:157); (size_t)-1 when empty
+ *       (:171-174).
+ *
+ *   orc_store_*   src/vector_database.c:81-195 -- positional store:
+ *       insert appends and adds a KD node with index = size (:113-115);
+ *       update replaces the row and adds a SECOND KD node (:169-177);
+ *       delete shifts later rows left and leaves the KD tree alone
+ *       (:185-195); out-of-range update/delete are ignored.
+ *
+ *   orc_fp64_*    the same three metric formulas carried in double.  Two
+ *       summation orders are provided: `seq` (i = 0..d-1, as the reference
+ *       loops) and `canon`, the order the GPU kernels use (element i goes to
+ *       partial sum (i/2)%4 with a fused multiply-add, result
+ *       (p0+p2)+(p1+p3)); both are exact restatements of the formulas, and
+ *       they agree to ~1e-16 relative.
+ *
+ *   orc_topk      FP64 brute force top-k (no reference symbol: /nearest is
+ *       top-1 only); order = (key ascending, id ascending) where key is the
+ *       distance for Euclidean and the negated value for cosine/dot, NaN
+ *       ranked last.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_COSINE 0
+#define ORC_EUCLIDEAN 1
+#define ORC_DOT 2
+
+/* ------------------------------------------------------------------------ */
+/* Reference-exact metrics (float accumulators).                             */
+/* ------------------------------------------------------------------------ */
+
+float orc_ref_cosine(const double* a, const double* b, size_t d) {
+    float dot = 0.0f, na = 0.0f, nb = 0.0f;
+    for (size_t i = 0; i < d; ++i) {
+        dot = (float)((double)dot + a[i] * b[i]);
+        na = (float)((double)na + a[i] * a[i]);
+        nb = (float)((double)nb + b[i] * b[i]);
+    }
+    return (float)((double)dot / (sqrt((double)na) * sqrt((double)nb)));
+}
+
+float orc_ref_euclidean(const double* a, const double* b, size_t d) {
+    float sum = 0.0f;
+    for (size_t i = 0; i < d; ++i) {
+        float diff = (float)(a[i] - b[i]);
+        sum = sum + diff * diff;
+    }
+    return (float)sqrt((double)sum);
+}
+
+float orc_ref_dot(const double* a, const double* b, size_t d) {
+    float r = 0.0f;
+    for (size_t i = 0; i < d; ++i) r = (float)((double)r + a[i] * b[i]);
+    return r;
+}
+
+/* metric on two vectors of possibly different dimension: -1.0f on mismatch,
+ * as every metric in src/vector_database.c:302-305 does. */
+float orc_ref_metric(int metric, const double* a, size_t da, const double* b, size_t db) {
+    if (da != db) return -1.0f;
+    switch (metric) {
+        case ORC_COSINE: return orc_ref_cosine(a, b, da);
+        case ORC_EUCLIDEAN: return orc_ref_euclidean(a, b, da);
+        default: return orc_ref_dot(a, b, da);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FP64 metrics.                                                             */
+/* ------------------------------------------------------------------------ */
+
+static double canon_dot(const double* a, const double* b, size_t d) {
+    double p[4] = {0.0, 0.0, 0.0, 0.0};
+    for (size_t i = 0; i < d; ++i) {
+        size_t s = (i >> 1) & 3u;
+        p[s] = fma(a[i], b[i], p[s]);
+    }
+    return (p[0] + p[2]) + (p[1] + p[3]);
+}
+
+static double canon_sqdist(const double* a, const double* b, size_t d) {
+    double p[4] = {0.0, 0.0, 0.0, 0.0};
+    for (size_t i = 0; i < d; ++i) {
+        size_t s = (i >> 1) & 3u;
+        double t = a[i] - b[i];
+        p[s] = fma(t, t, p[s]);
+    }
+    return (p[0] + p[2]) + (p[1] + p[3]);
+}
+
+double orc_canon_sumsq(const double* a, size_t d) { return canon_dot(a, a, d); }
+
+/* FP64 metric value in the canonical order; qn/xn are sqrt(canon sumsq). */
+static double canon_metric(int metric, const double* q, double qn, const double* x, double xn, size_t d) {
+    switch (metric) {
+        case ORC_COSINE: return canon_dot(q, x, d) / (qn * xn);
+        case ORC_EUCLIDEAN: return sqrt(canon_sqdist(q, x, d));
+        default: return canon_dot(q, x, d);
+    }
+}
+
+double orc_fp64_canon(int metric, const double* a, const double* b, size_t d) {
+    double an = sqrt(canon_dot(a, a, d)), bn = sqrt(canon_dot(b, b, d));
+    return canon_metric(metric, a, an, b, bn, d);
+}
+
+double orc_fp64_seq(int metric, const double* a, const double* b, size_t d) {
+    double dot = 0.0, na = 0.0, nb = 0.0, sq = 0.0;
+    for (size_t i = 0; i < d; ++i) {
+        dot += a[i] * b[i];
+        na += a[i] * a[i];
+        nb += b[i] * b[i];
+        double t = a[i] - b[i];
+        sq += t * t;
+    }
+    switch (metric) {
+        case ORC_COSINE: return dot / (sqrt(na) * sqrt(nb));
+        case ORC_EUCLIDEAN: return sqrt(sq);
+        default: return dot;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FP64 brute-force top-k.                                                   */
+/* ------------------------------------------------------------------------ */
+
+static double rank_key(int metric, double v) {
+    if (isnan(v)) return INFINITY;
+    return metric == ORC_EUCLIDEAN ? v : -v;
+}
+
+typedef struct {
+    int metric, seq;
+    const double* x;
+    const double* xn;
+    size_t n, d, k;
+    const double* q;
+    size_t nq;
+    int64_t* ids;
+    double* vals;
+    size_t next;
+    pthread_mutex_t lock;
+} topk_job;
+
+static void topk_one(topk_job* J, size_t qi, double* keys, int64_t* kid, double* kval) {
+    const double* q = J->q + qi * J->d;
+    double qn = sqrt(canon_dot(q, q, J->d));
+    size_t cnt = 0;
+    for (size_t r = 0; r < J->n; ++r) {
+        const double* x = J->x + r * J->d;
+        double v = J->seq ? orc_fp64_seq(J->metric, q, x, J->d)
+                          : canon_metric(J->metric, q, qn, x, J->xn[r], J->d);
+        double key = rank_key(J->metric, v);
+        if (cnt == J->k && !(key < keys[cnt - 1])) continue; /* ids ascend: equal key loses */
+        size_t pos = cnt < J->k ? cnt++ : J->k - 1;
+        while (pos > 0 && key < keys[pos - 1]) {
+            keys[pos] = keys[pos - 1];
+            kid[pos] = kid[pos - 1];
+            kval[pos] = kval[pos - 1];
+            --pos;
+        }
+        keys[pos] = key;
+        kid[pos] = (int64_t)r;
+        kval[pos] = v;
+    }
+    for (size_t j = 0; j < J->k; ++j) {
+        J->ids[qi * J->k + j] = j < cnt ? kid[j] : -1;
+        J->vals[qi * J->k + j] = j < cnt ? kval[j] : NAN;
+    }
+}
+
+static void* topk_worker(void* arg) {
+    topk_job* J = (topk_job*)arg;
+    double* keys = (double*)malloc(J->k * sizeof(double));
+    int64_t* kid = (int64_t*)malloc(J->k * sizeof(int64_t));
+    double* kval = (double*)malloc(J->k * sizeof(double));
+    for (;;) {
+        pthread_mutex_lock(&J->lock);
+        size_t qi = J->next++;
+        pthread_mutex_unlock(&J->lock);
+        if (qi >= J->nq) break;
+        topk_one(J, qi, keys, kid, kval);
+    }
+    free(keys);
+    free(kid);
+    free(kval);
+    return NULL;
+}
+
+/* Exact FP64 top-k of every query against all n rows.  seq=0: canonical
+ * summation order (bit-identical to the GPU kernels); seq=1: sequential. */
+int orc_topk(int metric, int seq, const double* x, size_t n, size_t d, const double* q, size_t nq,
+             size_t k, int64_t* ids, double* vals, int nthreads) {
+    if (k == 0) return 0;
+    double* xn = (double*)malloc((n ? n : 1) * sizeof(double));
+    if (!xn) return -1;
+    for (size_t r = 0; r < n; ++r) xn[r] = sqrt(canon_dot(x + r * d, x + r * d, d));
+    topk_job J = {metric, seq, x, xn, n, d, k, q, nq, ids, vals, 0, PTHREAD_MUTEX_INITIALIZER};
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc((size_t)nthreads * sizeof(pthread_t));
+    int started = 0;
+    for (int t = 1; t < nthreads; ++t)
+        if (pthread_create(&th[started], NULL, topk_worker, &J) == 0) ++started;
+    topk_worker(&J);
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    free(th);
+    free(xn);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Insertion-order KD tree (flat arrays).                                    */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    size_t dim, n, cap;
+    double* pts;   /* n * dim prefix copies (src/kdtree.c:26-28) */
+    size_t* index; /* stored index (src/kdtree.c:30) */
+    int64_t* left;
+    int64_t* right;
+} orc_kd;
+
+orc_kd* orc_kd_create(size_t dim) {
+    orc_kd* t = (orc_kd*)calloc(1, sizeof(orc_kd));
+    if (t) t->dim = dim;
+    return t;
+}
+
+void orc_kd_free(orc_kd* t) {
+    if (!t) return;
+    free(t->pts);
+    free(t->index);
+    free(t->left);
+    free(t->right);
+    free(t);
+}
+
+int orc_kd_insert(orc_kd* t, const double* p, size_t index) {
+    if (t->n == t->cap) {
+        size_t nc = t->cap ? 2 * t->cap : 64;
+        double* np = (double*)realloc(t->pts, nc * t->dim * sizeof(double));
+        if (!np) return -1;
+        t->pts = np;
+        size_t* ni = (size_t*)realloc(t->index, nc * sizeof(size_t));
+        if (!ni) return -1;
+        t->index = ni;
+        int64_t* nl = (int64_t*)realloc(t->left, nc * sizeof(int64_t));
+        if (!nl) return -1;
+        t->left = nl;
+        int64_t* nr = (int64_t*)realloc(t->right, nc * sizeof(int64_t));
+        if (!nr) return -1;
+        t->right = nr;
+        t->cap = nc;
+    }
+    int64_t id = (int64_t)t->n++;
+    memcpy(t->pts + (size_t)id * t->dim, p, t->dim * sizeof(double));
+    t->index[id] = index;
+    t->left[id] = t->right[id] = -1;
+    if (id == 0) return 0;
+    int64_t cur = 0;
+    size_t depth = 0;
+    for (;;) {
+        size_t cd = depth % t->dim;
+        int64_t* slot = p[cd] < t->pts[(size_t)cur * t->dim + cd] ? &t->left[cur] : &t->right[cur];
+        if (*slot < 0) {
+            *slot = id;
+            return 0;
+        }
+        cur = *slot;
+        ++depth;
+    }
+}
+
+static void kd_nearest_rec(const orc_kd* t, int64_t node, const double* q, size_t depth, int64_t* best,
+                           double* best_d) {
+    if (node < 0) return;
+    const double* p = t->pts + (size_t)node * t->dim;
+    double d = 0.0;
+    for (size_t i = 0; i < t->dim; ++i) d += (p[i] - q[i]) * (p[i] - q[i]);
+    if (d < *best_d) {
+        *best_d = d;
+        *best = node;
+    }
+    size_t cd = depth % t->dim;
+    int64_t nxt, oth;
+    if (q[cd] < p[cd]) {
+        nxt = t->left[node];
+        oth = t->right[node];
+    } else {
+        nxt = t->right[node];
+        oth = t->left[node];
+    }
+    kd_nearest_rec(t, nxt, q, depth + 1, best, best_d);
+    if ((q[cd] - p[cd]) * (q[cd] - p[cd]) < *best_d) kd_nearest_rec(t, oth, q, depth + 1, best, best_d);
+}
+
+size_t orc_kd_nearest(const orc_kd* t, const double* q) {
+    if (!t || t->n == 0) return (size_t)-1;
+    int64_t best = -1;
+    double best_d = INFINITY;
+    kd_nearest_rec(t, 0, q, 0, &best, &best_d);
+    return best >= 0 ? t->index[best] : (size_t)-1;
+}
+
+size_t orc_kd_size(const orc_kd* t) { return t->n; }
+
+/* ------------------------------------------------------------------------ */
+/* Positional store with the reference's mutation semantics.                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    size_t d, size, cap;
+    double* rows; /* size * d, logical order */
+    orc_kd* kd;
+} orc_store;
+
+orc_store* orc_store_create(size_t d, size_t kd_dim) {
+    orc_store* s = (orc_store*)calloc(1, sizeof(orc_store));
+    if (!s) return NULL;
+    s->d = d;
+    s->kd = orc_kd_create(kd_dim);
+    return s;
+}
+
+void orc_store_free(orc_store* s) {
+    if (!s) return;
+    free(s->rows);
+    orc_kd_free(s->kd);
+    free(s);
+}
+
+size_t orc_store_insert(orc_store* s, const double* v) {
+    if (s->size == s->cap) {
+        size_t nc = s->cap ? 2 * s->cap : 16;
+        double* nr = (double*)realloc(s->rows, nc * s->d * sizeof(double));
+        if (!nr) return (size_t)-1;
+        s->rows = nr;
+        s->cap = nc;
+    }
+    memcpy(s->rows + s->size * s->d, v, s->d * sizeof(double));
+    orc_kd_insert(s->kd, v, s->size);
+    return s->size++;
+}
+
+void orc_store_update(orc_store* s, size_t index, const double* v) {
+    if (index >= s->size) return;
+    memcpy(s->rows + index * s->d, v, s->d * sizeof(double));
+    orc_kd_insert(s->kd, v, index);
+}
+
+void orc_store_delete(orc_store* s, size_t index) {
+    if (index >= s->size) return;
+    memmove(s->rows + index * s->d, s->rows + (index + 1) * s->d, (s->size - index - 1) * s->d * sizeof(double));
+    s->size--;
+}
+
+size_t orc_store_size(const orc_store* s) { return s->size; }
+const double* orc_store_rows(const orc_store* s) { return s->rows; }
+
+/* /nearest as src/compare_handler.c:403-419 resolves it: the KD index, or
+ * (size_t)-1 for "No nearest neighbor found"; an index >= size is the
+ * "Nearest neighbor not found" outcome (the row was deleted). */
+size_t orc_store_nearest(const orc_store* s, const double* q) { return orc_kd_nearest(s->kd, q); }

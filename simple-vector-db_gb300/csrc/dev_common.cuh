@@ -1,0 +1,136 @@
+// dev_common.cuh -- helpers shared by the CUDA translation units.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "svdb_device.h"
+
+#define SVDB_CUDA(call)                                                                         \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            svdb_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return e_ == cudaErrorMemoryAllocation ? SVDB_ENOMEM : SVDB_ECUDA;                  \
+        }                                                                                       \
+    } while (0)
+
+#define SVDB_LAUNCH_CHECK()                                                                    \
+    do {                                                                                       \
+        cudaError_t e_ = cudaGetLastError();                                                   \
+        if (e_ != cudaSuccess) {                                                               \
+            svdb_set_error("%s:%d launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_));   \
+            return SVDB_ECUDA;                                                                 \
+        }                                                                                      \
+    } while (0)
+
+namespace svdb {
+
+constexpr int kRowAlign = 16;  // FP64 master row stride: multiple of 16 doubles (128 B)
+constexpr int kBf16Align = 64; // BF16 shadow row stride: multiple of 64 (one 128-B swizzle row)
+
+static inline size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
+
+// ---------------------------------------------------------------------------
+// Canonical FP64 reductions.  A row is reduced by a group of 4 lanes; lane s
+// of the group owns element pairs {8j+2s, 8j+2s+1} and accumulates them in
+// increasing order with fused multiply-adds; the group then combines
+// (p0+p2)+(p1+p3) with two xor-shuffles.  The oracle restates exactly this
+// order, so results are bit-identical.  Rows are zero-padded to a multiple
+// of 16 doubles, and fma(0,0,p) == p for the partials (never -0.0), so the
+// padding does not change the result.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double group4_sum(double p) {
+    p += __shfl_xor_sync(0xffffffffu, p, 2);
+    p += __shfl_xor_sync(0xffffffffu, p, 1);
+    return p;
+}
+
+// ordering key of a metric value: ascending key = better; NaN last
+__device__ __forceinline__ double rank_key(int metric, double v) {
+    double k = metric == SVDB_EUCLIDEAN ? v : -v;
+    return isnan(k) ? __longlong_as_double(0x7ff0000000000000ll) : k;
+}
+
+__device__ __forceinline__ bool key_less(double ka, int ia, double kb, int ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+
+// ---------------------------------------------------------------------------
+// WarpList<KS>: a warp-wide sorted list of up to 32*KS (key, id, value)
+// entries, best first; position p lives in slot p/32 of lane p%32.  All
+// calls are warp-uniform.  Empty entries have key +inf and id INT32_MAX.
+// ---------------------------------------------------------------------------
+template <int KS>
+struct WarpList {
+    double key[KS];
+    double val[KS];
+    int id[KS];
+
+    __device__ __forceinline__ void init() {
+#pragma unroll
+        for (int s = 0; s < KS; ++s) {
+            key[s] = __longlong_as_double(0x7ff0000000000000ll);
+            val[s] = __longlong_as_double(0x7ff8000000000000ll);
+            id[s] = 0x7fffffff;
+        }
+    }
+    // key/id of position p (p < 32*KS), broadcast to all lanes
+    __device__ __forceinline__ void at(int p, double& k, int& i) const {
+        const int s = p >> 5, l = p & 31;
+        double kk = key[0];
+        int ii = id[0];
+#pragma unroll
+        for (int t = 1; t < KS; ++t)
+            if (t == s) {
+                kk = key[t];
+                ii = id[t];
+            }
+        k = __shfl_sync(0xffffffffu, kk, l);
+        i = __shfl_sync(0xffffffffu, ii, l);
+    }
+    // insert one warp-uniform candidate if it beats position k-1
+    __device__ __forceinline__ void insert(double ck, int ci, double cv, int k) {
+        double wk;
+        int wi;
+        at(k - 1, wk, wi);
+        if (!key_less(ck, ci, wk, wi)) return;
+        const int lane = threadIdx.x & 31;
+        int pos = 0;
+#pragma unroll
+        for (int s = 0; s < KS; ++s) pos += __popc(__ballot_sync(0xffffffffu, key_less(key[s], id[s], ck, ci)));
+        double nk[KS], nv[KS];
+        int ni[KS];
+#pragma unroll
+        for (int s = 0; s < KS; ++s) {
+            double uk = __shfl_up_sync(0xffffffffu, key[s], 1);
+            double uv = __shfl_up_sync(0xffffffffu, val[s], 1);
+            int ui = __shfl_up_sync(0xffffffffu, id[s], 1);
+            if (s > 0) {
+                double pk = __shfl_sync(0xffffffffu, key[s - 1], 31);
+                double pv = __shfl_sync(0xffffffffu, val[s - 1], 31);
+                int pi = __shfl_sync(0xffffffffu, id[s - 1], 31);
+                if (lane == 0) {
+                    uk = pk;
+                    uv = pv;
+                    ui = pi;
+                }
+            }
+            const int p = s * 32 + lane;
+            nk[s] = p > pos ? uk : (p == pos ? ck : key[s]);
+            nv[s] = p > pos ? uv : (p == pos ? cv : val[s]);
+            ni[s] = p > pos ? ui : (p == pos ? ci : id[s]);
+        }
+#pragma unroll
+        for (int s = 0; s < KS; ++s) {
+            key[s] = nk[s];
+            val[s] = nv[s];
+            id[s] = ni[s];
+        }
+    }
+    // threshold key/id at position k-1
+    __device__ __forceinline__ void worst(int k, double& wk, int& wi) const { at(k - 1, wk, wi); }
+};
+
+}  // namespace svdb

@@ -1,0 +1,50 @@
+// dev_search.cuh -- pieces of the top-k search shared by the FP64 scan
+// (dev_search.cu) and the BF16 screen + re-rank (dev_gemm.cu).
+#pragma once
+
+#include "dev_common.cuh"
+#include "dev_store.cuh"
+
+namespace svdb {
+
+// one (value, slot) result; 16 bytes
+struct __align__(16) Entry {
+    double val;
+    int id;
+    int pad;
+};
+
+// device buffers of one search call (all in the store's scratch)
+struct SearchArgs {
+    const double* q;     // nq x ld, zero-padded
+    const double* qsq;   // nq canonical sums of squares
+    size_t nq, k;
+    int metric;
+    int64_t* ids;        // nq x k (device)
+    double* dists;       // nq x k (device)
+    double* err;         // nq x k (device) or null
+};
+
+// FP64 bound on |computed - exact| for one result (see dev_search.cu)
+__device__ __forceinline__ double result_err_bound(int metric, int d, double val, double qsq, double xsq) {
+    const double u = 1.1102230246251565e-16;  // 2^-53
+    if (isnan(val)) return val;
+    if (metric == SVDB_COSINE) return 2.0 * (d + 8) * u;
+    if (metric == SVDB_EUCLIDEAN) return val * (d + 8) * u;
+    return (d + 4) * u * sqrt(qsq) * sqrt(xsq) * (1.0 + 1e-15);
+}
+
+// queries (nq rows, stride qs) -> padded buffer (stride ld) + sums of squares
+int prep_queries_fp64(Store* s, const double* q_dev, size_t qs, size_t nq, double* qbuf, double* qsq);
+
+// exact FP64 scan + merge over all live slots, writing SearchArgs outputs
+int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, uint32_t* kernels);
+size_t search_fp64_scratch(const Store* s, size_t nq, size_t k);
+
+// BF16 screen + certified FP64 re-rank (dev_gemm.cu)
+int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st);
+size_t search_bf16_scratch(const Store* s, size_t nq, size_t k);
+
+int num_sms();
+
+}  // namespace svdb

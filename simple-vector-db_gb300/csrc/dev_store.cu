@@ -1,0 +1,591 @@
+// dev_store.cu -- device-resident vector store and the reference-exact
+// /compare kernel.
+//
+// HBM layout of one store (capacity C slots, dimension D):
+//   x64     C x ld   double   FP64 master, ld = D rounded up to 16 (128-B rows)
+//   xb      C x ldb  bf16     BF16 shadow of x64, ldb = D rounded up to 64
+//   sq64    C        double   canonical sum of squares of the master row
+//   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
+//   live    C        uint8    1 = searchable row, 2 = row of another dimension
+//                              (counted in positions, never searched), 0 = deleted
+//   logical C        int64    slot -> positional index (rank among live slots)
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "dev_store.cuh"
+
+namespace {
+thread_local char g_err[512];
+}
+
+extern "C" void svdb_set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+extern "C" SVDB_API const char* svdb_last_error(void) { return g_err; }
+
+namespace svdb {
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// Derived per-row arrays for slots [lo, hi) or for an explicit slot list.
+// One group of 4 lanes per row, canonical order for the sum of squares.
+__global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bfloat16* __restrict__ xb,
+                              size_t ldb, double* __restrict__ sq64, float4* __restrict__ rowp,
+                              const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
+                              const int64_t* __restrict__ list) {
+    const int lane = threadIdx.x & 31, s = lane & 3;
+    const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const int64_t nrow = list ? hi : hi - lo;
+    const bool active = gid < nrow;
+    const int64_t slot = active ? (list ? list[gid] : lo + gid) : 0;
+    const double* x = x64 + slot * ld;
+    __nv_bfloat16* xh = xb + slot * ldb;
+    double sq = 0.0, bh = 0.0, res = 0.0;
+    if (active) {
+        for (size_t j = 2 * s; j < ld; j += 8) {
+            const double2 v = *reinterpret_cast<const double2*>(x + j);
+            sq = fma(v.x, v.x, sq);
+            sq = fma(v.y, v.y, sq);
+            const __nv_bfloat16 hx = __double2bfloat16(v.x), hy = __double2bfloat16(v.y);
+            const double fx = (double)__bfloat162float(hx), fy = (double)__bfloat162float(hy);
+            bh = fma(fx, fx, bh);
+            bh = fma(fy, fy, bh);
+            res = fma(v.x - fx, v.x - fx, res);
+            res = fma(v.y - fy, v.y - fy, res);
+            xh[j] = hx;
+            xh[j + 1] = hy;
+        }
+        for (size_t j = ld + 2 * s; j < ldb; j += 8) {  // zero the BF16 tail beyond ld
+            xh[j] = __float2bfloat16(0.0f);
+            xh[j + 1] = __float2bfloat16(0.0f);
+        }
+    }
+    sq = group4_sum(sq);
+    bh = group4_sum(bh);
+    res = group4_sum(res);
+    if (active && s == 0) {
+        sq64[slot] = sq;
+        float4 p;
+        p.x = __double2float_ru(sqrt(sq));
+        p.y = __double2float_ru(sqrt(bh));
+        p.z = __double2float_ru(sqrt(res));
+        p.w = __double2float_rn(0.5 * sq);
+        // rows the BF16 screen cannot bound (overflow, non-finite): mark them
+        // always-candidate with an infinite error term; dead slots: |x| = -1
+        if (!(sq < 1e30) || !isfinite(p.y)) p.z = __int_as_float(0x7f800000);
+        if (live[slot] != 1) p.x = -1.0f;
+        rowp[slot] = p;
+    }
+}
+
+// Single-block exclusive scan of live flags -> slot->logical map, done in
+// chunks of 1024*4 slots carrying the running count.
+__global__ void k_logical_map(const uint8_t* __restrict__ live, int64_t n, int64_t* __restrict__ logical,
+                              int64_t* __restrict__ nlive_out) {
+    __shared__ int64_t warp_tot[32];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t base = 0; base < n; base += 4096) {
+        int64_t i0 = base + threadIdx.x * 4;
+        int c[4], tot = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            c[u] = (i0 + u < n) ? (live[i0 + u] != 0 ? 1 : 0) : 0;
+            tot += c[u];
+        }
+        int incl = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int64_t w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+            int64_t wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+            warp_tot[lane] = wi - w;  // exclusive
+        }
+        __syncthreads();
+        int64_t run = carry + warp_tot[warp] + (incl - tot);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (i0 + u < n) logical[i0 + u] = c[u] ? run : -1;
+            run += c[u];
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = run;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *nlive_out = carry;
+}
+
+__global__ void k_set_live(uint8_t* live, const int64_t* slots, int n, uint8_t v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) live[slots[i]] = v;
+}
+
+// Reference-exact metrics: the float-accumulating loops of
+// src/vector_database.c:301-352, one thread per pair, IEEE intrinsics so
+// nothing is contracted into an FMA.
+__device__ float ref_metric(int metric, const double* __restrict__ a, const double* __restrict__ b, int d) {
+    if (metric == SVDB_EUCLIDEAN) {
+        float sum = 0.0f;
+        for (int i = 0; i < d; ++i) {
+            const float diff = __double2float_rn(__dsub_rn(a[i], b[i]));
+            sum = __fadd_rn(sum, __fmul_rn(diff, diff));
+        }
+        return __double2float_rn(__dsqrt_rn((double)sum));
+    }
+    float dot = 0.0f, na = 0.0f, nb = 0.0f;
+    for (int i = 0; i < d; ++i) {
+        const double ai = a[i], bi = b[i];
+        dot = __double2float_rn(__dadd_rn((double)dot, __dmul_rn(ai, bi)));
+        if (metric == SVDB_COSINE) {
+            na = __double2float_rn(__dadd_rn((double)na, __dmul_rn(ai, ai)));
+            nb = __double2float_rn(__dadd_rn((double)nb, __dmul_rn(bi, bi)));
+        }
+    }
+    if (metric == SVDB_DOT) return dot;
+    return __double2float_rn(__ddiv_rn((double)dot, __dmul_rn(__dsqrt_rn((double)na), __dsqrt_rn((double)nb))));
+}
+
+__global__ void k_compare_slots(const double* __restrict__ x64, size_t ld, int d, int metric,
+                                const int64_t* __restrict__ s1, const int64_t* __restrict__ s2, int n,
+                                float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = ref_metric(metric, x64 + s1[i] * ld, x64 + s2[i] * ld, d);
+}
+
+__global__ void k_compare_vec(const double* __restrict__ a, const double* __restrict__ b, int d, int metric,
+                              float* __restrict__ out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = ref_metric(metric, a, b, d);
+}
+
+// ---------------------------------------------------------------------------
+// store
+// ---------------------------------------------------------------------------
+
+int Store::ensure() {
+    if (stream) return SVDB_OK;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        svdb_set_error("no usable CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "none found");
+        return SVDB_ENODEV;
+    }
+    cudaStream_t st = nullptr;
+    SVDB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(st);
+        svdb_set_error("device store: cannot allocate a counter");
+        return SVDB_ENOMEM;
+    }
+    stream = st;
+    return SVDB_OK;
+}
+
+int Store::grow(size_t need) {
+    int erc = ensure();
+    if (erc) return erc;
+    if (need <= cap) return SVDB_OK;
+    size_t nc = cap ? cap : 1024;
+    while (nc < need) nc *= 2;
+    double* nx = nullptr;
+    __nv_bfloat16* nb = nullptr;
+    double* nsq = nullptr;
+    float4* np = nullptr;
+    uint8_t* nl = nullptr;
+    int64_t* nlog = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&nx, nc * ld * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&nb, nc * ldb * sizeof(__nv_bfloat16));
+    if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&nl, nc);
+    if (e == cudaSuccess) e = cudaMalloc(&nlog, nc * sizeof(int64_t));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(nx);
+        cudaFree(nb);
+        cudaFree(nsq);
+        cudaFree(np);
+        cudaFree(nl);
+        cudaFree(nlog);
+        svdb_set_error("device store: cannot grow to %zu rows of dim %zu: %s", nc, dim, cudaGetErrorString(e));
+        return SVDB_ENOMEM;
+    }
+    if (slots) {
+        SVDB_CUDA(cudaMemcpyAsync(nx, x64, slots * ld * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nb, xb, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nl, live, slots, cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nlog, logical, slots * sizeof(int64_t), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaStreamSynchronize(stream));
+    }
+    cudaFree(x64);
+    cudaFree(xb);
+    cudaFree(sq64);
+    cudaFree(rowp);
+    cudaFree(live);
+    cudaFree(logical);
+    x64 = nx;
+    xb = nb;
+    sq64 = nsq;
+    rowp = np;
+    live = nl;
+    logical = nlog;
+    cap = nc;
+    return SVDB_OK;
+}
+
+int Store::scratch_reserve(size_t bytes) {
+    int erc = ensure();
+    if (erc) return erc;
+    if (bytes <= scratch_bytes) return SVDB_OK;
+    SVDB_CUDA(cudaStreamSynchronize(stream));
+    cudaFree(scratch);
+    scratch = nullptr;
+    scratch_bytes = 0;
+    size_t nb = round_up(bytes + bytes / 4, 1 << 20);
+    cudaError_t e = cudaMalloc(&scratch, nb);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        svdb_set_error("device scratch: cannot allocate %zu bytes: %s", nb, cudaGetErrorString(e));
+        return SVDB_ENOMEM;
+    }
+    scratch_bytes = nb;
+    return SVDB_OK;
+}
+
+int Store::pinned_reserve(size_t bytes) {
+    int erc = ensure();
+    if (erc) return erc;
+    if (bytes <= pin_bytes) return SVDB_OK;
+    SVDB_CUDA(cudaStreamSynchronize(stream));
+    cudaFreeHost(pin);
+    pin = nullptr;
+    pin_bytes = 0;
+    size_t nb = round_up(bytes + bytes / 4, 1 << 16);
+    SVDB_CUDA(cudaMallocHost(&pin, nb));
+    pin_bytes = nb;
+    return SVDB_OK;
+}
+
+// Move staged appends to the device: one pitched copy of the staging block.
+int Store::flush() {
+    if (stage_rows == 0) return SVDB_OK;
+    const size_t first = slots, n = stage_rows;
+    int rc = grow(first + n);
+    if (rc) return rc;
+    SVDB_CUDA(cudaStreamSynchronize(stream));  // the pinned stage buffer is reused below
+    rc = pinned_reserve(n * dim * sizeof(double));
+    if (rc) return rc;
+    std::memcpy(pin, stage.data(), n * dim * sizeof(double));
+    SVDB_CUDA(cudaMemsetAsync(x64 + first * ld, 0, n * ld * sizeof(double), stream));
+    SVDB_CUDA(cudaMemcpy2DAsync(x64 + first * ld, ld * sizeof(double), pin, dim * sizeof(double),
+                                dim * sizeof(double), n, cudaMemcpyHostToDevice, stream));
+    SVDB_CUDA(cudaMemcpyAsync(live + first, stage_live.data(), n, cudaMemcpyHostToDevice, stream));
+    SVDB_CUDA(cudaStreamSynchronize(stream));  // stage_live is pageable and cleared below
+    slots += n;
+    stage.clear();
+    stage_live.clear();
+    stage_rows = 0;
+    if (derive_lo < 0 || (int64_t)first < derive_lo) derive_lo = (int64_t)first;
+    derive_hi = (int64_t)slots;
+    map_dirty = true;
+    return SVDB_OK;
+}
+
+int Store::sync() {
+    int rc = ensure();
+    if (rc) return rc;
+    rc = flush();
+    if (rc) return rc;
+    if (derive_lo >= 0 && derive_hi > derive_lo) {
+        const int64_t n = derive_hi - derive_lo;
+        const int threads = 256;
+        const int64_t blocks = (n * 4 + threads - 1) / threads;
+        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, sq64, rowp, live, derive_lo,
+                                                              derive_hi, nullptr);
+        SVDB_LAUNCH_CHECK();
+    }
+    derive_lo = derive_hi = -1;
+    if (!dirty_list.empty()) {
+        const int64_t n = (int64_t)dirty_list.size();
+        int64_t* d = nullptr;
+        rc = scratch_reserve(n * sizeof(int64_t));
+        if (rc) return rc;
+        d = (int64_t*)scratch;
+        SVDB_CUDA(cudaMemcpyAsync(d, dirty_list.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
+        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, sq64, rowp, live, 0,
+                                                                         n, d);
+        SVDB_LAUNCH_CHECK();
+        SVDB_CUDA(cudaStreamSynchronize(stream));
+        dirty_list.clear();
+    }
+    if (map_dirty && slots) {
+        k_logical_map<<<1, 1024, 0, stream>>>(live, (int64_t)slots, logical, d_nlive);
+        SVDB_LAUNCH_CHECK();
+        SVDB_CUDA(cudaMemcpyAsync(&h_nlive, d_nlive, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
+        SVDB_CUDA(cudaStreamSynchronize(stream));
+        nlive = (size_t)h_nlive;
+        map_dirty = false;
+    } else if (!slots) {
+        nlive = 0;
+        map_dirty = false;
+    }
+    return SVDB_OK;
+}
+
+}  // namespace svdb
+
+using svdb::Store;
+
+extern "C" {
+
+svdbd_store* svdbd_store_create(size_t dim) {
+    if (dim == 0) {
+        svdb_set_error("device store: dimension 0");
+        return nullptr;
+    }
+    Store* s = new (std::nothrow) Store();
+    if (!s) return nullptr;
+    s->dim = dim;
+    s->ld = svdb::round_up(dim, svdb::kRowAlign);
+    s->ldb = svdb::round_up(dim, svdb::kBf16Align);
+    return reinterpret_cast<svdbd_store*>(s);
+}
+
+void svdbd_store_destroy(svdbd_store* hs) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if (!s) return;
+    if (!s->stream) {  // never touched the GPU
+        delete s;
+        return;
+    }
+    cudaStreamSynchronize(s->stream);
+    cudaFree(s->x64);
+    cudaFree(s->xb);
+    cudaFree(s->sq64);
+    cudaFree(s->rowp);
+    cudaFree(s->live);
+    cudaFree(s->logical);
+    cudaFree(s->scratch);
+    cudaFree(s->d_nlive);
+    cudaFreeHost(s->pin);
+    s->release_extra();
+    cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+void* svdbd_store_stream(svdbd_store* hs) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    return s->ensure() == SVDB_OK ? (void*)s->stream : nullptr;
+}
+size_t svdbd_store_dim(const svdbd_store* hs) { return reinterpret_cast<const Store*>(hs)->dim; }
+size_t svdbd_store_slots(const svdbd_store* hs) {
+    const Store* s = reinterpret_cast<const Store*>(hs);
+    return s->slots + s->stage_rows;
+}
+
+int svdbd_store_reserve(svdbd_store* hs, size_t rows) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    int rc = s->flush();
+    return rc ? rc : s->grow(rows);
+}
+
+int svdbd_store_append(svdbd_store* hs, const double* const* rows, const uint8_t* live, size_t n) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    const size_t d = s->dim;
+    try {
+        s->stage.resize((s->stage_rows + n) * d);
+        s->stage_live.resize(s->stage_rows + n);
+    } catch (...) {
+        svdb_set_error("device store: host staging allocation failed");
+        return SVDB_ENOMEM;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        double* dst = s->stage.data() + (s->stage_rows + i) * d;
+        const uint8_t flag = (rows[i] && (!live || live[i] == 1)) ? 1 : 2;
+        if (flag == 1)
+            std::memcpy(dst, rows[i], d * sizeof(double));
+        else
+            std::memset(dst, 0, d * sizeof(double));
+        s->stage_live[s->stage_rows + i] = flag;
+    }
+    s->stage_rows += n;
+    if (s->stage_rows >= 65536) return s->flush();
+    return SVDB_OK;
+}
+
+int svdbd_store_append_block(svdbd_store* hs, const double* rows, size_t n) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    int rc = s->flush();
+    if (rc) return rc;
+    const size_t first = s->slots;
+    rc = s->grow(first + n);
+    if (rc) return rc;
+    const size_t d = s->dim, chunk = 1 << 16;
+    rc = s->pinned_reserve(std::min(n, chunk) * d * sizeof(double));
+    if (rc) return rc;
+    SVDB_CUDA(cudaMemsetAsync(s->x64 + first * s->ld, 0, n * s->ld * sizeof(double), s->stream));
+    SVDB_CUDA(cudaMemsetAsync(s->live + first, 1, n, s->stream));
+    for (size_t off = 0; off < n; off += chunk) {
+        const size_t m = std::min(chunk, n - off);
+        SVDB_CUDA(cudaStreamSynchronize(s->stream));
+        std::memcpy(s->pin, rows + off * d, m * d * sizeof(double));
+        SVDB_CUDA(cudaMemcpy2DAsync(s->x64 + (first + off) * s->ld, s->ld * sizeof(double), s->pin,
+                                    d * sizeof(double), d * sizeof(double), m, cudaMemcpyHostToDevice, s->stream));
+    }
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    s->slots += n;
+    if (s->derive_lo < 0 || (int64_t)first < s->derive_lo) s->derive_lo = (int64_t)first;
+    s->derive_hi = (int64_t)s->slots;
+    s->map_dirty = true;
+    return SVDB_OK;
+}
+
+int svdbd_store_overwrite(svdbd_store* hs, int64_t slot, const double* row, int live) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if (slot >= 0 && (size_t)slot >= s->slots && (size_t)slot < s->slots + s->stage_rows) {  // still staged
+        const size_t st = (size_t)slot - s->slots;
+        const bool ok = row && live == 1;
+        if (ok)
+            std::memcpy(s->stage.data() + st * s->dim, row, s->dim * sizeof(double));
+        else
+            std::memset(s->stage.data() + st * s->dim, 0, s->dim * sizeof(double));
+        s->stage_live[st] = ok ? 1 : 2;
+        return SVDB_OK;
+    }
+    int rc = s->flush();
+    if (rc) return rc;
+    if (slot < 0 || (size_t)slot >= s->slots) {
+        svdb_set_error("overwrite: slot %lld out of range", (long long)slot);
+        return SVDB_EINVAL;
+    }
+    const uint8_t lv = (row && live == 1) ? 1 : 2;
+    SVDB_CUDA(cudaMemsetAsync(s->x64 + slot * s->ld, 0, s->ld * sizeof(double), s->stream));
+    if (lv == 1)
+        SVDB_CUDA(cudaMemcpyAsync(s->x64 + slot * s->ld, row, s->dim * sizeof(double), cudaMemcpyHostToDevice,
+                                  s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(s->live + slot, &lv, 1, cudaMemcpyHostToDevice, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    s->dirty_list.push_back(slot);
+    s->map_dirty = true;
+    return SVDB_OK;
+}
+
+int svdbd_store_kill(svdbd_store* hs, int64_t slot) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if ((size_t)slot >= s->slots) {  // still staged: drop it from the stage
+        const size_t st = (size_t)slot - s->slots;
+        if (slot < 0 || st >= s->stage_rows) {
+            svdb_set_error("kill: slot %lld out of range", (long long)slot);
+            return SVDB_EINVAL;
+        }
+        s->stage_live[st] = 0;
+        return SVDB_OK;
+    }
+    int rc = s->ensure();
+    if (rc) return rc;
+    const uint8_t zero = 0;
+    SVDB_CUDA(cudaMemcpyAsync(s->live + slot, &zero, 1, cudaMemcpyHostToDevice, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    s->dirty_list.push_back(slot);  // its row error term becomes +inf (never screened)
+    s->map_dirty = true;
+    return SVDB_OK;
+}
+
+int svdbd_store_sync(svdbd_store* hs) { return reinterpret_cast<Store*>(hs)->sync(); }
+
+int svdbd_store_wait(svdbd_store* hs) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if (!s->stream) return SVDB_OK;
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    return SVDB_OK;
+}
+
+int svdbd_compare_slots(svdbd_store* hs, int metric, const int64_t* slot1, const int64_t* slot2, size_t n,
+                        float* out) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if (n == 0) return SVDB_OK;
+    int rc = s->sync();
+    if (rc) return rc;
+    const size_t bytes = n * (2 * sizeof(int64_t) + sizeof(float));
+    rc = s->scratch_reserve(bytes);
+    if (!rc) rc = s->pinned_reserve(bytes);
+    if (rc) return rc;
+    int64_t* d1 = (int64_t*)s->scratch;
+    int64_t* d2 = d1 + n;
+    float* dout = (float*)(d2 + n);
+    std::memcpy(s->pin, slot1, n * sizeof(int64_t));
+    std::memcpy((int64_t*)s->pin + n, slot2, n * sizeof(int64_t));
+    SVDB_CUDA(cudaMemcpyAsync(d1, s->pin, 2 * n * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
+    svdb::k_compare_slots<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(s->x64, s->ld, (int)s->dim, metric,
+                                                                             d1, d2, (int)n, dout);
+    SVDB_LAUNCH_CHECK();
+    float* hout = (float*)((int64_t*)s->pin + 2 * n);
+    SVDB_CUDA(cudaMemcpyAsync(hout, dout, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    std::memcpy(out, hout, n * sizeof(float));
+    return SVDB_OK;
+}
+
+// The drop-in metric functions take two free-standing host vectors; they
+// share one small device buffer and stream guarded by a mutex.
+namespace {
+std::mutex g_vec_mu;
+double* g_vec_buf = nullptr;
+size_t g_vec_cap = 0;
+float* g_vec_out = nullptr;
+cudaStream_t g_vec_stream = nullptr;
+}  // namespace
+
+int svdbd_compare_vectors(int metric, const double* a, const double* b, size_t d, float* out) {
+    std::lock_guard<std::mutex> lk(g_vec_mu);
+    if (!g_vec_stream) {
+        SVDB_CUDA(cudaStreamCreateWithFlags(&g_vec_stream, cudaStreamNonBlocking));
+        SVDB_CUDA(cudaMalloc(&g_vec_out, sizeof(float)));
+    }
+    if (d * 2 > g_vec_cap) {
+        cudaFree(g_vec_buf);
+        g_vec_buf = nullptr;
+        g_vec_cap = 0;
+        size_t nc = svdb::round_up(d * 2, 4096);
+        SVDB_CUDA(cudaMalloc(&g_vec_buf, nc * sizeof(double)));
+        g_vec_cap = nc;
+    }
+    if (d) {
+        SVDB_CUDA(cudaMemcpyAsync(g_vec_buf, a, d * sizeof(double), cudaMemcpyHostToDevice, g_vec_stream));
+        SVDB_CUDA(cudaMemcpyAsync(g_vec_buf + d, b, d * sizeof(double), cudaMemcpyHostToDevice, g_vec_stream));
+    }
+    svdb::k_compare_vec<<<1, 32, 0, g_vec_stream>>>(g_vec_buf, g_vec_buf + d, (int)d, metric, g_vec_out);
+    SVDB_LAUNCH_CHECK();
+    SVDB_CUDA(cudaMemcpyAsync(out, g_vec_out, sizeof(float), cudaMemcpyDeviceToHost, g_vec_stream));
+    SVDB_CUDA(cudaStreamSynchronize(g_vec_stream));
+    return SVDB_OK;
+}
+
+}  // extern "C"

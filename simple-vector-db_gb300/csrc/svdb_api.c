@@ -1,0 +1,266 @@
+/*
+ * svdb_api.c -- the drop-in /compare metrics (reference
+ * include/vector_database.h:117-135) and the batch entry points of
+ * svdb_gb300.h.  Request validation mirrors compare_handler_callback
+ * (src/compare_handler.c:74-195); the arithmetic runs on the GPU.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "svdb_internal.h"
+
+int svdb_kd_nearest_batch(KDTree* tree, const double* q, size_t nq, size_t stride, int64_t* out);
+
+static float metric_vectors(int metric, Vector a, Vector b) {
+    if (a.dimension != b.dimension) {
+        fprintf(stderr, "Vectors have different dimensions\n"); /* src/vector_database.c:302-305 */
+        return -1.0f;
+    }
+    float out = NAN;
+    if (svdbd_compare_vectors(metric, a.data, b.data, a.dimension, &out) != SVDB_OK) {
+        fprintf(stderr, "metric: %s\n", svdb_last_error());
+        return NAN;
+    }
+    return out;
+}
+
+SVDB_API float cosine_similarity(Vector vec1, Vector vec2) { return metric_vectors(SVDB_COSINE, vec1, vec2); }
+SVDB_API float euclidean_distance(Vector vec1, Vector vec2) { return metric_vectors(SVDB_EUCLIDEAN, vec1, vec2); }
+SVDB_API float dot_product(Vector vec1, Vector vec2) { return metric_vectors(SVDB_DOT, vec1, vec2); }
+
+SVDB_API int svdb_compare_batch(VectorDatabase* db, int metric, const int64_t* index1, const int64_t* index2,
+                                size_t npairs, size_t expected_dim, float* out, int32_t* status) {
+    if (!db || (npairs && (!index1 || !index2 || !out || !status))) {
+        svdb_set_error("svdb_compare_batch: NULL argument");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    int rc = SVDB_OK;
+    int64_t* s1 = (int64_t*)malloc((npairs ? npairs : 1) * 2 * sizeof(int64_t));
+    size_t* pos = (size_t*)malloc((npairs ? npairs : 1) * sizeof(size_t));
+    float* res = (float*)malloc((npairs ? npairs : 1) * sizeof(float));
+    if (!s1 || !pos || !res) {
+        free(s1);
+        free(pos);
+        free(res);
+        svdb_set_error("svdb_compare_batch: out of host memory");
+        return SVDB_ENOMEM;
+    }
+    int64_t* s2 = s1 + npairs;
+    size_t ndev = 0;
+    pthread_mutex_lock(&db->mutex);
+    for (size_t i = 0; i < npairs; ++i) {
+        out[i] = NAN;
+        const int64_t a = index1[i], b = index2[i];
+        if (a < 0 || b < 0 || (size_t)a >= db->size || (size_t)b >= db->size) {
+            status[i] = SVDB_CMP_OUT_OF_BOUNDS;
+            continue;
+        }
+        const Vector* va = &db->vectors[a];
+        const Vector* vb = &db->vectors[b];
+        if (va->dimension != vb->dimension) {
+            status[i] = SVDB_CMP_DIFF_DIM;
+            continue;
+        }
+        if (expected_dim && (va->dimension != expected_dim || vb->dimension != expected_dim)) {
+            status[i] = SVDB_CMP_SIZE_MISMATCH;
+            continue;
+        }
+        if (metric < 0 || metric > 2) {
+            status[i] = SVDB_CMP_UNKNOWN_METHOD;
+            continue;
+        }
+        status[i] = SVDB_CMP_OK;
+        if (d->dev && va->dimension == d->dim) { /* both rows are in the device store */
+            s1[ndev] = d->slot_of[a];
+            s2[ndev] = d->slot_of[b];
+            pos[ndev++] = i;
+        } else { /* rows of another dimension: the free-standing vector kernel */
+            int r = svdbd_compare_vectors(metric, va->data, vb->data, va->dimension, &out[i]);
+            if (r && !rc) rc = r;
+        }
+    }
+    if (!rc && ndev) {
+        memmove(s1 + ndev, s2, ndev * sizeof(int64_t));
+        rc = svdbd_compare_slots(d->dev, metric, s1, s1 + ndev, ndev, res);
+        if (!rc)
+            for (size_t j = 0; j < ndev; ++j) out[pos[j]] = res[j];
+    }
+    pthread_mutex_unlock(&db->mutex);
+    free(s1);
+    free(pos);
+    free(res);
+    return rc;
+}
+
+SVDB_API int svdb_nearest_batch(VectorDatabase* db, const double* queries, size_t nq, size_t dim,
+                                int64_t* out_index) {
+    if (!db || (nq && (!queries || !out_index))) {
+        svdb_set_error("svdb_nearest_batch: NULL argument");
+        return SVDB_EINVAL;
+    }
+    if (nq && dim < db->kdtree->dimension) {
+        svdb_set_error("svdb_nearest_batch: query dimension %zu < KD dimension %zu", dim, db->kdtree->dimension);
+        return SVDB_EINVAL;
+    }
+    /* src/compare_handler.c:403 calls kdtree_nearest without the store lock */
+    return svdb_kd_nearest_batch(db->kdtree, queries, nq, dim, out_index);
+}
+
+static int search_common(VectorDatabase* db, const double* q, size_t nq, size_t dim, size_t k, int metric,
+                         int precision, int64_t* ids, double* dists, double* err, int on_device,
+                         svdb_search_stats* stats) {
+    if (!db || (nq && (!q || !ids || !dists))) {
+        svdb_set_error("svdb_search_topk: NULL argument");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc;
+    if (!d->dev) {
+        svdb_set_error("svdb_search_topk: the store holds no rows");
+        rc = SVDB_EINVAL;
+    } else if (dim != d->dim) {
+        svdb_set_error("svdb_search_topk: query dimension %zu != store dimension %zu", dim, d->dim);
+        rc = SVDB_EINVAL;
+    } else {
+        rc = svdbd_search(d->dev, q, nq, k, metric, precision, ids, dists, err, on_device, stats);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+SVDB_API int svdb_search_topk(VectorDatabase* db, const double* queries, size_t nq, size_t dim, size_t k, int metric,
+                              int precision, int64_t* ids, double* dists, double* err, svdb_search_stats* stats) {
+    return search_common(db, queries, nq, dim, k, metric, precision, ids, dists, err, 0, stats);
+}
+
+SVDB_API int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim, size_t k,
+                                     int metric, int precision, int64_t* d_ids, double* d_dists, double* d_err,
+                                     svdb_search_stats* stats) {
+    return search_common(db, d_queries, nq, dim, k, metric, precision, d_ids, d_dists, d_err, 1, stats);
+}
+
+void svdb_kd_insert_prefix(KDTree* tree, const double* point, size_t avail, size_t index);
+
+SVDB_API int svdb_insert_batch(VectorDatabase* db, const double* rows, size_t n, size_t dim, const char* uuids,
+                               size_t* first_index) {
+    if (!db || (n && !rows)) {
+        svdb_set_error("svdb_insert_batch: NULL argument");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = SVDB_OK;
+    const size_t first = db->size;
+    if (first_index) *first_index = first;
+    if (db->size + n > db->capacity) {
+        size_t need = db->size + n;
+        VectorDatabase* p = db;
+        /* same doubling as single inserts */
+        size_t nc = p->capacity;
+        while (nc < need) nc = nc > SIZE_MAX / 2 ? SIZE_MAX : nc * 2;
+        Vector* nv = (Vector*)realloc(p->vectors, nc * sizeof(Vector));
+        int64_t* ns = nv ? (int64_t*)realloc(d->slot_of, nc * sizeof(int64_t)) : NULL;
+        if (nv) p->vectors = nv;
+        if (ns) d->slot_of = ns;
+        if (!nv || !ns) {
+            pthread_mutex_unlock(&db->mutex);
+            svdb_set_error("svdb_insert_batch: out of host memory");
+            return SVDB_ENOMEM;
+        }
+        p->capacity = nc;
+    }
+    if (svdb_db_ensure_dev(d, dim) != SVDB_OK) {
+        pthread_mutex_unlock(&db->mutex);
+        return SVDB_ENOMEM;
+    }
+    /* host copies, owned by the store as if each came from vector_db_insert */
+    for (size_t i = 0; i < n; ++i) {
+        Vector v;
+        memset(&v, 0, sizeof(v));
+        if (uuids) {
+            memcpy(v.uuid, uuids + i * UUID_SIZE, UUID_SIZE);
+        }
+        v.dimension = dim;
+        v.data = (double*)malloc((dim ? dim : 1) * sizeof(double));
+        if (!v.data) {
+            rc = SVDB_ENOMEM;
+            svdb_set_error("svdb_insert_batch: out of host memory at row %zu", i);
+            n = i;
+            break;
+        }
+        memcpy(v.data, rows + i * dim, dim * sizeof(double));
+        db->vectors[db->size + i] = v;
+    }
+    if (d->dev && n) {
+        const size_t slot0 = svdbd_store_slots(d->dev);
+        int r = dim == d->dim ? svdbd_store_append_block(d->dev, rows, n) : SVDB_OK;
+        if (dim != d->dim) {
+            for (size_t i = 0; i < n && !r; ++i) {
+                const double* none = NULL;
+                uint8_t flag = 2;
+                r = svdbd_store_append(d->dev, &none, &flag, 1);
+            }
+        }
+        if (r) {
+            for (size_t i = 0; i < n; ++i) free(db->vectors[db->size + i].data);
+            pthread_mutex_unlock(&db->mutex);
+            return r;
+        }
+        for (size_t i = 0; i < n; ++i) d->slot_of[db->size + i] = (int64_t)(slot0 + i);
+    } else {
+        for (size_t i = 0; i < n; ++i) d->slot_of[db->size + i] = -1;
+    }
+    for (size_t i = 0; i < n; ++i)
+        svdb_kd_insert_prefix(db->kdtree, db->vectors[db->size + i].data, dim, db->size + i);
+    db->size += n;
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+SVDB_API int svdb_reserve(VectorDatabase* db, size_t rows, size_t dim) {
+    if (!db) return SVDB_EINVAL;
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = svdb_db_ensure_dev(d, dim);
+    if (!rc && d->dev) {
+        if (d->dim != dim) {
+            svdb_set_error("svdb_reserve: dimension %zu != store dimension %zu", dim, d->dim);
+            rc = SVDB_EINVAL;
+        } else {
+            rc = svdbd_store_reserve(d->dev, rows);
+        }
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+SVDB_API int svdb_sync(VectorDatabase* db) {
+    if (!db) return SVDB_EINVAL;
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = d->dev ? svdbd_store_sync(d->dev) : SVDB_OK;
+    if (!rc) {
+        svdb_kd* t = svdb_kd_of(db->kdtree);
+        pthread_mutex_lock(&t->lock);
+        if (t->n && t->pub.dimension) rc = svdb_kd_sync_locked(t);
+        pthread_mutex_unlock(&t->lock);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+SVDB_API void* svdb_stream(VectorDatabase* db) {
+    if (!db) return NULL;
+    svdb_db* d = svdb_of(db);
+    return d->dev ? svdbd_store_stream(d->dev) : NULL;
+}
+
+SVDB_API int svdb_wait(VectorDatabase* db) {
+    if (!db) return SVDB_EINVAL;
+    svdb_db* d = svdb_of(db);
+    return d->dev ? svdbd_store_wait(d->dev) : SVDB_OK;
+}

@@ -1,0 +1,84 @@
+/*
+ * svdb_device.h -- the thin C ABI between the C host layer (store, KD-tree
+ * bookkeeping, request validation) and the CUDA layer (device-resident
+ * store, kernels).  Private to libsvdb_gb300.so: plain pointers and sizes,
+ * no CUDA types, every call returns SVDB_OK or a negative SVDB_E* code and
+ * records a message with svdb_set_error().
+ *
+ * Row addressing: the device store keeps rows in PHYSICAL slots that never
+ * move (append, overwrite in place, tombstone on delete).  The reference's
+ * positional index (src/vector_database.c:185-195 shifts rows left on
+ * delete) is the rank of a slot among live slots; the host keeps
+ * logical->slot, the device derives slot->logical at sync time.
+ */
+#ifndef SVDB_DEVICE_H
+#define SVDB_DEVICE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/svdb_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SVDB_API __attribute__((visibility("default")))
+#else
+#define SVDB_API
+#endif
+
+typedef struct svdbd_store svdbd_store;
+typedef struct svdbd_kd svdbd_kd;
+
+/* thread-local error message */
+void svdb_set_error(const char* fmt, ...);
+
+/* ---- device store -------------------------------------------------------- */
+svdbd_store* svdbd_store_create(size_t dim);
+void svdbd_store_destroy(svdbd_store* s);
+void* svdbd_store_stream(svdbd_store* s);
+size_t svdbd_store_dim(const svdbd_store* s);
+size_t svdbd_store_slots(const svdbd_store* s);
+int svdbd_store_reserve(svdbd_store* s, size_t rows);
+/* append n rows; rows[i] are host pointers to dim doubles.  live[i] (or 1
+ * when live is NULL): 1 = searchable row, 2 = placeholder for a row of
+ * another dimension (kept in the positional order, never searched; also
+ * used when rows[i] is NULL).  overwrite takes the same flag; kill marks a
+ * slot deleted (0). */
+int svdbd_store_append(svdbd_store* s, const double* const* rows, const uint8_t* live, size_t n);
+/* append n rows from one contiguous host block (n x dim) */
+int svdbd_store_append_block(svdbd_store* s, const double* rows, size_t n);
+int svdbd_store_overwrite(svdbd_store* s, int64_t slot, const double* row, int live);
+int svdbd_store_kill(svdbd_store* s, int64_t slot);
+/* flush staged mutations, rebuild derived arrays and the slot->logical map */
+int svdbd_store_sync(svdbd_store* s);
+int svdbd_store_wait(svdbd_store* s);
+
+/* reference-exact /compare for n slot pairs (host arrays in/out) */
+int svdbd_compare_slots(svdbd_store* s, int metric, const int64_t* slot1, const int64_t* slot2, size_t n,
+                        float* out);
+/* reference-exact metric of two host vectors (the drop-in cosine_similarity
+ * etc. take Vectors that need not be stored rows) */
+int svdbd_compare_vectors(int metric, const double* a, const double* b, size_t d, float* out);
+
+/* exact top-k; q/ids/dists/err in host memory unless on_device */
+int svdbd_search(svdbd_store* s, const double* q, size_t nq, size_t k, int metric, int precision,
+                 int64_t* ids, double* dists, double* err, int on_device, svdb_search_stats* st);
+
+/* ---- KD tree mirror ------------------------------------------------------ */
+svdbd_kd* svdbd_kd_create(size_t kdim);
+void svdbd_kd_destroy(svdbd_kd* t);
+/* mirror nodes [synced, n) and apply parent-link patches for nodes < synced */
+int svdbd_kd_sync(svdbd_kd* t, const double* pts, const int64_t* index, const int32_t* left,
+                  const int32_t* right, size_t n, size_t synced, const int32_t* patch_nodes, size_t npatch,
+                  int height);
+/* nq queries (host, row stride qstride doubles); out: stored index or -1 */
+int svdbd_kd_nearest(svdbd_kd* t, const double* q, size_t nq, size_t qstride, int64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVDB_DEVICE_H */

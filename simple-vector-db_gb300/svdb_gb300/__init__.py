@@ -1,0 +1,325 @@
+"""Python binding of libsvdb_gb300.so (the C ABI declared in include/).
+
+Mirrors the reference's C API one to one -- ``vector_db_init``,
+``vector_db_insert``, ``vector_db_read``, ``vector_db_update``,
+``vector_db_delete``, ``vector_db_save``/``vector_db_load``,
+``cosine_similarity``/``euclidean_distance``/``dot_product`` and
+``kdtree_nearest`` (reference include/vector_database.h, include/kdtree.h)
+-- plus the batch entry points of include/svdb_gb300.h.  There is no
+Python compute path: every metric and search runs in the CUDA library, and
+importing this module fails if the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.environ.get("SVDB_LIB", os.path.join(_PKG, "_build", "libsvdb_gb300.so"))
+
+COSINE, EUCLIDEAN, DOT = 0, 1, 2
+PREC_FP64, PREC_BF16 = 0, 1
+METRIC_URLS = {"/compare/cosine_similarity": COSINE, "/compare/euclidean_distance": EUCLIDEAN,
+               "/compare/dot_product": DOT}
+CMP_OK, CMP_OUT_OF_BOUNDS, CMP_NOT_FOUND, CMP_DIFF_DIM, CMP_SIZE_MISMATCH, CMP_UNKNOWN_METHOD = range(6)
+# error bodies of compare_handler_callback (src/compare_handler.c:88-163)
+CMP_ERRORS = {
+    CMP_OUT_OF_BOUNDS: (400, "Index out of bounds"),
+    CMP_NOT_FOUND: (404, "Vector not found"),
+    CMP_DIFF_DIM: (400, "Vectors have different dimensions"),
+    CMP_SIZE_MISMATCH: (400, "Vector size mismatch"),
+    CMP_UNKNOWN_METHOD: (400, "Unknown comparison method"),
+}
+NOT_FOUND = 2**64 - 1  # (size_t)-1
+
+_dp = C.POINTER(C.c_double)
+_i64p = C.POINTER(C.c_int64)
+
+
+class Vector(C.Structure):
+    """include/vector_database.h (reference include/vector_database.h:14-18)."""
+    _fields_ = [("uuid", C.c_char * 37), ("dimension", C.c_size_t), ("data", _dp)]
+
+
+class SearchStats(C.Structure):
+    _fields_ = [("candidates", C.c_uint64), ("widened", C.c_uint32), ("kernels", C.c_uint32),
+                ("max_err_bound", C.c_double)]
+
+
+class SvdbError(RuntimeError):
+    pass
+
+
+def _load():
+    if not os.path.isfile(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with simple-vector-db_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    vp, sz = C.c_void_p, C.c_size_t
+    sig = {
+        "vector_db_init": (vp, [sz, sz]),
+        "vector_db_free": (None, [vp]),
+        "vector_db_insert": (sz, [vp, Vector]),
+        "vector_db_read": (C.POINTER(Vector), [vp, sz]),
+        "vector_db_read_by_uuid": (C.POINTER(Vector), [vp, C.c_char_p]),
+        "vector_db_update": (None, [vp, sz, Vector]),
+        "vector_db_delete": (None, [vp, sz]),
+        "vector_db_save": (None, [vp, C.c_char_p]),
+        "vector_db_load": (vp, [C.c_char_p, sz]),
+        "cosine_similarity": (C.c_float, [Vector, Vector]),
+        "euclidean_distance": (C.c_float, [Vector, Vector]),
+        "dot_product": (C.c_float, [Vector, Vector]),
+        "kdtree_create": (vp, [sz]),
+        "kdtree_insert": (None, [vp, _dp, sz]),
+        "kdtree_free": (None, [vp]),
+        "kdtree_nearest": (sz, [vp, _dp]),
+        "svdb_compare_batch": (C.c_int, [vp, C.c_int, _i64p, _i64p, sz, sz, C.POINTER(C.c_float),
+                                         C.POINTER(C.c_int32)]),
+        "svdb_nearest_batch": (C.c_int, [vp, _dp, sz, sz, _i64p]),
+        "svdb_search_topk": (C.c_int, [vp, _dp, sz, sz, sz, C.c_int, C.c_int, _i64p, _dp, _dp,
+                                       C.POINTER(SearchStats)]),
+        "svdb_search_topk_device": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, C.c_int, vp, vp, vp,
+                                              C.POINTER(SearchStats)]),
+        "svdb_insert_batch": (C.c_int, [vp, _dp, sz, sz, C.c_char_p, C.POINTER(C.c_size_t)]),
+        "svdb_reserve": (C.c_int, [vp, sz, sz]),
+        "svdb_sync": (C.c_int, [vp]),
+        "svdb_stream": (vp, [vp]),
+        "svdb_wait": (C.c_int, [vp]),
+        "svdb_last_error": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    return L
+
+
+lib = _load()
+_libc = C.CDLL(None)
+_libc.malloc.restype = C.c_void_p
+_libc.malloc.argtypes = [C.c_size_t]
+
+
+def last_error() -> str:
+    return (lib.svdb_last_error() or b"").decode(errors="replace")
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise SvdbError(f"{what} failed ({rc}): {last_error()}")
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def make_vector(data, uuid: bytes | str = b"", owned: bool = True) -> Vector:
+    """A Vector as the handlers build it.  owned=True mallocs the data (the
+    store takes ownership on insert/update and free()s it later); owned=False
+    points at the numpy buffer (for the metric functions, which only read)."""
+    a = _f64(data).ravel()
+    v = Vector()
+    if isinstance(uuid, str):
+        uuid = uuid.encode()
+    v.uuid = uuid[:36]
+    v.dimension = a.size
+    if owned:
+        p = _libc.malloc(max(a.size, 1) * 8)
+        if not p:
+            raise MemoryError
+        C.memmove(p, a.ctypes.data, a.size * 8)
+        v.data = C.cast(p, _dp)
+    else:
+        v.data = a.ctypes.data_as(_dp)
+        v._keep = a
+    return v
+
+
+def cosine_similarity(a, b) -> np.float32:
+    return np.float32(lib.cosine_similarity(make_vector(a, owned=False), make_vector(b, owned=False)))
+
+
+def euclidean_distance(a, b) -> np.float32:
+    return np.float32(lib.euclidean_distance(make_vector(a, owned=False), make_vector(b, owned=False)))
+
+
+def dot_product(a, b) -> np.float32:
+    return np.float32(lib.dot_product(make_vector(a, owned=False), make_vector(b, owned=False)))
+
+
+class VectorDatabase:
+    """Owner of one ``VectorDatabase*`` (vector_db_init / vector_db_load)."""
+
+    def __init__(self, initial_capacity: int = 0, kd_dimension: int = 3, _ptr=None):
+        self.ptr = _ptr if _ptr is not None else lib.vector_db_init(initial_capacity, kd_dimension)
+        if not self.ptr:
+            raise SvdbError("vector_db_init failed")
+        self.kd_dimension = kd_dimension
+
+    @classmethod
+    def load(cls, filename: str, kd_dimension: int = 3) -> "VectorDatabase":
+        p = lib.vector_db_load(filename.encode(), kd_dimension)
+        if not p:
+            raise SvdbError(f"vector_db_load({filename}) failed")
+        return cls(_ptr=p, kd_dimension=kd_dimension)
+
+    def close(self) -> None:
+        if self.ptr:
+            lib.vector_db_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- struct fields the handlers read (include/vector_database.h:24-30) --
+    @property
+    def size(self) -> int:
+        return C.cast(self.ptr + 8, C.POINTER(C.c_size_t))[0]
+
+    @property
+    def kdtree(self) -> int:
+        return C.cast(self.ptr + 24, C.POINTER(C.c_void_p))[0]
+
+    # -- vector_db_* ---------------------------------------------------------
+    def insert(self, data, uuid: bytes | str = b"") -> int:
+        r = lib.vector_db_insert(self.ptr, make_vector(data, uuid))
+        if r == NOT_FOUND:
+            raise SvdbError(f"vector_db_insert failed: {last_error()}")
+        return int(r)
+
+    def insert_batch(self, rows, uuids: bytes | None = None) -> int:
+        rows = _f64(rows)
+        first = C.c_size_t(0)
+        _check(lib.svdb_insert_batch(self.ptr, rows.ctypes.data_as(_dp), rows.shape[0], rows.shape[1], uuids,
+                                     C.byref(first)), "svdb_insert_batch")
+        return first.value
+
+    def read(self, index: int):
+        p = lib.vector_db_read(self.ptr, index)
+        if not p:
+            return None
+        v = p.contents
+        return np.ctypeslib.as_array(v.data, shape=(v.dimension,)).copy() if v.dimension else np.zeros(0)
+
+    def uuid(self, index: int) -> bytes | None:
+        p = lib.vector_db_read(self.ptr, index)
+        return bytes(p.contents.uuid).split(b"\0")[0] if p else None
+
+    def read_by_uuid(self, uuid: bytes | str):
+        if isinstance(uuid, str):
+            uuid = uuid.encode()
+        p = lib.vector_db_read_by_uuid(self.ptr, uuid)
+        if not p:
+            return None
+        v = p.contents
+        return np.ctypeslib.as_array(v.data, shape=(v.dimension,)).copy()
+
+    def update(self, index: int, data) -> None:
+        lib.vector_db_update(self.ptr, index, make_vector(data))
+
+    def delete(self, index: int) -> None:
+        lib.vector_db_delete(self.ptr, index)
+
+    def save(self, filename: str) -> None:
+        lib.vector_db_save(self.ptr, filename.encode())
+
+    def sync(self) -> None:
+        _check(lib.svdb_sync(self.ptr), "svdb_sync")
+
+    def reserve(self, rows: int, dim: int) -> None:
+        _check(lib.svdb_reserve(self.ptr, rows, dim), "svdb_reserve")
+
+    def stream(self) -> int:
+        return lib.svdb_stream(self.ptr) or 0
+
+    def wait(self) -> None:
+        _check(lib.svdb_wait(self.ptr), "svdb_wait")
+
+    # -- /nearest (KD tree) --------------------------------------------------
+    def kdtree_nearest(self, q) -> int:
+        """kdtree_nearest(db->kdtree, q) as src/compare_handler.c:403 calls it;
+        -1 for (size_t)-1."""
+        q = _f64(q)
+        r = lib.kdtree_nearest(self.kdtree, q.ctypes.data_as(_dp))
+        return -1 if r == NOT_FOUND else int(r)
+
+    def nearest_batch(self, queries) -> np.ndarray:
+        q = _f64(queries)
+        q = q.reshape(-1, q.shape[-1])
+        out = np.empty(q.shape[0], np.int64)
+        _check(lib.svdb_nearest_batch(self.ptr, q.ctypes.data_as(_dp), q.shape[0], q.shape[1],
+                                      out.ctypes.data_as(_i64p)), "svdb_nearest_batch")
+        return out
+
+    # -- /compare ------------------------------------------------------------
+    def compare_batch(self, metric: int, index1, index2, expected_dim: int = 0):
+        i1 = np.ascontiguousarray(index1, np.int64)
+        i2 = np.ascontiguousarray(index2, np.int64)
+        out = np.empty(i1.size, np.float32)
+        st = np.empty(i1.size, np.int32)
+        _check(lib.svdb_compare_batch(self.ptr, metric, i1.ctypes.data_as(_i64p), i2.ctypes.data_as(_i64p), i1.size,
+                                      expected_dim, out.ctypes.data_as(C.POINTER(C.c_float)),
+                                      st.ctypes.data_as(C.POINTER(C.c_int32))), "svdb_compare_batch")
+        return out, st
+
+    def compare(self, url: str, index1: int, index2: int, expected_dim: int = 0):
+        """GET /compare/<metric>?index1=&index2= -> (status, body dict)."""
+        metric = METRIC_URLS.get(url, -1)
+        out, st = self.compare_batch(metric, [index1], [index2], expected_dim)
+        if st[0] != CMP_OK:
+            code, msg = CMP_ERRORS[int(st[0])]
+            return code, {"error": msg}
+        return 200, {url.rsplit("/", 1)[1]: float(out[0])}
+
+    # -- top-k ---------------------------------------------------------------
+    def search(self, queries, k: int, metric: int = COSINE, precision: int = PREC_FP64, with_err: bool = False,
+               stats: SearchStats | None = None):
+        q = _f64(queries)
+        q = q.reshape(-1, q.shape[-1])
+        nq = q.shape[0]
+        ids = np.empty((nq, k), np.int64)
+        dists = np.empty((nq, k), np.float64)
+        err = np.empty((nq, k), np.float64) if with_err else None
+        _check(lib.svdb_search_topk(self.ptr, q.ctypes.data_as(_dp), nq, q.shape[1], k, metric, precision,
+                                    ids.ctypes.data_as(_i64p), dists.ctypes.data_as(_dp),
+                                    err.ctypes.data_as(_dp) if with_err else None,
+                                    C.byref(stats) if stats is not None else None), "svdb_search_topk")
+        return (ids, dists, err) if with_err else (ids, dists)
+
+    def search_device(self, q_ptr: int, nq: int, dim: int, k: int, metric: int, precision: int, ids_ptr: int,
+                      dists_ptr: int, err_ptr: int = 0, stats: SearchStats | None = None) -> None:
+        """Device-pointer variant (queued on self.stream(); does not wait)."""
+        _check(lib.svdb_search_topk_device(self.ptr, q_ptr, nq, dim, k, metric, precision, ids_ptr, dists_ptr,
+                                           err_ptr or None, C.byref(stats) if stats is not None else None),
+               "svdb_search_topk_device")
+
+
+class KDTree:
+    """Standalone kdtree_* (reference include/kdtree.h:32-57)."""
+
+    def __init__(self, dimension: int):
+        self.ptr = lib.kdtree_create(dimension)
+        self.dimension = dimension
+
+    def insert(self, point, index: int) -> None:
+        p = _f64(point)
+        lib.kdtree_insert(self.ptr, p.ctypes.data_as(_dp), index)
+
+    def nearest(self, q) -> int:
+        q = _f64(q)
+        r = lib.kdtree_nearest(self.ptr, q.ctypes.data_as(_dp))
+        return -1 if r == NOT_FOUND else int(r)
+
+    def close(self):
+        if self.ptr:
+            lib.kdtree_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,143 @@
+"""C-ABI boundary checks that need no GPU: the library loads, exports every
+function include/*.h declares, and the host-side store logic (positional
+indices, ownership, uuid, the save/load file format, /compare request
+validation) behaves as the reference's does."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        src = re.sub(r"#[^\n]*", "", src)
+        for m in re.finditer(r"([A-Za-z_]\w*)\s*\([^;{}]*\)\s*;", src):
+            names.add(m.group(1))
+    return names
+
+
+def test_exports_every_declared_symbol(svdb):
+    names = declared_functions()
+    assert {"vector_db_init", "kdtree_nearest", "cosine_similarity", "svdb_search_topk"} <= names
+    out = subprocess.run(["nm", "-D", "--defined-only", svdb.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    missing = names - exported
+    assert not missing, missing
+    lib = C.CDLL(svdb.LIB_PATH)
+    for n in names:
+        assert getattr(lib, n) is not None
+
+
+def test_struct_layout_matches_reference(svdb):
+    # include/vector_database.h:14-18 on LP64: uuid[37] + pad -> 40, dimension, data
+    assert C.sizeof(svdb.Vector) == 56
+    assert svdb.Vector.dimension.offset == 40 and svdb.Vector.data.offset == 48
+
+
+def test_positional_store_semantics_host(svdb):
+    """insert / read / update / delete / read_by_uuid as
+    src/vector_database.c:81-195 (host side; no GPU call is made)."""
+    db = svdb.VectorDatabase(0, 3)
+    rows = [np.full(8, float(i)) for i in range(6)]
+    for i, r in enumerate(rows):
+        assert db.insert(r, f"uuid-{i}") == i
+    assert db.size == 6
+    db.delete(2)  # shifts later rows left (src/vector_database.c:189-191)
+    assert db.size == 5
+    assert np.array_equal(db.read(2), rows[3])
+    assert db.uuid(2) == b"uuid-3"
+    db.delete(99)  # ignored
+    db.update(99, np.zeros(8))  # ignored
+    assert db.size == 5
+    db.update(0, np.full(8, 42.0))
+    assert np.array_equal(db.read(0), np.full(8, 42.0))
+    assert db.read(5) is None
+    assert np.array_equal(db.read_by_uuid("uuid-4"), rows[4])
+    assert db.read_by_uuid("nope") is None
+    db.close()
+
+
+def test_compare_validation_host(svdb):
+    """Error branches of compare_handler_callback (src/compare_handler.c:86-170)
+    for requests that never reach the arithmetic."""
+    db = svdb.VectorDatabase(0, 3)
+    db.insert(np.ones(4))
+    db.insert(np.ones(5))
+    db.insert(np.ones(4))
+    assert db.compare("/compare/cosine_similarity", 0, 3) == (400, {"error": "Index out of bounds"})
+    assert db.compare("/compare/cosine_similarity", -1, 0) == (400, {"error": "Index out of bounds"})
+    assert db.compare("/compare/dot_product", 0, 1) == (400, {"error": "Vectors have different dimensions"})
+    assert db.compare("/compare/dot_product", 0, 2, expected_dim=5) == (400, {"error": "Vector size mismatch"})
+    assert db.compare("/compare/manhattan", 0, 2) == (400, {"error": "Unknown comparison method"})
+    db.close()
+
+
+def test_save_load_roundtrip_and_format(svdb, tmp_path):
+    """vector_db_save writes the reference's format (src/vector_database.c:
+    212-223): size_t n, then uuid[37], size_t dim, double[dim] per row."""
+    db = svdb.VectorDatabase(0, 3)
+    r = np.random.default_rng(0)
+    X = r.uniform(-1, 1, (7, 5))
+    for i, x in enumerate(X):
+        db.insert(x, f"{i:036d}")
+    f = str(tmp_path / "a.db")
+    db.save(f)
+    raw = open(f, "rb").read()
+    assert len(raw) == 8 + 7 * (37 + 8 + 5 * 8)
+    assert int.from_bytes(raw[:8], "little") == 7
+    assert raw[8:8 + 36] == b"0" * 36
+    assert np.array_equal(np.frombuffer(raw[8 + 45:8 + 45 + 40], np.float64), X[0])
+    db2 = svdb.VectorDatabase.load(f, 3)
+    assert db2.size == 7
+    for i in range(7):
+        assert np.array_equal(db2.read(i), X[i])
+        assert db2.uuid(i) == f"{i:036d}".encode()
+    db.close()
+    db2.close()
+
+
+def test_save_file_identical_to_reference(svdb, refstore, tmp_path):
+    import oracle as O
+    r = np.random.default_rng(5)
+    X = r.uniform(-1, 1, (9, 6))
+    rs = O.RefStore(refstore, 3)
+    db = svdb.VectorDatabase(0, 3)
+    for i, x in enumerate(X):
+        u = f"{i:08d}-0000-0000-0000-000000000000".encode()
+        rs.insert(x, u)
+        db.insert(x, u)
+    rs.delete(3)
+    db.delete(3)
+    fr, fo = str(tmp_path / "r.db"), str(tmp_path / "o.db")
+    refstore.L.vector_db_save.argtypes = [C.c_void_p, C.c_char_p]
+    refstore.L.vector_db_save(rs.db, fr.encode())
+    db.save(fo)
+    assert open(fr, "rb").read() == open(fo, "rb").read()
+    rs.free()
+    db.close()
+
+
+def test_library_fails_loudly_without_gpu(svdb):
+    """No CPU fallback: without a usable GPU every compute call errors."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    db = svdb.VectorDatabase(0, 3)
+    db.insert(np.ones(4))
+    with pytest.raises(svdb.SvdbError):
+        db.search(np.ones(4), 1)
+    assert db.kdtree_nearest(np.ones(4)) == -1
+    assert np.isnan(svdb.cosine_similarity(np.ones(4), np.ones(4)))
+    db.close()
