@@ -1,0 +1,319 @@
+"""Benchmark of the similarity hot path: exact top-10 search over a
+1,000,000 x 768 FP64 store (1,024-centre Gaussian mixture, sigma 0.05, seed
+3), query batches drawn from the same mixture.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision bf16|fp64] [--q Q] [--metric cosine|euclidean|dot]
+
+One step = one batch of Q queries answered end to end by the library's
+top-k search.  `value` is queries/s with queries and results resident in HBM
+(svdb_search_topk_device, timed with CUDA events on the library's stream);
+`e2e` is the same metric through svdb_search_topk with host buffers
+(host->device query upload and device->host result read inside the timed
+region).  The store (6.1 GB FP64 + shadows) is far larger than L2, so every
+step streams it from HBM.
+
+--impl reference times the CPU path on the host cores instead: the FP64
+brute-force top-k restated from the reference's metric formulas
+(oracle/svdb_oracle.c), all host threads, on a bounded query sample.
+
+Under torchrun (N > 1) every rank holds a full replica of the store and
+answers its own query batches (replicas only: no collective); value is the
+queries of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "simple-vector-db_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRICS = {"cosine": 0, "euclidean": 1, "dot": 2}
+N_ROWS, DIM, K_TOP, SEED = 1_000_000, 768, 10, 3
+METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GPU; p50/p99 ms"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        j = json.load(open(p))
+        return j["hbm_gbs"], j["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(X, Q, metric, k, sample, threads):
+    """Oracle FP64 brute force on `sample` queries, all given threads."""
+    import oracle as O
+    O.build(ref=False)
+    o = O.Oracle()
+    q = Q[:sample]
+    t = time.perf_counter()
+    o.topk(metric, X, q, k, threads=threads)
+    dt = time.perf_counter() - t
+    return sample / dt, dt
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from svdb_gb300 import workloads as W
+    mix, X = W.config3(N_ROWS, DIM, SEED)
+    metric = METRICS[args.metric]
+    threads = os.cpu_count() or 1
+    times = []
+    sample = args.cpu_sample
+    Qs = mix.sample(sample * (args.steps + args.warmup), 1)
+    for s in range(args.warmup + args.steps):
+        _, dt = cpu_baseline(X, Qs[s * sample:], metric, K_TOP, sample, threads)
+        if s >= args.warmup:
+            times.append(dt)
+    tot = sum(times)
+    v = sample * args.steps / tot
+    line = {"impl": "reference", "metric": METRIC_NAME, "value": v, "unit": "queries/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "1M x 768 FP64 Gaussian mixture (1024 centres, sigma 0.05, "
+                                                         "seed 3), exact top-10 " + args.metric,
+                                            "query_batch": sample, "l2": "store (6.1 GB) larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} queries per step over the full 1M x 768 store"},
+            "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    metric = METRICS[args.metric]
+    prec = S.PREC_BF16 if args.precision == "bf16" else S.PREC_FP64
+    nq, k = args.q, K_TOP
+
+    t0 = time.perf_counter()
+    mix, X = W.config3(N_ROWS, DIM, SEED)
+    nbatch = 4
+    Qh = [mix.sample(nq, 1 + rank * nbatch + b) for b in range(nbatch)]
+    log(f"[bench] data {time.perf_counter() - t0:.1f}s")
+    t0 = time.perf_counter()
+    db = S.VectorDatabase(N_ROWS, 3)
+    db.reserve(N_ROWS, DIM)
+    db.insert_batch(X)
+    db.sync()
+    log(f"[bench] store load {time.perf_counter() - t0:.1f}s")
+
+    stream = torch.cuda.ExternalStream(db.stream())
+    Qd = [torch.from_numpy(q).cuda() for q in Qh]
+    ids = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+    dists = torch.empty((nq, k), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st = S.SearchStats()
+
+    def step(b):
+        q = Qd[b % nbatch]
+        db.search_device(q.data_ptr(), nq, DIM, k, metric, prec, ids.data_ptr(), dists.data_ptr(), 0, st)
+
+    # correctness guard on a slice of the first batch: ids equal the device FP64 scan
+    ids_ref, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP64)
+    ids_chk, _ = db.search(Qh[0][:8], k, metric, prec)
+    if not np.array_equal(ids_ref, ids_chk):
+        raise SystemExit("bench: top-k ids of the measured precision differ from the FP64 scan")
+
+    for w in range(args.warmup):
+        step(w)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    db.profile(True)
+    db.profile_read(reset=True)
+    clocks = Clocks(local)
+    kernels = 0
+    per_step = []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for s in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(s)
+        kernels += st.kernels
+        b.record(stream)
+        per_step.append((a, b))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    cl = clocks.stop()
+    ncalls, stage_ms = db.profile_read(reset=True)
+    db.profile(False)
+    ms = ev0.elapsed_time(ev1)
+    lat = sorted(a.elapsed_time(b) for a, b in per_step)
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * nq * args.steps / (ms / 1e3)
+
+    # e2e: host buffers through svdb_search_topk (query upload + result read inside)
+    for w in range(min(args.warmup, 2)):
+        db.search(Qh[w % nbatch], k, metric, prec)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t = time.perf_counter()
+    for s in range(args.steps):
+        db.search(Qh[s % nbatch], k, metric, prec)
+    e2e_s = time.perf_counter() - t
+    if dist:
+        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = ws * nq * args.steps / e2e_s
+
+    # plain FP64 GPU path on the same batches (the comparison the metric names)
+    plain = None
+    if prec != S.PREC_FP64 and args.plain_q:
+        pq = min(args.plain_q, nq)
+        db.search_device(Qd[0].data_ptr(), pq, DIM, k, metric, S.PREC_FP64, ids.data_ptr(), dists.data_ptr(), 0)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for s in range(2):
+            db.search_device(Qd[s % nbatch].data_ptr(), pq, DIM, k, metric, S.PREC_FP64, ids.data_ptr(),
+                             dists.data_ptr(), 0)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain = 2 * pq / (a.elapsed_time(b) / 1e3)
+
+    hbm, bf16, src = peaks()
+    scr = stage_ms[S.STAGE_SCREEN] / max(ncalls, 1)  # ms per launch of the dominant stage
+    if prec == S.PREC_BF16:
+        flops = 2.0 * nq * N_ROWS * DIM
+        ach = flops / (scr / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
+                "traffic": None, "peak_source": src, "kernel_ms": scr,
+                "algorithmic": f"2*Q*N*D = {flops:.3e} FLOP per launch"}
+    else:
+        nbytes = N_ROWS * (DIM * 8 + 1)
+        ach = nbytes / (scr / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                "peak_source": src, "kernel_ms": scr,
+                "algorithmic": f"N*(D*8+1) = {nbytes:.3e} bytes per launch (one pass over the FP64 master)"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and args.cpu_sample:
+        v, dt = cpu_baseline(X, Qh[0], metric, k, args.cpu_sample, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": "queries/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{args.cpu_sample} queries over the full 1M x 768 store ({dt:.1f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC_NAME, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16+f64" if prec == S.PREC_BF16 else "f64", "data": "synthetic",
+                "config": {"workload": f"1M x 768 FP64 Gaussian mixture (1024 centres, sigma 0.05, seed 3), "
+                                       f"exact top-{k} {args.metric}, {args.precision}",
+                           "query_batch": nq, "precision": args.precision, "parallelism": f"replicas{ws}",
+                           "l2": "store (6.1 GB FP64) larger than L2; no flush needed"},
+                "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+                "stage_ms_per_step": {n: float(stage_ms[i] / max(ncalls, 1)) for i, n in
+                                      enumerate(["prep", "screen", "select", "rerank"])},
+                "plain_fp64_qps": plain,
+                "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": nq * DIM * 8,
+                        "d2h_bytes_per_step": nq * k * 24},
+                "gpu_launches": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": cl}
+        print(json.dumps(line), flush=True)
+    db.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp64"])
+    ap.add_argument("--q", type=int, default=None, help="queries per step")
+    ap.add_argument("--metric", default="cosine", choices=list(METRICS))
+    ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--plain-q", type=int, default=64)
+    args = ap.parse_args()
+    if args.q is None:
+        args.q = 4096 if args.precision == "bf16" else 64
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -113,6 +113,18 @@ int svdb_reserve(VectorDatabase* db, size_t rows, size_t dim);
  * implicitly. */
 int svdb_sync(VectorDatabase* db);
 
+/* Stage timing.  With profiling on, every search records CUDA events on the
+ * database's stream around its stages; svdb_profile_read adds up the device
+ * time of each stage over the searches since the last reset (ms[i] for stage
+ * i) and returns how many searches that covers, or a negative code. */
+#define SVDB_STAGE_PREP 0   /* query upload + padding + norms */
+#define SVDB_STAGE_SCREEN 1 /* FP64 streaming scan, or the BF16 tensor-core GEMM screen */
+#define SVDB_STAGE_SELECT 2 /* top-k merge, or shortlist selection */
+#define SVDB_STAGE_RERANK 3 /* FP64 re-rank of the shortlist (BF16 precision only) */
+#define SVDB_NSTAGES 4
+int svdb_profile(VectorDatabase* db, int enable);
+int svdb_profile_read(VectorDatabase* db, double* ms, int reset);
+
 /* The CUDA stream (cudaStream_t) the database's kernels run on. */
 void* svdb_stream(VectorDatabase* db);
 

@@ -308,6 +308,7 @@ int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         default: svdb_set_error("search_fp64: no kernel for ks=%d qb=%d", p.ks, p.qb);
     }
     if (rc) return rc;
+    s->prof_mark(2);
     const unsigned blocks = (unsigned)((a.nq * 32 + 255) / 256);
     switch (p.ks) {
         case 1:
@@ -323,6 +324,7 @@ int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                           s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err);
     }
     SVDB_LAUNCH_CHECK();
+    s->prof_mark(3);
     if (kernels) *kernels += 2;
     return SVDB_OK;
 }
@@ -368,6 +370,7 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     unsigned char* outp = base + qbytes + sqbytes;
     unsigned char* kscr = outp + obytes;
     const double* qsrc = q;
+    s->prof_begin();
     if (!on_device) {
         double* qraw = (double*)(kscr + kbytes);
         rc = s->pinned_reserve(std::max(nq * s->dim * sizeof(double), out_n * (sizeof(int64_t) + 2 * sizeof(double))));
@@ -395,6 +398,7 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     rc = prep_queries_fp64(s, qsrc, s->dim, nq, qbuf, qsq);
     if (rc) return rc;
     ++kernels;
+    s->prof_mark(1);
     if (s->nlive == 0) {
         k_fill_empty<<<(unsigned)((out_n + 255) / 256), 256, 0, s->stream>>>(a.ids, a.dists, a.err, out_n);
         SVDB_LAUNCH_CHECK();
@@ -404,6 +408,8 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     } else {
         rc = search_bf16(s, a, kscr, kbytes, st);
     }
+    s->prof_mark(4);
+    s->prof_end();
     if (rc) return rc;
     if (st) st->kernels += kernels;
     if (!on_device) {

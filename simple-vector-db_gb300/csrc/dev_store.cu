@@ -11,6 +11,7 @@
 //   logical C        int64    slot -> positional index (rank among live slots)
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -178,6 +179,66 @@ __global__ void k_compare_slots(const double* __restrict__ x64, size_t ld, int d
 __global__ void k_compare_vec(const double* __restrict__ a, const double* __restrict__ b, int d, int metric,
                               float* __restrict__ out) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *out = ref_metric(metric, a, b, d);
+}
+
+// ---------------------------------------------------------------------------
+// stage timing
+// ---------------------------------------------------------------------------
+int Store::prof_enable(bool on) {
+    int rc = ensure();
+    if (rc) return rc;
+    if (on && !prof_events) {
+        for (int i = 0; i < kProfRing; ++i)
+            for (int j = 0; j < kProfMarks; ++j) SVDB_CUDA(cudaEventCreate(&pev[i][j]));
+        prof_events = true;
+    }
+    prof = on;
+    return SVDB_OK;
+}
+
+void Store::prof_begin() {
+    prof_cur = -1;
+    if (!prof) return;
+    if (prof_pending == kProfRing && prof_resolve_one() != SVDB_OK) return;
+    prof_cur = (prof_head + prof_pending) % kProfRing;
+    ++prof_pending;
+    prof_mark(0);
+}
+
+// records `boundary` and every later one, so a stage a search skips reads 0
+void Store::prof_mark(int boundary) {
+    if (prof_cur < 0) return;
+    for (int j = boundary; j < kProfMarks; ++j) cudaEventRecord(pev[prof_cur][j], stream);
+}
+
+int Store::prof_resolve_one() {
+    if (!prof_pending) return SVDB_OK;
+    cudaEvent_t* e = pev[prof_head];
+    SVDB_CUDA(cudaEventSynchronize(e[kProfMarks - 1]));
+    for (int j = 0; j < SVDB_NSTAGES; ++j) {
+        float ms = 0.0f;
+        SVDB_CUDA(cudaEventElapsedTime(&ms, e[j], e[j + 1]));
+        prof_ms[j] += ms;
+    }
+    ++prof_calls;
+    prof_head = (prof_head + 1) % kProfRing;
+    --prof_pending;
+    return SVDB_OK;
+}
+
+int Store::prof_read(double* ms, bool reset) {
+    while (prof_pending) {
+        int rc = prof_resolve_one();
+        if (rc) return rc;
+    }
+    if (ms)
+        for (int j = 0; j < SVDB_NSTAGES; ++j) ms[j] = prof_ms[j];
+    const int64_t n = prof_calls;
+    if (reset) {
+        for (int j = 0; j < SVDB_NSTAGES; ++j) prof_ms[j] = 0.0;
+        prof_calls = 0;
+    }
+    return (int)std::min<int64_t>(n, 0x7fffffff);
 }
 
 // ---------------------------------------------------------------------------
@@ -395,6 +456,9 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->scratch);
     cudaFree(s->d_nlive);
     cudaFreeHost(s->pin);
+    if (s->prof_events)
+        for (int i = 0; i < Store::kProfRing; ++i)
+            for (int j = 0; j < Store::kProfMarks; ++j) cudaEventDestroy(s->pev[i][j]);
     s->release_extra();
     cudaStreamDestroy(s->stream);
     delete s;
@@ -519,6 +583,12 @@ int svdbd_store_kill(svdbd_store* hs, int64_t slot) {
 }
 
 int svdbd_store_sync(svdbd_store* hs) { return reinterpret_cast<Store*>(hs)->sync(); }
+
+int svdbd_store_profile(svdbd_store* hs, int enable) { return reinterpret_cast<Store*>(hs)->prof_enable(enable != 0); }
+
+int svdbd_store_profile_read(svdbd_store* hs, double* ms, int reset) {
+    return reinterpret_cast<Store*>(hs)->prof_read(ms, reset != 0);
+}
 
 int svdbd_store_wait(svdbd_store* hs) {
     Store* s = reinterpret_cast<Store*>(hs);

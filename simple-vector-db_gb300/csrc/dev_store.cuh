@@ -8,6 +8,8 @@
 
 #include <vector>
 
+#include "svdb_device.h"
+
 namespace svdb {
 
 struct GemmPlanCache;  // dev_gemm.cu
@@ -45,6 +47,23 @@ struct Store {
     size_t pin_bytes = 0;
 
     GemmPlanCache* gemm = nullptr;
+
+    // stage timing (svdb_profile): a ring of per-search event sets, resolved
+    // lazily so profiling adds no host synchronisation to a search
+    static constexpr int kProfRing = 64;
+    static constexpr int kProfMarks = SVDB_NSTAGES + 1;
+    bool prof = false;
+    bool prof_events = false;
+    cudaEvent_t pev[kProfRing][kProfMarks];
+    int prof_head = 0, prof_pending = 0, prof_cur = -1;
+    double prof_ms[SVDB_NSTAGES] = {};
+    int64_t prof_calls = 0;
+    int prof_enable(bool on);
+    void prof_begin();
+    void prof_mark(int boundary);
+    void prof_end() { prof_cur = -1; }
+    int prof_resolve_one();
+    int prof_read(double* ms, bool reset);
 
     int ensure();
     int grow(size_t need);

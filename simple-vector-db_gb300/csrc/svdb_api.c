@@ -264,3 +264,22 @@ SVDB_API int svdb_wait(VectorDatabase* db) {
     svdb_db* d = svdb_of(db);
     return d->dev ? svdbd_store_wait(d->dev) : SVDB_OK;
 }
+
+SVDB_API int svdb_profile(VectorDatabase* db, int enable) {
+    if (!db) return SVDB_EINVAL;
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = d->dev ? svdbd_store_profile(d->dev, enable) : SVDB_EINVAL;
+    if (!d->dev) svdb_set_error("svdb_profile: the store holds no rows");
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+SVDB_API int svdb_profile_read(VectorDatabase* db, double* ms, int reset) {
+    if (!db) return SVDB_EINVAL;
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = d->dev ? svdbd_store_profile_read(d->dev, ms, reset) : 0;
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}

@@ -55,6 +55,9 @@ int svdbd_store_kill(svdbd_store* s, int64_t slot);
 /* flush staged mutations, rebuild derived arrays and the slot->logical map */
 int svdbd_store_sync(svdbd_store* s);
 int svdbd_store_wait(svdbd_store* s);
+/* stage timing (svdb_profile / svdb_profile_read) */
+int svdbd_store_profile(svdbd_store* s, int enable);
+int svdbd_store_profile_read(svdbd_store* s, double* ms, int reset);
 
 /* reference-exact /compare for n slot pairs (host arrays in/out) */
 int svdbd_compare_slots(svdbd_store* s, int metric, const int64_t* slot1, const int64_t* slot2, size_t n,

@@ -33,6 +33,8 @@ CMP_ERRORS = {
     CMP_UNKNOWN_METHOD: (400, "Unknown comparison method"),
 }
 NOT_FOUND = 2**64 - 1  # (size_t)-1
+STAGE_PREP, STAGE_SCREEN, STAGE_SELECT, STAGE_RERANK = range(4)
+NSTAGES = 4
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)
@@ -87,6 +89,8 @@ def _load():
         "svdb_stream": (vp, [vp]),
         "svdb_wait": (C.c_int, [vp]),
         "svdb_last_error": (C.c_char_p, []),
+        "svdb_profile": (C.c_int, [vp, C.c_int]),
+        "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -231,6 +235,17 @@ class VectorDatabase:
 
     def reserve(self, rows: int, dim: int) -> None:
         _check(lib.svdb_reserve(self.ptr, rows, dim), "svdb_reserve")
+
+    def profile(self, enable: bool = True) -> None:
+        _check(lib.svdb_profile(self.ptr, int(enable)), "svdb_profile")
+
+    def profile_read(self, reset: bool = True):
+        """(searches covered, device ms per stage: prep, screen, select, rerank)."""
+        ms = np.zeros(NSTAGES, np.float64)
+        n = lib.svdb_profile_read(self.ptr, ms.ctypes.data_as(_dp), int(reset))
+        if n < 0:
+            raise SvdbError(f"svdb_profile_read failed ({n}): {last_error()}")
+        return n, ms
 
     def stream(self) -> int:
         return lib.svdb_stream(self.ptr) or 0
