@@ -295,6 +295,7 @@ def run_ours(args, ws, rank, local):
 
 
 def main():
+    global N_ROWS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -305,7 +306,9 @@ def main():
     ap.add_argument("--metric", default="cosine", choices=list(METRICS))
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
+    ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
     args = ap.parse_args()
+    N_ROWS = args.rows
     if args.q is None:
         args.q = 4096 if args.precision == "bf16" else 64
     ws, rank, local = dist_env()
