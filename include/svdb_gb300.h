@@ -52,9 +52,12 @@ extern "C" {
 
 typedef struct svdb_search_stats {
     uint64_t candidates;   /* rows re-ranked in FP64 over the whole batch */
-    uint32_t widened;      /* queries whose shortlist overflowed and were answered by an exact scan */
+    uint32_t widened;      /* queries the screen could not certify, answered by the exact FP64 scan */
     uint32_t kernels;      /* kernel launches issued by the call */
     double max_err_bound;  /* max over results of the bound on |reported - exact real value| */
+    uint32_t bound_failures; /* queries whose screen bound did not hold against the exact value
+                                (re-answered by the exact scan; nonzero means the bound model is wrong) */
+    uint32_t reserved;
 } svdb_search_stats;
 
 /*

@@ -1,20 +1,1031 @@
-// dev_gemm.cu -- BF16 tensor-core screen + certified FP64 re-rank.
+// dev_gemm.cu -- BF16 tensor-core screen + certified FP64 re-rank (exact top-k).
+//
+// Stage 1, k_screen_bf16 (the dominant kernel): S = bf16(Q) . bf16(X)^T with
+// FP32 accumulation on the 5th-generation tensor cores.  One CTA owns one
+// tile of 128 queries (the MMA's M, one TMEM lane per query) and sweeps a
+// contiguous range of 256-row store tiles (the MMA's N):
+//   warp 0      TMA producer: 128B-swizzled K-major tiles of the BF16 query
+//               block and BF16 store shadow, 4-stage mbarrier ring;
+//   warp 1      TMEM allocator + MMA issuer: tcgen05.mma kind::f16, M=128,
+//               N=256, K=16, into two 256-column FP32 accumulators in TMEM
+//               (double buffered, so the epilogue of one row tile overlaps
+//               the MMAs of the next);
+//   warps 2-5   epilogue: tcgen05.ld of the accumulator (thread = query),
+//               screen key + certified error bound per (query, row), fused
+//               per-query running top-k of lower bounds, and emission of
+//               every row whose upper bound reaches the running threshold.
+// The distance matrix never reaches HBM: only candidates are written.
+// CTAs are grouped so that all query tiles of a group read the same store
+// tile at the same time (one HBM read, the rest L2 hits).
+//
+// Certification.  For query q and row x with BF16 copies bq, bx:
+//   |q.x - fl32(bq.bx)| <= |q|.|x - bx| + |q - bq|.|bx| + c_acc.|bq|.|bx|
+// (Cauchy-Schwarz on the quantisation residuals; c_acc bounds the FP32
+// accumulation of K products).  The screen key is the metric's ranking
+// quantity (cosine: q.x/|x|; dot: q.x; Euclidean: q.x - |x|^2/2, larger is
+// better) and E its bound, both in FP32 with directed rounding.  Any row
+// whose upper bound key+E is below the k-th largest lower bound key-E over
+// the store is strictly worse than k rows, so the candidates that survive
+// that test contain the exact FP64 top-k.  E also carries a margin for the
+// FP64 rounding of the reported values, so "strictly worse" holds for the
+// reported numbers and ties among survivors are resolved by the re-rank.
+//
+// Stage 2, k_select: per query, exact k-th largest lower bound over the
+// candidates (radix select), survivors = upper bound >= it.
+// Stage 3, k_rerank: survivors scored in FP64 against the master copy in the
+// canonical summation order (bit-identical to the FP64 scan), exact top-k by
+// (value, lowest index); the screen bound is re-checked against the exact
+// value for every survivor.
+// Queries the screen cannot certify (candidate overflow, non-finite or zero
+// query, fewer than k finite results, a bound check that failed) are
+// answered by the exact FP64 scan instead ("widened").
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "dev_search.cuh"
 
 namespace svdb {
 
-struct GemmPlanCache {};
+namespace scr {
+constexpr int kBM = 128;  // queries per tile (TMEM lanes)
+constexpr int kBN = 256;  // store rows per tile (accumulator columns)
+constexpr int kBK = 64;   // K per stage: one 128-byte swizzle row of BF16
+constexpr int kStages = 4;
+constexpr int kEpiWarps = 4;
+constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr uint32_t kTmemCols = 2 * kBN;
+constexpr uint32_t kStageA = kBM * kBK * 2;  // 16 KB
+constexpr uint32_t kStageB = kBN * kBK * 2;  // 32 KB
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitimate wait
+constexpr int kCap = 8192;                        // candidates kept per query
+constexpr float kC1 = 9.5367431640625e-07f;       // 2^-20: FP32 rounding of key / mult / m
+// flags
+constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4;
+
+struct Smem {
+    // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
+    uint8_t a[kStages][kStageA];
+    uint8_t b[kStages][kStageB];
+    float4 rp[2][kBN];
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t accfull[2];
+    uint64_t accempty[2];
+    uint64_t done;
+    uint32_t tmem_base;
+    int abort;
+};
+}  // namespace scr
+
+// ---------------------------------------------------------------------------
+// PTX wrappers (sm_100a family: tcgen05, TMA, mbarrier)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false when the limit ran out or another role raised `abort`.
+__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 31) == 0) {
+            if (*abort) return false;
+            if (gtimer() - t0 > limit_ns) {
+                *abort = 1;
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] . B[smem]^T, both K-major BF16, FP32 accumulate
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// arrive on `bar` once every tcgen05 op issued so far by this thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 32 lanes x 32 consecutive FP32 columns: thread t gets columns of its lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, rows 128 B apart,
+// 8-row swizzle atoms 1024 B apart (SBO); LBO unused for this layout.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4)                     // D format: F32
+           | (1u << 7)                   // A format: BF16
+           | (1u << 10)                  // B format: BF16
+           | ((uint32_t)(n >> 3) << 17)  // N / 8
+           | ((uint32_t)(m >> 4) << 24); // M / 16
+}
+
+// ---------------------------------------------------------------------------
+// shared arithmetic of the certified screen
+// ---------------------------------------------------------------------------
+// ordered-int image of a float: a < b  <=>  f2ord(a) < f2ord(b) (as signed int)
+__device__ __forceinline__ int f2ord(float f) {
+    const int b = __float_as_int(f);
+    return b >= 0 ? b : b ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord2f(int o) { return __int_as_float(o >= 0 ? o : o ^ 0x7fffffff); }
+
+// error bound of a screen key (FP32, rounded up).  p = row {mult, a, b, m},
+// qp = query {qn, eqq, eq0, valid}.
+__device__ __forceinline__ float screen_bound(float key, float4 p, float qn, float eqq, float eq0) {
+    float e = __fmaf_ru(qn, p.y, __fmaf_ru(eqq, p.z, eq0));
+    return __fmaf_ru(__fadd_ru(fabsf(key), p.w), scr::kC1, e);
+}
+
+// running k best lower bounds of one query (k <= KL); `mn` is the k-th best
+template <int KL>
+struct TopL {
+    float v[KL];
+    float mn;
+    int am;
+    __device__ __forceinline__ void init(int k) {
+#pragma unroll
+        for (int i = 0; i < KL; ++i) v[i] = i < k ? -INFINITY : INFINITY;
+        mn = -INFINITY;
+        am = 0;
+    }
+    __device__ __forceinline__ void push(float L) {
+#pragma unroll
+        for (int i = 0; i < KL; ++i)
+            if (i == am) v[i] = L;
+        mn = v[0];
+        am = 0;
+#pragma unroll
+        for (int i = 1; i < KL; ++i)
+            if (v[i] < mn) {
+                mn = v[i];
+                am = i;
+            }
+    }
+};
+
+struct ScreenParams {
+    const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
+    const float4* qpar;  // per query {qn, eqq, eq0, valid}
+    int* tau;            // per query: shared lower bound of the k-th best key (ordered int)
+    int* cnt;            // per query candidate count (may exceed cap: overflow)
+    int2* cand;          // per query: cap x {row slot, key bits}
+    int* err;            // set to 1 when a wait timed out
+    int nq, k, cap;
+    int ntq;      // query tiles
+    int ntr;      // row tiles
+    int rgroups;  // row groups per query tile
+    int kblocks;  // ldb / 64
+};
+
+template <int KL>
+__global__ void __launch_bounds__(scr::kThreads, 1)
+    k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
+                  const ScreenParams P) {
+    using namespace scr;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int qt = blockIdx.x % P.ntq;
+    const int grp = blockIdx.x / P.ntq;
+    const int r0 = (int)((int64_t)grp * P.ntr / P.rgroups);
+    const int r1 = (int)((int64_t)(grp + 1) * P.ntr / P.rgroups);
+    const int KB = P.kblocks;
+    volatile int* abort = &S.abort;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            mbar_init(&S.full[i], 1);
+            mbar_init(&S.empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&S.accfull[i], 1);
+            mbar_init(&S.accempty[i], kEpiWarps);
+        }
+        mbar_init(&S.done, 1);
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0 && lane == 0) {
+        tma_prefetch_desc(&tmq);
+        tma_prefetch_desc(&tmx);
+    }
+    if (warp == 1) tmem_alloc(&S.tmem_base, kTmemCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t issued = 0;  // loads issued (for draining on abort)
+            bool ok = true;
+            for (int r = r0; r < r1 && ok; ++r) {
+                for (int kb = 0; kb < KB; ++kb) {
+                    if (!mbar_wait(&S.empty[stage], phase ^ 1, abort, kWaitLimitNs)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(&S.full[stage], kStageA + kStageB);
+                    tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * kBK, qt * kBM);
+                    tma_load_2d(S.b[stage], &tmx, &S.full[stage], kb * kBK, r * kBN);
+                    ++issued;
+                    if (++stage == kStages) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+            }
+            // every issued load must have landed before the CTA may exit:
+            // wait (bounded) for the completion of the last kStages loads
+            const uint32_t last = issued < (uint32_t)kStages ? issued : (uint32_t)kStages;
+            for (uint32_t i = 0; i < last; ++i) {
+                const uint32_t n = issued - 1 - i;  // load number n went to stage n % S, phase (n / S) & 1
+                volatile int no_abort = 0;
+                mbar_wait(&S.full[n % kStages], (n / kStages) & 1u, &no_abort, kWaitLimitNs / 4);
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(kBM, kBN);
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            int j = 0;
+            for (int r = r0; r < r1 && ok; ++r, ++j) {
+                const int b = j & 1;
+                const uint32_t use = (uint32_t)j >> 1;
+                if (!mbar_wait(&S.accempty[b], (use & 1u) ^ 1u, abort, kWaitLimitNs)) break;
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(b * kBN);
+                for (int kb = 0; kb < KB; ++kb) {
+                    if (!mbar_wait(&S.full[stage], phase, abort, kWaitLimitNs)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint64_t ad = sdesc_sw128(smem_u32(S.a[stage]));
+                    const uint64_t bd = sdesc_sw128(smem_u32(S.b[stage]));
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle row
+                        mma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
+                    mma_commit(&S.empty[stage]);
+                    if (++stage == kStages) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+                if (ok) mma_commit(&S.accfull[b]);
+            }
+            // all MMAs issued by this thread complete before TMEM is released
+            mma_commit(&S.done);
+            volatile int no_abort = 0;
+            mbar_wait(&S.done, 0, &no_abort, kWaitLimitNs / 4);
+        }
+    } else {
+        // ------------------------------------------------------------ epilogue
+        const int quad = warp & 3;  // TMEM lane quadrant this warp may access
+        const int qi = quad * 32 + lane;
+        const int q = qt * kBM + qi;
+        const int etid = threadIdx.x - 64;  // 0..127
+        float qn = 0.f, eqq = 0.f, eq0 = 0.f;
+        bool valid = false;
+        if (q < P.nq) {
+            const float4 qp = P.qpar[q];
+            qn = qp.x;
+            eqq = qp.y;
+            eq0 = qp.z;
+            valid = qp.w != 0.f;
+        }
+        TopL<KL> top;
+        top.init(P.k);
+        float tau_c = -INFINITY, published = -INFINITY;
+        int2* cq = P.cand + (size_t)(q < P.nq ? q : 0) * P.cap;
+        int j = 0;
+        for (int r = r0; r < r1; ++r, ++j) {
+            const int b = j & 1;
+            const uint32_t use = (uint32_t)j >> 1;
+            float4* rps = S.rp[b];
+            rps[etid] = P.rpar[(size_t)r * kBN + etid];
+            rps[etid + 128] = P.rpar[(size_t)r * kBN + 128 + etid];
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (valid) tau_c = fmaxf(tau_c, ord2f(*(volatile int*)&P.tau[q]));
+            float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
+            if (!mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs)) break;
+            tc_fence_after();
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN);
+#pragma unroll 1
+            for (int c = 0; c < kBN / 32; ++c) {
+                uint32_t v[32];
+                tmem_ld32(tbase + (uint32_t)(c * 32), v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float4 p = rps[c * 32 + i];
+                    const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.w);
+                    const float e = screen_bound(key, p, qn, eqq, eq0);
+                    const float U = __fadd_ru(key, e);
+                    const float L = __fsub_rd(key, e);
+                    if (U >= thr && q < P.nq) {
+                        const int s = atomicAdd(&P.cnt[q], 1);
+                        if (s < P.cap) cq[s] = make_int2(r * kBN + c * 32 + i, __float_as_int(key));
+                    }
+                    if (L > top.mn && valid) {
+                        top.push(L);
+                        thr = fmaxf(top.mn, tau_c);
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.accempty[b]);
+            if (valid && top.mn > published) {
+                atomicMax(&P.tau[q], f2ord(top.mn));
+                published = top.mn;
+            }
+        }
+    }
+
+    __syncthreads();
+    if (threadIdx.x == 0 && S.abort) atomicExch(P.err, 1);
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, kTmemCols);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-search preparation
+// ---------------------------------------------------------------------------
+// BF16 copies of the (already padded FP64) queries + per-query bound terms.
+// 4 lanes per query, canonical FP64 reductions.
+__global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
+                            size_t ldb, int metric, __nv_bfloat16* __restrict__ qb, float4* __restrict__ qpar) {
+    const int lane = threadIdx.x & 31, s = lane & 3;
+    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
+    const bool active = qi < nq;
+    double res = 0.0, bsq = 0.0;
+    bool finite = true;
+    if (active) {
+        const double* src = qbuf + (size_t)qi * ld;
+        __nv_bfloat16* dst = qb + (size_t)qi * ldb;
+        for (size_t j = 2 * s; j < ld; j += 8) {
+            const double a = src[j], c = src[j + 1];
+            const __nv_bfloat16 ha = __double2bfloat16(a), hc = __double2bfloat16(c);
+            const double fa = (double)__bfloat162float(ha), fc = (double)__bfloat162float(hc);
+            finite = finite && isfinite(fa) && isfinite(fc);
+            bsq = fma(fa, fa, bsq);
+            bsq = fma(fc, fc, bsq);
+            res = fma(a - fa, a - fa, res);
+            res = fma(c - fc, c - fc, res);
+            dst[j] = ha;
+            dst[j + 1] = hc;
+        }
+        for (size_t j = ld + 2 * s; j < ldb; j += 8) {
+            dst[j] = __float2bfloat16(0.0f);
+            dst[j + 1] = __float2bfloat16(0.0f);
+        }
+    }
+    res = group4_sum(res);
+    bsq = group4_sum(bsq);
+    const unsigned all_finite = __all_sync(0xffffffffu, finite);  // conservative: any lane of the warp
+    if (active && s == 0) {
+        const double sq = qsq[qi];
+        const double up = 1.0 + 9.313225746154785e-10;  // 1 + 2^-30: FP64 rounding of the sums
+        const double qn = sqrt(sq) * up;
+        const double eq = sqrt(res) * up;
+        const double bqn = sqrt(bsq) * up;
+        // FP32 accumulation of K = ldb products in K/16 tensor-core steps
+        const double cacc = (double)(ldb / 16 + 1) * 20.0 * 1.1920928955078125e-07;
+        const double eqq = (eq + cacc * bqn) * (1.0 + 9.5367431640625e-07) + 3.637978807091713e-12 * qn;  // 2^-38
+        // FP64 rounding of the reported value (2^-40 of its scale) + an absolute floor for FP32 underflow
+        const double eq0 = 9.094947017729282e-13 * (metric == SVDB_EUCLIDEAN ? sq : qn) + 1e-30;
+        // |q| < 1e15 keeps every BF16 product and FP32 sum far from overflow (rows are held to the same)
+        const bool ok = all_finite && isfinite(sq) && sq < 1e30 && (metric != SVDB_COSINE || sq > 0.0);
+        float4 p;
+        p.x = __double2float_ru(qn);
+        p.y = __double2float_ru(eqq);
+        p.z = __double2float_ru(eq0);
+        p.w = ok && isfinite(p.x) && isfinite(p.y) ? 1.0f : 0.0f;
+        qpar[qi] = p;
+    }
+}
+
+// Per-row screen parameters for one metric; rows >= nslots (tile padding),
+// dead slots and placeholder rows get NaN (never candidates).
+__global__ void k_row_params(const float4* __restrict__ rowp, const double* __restrict__ sq64,
+                             const uint8_t* __restrict__ live, int64_t nslots, int64_t npad, int metric,
+                             float4* __restrict__ rpar) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    const float nan = __int_as_float(0x7fc00000);
+    float4 out = make_float4(nan, nan, nan, nan);
+    if (i < nslots && live[i] == 1) {
+        const float4 rp = rowp[i];  // {|x| up, |bx| up, |x - bx| up, |x|^2/2}
+        const double sq = sq64[i];
+        if (metric == SVDB_COSINE) {
+            if (sq > 0.0) {
+                const double ixn = 1.0 / sqrt(sq);
+                const double up = 1.0 + 9.313225746154785e-10;
+                out = make_float4(__double2float_rn(ixn), __double2float_ru((double)rp.z * ixn * up),
+                                  __double2float_ru((double)rp.y * ixn * up), 0.0f);
+            }
+        } else if (metric == SVDB_DOT) {
+            out = make_float4(1.0f, rp.z, rp.y, 0.0f);
+        } else {
+            out = make_float4(1.0f, rp.z, rp.y, __double2float_rn(0.5 * sq));
+        }
+    }
+    rpar[i] = out;
+}
+
+__global__ void k_init_search(int* tau, int* cnt, uint8_t* flags, int nq, int* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nq) {
+        tau[i] = f2ord(-INFINITY);
+        cnt[i] = 0;
+        flags[i] = scr::kOk;
+    }
+    if (i == 0) *err = 0;
+}
+
+// ---------------------------------------------------------------------------
+// stage 2: k-th largest lower bound over the candidates, survivors in place
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_select(int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
+                                                const float4* __restrict__ rpar, const float4* __restrict__ qpar,
+                                                int k, int* __restrict__ surv, uint8_t* __restrict__ flags) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    int2* cs = reinterpret_cast<int2*>(sm);
+    uint32_t* lo = reinterpret_cast<uint32_t*>(cs + cap);  // ordered lower bounds
+    __shared__ int hist[256];
+    __shared__ uint32_t s_prefix, s_mask;
+    __shared__ int s_rank, s_out;
+    const int q = blockIdx.x;
+    const float4 qp = qpar[q];
+    const int n = cnt[q];
+    if (qp.w == 0.f || n > cap) {
+        if (threadIdx.x == 0) {
+            flags[q] = qp.w == 0.f ? scr::kInvalidQuery : scr::kOverflow;
+            surv[q] = 0;
+        }
+        return;
+    }
+    int2* cq = cand + (size_t)q * cap;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int2 c = cq[i];
+        cs[i] = c;
+        const float key = __int_as_float(c.y);
+        const float L = __fsub_rd(key, screen_bound(key, rpar[c.x], qp.x, qp.y, qp.z));
+        const uint32_t b = __float_as_uint(L);
+        lo[i] = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    }
+    if (threadIdx.x == 0) {
+        s_prefix = 0;
+        s_mask = 0;
+        s_rank = k;
+        s_out = 0;
+    }
+    __syncthreads();
+    uint32_t thr_ord = 0;  // every candidate survives when fewer than k exist
+    if (n >= k) {
+        for (int shift = 24; shift >= 0; shift -= 8) {
+            hist[threadIdx.x] = 0;
+            __syncthreads();
+            const uint32_t pre = s_prefix, msk = s_mask;
+            for (int i = threadIdx.x; i < n; i += blockDim.x)
+                if ((lo[i] & msk) == pre) atomicAdd(&hist[(lo[i] >> shift) & 255u], 1);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int cum = 0, need = s_rank, dsel = 0;
+                for (int dgt = 255; dgt >= 0; --dgt) {
+                    if (cum + hist[dgt] >= need) {
+                        dsel = dgt;
+                        break;
+                    }
+                    cum += hist[dgt];
+                }
+                s_rank = need - cum;
+                s_prefix = pre | ((uint32_t)dsel << shift);
+                s_mask = msk | (255u << shift);
+            }
+            __syncthreads();
+        }
+        thr_ord = s_prefix;  // ordered image of the k-th largest lower bound
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int2 c = cs[i];
+        const float key = __int_as_float(c.y);
+        const float U = __fadd_ru(key, screen_bound(key, rpar[c.x], qp.x, qp.y, qp.z));
+        const uint32_t b = __float_as_uint(U);
+        const uint32_t uo = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+        if (uo >= thr_ord) cq[atomicAdd(&s_out, 1)] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) surv[q] = s_out;
+}
+
+// ---------------------------------------------------------------------------
+// stage 3: FP64 re-rank of the survivors in the canonical order
+// ---------------------------------------------------------------------------
+template <int KS, bool EUC>
+__global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, size_t ld,
+                                                const double* __restrict__ qbuf, const double* __restrict__ qsq,
+                                                const double* __restrict__ sq64, const int2* __restrict__ cand,
+                                                const int* __restrict__ surv, int cap, int k, int metric, int d,
+                                                const float4* __restrict__ rpar, const float4* __restrict__ qpar,
+                                                const int64_t* __restrict__ logical, int64_t* __restrict__ ids,
+                                                double* __restrict__ dists, double* __restrict__ err,
+                                                uint8_t* __restrict__ flags) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    double* qs = reinterpret_cast<double*>(sm);
+    const int q = blockIdx.x;
+    if (flags[q] != scr::kOk) return;  // answered by the exact scan
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
+    for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = qbuf[(size_t)q * ld + i];
+    __syncthreads();
+    const int n = surv[q];
+    const int2* cq = cand + (size_t)q * cap;
+    const double qq = qsq[q];
+    const double qn = sqrt(qq);
+    const float4 qp = qpar[q];
+    bool bound_ok = true;
+    WarpList<KS> Lw;
+    Lw.init();
+    for (int base = warp * 8; base < n; base += 64) {
+        const int i = base + g;
+        const bool act = i < n;
+        const int2 c = act ? cq[i] : make_int2(0, 0);
+        const int row = c.x;
+        double p = 0.0;
+        if (act) {
+            const double* x = x64 + (size_t)row * ld;
+            for (size_t j = 2 * s; j < ld; j += 8) {
+                const double2 v = *reinterpret_cast<const double2*>(x + j);
+                const double2 qv = *reinterpret_cast<const double2*>(qs + j);
+                if (EUC) {
+                    const double t0 = qv.x - v.x, t1 = qv.y - v.y;
+                    p = fma(t0, t0, p);
+                    p = fma(t1, t1, p);
+                } else {
+                    p = fma(qv.x, v.x, p);
+                    p = fma(qv.y, v.y, p);
+                }
+            }
+        }
+        p = group4_sum(p);
+        double val = 0.0, kex = 0.0;
+        if (act) {
+            const double xs = sq64[row];
+            if (EUC) {
+                val = sqrt(p);
+                kex = 0.5 * (qq - p);
+            } else if (metric == SVDB_COSINE) {
+                val = p / (qn * sqrt(xs));
+                kex = p / sqrt(xs);
+            } else {
+                val = p;
+                kex = p;
+            }
+            // the screen's bound must hold against the exact value
+            const float key = __int_as_float(c.y);
+            const float e = screen_bound(key, rpar[row], qp.x, qp.y, qp.z);
+            if (s == 0 && !(fabs(kex - (double)key) <= (double)e)) bound_ok = false;
+        }
+        const double kk = rank_key(metric, val);
+        double wk;
+        int wi;
+        Lw.worst(k, wk, wi);
+        const bool cand_ok = act && s == 0 && key_less(kk, row, wk, wi);
+        unsigned m = __ballot_sync(0xffffffffu, cand_ok);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            Lw.insert(__shfl_sync(0xffffffffu, kk, src), __shfl_sync(0xffffffffu, row, src),
+                      __shfl_sync(0xffffffffu, val, src), k);
+        }
+    }
+    if (!__all_sync(0xffffffffu, bound_ok) && lane == 0) flags[q] = scr::kBoundFail;
+    __syncthreads();  // query row no longer needed: reuse shared memory for the block merge
+    constexpr int KP = 32 * KS;
+    Entry* lists = reinterpret_cast<Entry*>(sm);
+#pragma unroll
+    for (int t = 0; t < KS; ++t) {
+        Entry e;
+        e.val = Lw.val[t];
+        e.id = Lw.id[t];
+        e.pad = 0;
+        lists[warp * KP + t * 32 + lane] = e;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        WarpList<KS> M;
+        M.init();
+        for (int w = 0; w < 8; ++w) {
+            for (int c0 = 0; c0 < k; c0 += 32) {
+                const int pp = c0 + lane;
+                const Entry e = lists[w * KP + min(pp, KP - 1)];
+                const double key = rank_key(metric, e.val);
+                double wk;
+                int wi;
+                M.worst(k, wk, wi);
+                const bool ok = pp < k && e.id != 0x7fffffff && key_less(key, e.id, wk, wi);
+                unsigned m = __ballot_sync(0xffffffffu, ok);
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+                    M.insert(__shfl_sync(0xffffffffu, key, src), __shfl_sync(0xffffffffu, e.id, src),
+                             __shfl_sync(0xffffffffu, e.val, src), k);
+                }
+            }
+        }
+        // exact only if the k results are finite: otherwise NaN-valued rows the
+        // screen never emits could belong in the list
+        bool fin = true;
+#pragma unroll
+        for (int t = 0; t < KS; ++t) {
+            const int pp = t * 32 + lane;
+            if (pp < k && (M.id[t] == 0x7fffffff || isnan(M.val[t]))) fin = false;
+        }
+        const bool all_fin = __all_sync(0xffffffffu, fin);
+        if (!all_fin) {
+            if (lane == 0 && flags[q] == scr::kOk) flags[q] = scr::kTooFew;
+        } else {
+#pragma unroll
+            for (int t = 0; t < KS; ++t) {
+                const int pp = t * 32 + lane;
+                if (pp < k) {
+                    const int slot = M.id[t];
+                    const size_t o = (size_t)q * k + pp;
+                    ids[o] = logical[slot];
+                    dists[o] = M.val[t];
+                    if (err) err[o] = result_err_bound(metric, d, M.val[t], qq, sq64[slot]);
+                }
+            }
+        }
+    }
+}
+
+// gather query rows (padded FP64) of the queries to re-answer; scatter back
+__global__ void k_gather_queries(const double* __restrict__ qbuf, const double* __restrict__ qsq, size_t ld,
+                                 const int* __restrict__ list, int n, double* __restrict__ qout,
+                                 double* __restrict__ qsq_out) {
+    const int i = blockIdx.x;
+    if (i >= n) return;
+    const int q = list[i];
+    for (size_t j = threadIdx.x; j < ld; j += blockDim.x) qout[(size_t)i * ld + j] = qbuf[(size_t)q * ld + j];
+    if (threadIdx.x == 0) qsq_out[i] = qsq[q];
+}
+
+__global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const double* __restrict__ d_in,
+                                  const double* __restrict__ e_in, const int* __restrict__ list, int n, int k,
+                                  int64_t* __restrict__ ids, double* __restrict__ dists, double* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * k) return;
+    const int qi = i / k, j = i % k;
+    const size_t o = (size_t)list[qi] * k + j;
+    ids[o] = ids_in[i];
+    dists[o] = d_in[i];
+    if (err) err[o] = e_in[i];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct GemmPlanCache {
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    bool attr_set[2] = {false, false};
+    size_t screen_smem = 0;
+};
+
+static int gemm_cache(Store* s, GemmPlanCache** out) {
+    if (!s->gemm) {
+        GemmPlanCache* c = new (std::nothrow) GemmPlanCache();
+        if (!c) {
+            svdb_set_error("search_bf16: out of host memory");
+            return SVDB_ENOMEM;
+        }
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) !=
+                cudaSuccess ||
+            qr != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            delete c;
+            svdb_set_error("search_bf16: cuTensorMapEncodeTiled is not available from the driver");
+            return SVDB_ECUDA;
+        }
+        c->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        c->screen_smem = sizeof(scr::Smem) + 1024;
+        s->gemm = c;
+    }
+    *out = s->gemm;
+    return SVDB_OK;
+}
 
 void Store::release_extra() {
     delete gemm;
     gemm = nullptr;
 }
 
-size_t search_bf16_scratch(const Store*, size_t, size_t) { return 256; }
+// 2-D BF16 tensor map over rows x ldb (row-major), box = 64 x box_rows, 128B swizzle
+static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t rows, size_t ldb, int box_rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)ldb, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(ldb * 2)};
+    const cuuint32_t box[2] = {(cuuint32_t)scr::kBK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = c->encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        svdb_set_error("search_bf16: cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return SVDB_ECUDA;
+    }
+    return SVDB_OK;
+}
 
-int search_bf16(Store*, const SearchArgs&, void*, size_t, svdb_search_stats*) {
-    svdb_set_error("search: BF16 precision is not available in this build");
-    return SVDB_EINVAL;
+struct Bf16Layout {
+    size_t qb, qpar, rpar, tau, cnt, cand, surv, flags, err, total;
+    int ntr;
+    size_t npad;
+};
+
+static Bf16Layout bf16_layout(const Store* s, size_t nq) {
+    Bf16Layout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += round_up(bytes, 1024);
+        return o;
+    };
+    L.ntr = (int)((std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN);
+    L.npad = (size_t)L.ntr * scr::kBN;
+    L.qb = take(nq * s->ldb * 2);
+    L.qpar = take(nq * sizeof(float4));
+    L.rpar = take(L.npad * sizeof(float4));
+    L.tau = take(nq * sizeof(int));
+    L.cnt = take(nq * sizeof(int));
+    L.cand = take(nq * (size_t)scr::kCap * sizeof(int2));
+    L.surv = take(nq * sizeof(int));
+    L.flags = take(nq);
+    L.err = take(sizeof(int));
+    L.total = off;
+    return L;
+}
+
+size_t search_bf16_scratch(const Store* s, size_t nq, size_t k) { return bf16_layout(s, nq).total; }
+
+bool bf16_supported(const Store* s, size_t k) { return k <= 32 && s->n_unscreen == 0 && s->nlive > 0; }
+
+int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st) {
+    GemmPlanCache* gc = nullptr;
+    int rc = gemm_cache(s, &gc);
+    if (rc) return rc;
+    const Bf16Layout L = bf16_layout(s, a.nq);
+    if (L.total > scratch_bytes) {
+        svdb_set_error("search_bf16: scratch too small");
+        return SVDB_EINVAL;
+    }
+    uint8_t* base = reinterpret_cast<uint8_t*>(scratch);
+    __nv_bfloat16* qb = reinterpret_cast<__nv_bfloat16*>(base + L.qb);
+    float4* qpar = reinterpret_cast<float4*>(base + L.qpar);
+    float4* rpar = reinterpret_cast<float4*>(base + L.rpar);
+    int* tau = reinterpret_cast<int*>(base + L.tau);
+    int* cnt = reinterpret_cast<int*>(base + L.cnt);
+    int2* cand = reinterpret_cast<int2*>(base + L.cand);
+    int* surv = reinterpret_cast<int*>(base + L.surv);
+    uint8_t* flags = base + L.flags;
+    int* derr = reinterpret_cast<int*>(base + L.err);
+    const int nq = (int)a.nq, k = (int)a.k;
+    uint32_t kernels = 0;
+
+    k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
+                                                                          qb, qpar);
+    SVDB_LAUNCH_CHECK();
+    k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
+                                                                          (int64_t)s->slots, (int64_t)L.npad,
+                                                                          a.metric, rpar);
+    SVDB_LAUNCH_CHECK();
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, cnt, flags, nq, derr);
+    SVDB_LAUNCH_CHECK();
+    kernels += 3;
+
+    CUtensorMap tmq, tmx;
+    rc = make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
+    if (!rc) rc = make_map(gc, &tmx, s->xb, s->slots, s->ldb, scr::kBN);
+    if (rc) return rc;
+
+    ScreenParams P;
+    P.rpar = rpar;
+    P.qpar = qpar;
+    P.tau = tau;
+    P.cnt = cnt;
+    P.cand = cand;
+    P.err = derr;
+    P.nq = nq;
+    P.k = k;
+    P.cap = scr::kCap;
+    P.ntq = (nq + scr::kBM - 1) / scr::kBM;
+    P.ntr = L.ntr;
+    P.kblocks = (int)(s->ldb / scr::kBK);
+    const int G = num_sms();
+    P.rgroups = std::max(1, std::min(G / std::max(P.ntq, 1), P.ntr));
+    const unsigned grid = (unsigned)(P.ntq * P.rgroups);
+    const int kl = k <= 16 ? 0 : 1;
+    if (!gc->attr_set[kl]) {
+        if (kl == 0)
+            SVDB_CUDA(cudaFuncSetAttribute(k_screen_bf16<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)gc->screen_smem));
+        else
+            SVDB_CUDA(cudaFuncSetAttribute(k_screen_bf16<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)gc->screen_smem));
+        gc->attr_set[kl] = true;
+    }
+    if (kl == 0)
+        k_screen_bf16<16><<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, tmx, P);
+    else
+        k_screen_bf16<32><<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, tmx, P);
+    SVDB_LAUNCH_CHECK();
+    ++kernels;
+    s->prof_mark(2);
+
+    const size_t sel_smem = (size_t)scr::kCap * (sizeof(int2) + sizeof(uint32_t));
+    static bool sel_attr = false;
+    if (!sel_attr) {
+        SVDB_CUDA(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sel_smem));
+        sel_attr = true;
+    }
+    k_select<<<(unsigned)nq, 256, sel_smem, s->stream>>>(cand, cnt, scr::kCap, rpar, qpar, k, surv, flags);
+    SVDB_LAUNCH_CHECK();
+    ++kernels;
+    s->prof_mark(3);
+
+    const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));
+    if (a.metric == SVDB_EUCLIDEAN)
+        k_rerank<1, true><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
+            s->x64, s->ld, a.q, a.qsq, s->sq64, cand, surv, scr::kCap, k, a.metric, (int)s->dim, rpar, qpar,
+            s->logical, a.ids, a.dists, a.err, flags);
+    else
+        k_rerank<1, false><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
+            s->x64, s->ld, a.q, a.qsq, s->sq64, cand, surv, scr::kCap, k, a.metric, (int)s->dim, rpar, qpar,
+            s->logical, a.ids, a.dists, a.err, flags);
+    SVDB_LAUNCH_CHECK();
+    ++kernels;
+
+    // queries the screen could not certify: exact FP64 scan
+    std::vector<uint8_t> hflags(a.nq);
+    std::vector<int> hsurv(a.nq);
+    int herr = 0;
+    SVDB_CUDA(cudaMemcpyAsync(hflags.data(), flags, a.nq, cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(hsurv.data(), surv, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    if (herr) {
+        svdb_set_error("search_bf16: the screen kernel's bounded wait ran out");
+        return SVDB_ETIMEOUT;
+    }
+    std::vector<int> redo;
+    uint64_t cands = 0;
+    uint32_t bound_fail = 0;
+    for (size_t i = 0; i < a.nq; ++i) {
+        if (hflags[i] != scr::kOk) redo.push_back((int)i);
+        if (hflags[i] == scr::kBoundFail) ++bound_fail;
+        cands += (uint64_t)hsurv[i];
+    }
+    if (st) {
+        st->candidates += cands;
+        st->widened += (uint32_t)redo.size();
+        st->bound_failures += bound_fail;
+    }
+    if (!redo.empty()) {
+        const size_t nr = redo.size();
+        const size_t need = round_up(nr * s->ld * sizeof(double), 256) + round_up(nr * sizeof(double), 256) +
+                            round_up(nr * sizeof(int), 256) +
+                            round_up(nr * a.k * (sizeof(int64_t) + 2 * sizeof(double)), 256) +
+                            search_fp64_scratch(s, nr, a.k);
+        rc = s->scratch2_reserve(need);
+        if (rc) return rc;
+        uint8_t* b2 = reinterpret_cast<uint8_t*>(s->scratch2);
+        double* rq = reinterpret_cast<double*>(b2);
+        b2 += round_up(nr * s->ld * sizeof(double), 256);
+        double* rsq = reinterpret_cast<double*>(b2);
+        b2 += round_up(nr * sizeof(double), 256);
+        int* rlist = reinterpret_cast<int*>(b2);
+        b2 += round_up(nr * sizeof(int), 256);
+        int64_t* rids = reinterpret_cast<int64_t*>(b2);
+        double* rd = reinterpret_cast<double*>(rids + nr * a.k);
+        double* re = rd + nr * a.k;
+        b2 += round_up(nr * a.k * (sizeof(int64_t) + 2 * sizeof(double)), 256);
+        SVDB_CUDA(cudaMemcpyAsync(rlist, redo.data(), nr * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        k_gather_queries<<<(unsigned)nr, 256, 0, s->stream>>>(a.q, a.qsq, s->ld, rlist, (int)nr, rq, rsq);
+        SVDB_LAUNCH_CHECK();
+        SearchArgs b = a;
+        b.q = rq;
+        b.qsq = rsq;
+        b.nq = nr;
+        b.ids = rids;
+        b.dists = rd;
+        b.err = re;
+        uint32_t kk = 0;
+        rc = search_fp64(s, b, b2, search_fp64_scratch(s, nr, a.k), &kk, false);
+        if (rc) return rc;
+        k_scatter_results<<<(unsigned)((nr * a.k + 255) / 256), 256, 0, s->stream>>>(rids, rd, re, rlist, (int)nr,
+                                                                                  (int)a.k, a.ids, a.dists, a.err);
+        SVDB_LAUNCH_CHECK();
+        SVDB_CUDA(cudaStreamSynchronize(s->stream));  // redo (host vector) and the pinned lists go out of scope
+        kernels += kk + 2;
+    }
+    s->prof_mark(4);
+    if (st) st->kernels += kernels;
+    return SVDB_OK;
 }
 
 }  // namespace svdb

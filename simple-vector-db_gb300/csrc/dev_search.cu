@@ -287,7 +287,7 @@ static int launch_scan_m(Store* s, const ScanPlan& p, const SearchArgs& a, Entry
                                       : launch_scan<QB, KS, false>(s, p, a, part);
 }
 
-int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, uint32_t* kernels) {
+int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, uint32_t* kernels, bool marks) {
     ScanPlan p = plan_scan(s, a.nq, a.k);
     Entry* part = reinterpret_cast<Entry*>(scratch);
     if (search_fp64_scratch(s, a.nq, a.k) > scratch_bytes) {
@@ -308,7 +308,7 @@ int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         default: svdb_set_error("search_fp64: no kernel for ks=%d qb=%d", p.ks, p.qb);
     }
     if (rc) return rc;
-    s->prof_mark(2);
+    if (marks) s->prof_mark(2);
     const unsigned blocks = (unsigned)((a.nq * 32 + 255) / 256);
     switch (p.ks) {
         case 1:
@@ -324,7 +324,7 @@ int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                           s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err);
     }
     SVDB_LAUNCH_CHECK();
-    s->prof_mark(3);
+    if (marks) s->prof_mark(3);
     if (kernels) *kernels += 2;
     return SVDB_OK;
 }
@@ -358,9 +358,11 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     const size_t qbytes = round_up(nq * s->ld * sizeof(double), 256);
     const size_t sqbytes = round_up(nq * sizeof(double), 256);
     const size_t obytes = on_device ? 0 : round_up(out_n * (sizeof(int64_t) + 2 * sizeof(double)), 256);
+    // the screen certifies k <= 32 on stores without unscreenable rows; the
+    // rest is answered by the exact scan
+    const bool use_bf16 = precision == SVDB_PREC_BF16 && bf16_supported(s, k);
     size_t kbytes = 0;
-    if (s->nlive)
-        kbytes = precision == SVDB_PREC_FP64 ? search_fp64_scratch(s, nq, k) : search_bf16_scratch(s, nq, k);
+    if (s->nlive) kbytes = use_bf16 ? search_bf16_scratch(s, nq, k) : search_fp64_scratch(s, nq, k);
     const size_t qin = on_device ? 0 : round_up(nq * s->dim * sizeof(double), 256);
     rc = s->scratch_reserve(qbytes + sqbytes + obytes + kbytes + qin);
     if (rc) return rc;
@@ -403,8 +405,9 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
         k_fill_empty<<<(unsigned)((out_n + 255) / 256), 256, 0, s->stream>>>(a.ids, a.dists, a.err, out_n);
         SVDB_LAUNCH_CHECK();
         ++kernels;
-    } else if (precision == SVDB_PREC_FP64) {
+    } else if (!use_bf16) {
         rc = search_fp64(s, a, kscr, kbytes, &kernels);
+        if (st && precision == SVDB_PREC_BF16) st->widened += (uint32_t)nq;
     } else {
         rc = search_bf16(s, a, kscr, kbytes, st);
     }

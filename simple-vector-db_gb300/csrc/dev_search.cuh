@@ -38,12 +38,16 @@ __device__ __forceinline__ double result_err_bound(int metric, int d, double val
 int prep_queries_fp64(Store* s, const double* q_dev, size_t qs, size_t nq, double* qbuf, double* qsq);
 
 // exact FP64 scan + merge over all live slots, writing SearchArgs outputs
-int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, uint32_t* kernels);
+// marks=false: called as the fallback of another stage (no profiling marks)
+int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, uint32_t* kernels,
+                bool marks = true);
 size_t search_fp64_scratch(const Store* s, size_t nq, size_t k);
 
 // BF16 screen + certified FP64 re-rank (dev_gemm.cu)
 int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st);
 size_t search_bf16_scratch(const Store* s, size_t nq, size_t k);
+// the screen certifies k <= 32 on stores without unscreenable rows
+bool bf16_supported(const Store* s, size_t k);
 
 int num_sms();
 

@@ -138,6 +138,16 @@ __global__ void k_logical_map(const uint8_t* __restrict__ live, int64_t n, int64
     if (threadIdx.x == 0) *nlive_out = carry;
 }
 
+// live rows whose BF16 screen terms are unbounded (marked +inf by k_derive_rows)
+__global__ void k_count_unscreenable(const float4* __restrict__ rowp, const uint8_t* __restrict__ live, int64_t n,
+                                     int* __restrict__ count) {
+    int c = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        c += (live[i] == 1 && !(rowp[i].z < 3.0e38f)) ? 1 : 0;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
 __global__ void k_set_live(uint8_t* live, const int64_t* slots, int n, uint8_t v) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) live[slots[i]] = v;
@@ -256,7 +266,7 @@ int Store::ensure() {
     }
     cudaStream_t st = nullptr;
     SVDB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess) {
+    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         cudaStreamDestroy(st);
         svdb_set_error("device store: cannot allocate a counter");
@@ -340,6 +350,23 @@ int Store::scratch_reserve(size_t bytes) {
     return SVDB_OK;
 }
 
+int Store::scratch2_reserve(size_t bytes) {
+    if (bytes <= scratch2_bytes) return SVDB_OK;
+    SVDB_CUDA(cudaStreamSynchronize(stream));
+    cudaFree(scratch2);
+    scratch2 = nullptr;
+    scratch2_bytes = 0;
+    size_t nb = round_up(bytes + bytes / 4, 1 << 20);
+    cudaError_t e = cudaMalloc(&scratch2, nb);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        svdb_set_error("device scratch: cannot allocate %zu bytes: %s", nb, cudaGetErrorString(e));
+        return SVDB_ENOMEM;
+    }
+    scratch2_bytes = nb;
+    return SVDB_OK;
+}
+
 int Store::pinned_reserve(size_t bytes) {
     int erc = ensure();
     if (erc) return erc;
@@ -409,9 +436,16 @@ int Store::sync() {
     if (map_dirty && slots) {
         k_logical_map<<<1, 1024, 0, stream>>>(live, (int64_t)slots, logical, d_nlive);
         SVDB_LAUNCH_CHECK();
+        SVDB_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
+        k_count_unscreenable<<<(unsigned)std::min<size_t>((slots + 255) / 256, 1024), 256, 0, stream>>>(
+            rowp, live, (int64_t)slots, d_count);
+        SVDB_LAUNCH_CHECK();
+        int hc = 0;
         SVDB_CUDA(cudaMemcpyAsync(&h_nlive, d_nlive, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
+        SVDB_CUDA(cudaMemcpyAsync(&hc, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
         SVDB_CUDA(cudaStreamSynchronize(stream));
         nlive = (size_t)h_nlive;
+        n_unscreen = hc;
         map_dirty = false;
     } else if (!slots) {
         nlive = 0;
@@ -455,6 +489,8 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->logical);
     cudaFree(s->scratch);
     cudaFree(s->d_nlive);
+    cudaFree(s->d_count);
+    cudaFree(s->scratch2);
     cudaFreeHost(s->pin);
     if (s->prof_events)
         for (int i = 0; i < Store::kProfRing; ++i)

@@ -40,9 +40,16 @@ struct Store {
     std::vector<int64_t> dirty_list;
     bool map_dirty = false;
 
-    // per-call scratch (device) and staging (pinned host)
+    // live rows the BF16 screen cannot bound (|x| >= 1e15 or non-finite); as of the last sync
+    int64_t n_unscreen = 0;
+    int* d_count = nullptr;
+
+    // per-call scratch (device) and staging (pinned host); scratch2 serves a
+    // stage's fallback while scratch is still in use
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
+    void* scratch2 = nullptr;
+    size_t scratch2_bytes = 0;
     void* pin = nullptr;
     size_t pin_bytes = 0;
 
@@ -70,6 +77,7 @@ struct Store {
     int flush();
     int sync();
     int scratch_reserve(size_t bytes);
+    int scratch2_reserve(size_t bytes);
     int pinned_reserve(size_t bytes);
     void release_extra();
 };

@@ -1,0 +1,160 @@
+"""GPU parity of the BF16 tensor-core screen + certified FP64 re-rank.
+
+Bar: ids identical to the FP64 oracle (ties to the lowest index) and FP64
+values bit-identical to the oracle's canonical order, on data built to have
+near-ties (Gaussian mixtures with sigma 0.05), exact duplicates, partial
+tiles, query batches that cross the 128-query tile, deletes and updates.
+Queries the screen cannot certify must still come back exact (through the
+FP64 scan) and be counted in stats.widened; the screen's error bound must
+never fail against the exact value (stats.bound_failures == 0).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S(svdb):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return svdb
+
+
+def _mixture(rng, n, d, centres, sigma=0.05):
+    C = rng.normal(size=(centres, d))
+    return C, C[rng.integers(0, centres, n)] + sigma * rng.normal(size=(n, d))
+
+
+def _search_both(S, db, Q, k, metric):
+    st = S.SearchStats()
+    ids, vals = db.search(Q, k, metric, S.PREC_BF16, stats=st)
+    return ids, vals, st
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+@pytest.mark.parametrize("d", [64, 128, 200, 768])
+def test_bf16_mixture_near_ties(S, oracle, metric, d):
+    rng = np.random.default_rng(50 + d + metric)
+    n = 30000 if d <= 200 else 12000
+    C, X = _mixture(rng, n, d, 32)
+    Q = C[rng.integers(0, 32, 40)] + 0.05 * rng.normal(size=(40, d))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for k in (1, 10):
+        ids, vals, st = _search_both(S, db, Q, k, metric)
+        wid, wval = oracle.topk(metric, X, Q, k)
+        assert np.array_equal(ids, wid), (k, st.widened)
+        assert np.array_equal(vals, wval)
+        assert st.bound_failures == 0
+        assert st.widened < Q.shape[0]  # the screen answered at least part of the batch
+    db.close()
+
+
+@pytest.mark.parametrize("nq", [1, 127, 128, 129, 300])
+def test_bf16_query_tiles_and_partial_row_tiles(S, oracle, nq):
+    rng = np.random.default_rng(nq)
+    X = rng.uniform(-1, 1, (10_000 + 37, 96))  # not a multiple of the 256-row tile
+    Q = rng.uniform(-1, 1, (nq, 96))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for metric in range(3):
+        ids, vals, st = _search_both(S, db, Q, 10, metric)
+        wid, wval = oracle.topk(metric, X, Q, 10)
+        assert np.array_equal(ids, wid) and np.array_equal(vals, wval), metric
+        assert st.bound_failures == 0 and st.widened == 0
+    db.close()
+
+
+def test_bf16_duplicates_tie_to_lowest_index(S, oracle):
+    rng = np.random.default_rng(9)
+    X = rng.normal(size=(5000, 32))
+    for i in range(0, 60, 3):
+        X[4000 + i] = X[i]  # exact duplicates at higher indices
+    Q = X[:60:3] + 1e-9
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for metric in range(3):
+        for k in (2, 16, 32):
+            ids, vals, st = _search_both(S, db, Q, k, metric)
+            wid, wval = oracle.topk(metric, X, Q, k)
+            assert np.array_equal(ids, wid) and np.array_equal(vals, wval), (metric, k)
+    db.close()
+
+
+def test_bf16_after_deletes_and_updates(S, oracle):
+    rng = np.random.default_rng(31)
+    C, X = _mixture(rng, 20000, 64, 16)
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    host = list(X)
+    for step in range(400):
+        i = int(rng.integers(0, len(host)))
+        if step % 4 == 0:
+            v = C[rng.integers(0, 16)] + 0.05 * rng.normal(size=64)
+            db.update(i, v)
+            host[i] = v
+        else:
+            db.delete(i)
+            host.pop(i)
+    H = np.stack(host)
+    Q = C[rng.integers(0, 16, 25)] + 0.05 * rng.normal(size=(25, 64))
+    for metric in range(3):
+        ids, vals, st = _search_both(S, db, Q, 10, metric)
+        wid, wval = oracle.topk(metric, H, Q, 10)
+        assert np.array_equal(ids, wid) and np.array_equal(vals, wval), metric
+    db.close()
+
+
+def test_bf16_large_k_and_degenerate_queries_fall_back(S, oracle):
+    rng = np.random.default_rng(17)
+    X = rng.normal(size=(3000, 48))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    Q = rng.normal(size=(4, 48))
+    Q[1] = 0.0  # zero query: cosine undefined for every row -> exact scan
+    Q[2, 5] = np.nan
+    for metric in range(3):
+        for k in (10, 100):  # k > 32 is beyond the screen's running top-k
+            ids, vals, st = _search_both(S, db, Q, k, metric)
+            wid, wval = oracle.topk(metric, X, Q, k)
+            assert np.array_equal(ids, wid), (metric, k)
+            same = (vals == wval) | (np.isnan(vals) & np.isnan(wval))
+            assert same.all(), (metric, k)
+            if k > 32:
+                assert st.widened == 4
+    db.close()
+
+
+def test_bf16_small_store_and_unscreenable_rows(S, oracle):
+    rng = np.random.default_rng(23)
+    X = rng.normal(size=(6, 40))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    ids, vals, st = _search_both(S, db, X[:3], 10, 1)  # k > rows: -1 / NaN tail
+    wid, wval = oracle.topk(1, X, X[:3], 10)
+    assert np.array_equal(ids, wid) and (ids[:, 6:] == -1).all()
+    db.insert(np.full(40, 1e200))  # beyond what the BF16 screen can bound
+    X2 = np.concatenate([X, np.full((1, 40), 1e200)])
+    ids, vals, st = _search_both(S, db, X[:3], 3, 2)
+    wid, wval = oracle.topk(2, X2, X[:3], 3)
+    assert np.array_equal(ids, wid) and st.widened == 3
+    db.close()
+
+
+def test_bf16_values_within_fp64_tolerance(S, oracle):
+    """Reported distances agree with the sequential FP64 formulas to 1e-12 relative."""
+    rng = np.random.default_rng(71)
+    C, X = _mixture(rng, 8000, 128, 8)
+    Q = X[rng.integers(0, 8000, 10)] + 0.01 * rng.normal(size=(10, 128))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for metric in range(3):
+        ids, vals, err = db.search(Q, 10, metric, S.PREC_BF16, with_err=True)
+        for qi in range(10):
+            for j in range(10):
+                s = oracle.fp64(metric, Q[qi], X[ids[qi, j]], seq=True)
+                assert abs(vals[qi, j] - s) <= 1e-12 * max(1.0, abs(s))
+                assert abs(vals[qi, j] - s) <= err[qi, j] + abs(s) * 2**-52
+    db.close()
