@@ -55,14 +55,17 @@ constexpr int kBM = 128;  // queries per tile (TMEM lanes)
 constexpr int kBN = 256;  // store rows per tile (accumulator columns)
 constexpr int kBK = 64;   // K per stage: one 128-byte swizzle row of BF16
 constexpr int kStages = 4;
-constexpr int kEpiWarps = 4;
+constexpr int kEpiWarps = 8;  // two per TMEM lane quadrant, each owning half of the columns
+constexpr int kChunk = 16;    // accumulator columns per tcgen05.ld in the epilogue
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kTmemCols = 2 * kBN;
 constexpr uint32_t kStageA = kBM * kBK * 2;  // 16 KB
 constexpr uint32_t kStageB = kBN * kBK * 2;  // 32 KB
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitimate wait
-constexpr int kCap = 8192;                        // candidates kept per query
-constexpr float kC1 = 9.5367431640625e-07f;       // 2^-20: FP32 rounding of key / mult / m
+constexpr int kCapMin = 8192, kCapMax = 65536;   // candidates kept per query (adaptive)
+constexpr int kSurvCap = 8192;                    // survivors re-ranked per query
+constexpr size_t kCandBudget = size_t(512) << 20; // bytes of candidate lists per search
+constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key and m, per unit of m
 // flags
 constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4;
 
@@ -70,7 +73,7 @@ struct Smem {
     // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
     uint8_t a[kStages][kStageA];
     uint8_t b[kStages][kStageB];
-    float4 rp[2][kBN];
+    float4 rp[2][kBN];  // row parameters of the tile in the accumulator of the same index
     uint64_t full[kStages];
     uint64_t empty[kStages];
     uint64_t accfull[2];
@@ -180,6 +183,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
           "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
 }
+// 32 lanes x 16 consecutive FP32 columns
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // UMMA shared-memory descriptor: K-major, 128-byte swizzle, rows 128 B apart,
@@ -213,11 +225,13 @@ __device__ __forceinline__ int f2ord(float f) {
 }
 __device__ __forceinline__ float ord2f(int o) { return __int_as_float(o >= 0 ? o : o ^ 0x7fffffff); }
 
-// error bound of a screen key (FP32, rounded up).  p = row {mult, a, b, m},
-// qp = query {qn, eqq, eq0, valid}.
-__device__ __forceinline__ float screen_bound(float key, float4 p, float qn, float eqq, float eq0) {
-    float e = __fmaf_ru(qn, p.y, __fmaf_ru(eqq, p.z, eq0));
-    return __fmaf_ru(__fadd_ru(fabsf(key), p.w), scr::kC1, e);
+// Error bound of a screen key (FP32, rounded up): E = qn.a + eqq.b + 2^-19.m + eq0
+// with row p = {mult, a, b, m} and query {qn, eqq, eq0}.  The FP32 rounding of
+// the key itself (<= 2^-22 (|g|.mult + m), |g| <= (1 + c_acc)|bq||bx|) is
+// folded into eqq (a multiple of |bq|) and the m term, so E does not depend
+// on the key and the epilogue computes it with three FMAs.
+__device__ __forceinline__ float screen_bound(float4 p, float qn, float eqq, float eq0) {
+    return __fmaf_ru(qn, p.y, __fmaf_ru(eqq, p.z, __fmaf_ru(scr::kC2, p.w, eq0)));
 }
 
 // running k best lower bounds of one query (k <= KL); `mn` is the k-th best
@@ -229,7 +243,7 @@ struct TopL {
     __device__ __forceinline__ void init(int k) {
 #pragma unroll
         for (int i = 0; i < KL; ++i) v[i] = i < k ? -INFINITY : INFINITY;
-        mn = -INFINITY;
+        mn = k > 0 ? -INFINITY : INFINITY;
         am = 0;
     }
     __device__ __forceinline__ void push(float L) {
@@ -372,10 +386,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         }
     } else {
         // ------------------------------------------------------------ epilogue
-        const int quad = warp & 3;  // TMEM lane quadrant this warp may access
+        // warp w >= 2: lane quadrant w % 4 (the TMEM lanes it may read), column
+        // half (w - 2) / 4; thread = one query of the tile, 128 rows per tile
+        const int quad = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int qi = quad * 32 + lane;
         const int q = qt * kBM + qi;
-        const int etid = threadIdx.x - 64;  // 0..127
+        const int etid = threadIdx.x - 64;  // 0..255
         float qn = 0.f, eqq = 0.f, eq0 = 0.f;
         bool valid = false;
         if (q < P.nq) {
@@ -386,42 +403,59 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             valid = qp.w != 0.f;
         }
         TopL<KL> top;
-        top.init(P.k);
+        top.init(valid ? P.k : 0);  // invalid queries: threshold +inf, never emit, never push
         float tau_c = -INFINITY, published = -INFINITY;
         int2* cq = P.cand + (size_t)(q < P.nq ? q : 0) * P.cap;
+        const int col0 = half * (kBN / 2);
         int j = 0;
         for (int r = r0; r < r1; ++r, ++j) {
             const int b = j & 1;
             const uint32_t use = (uint32_t)j >> 1;
-            float4* rps = S.rp[b];
-            rps[etid] = P.rpar[(size_t)r * kBN + etid];
-            rps[etid + 128] = P.rpar[(size_t)r * kBN + 128 + etid];
-            asm volatile("bar.sync 1, 128;" ::: "memory");
+            const float4* rps = S.rp[b] + col0;
+            S.rp[b][etid] = P.rpar[(size_t)r * kBN + etid];
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory");
             if (valid) tau_c = fmaxf(tau_c, ord2f(*(volatile int*)&P.tau[q]));
             float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
             if (!mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs)) break;
             tc_fence_after();
-            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN);
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN + col0);
+            const int row0 = r * kBN + col0;
 #pragma unroll 1
-            for (int c = 0; c < kBN / 32; ++c) {
-                uint32_t v[32];
-                tmem_ld32(tbase + (uint32_t)(c * 32), v);
+            for (int c = 0; c < kBN / 2 / kChunk; ++c) {
+                uint32_t v[kChunk];
+                tmem_ld16(tbase + (uint32_t)(c * kChunk), v);
                 tmem_ld_wait();
+                const float4* rc = rps + c * kChunk;
+                // branch-free pass: keys, best lower bound, emission count
+                float maxl = -INFINITY;
+                int ne = 0;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float4 p = rps[c * 32 + i];
+                for (int i = 0; i < kChunk; ++i) {
+                    const float4 p = rc[i];
                     const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.w);
-                    const float e = screen_bound(key, p, qn, eqq, eq0);
-                    const float U = __fadd_ru(key, e);
-                    const float L = __fsub_rd(key, e);
-                    if (U >= thr && q < P.nq) {
-                        const int s = atomicAdd(&P.cnt[q], 1);
-                        if (s < P.cap) cq[s] = make_int2(r * kBN + c * 32 + i, __float_as_int(key));
+                    const float e = screen_bound(p, qn, eqq, eq0);
+                    maxl = fmaxf(maxl, __fsub_rd(key, e));
+                    ne += __fadd_ru(key, e) >= thr ? 1 : 0;
+                    v[i] = __float_as_uint(key);
+                }
+                if (ne && q < P.nq) {  // rows whose upper bound reaches the threshold: one atomic, predicated stores
+                    int slot = atomicAdd(&P.cnt[q], ne);
+#pragma unroll
+                    for (int i = 0; i < kChunk; ++i) {
+                        const float key = __uint_as_float(v[i]);
+                        if (__fadd_ru(key, screen_bound(rc[i], qn, eqq, eq0)) >= thr) {
+                            if (slot < P.cap) cq[slot] = make_int2(row0 + c * kChunk + i, (int)v[i]);
+                            ++slot;
+                        }
                     }
-                    if (L > top.mn && valid) {
-                        top.push(L);
-                        thr = fmaxf(top.mn, tau_c);
+                }
+                if (maxl > top.mn) {  // rare after warm-up: fold lower bounds into the running k best
+#pragma unroll
+                    for (int i = 0; i < kChunk; ++i) {
+                        const float l = __fsub_rd(__uint_as_float(v[i]), screen_bound(rc[i], qn, eqq, eq0));
+                        if (l > top.mn) top.push(l);
                     }
+                    thr = fmaxf(top.mn, tau_c);
                 }
             }
             tc_fence_before();
@@ -485,7 +519,10 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
         const double bqn = sqrt(bsq) * up;
         // FP32 accumulation of K = ldb products in K/16 tensor-core steps
         const double cacc = (double)(ldb / 16 + 1) * 20.0 * 1.1920928955078125e-07;
-        const double eqq = (eq + cacc * bqn) * (1.0 + 9.5367431640625e-07) + 3.637978807091713e-12 * qn;  // 2^-38
+        // quantisation + accumulation, FP64 rounding of the reported value (2^-38 qn),
+        // and the FP32 rounding of the key (2^-20 (1 + c_acc) 1.02 |bq|, see screen_bound)
+        const double eqq = (eq + cacc * bqn) * (1.0 + 9.5367431640625e-07) + 3.637978807091713e-12 * qn +
+                           9.5367431640625e-07 * (1.0 + cacc) * 1.02 * bqn;
         // FP64 rounding of the reported value (2^-40 of its scale) + an absolute floor for FP32 underflow
         const double eq0 = 9.094947017729282e-13 * (metric == SVDB_EUCLIDEAN ? sq : qn) + 1e-30;
         // |q| < 1e15 keeps every BF16 product and FP32 sum far from overflow (rows are held to the same)
@@ -538,14 +575,18 @@ __global__ void k_init_search(int* tau, int* cnt, uint8_t* flags, int nq, int* e
 }
 
 // ---------------------------------------------------------------------------
-// stage 2: k-th largest lower bound over the candidates, survivors in place
+// stage 2: k-th largest lower bound over the candidates; survivors = upper
+// bound >= it, copied to the per-query survivor list
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_select(int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
+__device__ __forceinline__ uint32_t f2u_ord(float f) {
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__global__ void __launch_bounds__(256) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
                                                 const float4* __restrict__ rpar, const float4* __restrict__ qpar,
-                                                int k, int* __restrict__ surv, uint8_t* __restrict__ flags) {
-    extern __shared__ __align__(16) uint8_t sm[];
-    int2* cs = reinterpret_cast<int2*>(sm);
-    uint32_t* lo = reinterpret_cast<uint32_t*>(cs + cap);  // ordered lower bounds
+                                                int k, int2* __restrict__ surv, int* __restrict__ nsurv,
+                                                uint8_t* __restrict__ flags) {
     __shared__ int hist[256];
     __shared__ uint32_t s_prefix, s_mask;
     __shared__ int s_rank, s_out;
@@ -555,19 +596,11 @@ __global__ void __launch_bounds__(256) k_select(int2* __restrict__ cand, const i
     if (qp.w == 0.f || n > cap) {
         if (threadIdx.x == 0) {
             flags[q] = qp.w == 0.f ? scr::kInvalidQuery : scr::kOverflow;
-            surv[q] = 0;
+            nsurv[q] = 0;
         }
         return;
     }
-    int2* cq = cand + (size_t)q * cap;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int2 c = cq[i];
-        cs[i] = c;
-        const float key = __int_as_float(c.y);
-        const float L = __fsub_rd(key, screen_bound(key, rpar[c.x], qp.x, qp.y, qp.z));
-        const uint32_t b = __float_as_uint(L);
-        lo[i] = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-    }
+    const int2* cq = cand + (size_t)q * cap;
     if (threadIdx.x == 0) {
         s_prefix = 0;
         s_mask = 0;
@@ -575,14 +608,18 @@ __global__ void __launch_bounds__(256) k_select(int2* __restrict__ cand, const i
         s_out = 0;
     }
     __syncthreads();
-    uint32_t thr_ord = 0;  // every candidate survives when fewer than k exist
+    uint32_t thr_ord = 0;  // fewer than k candidates: every one survives
     if (n >= k) {
         for (int shift = 24; shift >= 0; shift -= 8) {
             hist[threadIdx.x] = 0;
             __syncthreads();
             const uint32_t pre = s_prefix, msk = s_mask;
-            for (int i = threadIdx.x; i < n; i += blockDim.x)
-                if ((lo[i] & msk) == pre) atomicAdd(&hist[(lo[i] >> shift) & 255u], 1);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int2 c = cq[i];
+                const float L = __fsub_rd(__int_as_float(c.y), screen_bound(rpar[c.x], qp.x, qp.y, qp.z));
+                const uint32_t lo = f2u_ord(L);
+                if ((lo & msk) == pre) atomicAdd(&hist[(lo >> shift) & 255u], 1);
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
                 int cum = 0, need = s_rank, dsel = 0;
@@ -601,49 +638,53 @@ __global__ void __launch_bounds__(256) k_select(int2* __restrict__ cand, const i
         }
         thr_ord = s_prefix;  // ordered image of the k-th largest lower bound
     }
+    int2* sq = surv + (size_t)q * scr::kSurvCap;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int2 c = cs[i];
-        const float key = __int_as_float(c.y);
-        const float U = __fadd_ru(key, screen_bound(key, rpar[c.x], qp.x, qp.y, qp.z));
-        const uint32_t b = __float_as_uint(U);
-        const uint32_t uo = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-        if (uo >= thr_ord) cq[atomicAdd(&s_out, 1)] = c;
+        const int2 c = cq[i];
+        const float U = __fadd_ru(__int_as_float(c.y), screen_bound(rpar[c.x], qp.x, qp.y, qp.z));
+        if (f2u_ord(U) >= thr_ord) {
+            const int o = atomicAdd(&s_out, 1);
+            if (o < scr::kSurvCap) sq[o] = c;
+        }
     }
     __syncthreads();
-    if (threadIdx.x == 0) surv[q] = s_out;
+    if (threadIdx.x == 0) {
+        nsurv[q] = s_out;
+        if (s_out > scr::kSurvCap) flags[q] = scr::kOverflow;
+    }
 }
 
 // ---------------------------------------------------------------------------
-// stage 3: FP64 re-rank of the survivors in the canonical order
+// stage 3: FP64 re-rank of the survivors in the canonical order.  Block
+// (q, split) scores survivors split, split + splits, ... (64 rows at a time,
+// 4 lanes per row) and writes its best k as a partial list.
 // ---------------------------------------------------------------------------
 template <int KS, bool EUC>
 __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, size_t ld,
                                                 const double* __restrict__ qbuf, const double* __restrict__ qsq,
-                                                const double* __restrict__ sq64, const int2* __restrict__ cand,
-                                                const int* __restrict__ surv, int cap, int k, int metric, int d,
+                                                const double* __restrict__ sq64, const int2* __restrict__ surv,
+                                                const int* __restrict__ nsurv, int k, int metric,
                                                 const float4* __restrict__ rpar, const float4* __restrict__ qpar,
-                                                const int64_t* __restrict__ logical, int64_t* __restrict__ ids,
-                                                double* __restrict__ dists, double* __restrict__ err,
-                                                uint8_t* __restrict__ flags) {
+                                                Entry* __restrict__ part, uint8_t* __restrict__ flags) {
     extern __shared__ __align__(16) uint8_t sm[];
     double* qs = reinterpret_cast<double*>(sm);
-    const int q = blockIdx.x;
+    const int q = blockIdx.x, split = blockIdx.y, splits = gridDim.y;
     if (flags[q] != scr::kOk) return;  // answered by the exact scan
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
     for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = qbuf[(size_t)q * ld + i];
     __syncthreads();
-    const int n = surv[q];
-    const int2* cq = cand + (size_t)q * cap;
+    const int n = nsurv[q];
+    const int2* sq = surv + (size_t)q * scr::kSurvCap;
     const double qq = qsq[q];
     const double qn = sqrt(qq);
     const float4 qp = qpar[q];
     bool bound_ok = true;
     WarpList<KS> Lw;
     Lw.init();
-    for (int base = warp * 8; base < n; base += 64) {
+    for (int base = (split * 8 + warp) * 8; base < n; base += splits * 64) {
         const int i = base + g;
         const bool act = i < n;
-        const int2 c = act ? cq[i] : make_int2(0, 0);
+        const int2 c = act ? sq[i] : make_int2(0, 0);
         const int row = c.x;
         double p = 0.0;
         if (act) {
@@ -662,9 +703,10 @@ __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, 
             }
         }
         p = group4_sum(p);
-        double val = 0.0, kex = 0.0;
+        double val = 0.0;
         if (act) {
             const double xs = sq64[row];
+            double kex;
             if (EUC) {
                 val = sqrt(p);
                 kex = 0.5 * (qq - p);
@@ -677,7 +719,7 @@ __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, 
             }
             // the screen's bound must hold against the exact value
             const float key = __int_as_float(c.y);
-            const float e = screen_bound(key, rpar[row], qp.x, qp.y, qp.z);
+            const float e = screen_bound(rpar[row], qp.x, qp.y, qp.z);
             if (s == 0 && !(fabs(kex - (double)key) <= (double)e)) bound_ok = false;
         }
         const double kk = rank_key(metric, val);
@@ -727,29 +769,74 @@ __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, 
                 }
             }
         }
-        // exact only if the k results are finite: otherwise NaN-valued rows the
-        // screen never emits could belong in the list
-        bool fin = true;
+        Entry* out = part + ((size_t)q * splits + split) * k;
 #pragma unroll
         for (int t = 0; t < KS; ++t) {
             const int pp = t * 32 + lane;
-            if (pp < k && (M.id[t] == 0x7fffffff || isnan(M.val[t]))) fin = false;
-        }
-        const bool all_fin = __all_sync(0xffffffffu, fin);
-        if (!all_fin) {
-            if (lane == 0 && flags[q] == scr::kOk) flags[q] = scr::kTooFew;
-        } else {
-#pragma unroll
-            for (int t = 0; t < KS; ++t) {
-                const int pp = t * 32 + lane;
-                if (pp < k) {
-                    const int slot = M.id[t];
-                    const size_t o = (size_t)q * k + pp;
-                    ids[o] = logical[slot];
-                    dists[o] = M.val[t];
-                    if (err) err[o] = result_err_bound(metric, d, M.val[t], qq, sq64[slot]);
-                }
+            if (pp < k) {
+                Entry e;
+                e.val = M.val[t];
+                e.id = M.id[t];
+                e.pad = 0;
+                out[pp] = e;
             }
+        }
+    }
+}
+
+// one warp per query: merge the partial lists of the re-rank; the result is
+// exact only if all k entries are finite (NaN-valued rows, which the screen
+// never emits, could otherwise belong in the list)
+template <int KS>
+__global__ void k_merge_rerank(const Entry* __restrict__ part, int splits, int nq, int k, int metric, int d,
+                               const int64_t* __restrict__ logical, const double* __restrict__ qsq,
+                               const double* __restrict__ sq64, int64_t* __restrict__ ids,
+                               double* __restrict__ dists, double* __restrict__ err, uint8_t* __restrict__ flags) {
+    const int q = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (q >= nq || flags[q] != scr::kOk) return;
+    WarpList<KS> M;
+    M.init();
+    const Entry* src = part + (size_t)q * splits * k;
+    const int total = splits * k;
+    for (int c = 0; c < total; c += 32) {
+        const int p = c + lane;
+        Entry e;
+        e.val = 0.0;
+        e.id = 0x7fffffff;
+        if (p < total) e = src[p];
+        const double key = rank_key(metric, e.val);
+        double wk;
+        int wi;
+        M.worst(k, wk, wi);
+        const bool cand = p < total && e.id != 0x7fffffff && key_less(key, e.id, wk, wi);
+        unsigned m = __ballot_sync(0xffffffffu, cand);
+        while (m) {
+            const int sl = __ffs(m) - 1;
+            m &= m - 1;
+            M.insert(__shfl_sync(0xffffffffu, key, sl), __shfl_sync(0xffffffffu, e.id, sl),
+                     __shfl_sync(0xffffffffu, e.val, sl), k);
+        }
+    }
+    bool fin = true;
+#pragma unroll
+    for (int t = 0; t < KS; ++t) {
+        const int pp = t * 32 + lane;
+        if (pp < k && (M.id[t] == 0x7fffffff || isnan(M.val[t]))) fin = false;
+    }
+    if (!__all_sync(0xffffffffu, fin)) {
+        if (lane == 0) flags[q] = scr::kTooFew;
+        return;
+    }
+#pragma unroll
+    for (int t = 0; t < KS; ++t) {
+        const int pp = t * 32 + lane;
+        if (pp < k) {
+            const int slot = M.id[t];
+            const size_t o = (size_t)q * k + pp;
+            ids[o] = logical[slot];
+            dists[o] = M.val[t];
+            if (err) err[o] = result_err_bound(metric, d, M.val[t], qsq[q], sq64[slot]);
         }
     }
 }
@@ -833,8 +920,8 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, qpar, rpar, tau, cnt, cand, surv, flags, err, total;
-    int ntr;
+    size_t qb, qpar, rpar, tau, cnt, cand, surv, nsurv, part, flags, err, total;
+    int ntr, cap, splits;
     size_t npad;
 };
 
@@ -853,8 +940,17 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.rpar = take(L.npad * sizeof(float4));
     L.tau = take(nq * sizeof(int));
     L.cnt = take(nq * sizeof(int));
-    L.cand = take(nq * (size_t)scr::kCap * sizeof(int2));
-    L.surv = take(nq * sizeof(int));
+    // candidate lists: as long as the budget allows (small batches emit more
+    // per query before the running thresholds settle)
+    size_t cap = scr::kCapMax;
+    while (cap > (size_t)scr::kCapMin && nq * cap * sizeof(int2) > scr::kCandBudget) cap >>= 1;
+    L.cap = (int)cap;
+    L.cand = take(nq * cap * sizeof(int2));
+    L.surv = take(nq * (size_t)scr::kSurvCap * sizeof(int2));
+    L.nsurv = take(nq * sizeof(int));
+    // re-rank splits: spread small batches over the SMs
+    L.splits = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(2 * num_sms()) / std::max<size_t>(nq, 1)));
+    L.part = take(nq * (size_t)L.splits * 32 * sizeof(Entry));
     L.flags = take(nq);
     L.err = take(sizeof(int));
     L.total = off;
@@ -881,7 +977,9 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     int* tau = reinterpret_cast<int*>(base + L.tau);
     int* cnt = reinterpret_cast<int*>(base + L.cnt);
     int2* cand = reinterpret_cast<int2*>(base + L.cand);
-    int* surv = reinterpret_cast<int*>(base + L.surv);
+    int2* surv = reinterpret_cast<int2*>(base + L.surv);
+    int* nsurv = reinterpret_cast<int*>(base + L.nsurv);
+    Entry* part = reinterpret_cast<Entry*>(base + L.part);
     uint8_t* flags = base + L.flags;
     int* derr = reinterpret_cast<int*>(base + L.err);
     const int nq = (int)a.nq, k = (int)a.k;
@@ -912,7 +1010,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.err = derr;
     P.nq = nq;
     P.k = k;
-    P.cap = scr::kCap;
+    P.cap = L.cap;
     P.ntq = (nq + scr::kBM - 1) / scr::kBM;
     P.ntr = L.ntr;
     P.kblocks = (int)(s->ldb / scr::kBK);
@@ -937,35 +1035,31 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     ++kernels;
     s->prof_mark(2);
 
-    const size_t sel_smem = (size_t)scr::kCap * (sizeof(int2) + sizeof(uint32_t));
-    static bool sel_attr = false;
-    if (!sel_attr) {
-        SVDB_CUDA(cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sel_smem));
-        sel_attr = true;
-    }
-    k_select<<<(unsigned)nq, 256, sel_smem, s->stream>>>(cand, cnt, scr::kCap, rpar, qpar, k, surv, flags);
+    k_select<<<(unsigned)nq, 256, 0, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv, nsurv, flags);
     SVDB_LAUNCH_CHECK();
     ++kernels;
     s->prof_mark(3);
 
     const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));
+    const dim3 rgrid((unsigned)nq, (unsigned)L.splits);
     if (a.metric == SVDB_EUCLIDEAN)
-        k_rerank<1, true><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
-            s->x64, s->ld, a.q, a.qsq, s->sq64, cand, surv, scr::kCap, k, a.metric, (int)s->dim, rpar, qpar,
-            s->logical, a.ids, a.dists, a.err, flags);
+        k_rerank<1, true><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nsurv, k,
+                                                              a.metric, rpar, qpar, part, flags);
     else
-        k_rerank<1, false><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
-            s->x64, s->ld, a.q, a.qsq, s->sq64, cand, surv, scr::kCap, k, a.metric, (int)s->dim, rpar, qpar,
-            s->logical, a.ids, a.dists, a.err, flags);
+        k_rerank<1, false><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nsurv, k,
+                                                               a.metric, rpar, qpar, part, flags);
     SVDB_LAUNCH_CHECK();
-    ++kernels;
+    k_merge_rerank<1><<<(unsigned)((a.nq * 32 + 255) / 256), 256, 0, s->stream>>>(
+        part, L.splits, nq, k, a.metric, (int)s->dim, s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err, flags);
+    SVDB_LAUNCH_CHECK();
+    kernels += 2;
 
     // queries the screen could not certify: exact FP64 scan
     std::vector<uint8_t> hflags(a.nq);
     std::vector<int> hsurv(a.nq);
     int herr = 0;
     SVDB_CUDA(cudaMemcpyAsync(hflags.data(), flags, a.nq, cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaMemcpyAsync(hsurv.data(), surv, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(hsurv.data(), nsurv, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SVDB_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     if (herr) {
