@@ -73,7 +73,6 @@ struct Smem {
     // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
     uint8_t a[kStages][kStageA];
     uint8_t b[kStages][kStageB];
-    float4 rp[2][kBN];  // row parameters of the tile in the accumulator of the same index
     uint64_t full[kStages];
     uint64_t empty[kStages];
     uint64_t accfull[2];
@@ -392,7 +391,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         const int half = (warp - 2) >> 2;
         const int qi = quad * 32 + lane;
         const int q = qt * kBM + qi;
-        const int etid = threadIdx.x - 64;  // 0..255
         float qn = 0.f, eqq = 0.f, eq0 = 0.f;
         bool valid = false;
         if (q < P.nq) {
@@ -411,9 +409,9 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         for (int r = r0; r < r1; ++r, ++j) {
             const int b = j & 1;
             const uint32_t use = (uint32_t)j >> 1;
-            const float4* rps = S.rp[b] + col0;
-            S.rp[b][etid] = P.rpar[(size_t)r * kBN + etid];
-            asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory");
+            // row parameters of this warp's 128 rows: every lane reads the same
+            // address (one L1 wavefront), so no shared staging or barrier
+            const float4* __restrict__ rps = P.rpar + (size_t)r * kBN + col0;
             if (valid) tau_c = fmaxf(tau_c, ord2f(*(volatile int*)&P.tau[q]));
             float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
             if (!mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs)) break;
@@ -426,35 +424,33 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 tmem_ld16(tbase + (uint32_t)(c * kChunk), v);
                 tmem_ld_wait();
                 const float4* rc = rps + c * kChunk;
-                // branch-free pass: keys, best lower bound, emission count
+                // branch-free pass: keys, the chunk's best lower bound, emission mask
                 float maxl = -INFINITY;
-                int ne = 0;
+                uint32_t mask = 0;
 #pragma unroll
                 for (int i = 0; i < kChunk; ++i) {
-                    const float4 p = rc[i];
+                    const float4 p = __ldg(rc + i);
                     const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.w);
                     const float e = screen_bound(p, qn, eqq, eq0);
                     maxl = fmaxf(maxl, __fsub_rd(key, e));
-                    ne += __fadd_ru(key, e) >= thr ? 1 : 0;
+                    mask |= (__fadd_ru(key, e) >= thr ? 1u : 0u) << i;
                     v[i] = __float_as_uint(key);
                 }
-                if (ne && q < P.nq) {  // rows whose upper bound reaches the threshold: one atomic, predicated stores
-                    int slot = atomicAdd(&P.cnt[q], ne);
+                if (mask && q < P.nq) {  // rows whose upper bound reaches the threshold
+                    int slot = atomicAdd(&P.cnt[q], __popc(mask));
 #pragma unroll
                     for (int i = 0; i < kChunk; ++i) {
-                        const float key = __uint_as_float(v[i]);
-                        if (__fadd_ru(key, screen_bound(rc[i], qn, eqq, eq0)) >= thr) {
+                        if (mask & (1u << i)) {
                             if (slot < P.cap) cq[slot] = make_int2(row0 + c * kChunk + i, (int)v[i]);
                             ++slot;
                         }
                     }
                 }
-                if (maxl > top.mn) {  // rare after warm-up: fold lower bounds into the running k best
-#pragma unroll
-                    for (int i = 0; i < kChunk; ++i) {
-                        const float l = __fsub_rd(__uint_as_float(v[i]), screen_bound(rc[i], qn, eqq, eq0));
-                        if (l > top.mn) top.push(l);
-                    }
+                // The running threshold is the k-th best of the chunk maxima: k
+                // distinct chunks hold k distinct rows with a lower bound at
+                // least that large, so it never exceeds the k-th best lower bound.
+                if (maxl > top.mn) {
+                    top.push(maxl);
                     thr = fmaxf(top.mn, tau_c);
                 }
             }
@@ -482,7 +478,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
 // BF16 copies of the (already padded FP64) queries + per-query bound terms.
 // 4 lanes per query, canonical FP64 reductions.
 __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
-                            size_t ldb, int metric, __nv_bfloat16* __restrict__ qb, float4* __restrict__ qpar) {
+                            size_t ldb, int metric, __nv_bfloat16* __restrict__ qb, float* __restrict__ q32,
+                            float4* __restrict__ qpar) {
     const int lane = threadIdx.x & 31, s = lane & 3;
     const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
     const bool active = qi < nq;
@@ -491,6 +488,7 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
     if (active) {
         const double* src = qbuf + (size_t)qi * ld;
         __nv_bfloat16* dst = qb + (size_t)qi * ldb;
+        float* dst32 = q32 + (size_t)qi * ld;
         for (size_t j = 2 * s; j < ld; j += 8) {
             const double a = src[j], c = src[j + 1];
             const __nv_bfloat16 ha = __double2bfloat16(a), hc = __double2bfloat16(c);
@@ -502,6 +500,7 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
             res = fma(c - fc, c - fc, res);
             dst[j] = ha;
             dst[j + 1] = hc;
+            *reinterpret_cast<float2*>(dst32 + j) = make_float2(__double2float_rn(a), __double2float_rn(c));
         }
         for (size_t j = ld + 2 * s; j < ldb; j += 8) {
             dst[j] = __float2bfloat16(0.0f);
@@ -652,6 +651,161 @@ __global__ void __launch_bounds__(256) k_select(const int2* __restrict__ cand, c
         nsurv[q] = s_out;
         if (s_out > scr::kSurvCap) flags[q] = scr::kOverflow;
     }
+}
+
+// ---------------------------------------------------------------------------
+// stage 2b: FP32 refinement.  For each survivor, S = sum (q32 - x32)^2 in
+// FP32 from the FP32 shadows; the key follows from the exact FP64 norms,
+//   cosine: (|q|^2 + |x|^2 - S) / (2|x|), dot: (|q|^2 + |x|^2 - S) / 2,
+//   Euclidean: (|q|^2 - S) / 2,
+// with a certified bound on |S - |q - x|^2|:
+//   eta = 2^-23 (|q| + |x|) bounds the FP32 rounding of q, x and q - x,
+//   |S_exact - |q - x|^2| <= eta (2 |t| + eta), |S - S_exact| <= gamma S,
+// gamma = (chain length + 3) 2^-24 for the FP32 accumulation.  Working from
+// differences keeps the error proportional to |q - x| (small for the near
+// rows that survive the screen) instead of |q| |x|.  Survivors whose upper
+// bound is below the k-th largest refined lower bound are dropped.
+// ---------------------------------------------------------------------------
+constexpr int kRefThreads = 512;
+
+__global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict__ x32, size_t ld,
+                                                        const float* __restrict__ q32, const double* __restrict__ qsq,
+                                                        const double* __restrict__ sq64,
+                                                        const float4* __restrict__ rowp,
+                                                        const float4* __restrict__ rpar,
+                                                        const float4* __restrict__ qpar, int2* __restrict__ surv,
+                                                        int* __restrict__ nsurv, int k, int metric,
+                                                        uint8_t* __restrict__ flags) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    float* ur = reinterpret_cast<float*>(sm);  // refined upper bound per survivor
+    float* qs = ur + scr::kSurvCap;            // the query in FP32 (ld floats, 16-float multiple)
+    Entry* lists = reinterpret_cast<Entry*>(qs + ld);
+    __shared__ double s_tau;
+    __shared__ int s_out;
+    constexpr int kWarps = kRefThreads / 32;
+    const int q = blockIdx.x;
+    if (flags[q] != scr::kOk) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
+    for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = q32[(size_t)q * ld + i];
+    if (threadIdx.x == 0) s_out = 0;
+    __syncthreads();
+    const int n = nsurv[q];
+    int2* sq = surv + (size_t)q * scr::kSurvCap;
+    const double qq = qsq[q];
+    const float qn_up = qpar[q].x;
+    // each lane: ld/16 float4 steps into 4 accumulators, then 3 + 2 additions
+    const float gamma = (float)(ld / 16 + 6) * 5.9604644775390625e-08f * 1.0001f;
+    WarpList<1> W;
+    W.init();
+    for (int base = warp * 8; base < n; base += kWarps * 8) {
+        const int i = base + g;
+        const bool act = i < n;
+        const int row = act ? sq[i].x : 0;
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        if (act) {
+            const float4* x = reinterpret_cast<const float4*>(x32 + (size_t)row * ld);
+            const float4* qv = reinterpret_cast<const float4*>(qs);
+#pragma unroll 4
+            for (size_t j = s; j < ld / 4; j += 4) {
+                const float4 xv = __ldg(x + j);
+                const float4 qq4 = qv[j];
+                const float t0 = qq4.x - xv.x, t1 = qq4.y - xv.y, t2 = qq4.z - xv.z, t3 = qq4.w - xv.w;
+                a0 = fmaf(t0, t0, a0);
+                a1 = fmaf(t1, t1, a1);
+                a2 = fmaf(t2, t2, a2);
+                a3 = fmaf(t3, t3, a3);
+            }
+        }
+        float p = (a0 + a1) + (a2 + a3);
+        p += __shfl_xor_sync(0xffffffffu, p, 2);
+        p += __shfl_xor_sync(0xffffffffu, p, 1);
+        double L = -INFINITY;
+        if (act && s == 0) {
+            const double S = (double)p;
+            const double xs = sq64[row];
+            const float xn_up = rowp[row].x;
+            const float sup = __fmul_ru(p, 1.0f + gamma);
+            const float eta = __fmul_ru(1.1921875e-07f, __fadd_ru(qn_up, xn_up));  // 2^-23 (1 + 2^-13)
+            float ed2 = __fmaf_ru(gamma, sup, __fmul_ru(eta, __fadd_ru(__fmul_ru(2.0f, __fsqrt_ru(sup)), eta)));
+            ed2 = __fmaf_ru(9.094947e-13f, __double2float_ru(qq + xs), __fmul_ru(ed2, 1.000001f));  // + 2^-40 scale
+            double key, e;
+            if (metric == SVDB_EUCLIDEAN) {
+                key = 0.5 * (qq - S);
+                e = 0.5 * (double)ed2;
+            } else if (metric == SVDB_DOT) {
+                key = 0.5 * ((qq + xs) - S);
+                e = 0.5 * (double)ed2;
+            } else {
+                const double mult = (double)rpar[row].x;  // 1/|x| to 2^-24 relative
+                key = 0.5 * ((qq + xs) - S) * mult;
+                e = 0.5 * (double)ed2 * mult * (1.0 + 2.384185791015625e-07) + fabs(key) * 2.384185791015625e-07;
+            }
+            L = key - e;
+            ur[i] = __double2float_ru(key + e);
+        }
+        // k best refined lower bounds of this warp (ascending key -L, then row)
+        double wk;
+        int wi;
+        W.worst(k, wk, wi);
+        const bool cand = act && s == 0 && key_less(-L, row, wk, wi);
+        unsigned m = __ballot_sync(0xffffffffu, cand);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const double lv = __shfl_sync(0xffffffffu, L, src);
+            W.insert(-lv, __shfl_sync(0xffffffffu, row, src), lv, k);
+        }
+    }
+    Entry* mine = lists + warp * 32;
+    {
+        Entry e;
+        e.val = W.val[0];
+        e.id = W.id[0];
+        e.pad = 0;
+        mine[lane] = e;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        WarpList<1> M;
+        M.init();
+        for (int w = 0; w < kWarps; ++w) {
+            const Entry e = lists[w * 32 + lane];
+            double wk;
+            int wi;
+            M.worst(k, wk, wi);
+            const bool ok = lane < k && e.id != 0x7fffffff && key_less(-e.val, e.id, wk, wi);
+            unsigned m = __ballot_sync(0xffffffffu, ok);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const double lv = __shfl_sync(0xffffffffu, e.val, src);
+                M.insert(-lv, __shfl_sync(0xffffffffu, e.id, src), lv, k);
+            }
+        }
+        double kth, dummy;
+        int kid;
+        M.at(k - 1, dummy, kid);
+        kth = __shfl_sync(0xffffffffu, M.val[0], (k - 1) & 31);
+        if (lane == 0) s_tau = kid == 0x7fffffff ? -INFINITY : kth;  // fewer than k: keep all
+    }
+    __syncthreads();
+    // compaction in two phases: every read of the list precedes every write
+    const float tau = __double2float_rd(s_tau);
+    constexpr int kPer = scr::kSurvCap / kRefThreads;
+    int2 keep[kPer];
+    int nk = 0;
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int i = threadIdx.x + m * kRefThreads;
+        if (i < n && ur[i] >= tau) keep[nk++] = sq[i];
+    }
+    __syncthreads();
+    const int o = nk ? atomicAdd(&s_out, nk) : 0;
+#pragma unroll
+    for (int m = 0; m < kPer; ++m)
+        if (m < nk) sq[o + m] = keep[m];
+    __syncthreads();
+    if (threadIdx.x == 0) nsurv[q] = s_out;
 }
 
 // ---------------------------------------------------------------------------
@@ -870,6 +1024,7 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     bool attr_set[2] = {false, false};
+    bool refine_attr = false;
     size_t screen_smem = 0;
 };
 
@@ -920,7 +1075,7 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, qpar, rpar, tau, cnt, cand, surv, nsurv, part, flags, err, total;
+    size_t qb, q32, qpar, rpar, tau, cnt, cand, surv, nsurv, part, flags, err, total;
     int ntr, cap, splits;
     size_t npad;
 };
@@ -936,6 +1091,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.ntr = (int)((std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN);
     L.npad = (size_t)L.ntr * scr::kBN;
     L.qb = take(nq * s->ldb * 2);
+    L.q32 = take(nq * s->ld * sizeof(float));
     L.qpar = take(nq * sizeof(float4));
     L.rpar = take(L.npad * sizeof(float4));
     L.tau = take(nq * sizeof(int));
@@ -972,6 +1128,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     }
     uint8_t* base = reinterpret_cast<uint8_t*>(scratch);
     __nv_bfloat16* qb = reinterpret_cast<__nv_bfloat16*>(base + L.qb);
+    float* q32 = reinterpret_cast<float*>(base + L.q32);
     float4* qpar = reinterpret_cast<float4*>(base + L.qpar);
     float4* rpar = reinterpret_cast<float4*>(base + L.rpar);
     int* tau = reinterpret_cast<int*>(base + L.tau);
@@ -986,7 +1143,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     uint32_t kernels = 0;
 
     k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
-                                                                          qb, qpar);
+                                                                          qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
@@ -1037,7 +1194,16 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     k_select<<<(unsigned)nq, 256, 0, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv, nsurv, flags);
     SVDB_LAUNCH_CHECK();
-    ++kernels;
+    const size_t ref_smem = (size_t)scr::kSurvCap * sizeof(float) + s->ld * sizeof(float) +
+                            (size_t)(kRefThreads / 32) * 32 * sizeof(Entry);
+    if (!gc->refine_attr) {
+        SVDB_CUDA(cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        gc->refine_attr = true;
+    }
+    k_refine<<<(unsigned)nq, kRefThreads, ref_smem, s->stream>>>(s->x32, s->ld, q32, a.qsq, s->sq64, s->rowp, rpar,
+                                                                 qpar, surv, nsurv, k, a.metric, flags);
+    SVDB_LAUNCH_CHECK();
+    kernels += 2;
     s->prof_mark(3);
 
     const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));

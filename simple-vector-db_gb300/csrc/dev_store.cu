@@ -4,6 +4,7 @@
 // HBM layout of one store (capacity C slots, dimension D):
 //   x64     C x ld   double   FP64 master, ld = D rounded up to 16 (128-B rows)
 //   xb      C x ldb  bf16     BF16 shadow of x64, ldb = D rounded up to 64
+//   x32     C x ld   float    FP32 shadow of x64 (refinement stage)
 //   sq64    C        double   canonical sum of squares of the master row
 //   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
 //   live    C        uint8    1 = searchable row, 2 = row of another dimension
@@ -41,7 +42,7 @@ namespace svdb {
 // Derived per-row arrays for slots [lo, hi) or for an explicit slot list.
 // One group of 4 lanes per row, canonical order for the sum of squares.
 __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bfloat16* __restrict__ xb,
-                              size_t ldb, double* __restrict__ sq64, float4* __restrict__ rowp,
+                              size_t ldb, float* __restrict__ x32, double* __restrict__ sq64, float4* __restrict__ rowp,
                               const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
                               const int64_t* __restrict__ list) {
     const int lane = threadIdx.x & 31, s = lane & 3;
@@ -51,6 +52,7 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     const int64_t slot = active ? (list ? list[gid] : lo + gid) : 0;
     const double* x = x64 + slot * ld;
     __nv_bfloat16* xh = xb + slot * ldb;
+    float* xf = x32 + slot * ld;
     double sq = 0.0, bh = 0.0, res = 0.0;
     if (active) {
         for (size_t j = 2 * s; j < ld; j += 8) {
@@ -65,6 +67,7 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
             res = fma(v.y - fy, v.y - fy, res);
             xh[j] = hx;
             xh[j + 1] = hy;
+            *reinterpret_cast<float2*>(xf + j) = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
         }
         for (size_t j = ld + 2 * s; j < ldb; j += 8) {  // zero the BF16 tail beyond ld
             xh[j] = __float2bfloat16(0.0f);
@@ -284,6 +287,7 @@ int Store::grow(size_t need) {
     while (nc < need) nc *= 2;
     double* nx = nullptr;
     __nv_bfloat16* nb = nullptr;
+    float* nf = nullptr;
     double* nsq = nullptr;
     float4* np = nullptr;
     uint8_t* nl = nullptr;
@@ -291,6 +295,7 @@ int Store::grow(size_t need) {
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = cudaMalloc(&nx, nc * ld * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&nb, nc * ldb * sizeof(__nv_bfloat16));
+    if (e == cudaSuccess) e = cudaMalloc(&nf, nc * ld * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nl, nc);
@@ -299,6 +304,7 @@ int Store::grow(size_t need) {
         cudaGetLastError();
         cudaFree(nx);
         cudaFree(nb);
+        cudaFree(nf);
         cudaFree(nsq);
         cudaFree(np);
         cudaFree(nl);
@@ -309,6 +315,7 @@ int Store::grow(size_t need) {
     if (slots) {
         SVDB_CUDA(cudaMemcpyAsync(nx, x64, slots * ld * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nb, xb, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nf, x32, slots * ld * sizeof(float), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nl, live, slots, cudaMemcpyDeviceToDevice, stream));
@@ -317,12 +324,14 @@ int Store::grow(size_t need) {
     }
     cudaFree(x64);
     cudaFree(xb);
+    cudaFree(x32);
     cudaFree(sq64);
     cudaFree(rowp);
     cudaFree(live);
     cudaFree(logical);
     x64 = nx;
     xb = nb;
+    x32 = nf;
     sq64 = nsq;
     rowp = np;
     live = nl;
@@ -415,7 +424,7 @@ int Store::sync() {
         const int64_t n = derive_hi - derive_lo;
         const int threads = 256;
         const int64_t blocks = (n * 4 + threads - 1) / threads;
-        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, sq64, rowp, live, derive_lo,
+        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, sq64, rowp, live, derive_lo,
                                                               derive_hi, nullptr);
         SVDB_LAUNCH_CHECK();
     }
@@ -427,7 +436,7 @@ int Store::sync() {
         if (rc) return rc;
         d = (int64_t*)scratch;
         SVDB_CUDA(cudaMemcpyAsync(d, dirty_list.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
-        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, sq64, rowp, live, 0,
+        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, sq64, rowp, live, 0,
                                                                          n, d);
         SVDB_LAUNCH_CHECK();
         SVDB_CUDA(cudaStreamSynchronize(stream));
@@ -483,6 +492,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaStreamSynchronize(s->stream);
     cudaFree(s->x64);
     cudaFree(s->xb);
+    cudaFree(s->x32);
     cudaFree(s->sq64);
     cudaFree(s->rowp);
     cudaFree(s->live);

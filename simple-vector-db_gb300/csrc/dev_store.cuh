@@ -23,6 +23,7 @@ struct Store {
 
     double* x64 = nullptr;
     __nv_bfloat16* xb = nullptr;
+    float* x32 = nullptr;  // FP32 shadow (cap x ld), read by the refinement stage
     double* sq64 = nullptr;
     float4* rowp = nullptr;  // {|x| up (-1: dead slot), |bf16 x| up, |x - bf16 x| up (inf: unscreenable), |x|^2/2}
     uint8_t* live = nullptr;
