@@ -285,6 +285,9 @@ def run_ours(args, ws, rank, local):
                 "stage_ms_per_step": {n: float(stage_ms[i] / max(ncalls, 1)) for i, n in
                                       enumerate(["prep", "screen", "select", "rerank"])},
                 "plain_fp64_qps": plain,
+                "funnel_per_query": {"screen_candidates": st.candidates / nq, "survivors": st.survivors / nq,
+                                     "fp64_reranked": st.reranked / nq, "widened_queries": st.widened,
+                                     "bound_failures": st.bound_failures},
                 "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": nq * DIM * 8,
                         "d2h_bytes_per_step": nq * k * 24},
                 "gpu_launches": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": cl}

@@ -51,13 +51,15 @@ extern "C" {
 #define SVDB_CMP_UNKNOWN_METHOD 5 /* "Unknown comparison method", 400 (:161-170) */
 
 typedef struct svdb_search_stats {
-    uint64_t candidates;   /* rows re-ranked in FP64 over the whole batch */
-    uint32_t widened;      /* queries the screen could not certify, answered by the exact FP64 scan */
-    uint32_t kernels;      /* kernel launches issued by the call */
-    double max_err_bound;  /* max over results of the bound on |reported - exact real value| */
+    uint64_t candidates;     /* rows the BF16 screen emitted, over the batch (FP64 scan: rows scanned) */
+    uint64_t survivors;      /* rows left after the exact k-th lower-bound filter of the screen */
+    uint64_t reranked;       /* rows scored in FP64 against the master copy (after FP32 refinement) */
+    uint32_t widened;        /* queries the screen could not certify, answered by the exact FP64 scan */
+    uint32_t kernels;        /* kernel launches issued by the call */
     uint32_t bound_failures; /* queries whose screen bound did not hold against the exact value
                                 (re-answered by the exact scan; nonzero means the bound model is wrong) */
     uint32_t reserved;
+    double max_err_bound;    /* max over results of the bound on |reported - exact real value| */
 } svdb_search_stats;
 
 /*

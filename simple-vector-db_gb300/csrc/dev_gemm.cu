@@ -264,6 +264,7 @@ struct ScreenParams {
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
     const float4* qpar;  // per query {qn, eqq, eq0, valid}
     int* tau;            // per query: shared lower bound of the k-th best key (ordered int)
+    int* bins;           // per query, k bins: best chunk maximum of the chunks whose index % k is the bin
     int* cnt;            // per query candidate count (may exceed cap: overflow)
     int2* cand;          // per query: cap x {row slot, key bits}
     int* err;            // set to 1 when a wait timed out
@@ -412,15 +413,55 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // row parameters of this warp's 128 rows: every lane reads the same
             // address (one L1 wavefront), so no shared staging or barrier
             const float4* __restrict__ rps = P.rpar + (size_t)r * kBN + col0;
-            if (valid) tau_c = fmaxf(tau_c, ord2f(*(volatile int*)&P.tau[q]));
-            float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
-            if (!mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs)) break;
+            // tcgen05.ld is warp-collective (.sync.aligned): every branch that
+            // leads to one must be taken by the whole warp, including this wait
+            const bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
+            if (!__all_sync(0xffffffffu, got)) break;
             tc_fence_after();
             const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN + col0);
             const int row0 = r * kBN + col0;
+            if (j == 0) {  // warp-uniform: lanes of invalid queries load and discard
+                // Warm-up on the first tile, before anything is emitted: fold the
+                // lower bound of every row into the running k best (rows, not chunk
+                // maxima, so k values exist after one tile) and publish the chunk
+                // maxima to the bins.  The emitting pass below then skips its pushes
+                // for this tile, so no row is counted twice.
+#pragma unroll 1
+                for (int c = 0; c < kBN / 2 / kChunk; ++c) {
+                    uint32_t v[kChunk];
+                    __syncwarp();  // converged warp for the collective load
+                    tmem_ld16(tbase + (uint32_t)(c * kChunk), v);
+                    tmem_ld_wait();
+                    const float4* rc = rps + c * kChunk;
+                    float maxl = -INFINITY;
+#pragma unroll
+                    for (int i = 0; i < kChunk; ++i) {
+                        const float4 p = __ldg(rc + i);
+                        const float l = __fsub_rd(__fmaf_rn(__uint_as_float(v[i]), p.x, -p.w),
+                                                  screen_bound(p, qn, eqq, eq0));
+                        maxl = fmaxf(maxl, l);
+                        if (valid && l > top.mn) top.push(l);
+                    }
+                    if (valid && maxl > -INFINITY) {
+                        const int chunk = (row0 + c * kChunk) / kChunk;
+                        atomicMax(&P.bins[(size_t)q * P.k + chunk % P.k], f2ord(maxl));
+                    }
+                }
+            }
+            if (valid && (j < 8 || (j & 7) == 0)) {
+                // The k bins hold lower bounds of k distinct rows (chunks of different
+                // bins are different rows), so their minimum is a valid threshold; it
+                // reflects what every CTA has seen of this query, not only this one.
+                const int* bq = P.bins + (size_t)q * P.k;
+                int bmin = 0x7fffffff;
+                for (int t = 0; t < P.k; ++t) bmin = min(bmin, __ldcg(bq + t));
+                tau_c = fmaxf(tau_c, fmaxf(ord2f(__ldcg(P.tau + q)), ord2f(bmin)));
+            }
+            float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
 #pragma unroll 1
             for (int c = 0; c < kBN / 2 / kChunk; ++c) {
                 uint32_t v[kChunk];
+                __syncwarp();  // converged warp for the collective load
                 tmem_ld16(tbase + (uint32_t)(c * kChunk), v);
                 tmem_ld_wait();
                 const float4* rc = rps + c * kChunk;
@@ -449,7 +490,11 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 // The running threshold is the k-th best of the chunk maxima: k
                 // distinct chunks hold k distinct rows with a lower bound at
                 // least that large, so it never exceeds the k-th best lower bound.
-                if (maxl > top.mn) {
+                if (maxl > thr && valid) {
+                    const int chunk = (row0 + c * kChunk) / kChunk;
+                    atomicMax(&P.bins[(size_t)q * P.k + chunk % P.k], f2ord(maxl));
+                }
+                if (maxl > top.mn && j > 0) {
                     top.push(maxl);
                     thr = fmaxf(top.mn, tau_c);
                 }
@@ -563,10 +608,11 @@ __global__ void k_row_params(const float4* __restrict__ rowp, const double* __re
     rpar[i] = out;
 }
 
-__global__ void k_init_search(int* tau, int* cnt, uint8_t* flags, int nq, int* err) {
+__global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int nq, int k, int* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nq) {
         tau[i] = f2ord(-INFINITY);
+        for (int t = 0; t < k; ++t) bins[(size_t)i * k + t] = f2ord(-INFINITY);
         cnt[i] = 0;
         flags[i] = scr::kOk;
     }
@@ -582,10 +628,15 @@ __device__ __forceinline__ uint32_t f2u_ord(float f) {
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
-__global__ void __launch_bounds__(256) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
-                                                const float4* __restrict__ rpar, const float4* __restrict__ qpar,
-                                                int k, int2* __restrict__ surv, int* __restrict__ nsurv,
-                                                uint8_t* __restrict__ flags) {
+// Pass 1: every thread keeps the k best lower bounds of its candidates
+// (registers); their union holds the k best overall, so a radix select over
+// it in shared memory gives the exact k-th largest.  Pass 2: survivors.
+template <int KL>
+__global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
+                                                 const float4* __restrict__ rpar, const float4* __restrict__ qpar,
+                                                 int k, int2* __restrict__ surv, int* __restrict__ nsurv,
+                                                 uint8_t* __restrict__ flags) {
+    extern __shared__ uint32_t vals[];  // blockDim.x * k ordered lower bounds
     __shared__ int hist[256];
     __shared__ uint32_t s_prefix, s_mask;
     __shared__ int s_rank, s_out;
@@ -600,6 +651,17 @@ __global__ void __launch_bounds__(256) k_select(const int2* __restrict__ cand, c
         return;
     }
     const int2* cq = cand + (size_t)q * cap;
+    const int bd = blockDim.x;
+    TopL<KL> top;
+    top.init(k);
+    for (int i = threadIdx.x; i < n; i += bd) {
+        const int2 c = cq[i];
+        const float L = __fsub_rd(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
+        if (L > top.mn) top.push(L);
+    }
+#pragma unroll
+    for (int j = 0; j < KL; ++j)
+        if (j < k) vals[threadIdx.x * k + j] = f2u_ord(top.v[j]);
     if (threadIdx.x == 0) {
         s_prefix = 0;
         s_mask = 0;
@@ -607,16 +669,15 @@ __global__ void __launch_bounds__(256) k_select(const int2* __restrict__ cand, c
         s_out = 0;
     }
     __syncthreads();
+    const int m = bd * k;
     uint32_t thr_ord = 0;  // fewer than k candidates: every one survives
     if (n >= k) {
         for (int shift = 24; shift >= 0; shift -= 8) {
-            hist[threadIdx.x] = 0;
+            for (int i = threadIdx.x; i < 256; i += bd) hist[i] = 0;
             __syncthreads();
             const uint32_t pre = s_prefix, msk = s_mask;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const int2 c = cq[i];
-                const float L = __fsub_rd(__int_as_float(c.y), screen_bound(rpar[c.x], qp.x, qp.y, qp.z));
-                const uint32_t lo = f2u_ord(L);
+            for (int i = threadIdx.x; i < m; i += bd) {
+                const uint32_t lo = vals[i];
                 if ((lo & msk) == pre) atomicAdd(&hist[(lo >> shift) & 255u], 1);
             }
             __syncthreads();
@@ -638,9 +699,9 @@ __global__ void __launch_bounds__(256) k_select(const int2* __restrict__ cand, c
         thr_ord = s_prefix;  // ordered image of the k-th largest lower bound
     }
     int2* sq = surv + (size_t)q * scr::kSurvCap;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = threadIdx.x; i < n; i += bd) {
         const int2 c = cq[i];
-        const float U = __fadd_ru(__int_as_float(c.y), screen_bound(rpar[c.x], qp.x, qp.y, qp.z));
+        const float U = __fadd_ru(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
         if (f2u_ord(U) >= thr_ord) {
             const int o = atomicAdd(&s_out, 1);
             if (o < scr::kSurvCap) sq[o] = c;
@@ -674,8 +735,8 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
                                                         const float4* __restrict__ rowp,
                                                         const float4* __restrict__ rpar,
                                                         const float4* __restrict__ qpar, int2* __restrict__ surv,
-                                                        int* __restrict__ nsurv, int k, int metric,
-                                                        uint8_t* __restrict__ flags) {
+                                                        const int* __restrict__ nsurv, int* __restrict__ nref, int k,
+                                                        int metric, uint8_t* __restrict__ flags) {
     extern __shared__ __align__(16) uint8_t sm[];
     float* ur = reinterpret_cast<float*>(sm);  // refined upper bound per survivor
     float* qs = ur + scr::kSurvCap;            // the query in FP32 (ld floats, 16-float multiple)
@@ -684,7 +745,10 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
     __shared__ int s_out;
     constexpr int kWarps = kRefThreads / 32;
     const int q = blockIdx.x;
-    if (flags[q] != scr::kOk) return;
+    if (flags[q] != scr::kOk) {
+        if (threadIdx.x == 0) nref[q] = 0;
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
     for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = q32[(size_t)q * ld + i];
     if (threadIdx.x == 0) s_out = 0;
@@ -805,7 +869,7 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
     for (int m = 0; m < kPer; ++m)
         if (m < nk) sq[o + m] = keep[m];
     __syncthreads();
-    if (threadIdx.x == 0) nsurv[q] = s_out;
+    if (threadIdx.x == 0) nref[q] = s_out;
 }
 
 // ---------------------------------------------------------------------------
@@ -1025,6 +1089,7 @@ struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     bool attr_set[2] = {false, false};
     bool refine_attr = false;
+    bool select_attr = false;
     size_t screen_smem = 0;
 };
 
@@ -1075,7 +1140,7 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, q32, qpar, rpar, tau, cnt, cand, surv, nsurv, part, flags, err, total;
+    size_t qb, q32, qpar, rpar, tau, bins, cnt, cand, surv, nsurv, nref, part, flags, err, total;
     int ntr, cap, splits;
     size_t npad;
 };
@@ -1095,6 +1160,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.qpar = take(nq * sizeof(float4));
     L.rpar = take(L.npad * sizeof(float4));
     L.tau = take(nq * sizeof(int));
+    L.bins = take(nq * 32 * sizeof(int));
     L.cnt = take(nq * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
     // per query before the running thresholds settle)
@@ -1104,6 +1170,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.cand = take(nq * cap * sizeof(int2));
     L.surv = take(nq * (size_t)scr::kSurvCap * sizeof(int2));
     L.nsurv = take(nq * sizeof(int));
+    L.nref = take(nq * sizeof(int));
     // re-rank splits: spread small batches over the SMs
     L.splits = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(2 * num_sms()) / std::max<size_t>(nq, 1)));
     L.part = take(nq * (size_t)L.splits * 32 * sizeof(Entry));
@@ -1132,10 +1199,12 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     float4* qpar = reinterpret_cast<float4*>(base + L.qpar);
     float4* rpar = reinterpret_cast<float4*>(base + L.rpar);
     int* tau = reinterpret_cast<int*>(base + L.tau);
+    int* bins = reinterpret_cast<int*>(base + L.bins);
     int* cnt = reinterpret_cast<int*>(base + L.cnt);
     int2* cand = reinterpret_cast<int2*>(base + L.cand);
     int2* surv = reinterpret_cast<int2*>(base + L.surv);
     int* nsurv = reinterpret_cast<int*>(base + L.nsurv);
+    int* nref = reinterpret_cast<int*>(base + L.nref);
     Entry* part = reinterpret_cast<Entry*>(base + L.part);
     uint8_t* flags = base + L.flags;
     int* derr = reinterpret_cast<int*>(base + L.err);
@@ -1149,7 +1218,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                                           (int64_t)s->slots, (int64_t)L.npad,
                                                                           a.metric, rpar);
     SVDB_LAUNCH_CHECK();
-    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, cnt, flags, nq, derr);
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, flags, nq, k, derr);
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
@@ -1162,6 +1231,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.rpar = rpar;
     P.qpar = qpar;
     P.tau = tau;
+    P.bins = bins;
     P.cnt = cnt;
     P.cand = cand;
     P.err = derr;
@@ -1192,7 +1262,22 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     ++kernels;
     s->prof_mark(2);
 
-    k_select<<<(unsigned)nq, 256, 0, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv, nsurv, flags);
+    {
+        // small batches carry many candidates per query: wider blocks
+        const int sel_threads = nq >= 256 ? 256 : 1024;
+        const size_t sel_smem = (size_t)sel_threads * k * sizeof(uint32_t);
+        if (!gc->select_attr) {
+            SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+            gc->select_attr = true;
+        }
+        if (k <= 16)
+            k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
+                                                                             nsurv, flags);
+        else
+            k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
+                                                                             nsurv, flags);
+    }
     SVDB_LAUNCH_CHECK();
     const size_t ref_smem = (size_t)scr::kSurvCap * sizeof(float) + s->ld * sizeof(float) +
                             (size_t)(kRefThreads / 32) * 32 * sizeof(Entry);
@@ -1201,7 +1286,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         gc->refine_attr = true;
     }
     k_refine<<<(unsigned)nq, kRefThreads, ref_smem, s->stream>>>(s->x32, s->ld, q32, a.qsq, s->sq64, s->rowp, rpar,
-                                                                 qpar, surv, nsurv, k, a.metric, flags);
+                                                                 qpar, surv, nsurv, nref, k, a.metric, flags);
     SVDB_LAUNCH_CHECK();
     kernels += 2;
     s->prof_mark(3);
@@ -1209,10 +1294,10 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));
     const dim3 rgrid((unsigned)nq, (unsigned)L.splits);
     if (a.metric == SVDB_EUCLIDEAN)
-        k_rerank<1, true><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nsurv, k,
+        k_rerank<1, true><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nref, k,
                                                               a.metric, rpar, qpar, part, flags);
     else
-        k_rerank<1, false><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nsurv, k,
+        k_rerank<1, false><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nref, k,
                                                                a.metric, rpar, qpar, part, flags);
     SVDB_LAUNCH_CHECK();
     k_merge_rerank<1><<<(unsigned)((a.nq * 32 + 255) / 256), 256, 0, s->stream>>>(
@@ -1222,10 +1307,12 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     // queries the screen could not certify: exact FP64 scan
     std::vector<uint8_t> hflags(a.nq);
-    std::vector<int> hsurv(a.nq);
+    std::vector<int> hcnt(3 * a.nq);
     int herr = 0;
     SVDB_CUDA(cudaMemcpyAsync(hflags.data(), flags, a.nq, cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaMemcpyAsync(hsurv.data(), nsurv, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(hcnt.data(), cnt, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(hcnt.data() + a.nq, nsurv, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(hcnt.data() + 2 * a.nq, nref, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SVDB_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     if (herr) {
@@ -1233,15 +1320,19 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         return SVDB_ETIMEOUT;
     }
     std::vector<int> redo;
-    uint64_t cands = 0;
+    uint64_t c0 = 0, c1 = 0, c2 = 0;
     uint32_t bound_fail = 0;
     for (size_t i = 0; i < a.nq; ++i) {
         if (hflags[i] != scr::kOk) redo.push_back((int)i);
         if (hflags[i] == scr::kBoundFail) ++bound_fail;
-        cands += (uint64_t)hsurv[i];
+        c0 += (uint64_t)hcnt[i];
+        c1 += (uint64_t)hcnt[a.nq + i];
+        c2 += (uint64_t)hcnt[2 * a.nq + i];
     }
     if (st) {
-        st->candidates += cands;
+        st->candidates += c0;
+        st->survivors += c1;
+        st->reranked += c2;
         st->widened += (uint32_t)redo.size();
         st->bound_failures += bound_fail;
     }

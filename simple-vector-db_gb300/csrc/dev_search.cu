@@ -407,7 +407,12 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
         ++kernels;
     } else if (!use_bf16) {
         rc = search_fp64(s, a, kscr, kbytes, &kernels);
-        if (st && precision == SVDB_PREC_BF16) st->widened += (uint32_t)nq;
+        if (st) {
+            if (precision == SVDB_PREC_BF16) st->widened += (uint32_t)nq;
+            st->candidates += (uint64_t)nq * s->nlive;
+            st->survivors += (uint64_t)nq * s->nlive;
+            st->reranked += (uint64_t)nq * s->nlive;
+        }
     } else {
         rc = search_bf16(s, a, kscr, kbytes, st);
     }

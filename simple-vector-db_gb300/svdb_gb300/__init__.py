@@ -46,8 +46,9 @@ class Vector(C.Structure):
 
 
 class SearchStats(C.Structure):
-    _fields_ = [("candidates", C.c_uint64), ("widened", C.c_uint32), ("kernels", C.c_uint32),
-                ("max_err_bound", C.c_double), ("bound_failures", C.c_uint32), ("reserved", C.c_uint32)]
+    _fields_ = [("candidates", C.c_uint64), ("survivors", C.c_uint64), ("reranked", C.c_uint64),
+                ("widened", C.c_uint32), ("kernels", C.c_uint32), ("bound_failures", C.c_uint32),
+                ("reserved", C.c_uint32), ("max_err_bound", C.c_double)]
 
 
 class SvdbError(RuntimeError):
