@@ -283,7 +283,7 @@ def run_ours(args, ws, rank, local):
                            "l2": "store (6.1 GB FP64) larger than L2; no flush needed"},
                 "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
                 "stage_ms_per_step": {n: float(stage_ms[i] / max(ncalls, 1)) for i, n in
-                                      enumerate(["prep", "screen", "select", "rerank"])},
+                                      enumerate(["prep", "screen", "select", "refine", "rerank"])},
                 "plain_fp64_qps": plain,
                 "funnel_per_query": {"screen_candidates": st.candidates / nq, "survivors": st.survivors / nq,
                                      "fp64_reranked": st.reranked / nq, "widened_queries": st.widened,

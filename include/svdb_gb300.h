@@ -124,9 +124,10 @@ int svdb_sync(VectorDatabase* db);
  * i) and returns how many searches that covers, or a negative code. */
 #define SVDB_STAGE_PREP 0   /* query upload + padding + norms */
 #define SVDB_STAGE_SCREEN 1 /* FP64 streaming scan, or the BF16 tensor-core GEMM screen */
-#define SVDB_STAGE_SELECT 2 /* top-k merge, or shortlist selection */
-#define SVDB_STAGE_RERANK 3 /* FP64 re-rank of the shortlist (BF16 precision only) */
-#define SVDB_NSTAGES 4
+#define SVDB_STAGE_SELECT 2 /* top-k merge, or exact k-th lower-bound shortlist selection */
+#define SVDB_STAGE_REFINE 3 /* FP32 refinement of the shortlist (BF16 precision only) */
+#define SVDB_STAGE_RERANK 4 /* FP64 re-rank of what the refinement keeps (BF16 precision only) */
+#define SVDB_NSTAGES 5
 int svdb_profile(VectorDatabase* db, int enable);
 int svdb_profile_read(VectorDatabase* db, double* ms, int reset);
 

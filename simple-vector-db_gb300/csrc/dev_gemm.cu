@@ -1279,6 +1279,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                                              nsurv, flags);
     }
     SVDB_LAUNCH_CHECK();
+    s->prof_mark(3);
     const size_t ref_smem = (size_t)scr::kSurvCap * sizeof(float) + s->ld * sizeof(float) +
                             (size_t)(kRefThreads / 32) * 32 * sizeof(Entry);
     if (!gc->refine_attr) {
@@ -1289,7 +1290,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                                  qpar, surv, nsurv, nref, k, a.metric, flags);
     SVDB_LAUNCH_CHECK();
     kernels += 2;
-    s->prof_mark(3);
+    s->prof_mark(4);
 
     const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));
     const dim3 rgrid((unsigned)nq, (unsigned)L.splits);
@@ -1374,7 +1375,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         SVDB_CUDA(cudaStreamSynchronize(s->stream));  // redo (host vector) and the pinned lists go out of scope
         kernels += kk + 2;
     }
-    s->prof_mark(4);
+    s->prof_mark(5);
     if (st) st->kernels += kernels;
     return SVDB_OK;
 }

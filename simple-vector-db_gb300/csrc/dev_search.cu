@@ -416,7 +416,7 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     } else {
         rc = search_bf16(s, a, kscr, kbytes, st);
     }
-    s->prof_mark(4);
+    s->prof_mark(SVDB_NSTAGES);
     s->prof_end();
     if (rc) return rc;
     if (st) st->kernels += kernels;

@@ -33,8 +33,8 @@ CMP_ERRORS = {
     CMP_UNKNOWN_METHOD: (400, "Unknown comparison method"),
 }
 NOT_FOUND = 2**64 - 1  # (size_t)-1
-STAGE_PREP, STAGE_SCREEN, STAGE_SELECT, STAGE_RERANK = range(4)
-NSTAGES = 4
+STAGE_PREP, STAGE_SCREEN, STAGE_SELECT, STAGE_REFINE, STAGE_RERANK = range(5)
+NSTAGES = 5
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)
@@ -241,7 +241,7 @@ class VectorDatabase:
         _check(lib.svdb_profile(self.ptr, int(enable)), "svdb_profile")
 
     def profile_read(self, reset: bool = True):
-        """(searches covered, device ms per stage: prep, screen, select, rerank)."""
+        """(searches covered, device ms per stage: prep, screen, select, refine, rerank)."""
         ms = np.zeros(NSTAGES, np.float64)
         n = lib.svdb_profile_read(self.ptr, ms.ctypes.data_as(_dp), int(reset))
         if n < 0:
