@@ -73,6 +73,9 @@ struct Smem {
     // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
     uint8_t a[kStages][kStageA];
     uint8_t b[kStages][kStageB];
+    float4 rp[2][kBN];  // screen parameters of the store tile in the accumulator of the same index
+    uint64_t rp_full[2];
+    uint64_t rp_empty[2];
     uint64_t full[kStages];
     uint64_t empty[kStages];
     uint64_t accfull[2];
@@ -137,6 +140,13 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
             smem_u32(dst)),
         "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
         : "memory");
+}
+// plain bulk copy global -> shared (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
@@ -262,6 +272,8 @@ struct TopL {
 
 struct ScreenParams {
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
+    const float4* spar;  // per row {mult, b, m, 2^-19 m}: the screen's one-FMA form of the bound
+    const int* alpha;    // max over rows of a/b (float bits): |q| a <= |q| alpha b
     const float4* qpar;  // per query {qn, eqq, eq0, valid}
     int* tau;            // per query: shared lower bound of the k-th best key (ordered int)
     int* bins;           // per query, k bins: best chunk maximum of the chunks whose index % k is the bin
@@ -300,6 +312,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             mbar_init(&S.accempty[i], kEpiWarps);
         }
         mbar_init(&S.done, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&S.rp_full[i], 1);
+            mbar_init(&S.rp_empty[i], kEpiWarps);
+        }
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -320,8 +336,16 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             int stage = 0;
             uint32_t phase = 0;
             uint32_t issued = 0;  // loads issued (for draining on abort)
+            uint32_t rp_issued = 0;
             bool ok = true;
             for (int r = r0; r < r1 && ok; ++r) {
+                {  // the tile's screen parameters into the 2-slot ring (freed by the epilogue)
+                    const uint32_t jt = (uint32_t)(r - r0), slot = jt & 1u;
+                    if (!mbar_wait(&S.rp_empty[slot], ((jt >> 1) & 1u) ^ 1u, abort, kWaitLimitNs)) break;
+                    mbar_expect_tx(&S.rp_full[slot], kBN * sizeof(float4));
+                    bulk_load(S.rp[slot], P.spar + (size_t)r * kBN, kBN * sizeof(float4), &S.rp_full[slot]);
+                    ++rp_issued;
+                }
                 for (int kb = 0; kb < KB; ++kb) {
                     if (!mbar_wait(&S.empty[stage], phase ^ 1, abort, kWaitLimitNs)) {
                         ok = false;
@@ -340,10 +364,15 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // every issued load must have landed before the CTA may exit:
             // wait (bounded) for the completion of the last kStages loads
             const uint32_t last = issued < (uint32_t)kStages ? issued : (uint32_t)kStages;
+            volatile int no_abort = 0;
             for (uint32_t i = 0; i < last; ++i) {
                 const uint32_t n = issued - 1 - i;  // load number n went to stage n % S, phase (n / S) & 1
-                volatile int no_abort = 0;
                 mbar_wait(&S.full[n % kStages], (n / kStages) & 1u, &no_abort, kWaitLimitNs / 4);
+            }
+            const uint32_t rlast = rp_issued < 2u ? rp_issued : 2u;
+            for (uint32_t i = 0; i < rlast; ++i) {
+                const uint32_t n = rp_issued - 1 - i;
+                mbar_wait(&S.rp_full[n & 1u], (n >> 1) & 1u, &no_abort, kWaitLimitNs / 4);
             }
         }
     } else if (warp == 1) {
@@ -392,12 +421,11 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         const int half = (warp - 2) >> 2;
         const int qi = quad * 32 + lane;
         const int q = qt * kBM + qi;
-        float qn = 0.f, eqq = 0.f, eq0 = 0.f;
+        float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0
         bool valid = false;
         if (q < P.nq) {
             const float4 qp = P.qpar[q];
-            qn = qp.x;
-            eqq = qp.y;
+            eq = __fmaf_ru(qp.x, __int_as_float(__ldg(P.alpha)), qp.y);
             eq0 = qp.z;
             valid = qp.w != 0.f;
         }
@@ -410,12 +438,11 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         for (int r = r0; r < r1; ++r, ++j) {
             const int b = j & 1;
             const uint32_t use = (uint32_t)j >> 1;
-            // row parameters of this warp's 128 rows: every lane reads the same
-            // address (one L1 wavefront), so no shared staging or barrier
-            const float4* __restrict__ rps = P.rpar + (size_t)r * kBN + col0;
+            const float4* rps = S.rp[b] + col0;  // this warp's 128 rows, staged by the producer
             // tcgen05.ld is warp-collective (.sync.aligned): every branch that
             // leads to one must be taken by the whole warp, including this wait
-            const bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
+            bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
+            got = got && mbar_wait(&S.rp_full[b], use & 1u, abort, kWaitLimitNs);
             if (!__all_sync(0xffffffffu, got)) break;
             tc_fence_after();
             const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN + col0);
@@ -436,9 +463,9 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     float maxl = -INFINITY;
 #pragma unroll
                     for (int i = 0; i < kChunk; ++i) {
-                        const float4 p = __ldg(rc + i);
-                        const float l = __fsub_rd(__fmaf_rn(__uint_as_float(v[i]), p.x, -p.w),
-                                                  screen_bound(p, qn, eqq, eq0));
+                        const float4 p = rc[i];
+                        const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
+                        const float l = __fsub_rd(__fsub_rd(key, __fmaf_ru(eq, p.y, p.w)), eq0);
                         maxl = fmaxf(maxl, l);
                         if (valid && l > top.mn) top.push(l);
                     }
@@ -466,17 +493,20 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 tmem_ld_wait();
                 const float4* rc = rps + c * kChunk;
                 // branch-free pass: keys, the chunk's best lower bound, emission mask
+                // (the query's eq0 is folded into the threshold and the chunk maximum)
+                const float thr2 = __fsub_rd(thr, eq0);
                 float maxl = -INFINITY;
                 uint32_t mask = 0;
 #pragma unroll
                 for (int i = 0; i < kChunk; ++i) {
-                    const float4 p = __ldg(rc + i);
-                    const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.w);
-                    const float e = screen_bound(p, qn, eqq, eq0);
+                    const float4 p = rc[i];
+                    const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
+                    const float e = __fmaf_ru(eq, p.y, p.w);
                     maxl = fmaxf(maxl, __fsub_rd(key, e));
-                    mask |= (__fadd_ru(key, e) >= thr ? 1u : 0u) << i;
+                    mask |= (__fadd_ru(key, e) >= thr2 ? 1u : 0u) << i;
                     v[i] = __float_as_uint(key);
                 }
+                maxl = __fsub_rd(maxl, eq0);
                 if (mask && q < P.nq) {  // rows whose upper bound reaches the threshold
                     int slot = atomicAdd(&P.cnt[q], __popc(mask));
 #pragma unroll
@@ -501,7 +531,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&S.accempty[b]);
+            if (lane == 0) {
+                mbar_arrive(&S.accempty[b]);
+                mbar_arrive(&S.rp_empty[b]);
+            }
             if (valid && top.mn > published) {
                 atomicMax(&P.tau[q], f2ord(top.mn));
                 published = top.mn;
@@ -582,33 +615,51 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
 
 // Per-row screen parameters for one metric; rows >= nslots (tile padding),
 // dead slots and placeholder rows get NaN (never candidates).
-__global__ void k_row_params(const float4* __restrict__ rowp, const double* __restrict__ sq64,
-                             const uint8_t* __restrict__ live, int64_t nslots, int64_t npad, int metric,
-                             float4* __restrict__ rpar) {
+//   rpar = {mult, a, b, m}: the tight bound E = |q| a + eqq b + 2^-19 m + eq0
+//   spar = {mult, b, m, 2^-19 m}: the screen's one-FMA form, with a <= alpha b
+// alpha = max over rows of a / b (float bits, one atomic per block).  A row with
+// b = 0 has a = 0; rows where that fails are unscreenable and never reach here.
+__global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ rowp, const double* __restrict__ sq64,
+                                                    const uint8_t* __restrict__ live, int64_t nslots, int64_t npad,
+                                                    int metric, float4* __restrict__ rpar,
+                                                    float4* __restrict__ spar, int* __restrict__ alpha) {
+    __shared__ int wmax[8];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npad) return;
-    const float nan = __int_as_float(0x7fc00000);
-    float4 out = make_float4(nan, nan, nan, nan);
-    if (i < nslots && live[i] == 1) {
-        const float4 rp = rowp[i];  // {|x| up, |bx| up, |x - bx| up, |x|^2/2}
-        const double sq = sq64[i];
-        if (metric == SVDB_COSINE) {
-            if (sq > 0.0) {
-                const double ixn = 1.0 / sqrt(sq);
-                const double up = 1.0 + 9.313225746154785e-10;
-                out = make_float4(__double2float_rn(ixn), __double2float_ru((double)rp.z * ixn * up),
-                                  __double2float_ru((double)rp.y * ixn * up), 0.0f);
+    float ratio = 0.f;
+    if (i < npad) {
+        const float nan = __int_as_float(0x7fc00000);
+        float4 out = make_float4(nan, nan, nan, nan);
+        if (i < nslots && live[i] == 1) {
+            const float4 rp = rowp[i];  // {|x| up, |bx| up, |x - bx| up, |x|^2/2}
+            const double sq = sq64[i];
+            if (metric == SVDB_COSINE) {
+                if (sq > 0.0) {
+                    const double ixn = 1.0 / sqrt(sq);
+                    const double up = 1.0 + 9.313225746154785e-10;
+                    out = make_float4(__double2float_rn(ixn), __double2float_ru((double)rp.z * ixn * up),
+                                      __double2float_ru((double)rp.y * ixn * up), 0.0f);
+                }
+            } else if (metric == SVDB_DOT) {
+                out = make_float4(1.0f, rp.z, rp.y, 0.0f);
+            } else {
+                out = make_float4(1.0f, rp.z, rp.y, __double2float_rn(0.5 * sq));
             }
-        } else if (metric == SVDB_DOT) {
-            out = make_float4(1.0f, rp.z, rp.y, 0.0f);
-        } else {
-            out = make_float4(1.0f, rp.z, rp.y, __double2float_rn(0.5 * sq));
         }
+        rpar[i] = out;
+        spar[i] = make_float4(out.x, out.z, out.w, out.w * scr::kC2);
+        if (out.z > 0.f) ratio = __fdiv_ru(out.y, out.z);
     }
-    rpar[i] = out;
+    int r = __reduce_max_sync(0xffffffffu, __float_as_int(ratio));  // ratio >= 0: int order = float order
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = max(r, wmax[w]);
+        r = max(r, wmax[0]);
+        if (r > 0) atomicMax(alpha, r);
+    }
 }
 
-__global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int nq, int k, int* err) {
+__global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int nq, int k, int* err, int* alpha) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nq) {
         tau[i] = f2ord(-INFINITY);
@@ -616,7 +667,10 @@ __global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int
         cnt[i] = 0;
         flags[i] = scr::kOk;
     }
-    if (i == 0) *err = 0;
+    if (i == 0) {
+        *err = 0;
+        *alpha = 0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1140,7 +1194,7 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, q32, qpar, rpar, tau, bins, cnt, cand, surv, nsurv, nref, part, flags, err, total;
+    size_t qb, q32, qpar, rpar, spar, tau, bins, cnt, cand, surv, nsurv, nref, part, flags, err, alpha, total;
     int ntr, cap, splits;
     size_t npad;
 };
@@ -1159,6 +1213,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.q32 = take(nq * s->ld * sizeof(float));
     L.qpar = take(nq * sizeof(float4));
     L.rpar = take(L.npad * sizeof(float4));
+    L.spar = take(L.npad * sizeof(float4));
     L.tau = take(nq * sizeof(int));
     L.bins = take(nq * 32 * sizeof(int));
     L.cnt = take(nq * sizeof(int));
@@ -1176,6 +1231,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.part = take(nq * (size_t)L.splits * 32 * sizeof(Entry));
     L.flags = take(nq);
     L.err = take(sizeof(int));
+    L.alpha = take(sizeof(int));
     L.total = off;
     return L;
 }
@@ -1198,6 +1254,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     float* q32 = reinterpret_cast<float*>(base + L.q32);
     float4* qpar = reinterpret_cast<float4*>(base + L.qpar);
     float4* rpar = reinterpret_cast<float4*>(base + L.rpar);
+    float4* spar = reinterpret_cast<float4*>(base + L.spar);
+    int* alpha = reinterpret_cast<int*>(base + L.alpha);
     int* tau = reinterpret_cast<int*>(base + L.tau);
     int* bins = reinterpret_cast<int*>(base + L.bins);
     int* cnt = reinterpret_cast<int*>(base + L.cnt);
@@ -1214,11 +1272,11 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
                                                                           qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, flags, nq, k, derr, alpha);
+    SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
-                                                                          a.metric, rpar);
-    SVDB_LAUNCH_CHECK();
-    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, flags, nq, k, derr);
+                                                                          a.metric, rpar, spar, alpha);
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
@@ -1229,6 +1287,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     ScreenParams P;
     P.rpar = rpar;
+    P.spar = spar;
+    P.alpha = alpha;
     P.qpar = qpar;
     P.tau = tau;
     P.bins = bins;

@@ -86,7 +86,7 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
         p.w = __double2float_rn(0.5 * sq);
         // rows the BF16 screen cannot bound (overflow, non-finite): mark them
         // always-candidate with an infinite error term; dead slots: |x| = -1
-        if (!(sq < 1e30) || !isfinite(p.y)) p.z = __int_as_float(0x7f800000);
+        if (!(sq < 1e30) || !isfinite(p.y) || (bh == 0.0 && res > 0.0)) p.z = __int_as_float(0x7f800000);
         if (live[slot] != 1) p.x = -1.0f;
         rowp[slot] = p;
     }
