@@ -274,6 +274,8 @@ struct ScreenParams {
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
     const float4* spar;  // per row {mult, b, m, 2^-19 m}: the screen's one-FMA form of the bound
     const int* alpha;    // max over rows of a/b (float bits): |q| a <= |q| alpha b
+    const uint32_t* vbits;  // cosine: 1 bit per row (searchable with |x| > 0), whole 256-row tiles
+    const int* nmax;        // cosine: {max |x/|x| - bxn|, max |bxn|} over the store (float bits)
     const float4* qpar;  // per query {qn, eqq, eq0, valid}
     int* tau;            // per query: shared lower bound of the k-th best key (ordered int)
     int* bins;           // per query, k bins: best chunk maximum of the chunks whose index % k is the bin
@@ -287,7 +289,12 @@ struct ScreenParams {
     int kblocks;  // ldb / 64
 };
 
-template <int KL>
+// NORM (cosine): the B operand is the unit-norm shadow, so the key is the
+// accumulator itself and the bound is one constant per query,
+//   E = |q| max|x/|x| - bxn| + eqq max|bxn| + eq0;
+// the epilogue is a max, a compare and a mask per element, and a validity
+// bit per row keeps dead, zero and padding rows out of the lower bounds.
+template <int KL, bool NORM>
 __global__ void __launch_bounds__(scr::kThreads, 1)
     k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
                   const ScreenParams P) {
@@ -339,7 +346,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             uint32_t rp_issued = 0;
             bool ok = true;
             for (int r = r0; r < r1 && ok; ++r) {
-                {  // the tile's screen parameters into the 2-slot ring (freed by the epilogue)
+                if (!NORM) {  // the tile's screen parameters into the 2-slot ring (freed by the epilogue)
                     const uint32_t jt = (uint32_t)(r - r0), slot = jt & 1u;
                     if (!mbar_wait(&S.rp_empty[slot], ((jt >> 1) & 1u) ^ 1u, abort, kWaitLimitNs)) break;
                     mbar_expect_tx(&S.rp_full[slot], kBN * sizeof(float4));
@@ -421,12 +428,17 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         const int half = (warp - 2) >> 2;
         const int qi = quad * 32 + lane;
         const int q = qt * kBM + qi;
-        float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0
+        float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0 (NORM: eq0 = E)
         bool valid = false;
         if (q < P.nq) {
             const float4 qp = P.qpar[q];
-            eq = __fmaf_ru(qp.x, __int_as_float(__ldg(P.alpha)), qp.y);
-            eq0 = qp.z;
+            if (NORM) {
+                eq0 = __fmaf_ru(qp.x, __int_as_float(__ldg(P.nmax)),
+                                __fmaf_ru(qp.y, __int_as_float(__ldg(P.nmax + 1)), qp.z));
+            } else {
+                eq = __fmaf_ru(qp.x, __int_as_float(__ldg(P.alpha)), qp.y);
+                eq0 = qp.z;
+            }
             valid = qp.w != 0.f;
         }
         TopL<KL> top;
@@ -442,7 +454,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // tcgen05.ld is warp-collective (.sync.aligned): every branch that
             // leads to one must be taken by the whole warp, including this wait
             bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
-            got = got && mbar_wait(&S.rp_full[b], use & 1u, abort, kWaitLimitNs);
+            if (!NORM) got = got && mbar_wait(&S.rp_full[b], use & 1u, abort, kWaitLimitNs);
             if (!__all_sync(0xffffffffu, got)) break;
             tc_fence_after();
             const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN + col0);
@@ -461,13 +473,25 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     tmem_ld_wait();
                     const float4* rc = rps + c * kChunk;
                     float maxl = -INFINITY;
+                    if (NORM) {
+                        const int rw = row0 + c * kChunk;
+                        const uint32_t vb = __ldg(P.vbits + (rw >> 5)) >> (rw & 31);
 #pragma unroll
-                    for (int i = 0; i < kChunk; ++i) {
-                        const float4 p = rc[i];
-                        const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
-                        const float l = __fsub_rd(__fsub_rd(key, __fmaf_ru(eq, p.y, p.w)), eq0);
-                        maxl = fmaxf(maxl, l);
-                        if (valid && l > top.mn) top.push(l);
+                        for (int i = 0; i < kChunk; ++i) {
+                            // masked rows are NaN: every comparison with them is false
+                            const float l = ((vb >> i) & 1u) ? __fsub_rd(__uint_as_float(v[i]), eq0) : __int_as_float(0x7fc00000);
+                            maxl = fmaxf(maxl, l);
+                            if (valid && l > top.mn) top.push(l);
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < kChunk; ++i) {
+                            const float4 p = rc[i];
+                            const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
+                            const float l = __fsub_rd(__fsub_rd(key, __fmaf_ru(eq, p.y, p.w)), eq0);
+                            maxl = fmaxf(maxl, l);
+                            if (valid && l > top.mn) top.push(l);
+                        }
                     }
                     if (valid && maxl > -INFINITY) {
                         const int chunk = (row0 + c * kChunk) / kChunk;
@@ -497,14 +521,35 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 const float thr2 = __fsub_rd(thr, eq0);
                 float maxl = -INFINITY;
                 uint32_t mask = 0;
+                if (NORM) {
+                    const int rw = row0 + c * kChunk;
+                    const uint32_t vb = (__ldg(P.vbits + (rw >> 5)) >> (rw & 31)) & 0xFFFFu;
+                    if (vb == 0xFFFFu) {  // every row of the chunk is searchable (warp-uniform)
 #pragma unroll
-                for (int i = 0; i < kChunk; ++i) {
-                    const float4 p = rc[i];
-                    const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
-                    const float e = __fmaf_ru(eq, p.y, p.w);
-                    maxl = fmaxf(maxl, __fsub_rd(key, e));
-                    mask |= (__fadd_ru(key, e) >= thr2 ? 1u : 0u) << i;
-                    v[i] = __float_as_uint(key);
+                        for (int i = 0; i < kChunk; ++i) {
+                            const float g = __uint_as_float(v[i]);
+                            maxl = fmaxf(maxl, g);
+                            mask |= (g >= thr2 ? 1u : 0u) << i;
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < kChunk; ++i) {
+                            // NaN, not -inf: -inf >= thr2 holds while thr2 is still -inf
+                            const float g = ((vb >> i) & 1u) ? __uint_as_float(v[i]) : __int_as_float(0x7fc00000);
+                            maxl = fmaxf(maxl, g);
+                            mask |= (g >= thr2 ? 1u : 0u) << i;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < kChunk; ++i) {
+                        const float4 p = rc[i];
+                        const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
+                        const float e = __fmaf_ru(eq, p.y, p.w);
+                        maxl = fmaxf(maxl, __fsub_rd(key, e));
+                        mask |= (__fadd_ru(key, e) >= thr2 ? 1u : 0u) << i;
+                        v[i] = __float_as_uint(key);
+                    }
                 }
                 maxl = __fsub_rd(maxl, eq0);
                 if (mask && q < P.nq) {  // rows whose upper bound reaches the threshold
@@ -533,7 +578,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             __syncwarp();
             if (lane == 0) {
                 mbar_arrive(&S.accempty[b]);
-                mbar_arrive(&S.rp_empty[b]);
+                if (!NORM) mbar_arrive(&S.rp_empty[b]);
             }
             if (valid && top.mn > published) {
                 atomicMax(&P.tau[q], f2ord(top.mn));
@@ -617,38 +662,42 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
 // dead slots and placeholder rows get NaN (never candidates).
 //   rpar = {mult, a, b, m}: the tight bound E = |q| a + eqq b + 2^-19 m + eq0
 //   spar = {mult, b, m, 2^-19 m}: the screen's one-FMA form, with a <= alpha b
+//   vbits: 1 bit per row whose parameters are finite (the cosine screen's mask)
 // alpha = max over rows of a / b (float bits, one atomic per block).  A row with
 // b = 0 has a = 0; rows where that fails are unscreenable and never reach here.
+// Cosine runs on the unit-norm shadow: key = q . x/|x|, a = |x/|x| - bxn|,
+// b = |bxn| (zero rows: NaN, their cosine is NaN and ranks last).
 __global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ rowp, const double* __restrict__ sq64,
                                                     const uint8_t* __restrict__ live, int64_t nslots, int64_t npad,
-                                                    int metric, float4* __restrict__ rpar,
-                                                    float4* __restrict__ spar, int* __restrict__ alpha) {
+                                                    int metric, const float2* __restrict__ rowpn,
+                                                    float4* __restrict__ rpar, float4* __restrict__ spar,
+                                                    int* __restrict__ alpha, uint32_t* __restrict__ vbits) {
     __shared__ int wmax[8];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float nan = __int_as_float(0x7fc00000);
+    float4 out = make_float4(nan, nan, nan, nan);
+    if (i < nslots && live[i] == 1) {
+        const float4 rp = rowp[i];  // {|x| up, |bx| up, |x - bx| up, |x|^2/2}
+        const double sq = sq64[i];
+        if (metric == SVDB_COSINE) {
+            if (sq > 0.0) {
+                const float2 pn = rowpn[i];
+                out = make_float4(1.0f, pn.y, pn.x, 0.0f);
+            }
+        } else if (metric == SVDB_DOT) {
+            out = make_float4(1.0f, rp.z, rp.y, 0.0f);
+        } else {
+            out = make_float4(1.0f, rp.z, rp.y, __double2float_rn(0.5 * sq));
+        }
+    }
     float ratio = 0.f;
     if (i < npad) {
-        const float nan = __int_as_float(0x7fc00000);
-        float4 out = make_float4(nan, nan, nan, nan);
-        if (i < nslots && live[i] == 1) {
-            const float4 rp = rowp[i];  // {|x| up, |bx| up, |x - bx| up, |x|^2/2}
-            const double sq = sq64[i];
-            if (metric == SVDB_COSINE) {
-                if (sq > 0.0) {
-                    const double ixn = 1.0 / sqrt(sq);
-                    const double up = 1.0 + 9.313225746154785e-10;
-                    out = make_float4(__double2float_rn(ixn), __double2float_ru((double)rp.z * ixn * up),
-                                      __double2float_ru((double)rp.y * ixn * up), 0.0f);
-                }
-            } else if (metric == SVDB_DOT) {
-                out = make_float4(1.0f, rp.z, rp.y, 0.0f);
-            } else {
-                out = make_float4(1.0f, rp.z, rp.y, __double2float_rn(0.5 * sq));
-            }
-        }
         rpar[i] = out;
         spar[i] = make_float4(out.x, out.z, out.w, out.w * scr::kC2);
         if (out.z > 0.f) ratio = __fdiv_ru(out.y, out.z);
     }
+    const unsigned vb = __ballot_sync(0xffffffffu, !isnan(out.x));
+    if ((threadIdx.x & 31) == 0 && i < npad) vbits[i >> 5] = vb;  // npad is a multiple of 256
     int r = __reduce_max_sync(0xffffffffu, __float_as_int(ratio));  // ratio >= 0: int order = float order
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = r;
     __syncthreads();
@@ -756,7 +805,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     for (int i = threadIdx.x; i < n; i += bd) {
         const int2 c = cq[i];
         const float U = __fadd_ru(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
-        if (f2u_ord(U) >= thr_ord) {
+        if (!isnan(U) && f2u_ord(U) >= thr_ord) {  // rows with NaN parameters never survive
             const int o = atomicAdd(&s_out, 1);
             if (o < scr::kSurvCap) sq[o] = c;
         }
@@ -854,9 +903,10 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
                 key = 0.5 * ((qq + xs) - S);
                 e = 0.5 * (double)ed2;
             } else {
-                const double mult = (double)rpar[row].x;  // 1/|x| to 2^-24 relative
+                // 1/|x| in FP32: relative error <= 2^-22 (conversion, sqrt, reciprocal)
+                const double mult = (double)__frcp_rn(__fsqrt_rn(__double2float_rn(xs)));
                 key = 0.5 * ((qq + xs) - S) * mult;
-                e = 0.5 * (double)ed2 * mult * (1.0 + 2.384185791015625e-07) + fabs(key) * 2.384185791015625e-07;
+                e = 0.5 * (double)ed2 * mult * (1.0 + 4.76837158203125e-07) + fabs(key) * 4.76837158203125e-07;
             }
             L = key - e;
             ur[i] = __double2float_ru(key + e);
@@ -1141,7 +1191,7 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 // ---------------------------------------------------------------------------
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    bool attr_set[2] = {false, false};
+    bool attr_set[4] = {false, false, false, false};
     bool refine_attr = false;
     bool select_attr = false;
     size_t screen_smem = 0;
@@ -1194,7 +1244,7 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, q32, qpar, rpar, spar, tau, bins, cnt, cand, surv, nsurv, nref, part, flags, err, alpha, total;
+    size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, part, flags, err, alpha, total;
     int ntr, cap, splits;
     size_t npad;
 };
@@ -1214,6 +1264,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.qpar = take(nq * sizeof(float4));
     L.rpar = take(L.npad * sizeof(float4));
     L.spar = take(L.npad * sizeof(float4));
+    L.vbits = take(L.npad / 8);
     L.tau = take(nq * sizeof(int));
     L.bins = take(nq * 32 * sizeof(int));
     L.cnt = take(nq * sizeof(int));
@@ -1256,6 +1307,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     float4* rpar = reinterpret_cast<float4*>(base + L.rpar);
     float4* spar = reinterpret_cast<float4*>(base + L.spar);
     int* alpha = reinterpret_cast<int*>(base + L.alpha);
+    uint32_t* vbits = reinterpret_cast<uint32_t*>(base + L.vbits);
     int* tau = reinterpret_cast<int*>(base + L.tau);
     int* bins = reinterpret_cast<int*>(base + L.bins);
     int* cnt = reinterpret_cast<int*>(base + L.cnt);
@@ -1276,19 +1328,22 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
-                                                                          a.metric, rpar, spar, alpha);
+                                                                          a.metric, s->rowpn, rpar, spar, alpha, vbits);
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
     CUtensorMap tmq, tmx;
     rc = make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
-    if (!rc) rc = make_map(gc, &tmx, s->xb, s->slots, s->ldb, scr::kBN);
+    const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
+    if (!rc) rc = make_map(gc, &tmx, norm ? s->xbn : s->xb, s->slots, s->ldb, scr::kBN);
     if (rc) return rc;
 
     ScreenParams P;
     P.rpar = rpar;
     P.spar = spar;
     P.alpha = alpha;
+    P.vbits = vbits;
+    P.nmax = s->d_count + 1;
     P.qpar = qpar;
     P.tau = tau;
     P.bins = bins;
@@ -1304,20 +1359,16 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     const int G = num_sms();
     P.rgroups = std::max(1, std::min(G / std::max(P.ntq, 1), P.ntr));
     const unsigned grid = (unsigned)(P.ntq * P.rgroups);
-    const int kl = k <= 16 ? 0 : 1;
-    if (!gc->attr_set[kl]) {
-        if (kl == 0)
-            SVDB_CUDA(cudaFuncSetAttribute(k_screen_bf16<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)gc->screen_smem));
-        else
-            SVDB_CUDA(cudaFuncSetAttribute(k_screen_bf16<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)gc->screen_smem));
-        gc->attr_set[kl] = true;
+    {
+        auto kern = k <= 16 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
+                            : (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>);
+        const int v = (k <= 16 ? 0 : 2) + (norm ? 1 : 0);
+        if (!gc->attr_set[v]) {
+            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
+            gc->attr_set[v] = true;
+        }
+        kern<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, tmx, P);
     }
-    if (kl == 0)
-        k_screen_bf16<16><<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, tmx, P);
-    else
-        k_screen_bf16<32><<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, tmx, P);
     SVDB_LAUNCH_CHECK();
     ++kernels;
     s->prof_mark(2);

@@ -5,6 +5,8 @@
 //   x64     C x ld   double   FP64 master, ld = D rounded up to 16 (128-B rows)
 //   xb      C x ldb  bf16     BF16 shadow of x64, ldb = D rounded up to 64
 //   x32     C x ld   float    FP32 shadow of x64 (refinement stage)
+//   xbn     C x ldb  bf16     BF16 shadow of x64 / |x| (cosine screen)
+//   rowpn   C        float2   {|bxn| up, |x/|x| - bxn| up}
 //   sq64    C        double   canonical sum of squares of the master row
 //   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
 //   live    C        uint8    1 = searchable row, 2 = row of another dimension
@@ -42,7 +44,8 @@ namespace svdb {
 // Derived per-row arrays for slots [lo, hi) or for an explicit slot list.
 // One group of 4 lanes per row, canonical order for the sum of squares.
 __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bfloat16* __restrict__ xb,
-                              size_t ldb, float* __restrict__ x32, double* __restrict__ sq64, float4* __restrict__ rowp,
+                              size_t ldb, float* __restrict__ x32, __nv_bfloat16* __restrict__ xbn,
+                              float2* __restrict__ rowpn, double* __restrict__ sq64, float4* __restrict__ rowp,
                               const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
                               const int64_t* __restrict__ list) {
     const int lane = threadIdx.x & 31, s = lane & 3;
@@ -77,7 +80,34 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     sq = group4_sum(sq);
     bh = group4_sum(bh);
     res = group4_sum(res);
+    // second pass: the unit-norm row for the cosine screen, its BF16 copy and residual
+    double nbh = 0.0, nres = 0.0;
+    if (active) {
+        const double ixn = sq > 0.0 ? 1.0 / sqrt(sq) : 0.0;
+        __nv_bfloat16* xn = xbn + slot * ldb;
+        for (size_t j = 2 * s; j < ld; j += 8) {
+            const double2 v = *reinterpret_cast<const double2*>(x + j);
+            const double ux = v.x * ixn, uy = v.y * ixn;
+            const __nv_bfloat16 hx = __double2bfloat16(ux), hy = __double2bfloat16(uy);
+            const double fx = (double)__bfloat162float(hx), fy = (double)__bfloat162float(hy);
+            nbh = fma(fx, fx, nbh);
+            nbh = fma(fy, fy, nbh);
+            nres = fma(ux - fx, ux - fx, nres);
+            nres = fma(uy - fy, uy - fy, nres);
+            xn[j] = hx;
+            xn[j + 1] = hy;
+        }
+        for (size_t j = ld + 2 * s; j < ldb; j += 8) {
+            xn[j] = __float2bfloat16(0.0f);
+            xn[j + 1] = __float2bfloat16(0.0f);
+        }
+    }
+    nbh = group4_sum(nbh);
+    nres = group4_sum(nres);
     if (active && s == 0) {
+        // x/|x| is itself rounded (relative 2^-52 per element): the 2^-30 margin covers it
+        const double up = 1.0 + 9.313225746154785e-10;
+        rowpn[slot] = make_float2(__double2float_ru(sqrt(nbh) * up), __double2float_ru(sqrt(nres) * up + 1e-300));
         sq64[slot] = sq;
         float4 p;
         p.x = __double2float_ru(sqrt(sq));
@@ -142,13 +172,26 @@ __global__ void k_logical_map(const uint8_t* __restrict__ live, int64_t n, int64
 }
 
 // live rows whose BF16 screen terms are unbounded (marked +inf by k_derive_rows)
-__global__ void k_count_unscreenable(const float4* __restrict__ rowp, const uint8_t* __restrict__ live, int64_t n,
-                                     int* __restrict__ count) {
-    int c = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        c += (live[i] == 1 && !(rowp[i].z < 3.0e38f)) ? 1 : 0;
+// ... and the store-wide maxima of the unit-norm shadow's residual and norm
+// (count[1], count[2], float bits; non-negative floats order as ints)
+__global__ void k_count_unscreenable(const float4* __restrict__ rowp, const float2* __restrict__ rowpn,
+                                     const uint8_t* __restrict__ live, int64_t n, int* __restrict__ count) {
+    int c = 0, ra = 0, rb = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (live[i] != 1) continue;
+        c += !(rowp[i].z < 3.0e38f) ? 1 : 0;
+        const float2 pn = rowpn[i];
+        ra = max(ra, __float_as_int(pn.y));
+        rb = max(rb, __float_as_int(pn.x));
+    }
     c = __reduce_add_sync(0xffffffffu, c);
-    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+    ra = __reduce_max_sync(0xffffffffu, ra);
+    rb = __reduce_max_sync(0xffffffffu, rb);
+    if ((threadIdx.x & 31) == 0) {
+        if (c) atomicAdd(count, c);
+        atomicMax(count + 1, ra);
+        atomicMax(count + 2, rb);
+    }
 }
 
 __global__ void k_set_live(uint8_t* live, const int64_t* slots, int n, uint8_t v) {
@@ -269,7 +312,7 @@ int Store::ensure() {
     }
     cudaStream_t st = nullptr;
     SVDB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, sizeof(int)) != cudaSuccess) {
+    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, 4 * sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         cudaStreamDestroy(st);
         svdb_set_error("device store: cannot allocate a counter");
@@ -288,6 +331,8 @@ int Store::grow(size_t need) {
     double* nx = nullptr;
     __nv_bfloat16* nb = nullptr;
     float* nf = nullptr;
+    __nv_bfloat16* nbn = nullptr;
+    float2* npn = nullptr;
     double* nsq = nullptr;
     float4* np = nullptr;
     uint8_t* nl = nullptr;
@@ -296,6 +341,8 @@ int Store::grow(size_t need) {
     if (e == cudaSuccess) e = cudaMalloc(&nx, nc * ld * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&nb, nc * ldb * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc(&nf, nc * ld * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&nbn, nc * ldb * sizeof(__nv_bfloat16));
+    if (e == cudaSuccess) e = cudaMalloc(&npn, nc * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nl, nc);
@@ -305,6 +352,8 @@ int Store::grow(size_t need) {
         cudaFree(nx);
         cudaFree(nb);
         cudaFree(nf);
+        cudaFree(nbn);
+        cudaFree(npn);
         cudaFree(nsq);
         cudaFree(np);
         cudaFree(nl);
@@ -316,6 +365,8 @@ int Store::grow(size_t need) {
         SVDB_CUDA(cudaMemcpyAsync(nx, x64, slots * ld * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nb, xb, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nf, x32, slots * ld * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nbn, xbn, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(npn, rowpn, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nl, live, slots, cudaMemcpyDeviceToDevice, stream));
@@ -325,6 +376,8 @@ int Store::grow(size_t need) {
     cudaFree(x64);
     cudaFree(xb);
     cudaFree(x32);
+    cudaFree(xbn);
+    cudaFree(rowpn);
     cudaFree(sq64);
     cudaFree(rowp);
     cudaFree(live);
@@ -332,6 +385,8 @@ int Store::grow(size_t need) {
     x64 = nx;
     xb = nb;
     x32 = nf;
+    xbn = nbn;
+    rowpn = npn;
     sq64 = nsq;
     rowp = np;
     live = nl;
@@ -424,7 +479,7 @@ int Store::sync() {
         const int64_t n = derive_hi - derive_lo;
         const int threads = 256;
         const int64_t blocks = (n * 4 + threads - 1) / threads;
-        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, sq64, rowp, live, derive_lo,
+        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sq64, rowp, live, derive_lo,
                                                               derive_hi, nullptr);
         SVDB_LAUNCH_CHECK();
     }
@@ -436,7 +491,7 @@ int Store::sync() {
         if (rc) return rc;
         d = (int64_t*)scratch;
         SVDB_CUDA(cudaMemcpyAsync(d, dirty_list.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
-        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, sq64, rowp, live, 0,
+        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sq64, rowp, live, 0,
                                                                          n, d);
         SVDB_LAUNCH_CHECK();
         SVDB_CUDA(cudaStreamSynchronize(stream));
@@ -445,9 +500,9 @@ int Store::sync() {
     if (map_dirty && slots) {
         k_logical_map<<<1, 1024, 0, stream>>>(live, (int64_t)slots, logical, d_nlive);
         SVDB_LAUNCH_CHECK();
-        SVDB_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
+        SVDB_CUDA(cudaMemsetAsync(d_count, 0, 3 * sizeof(int), stream));
         k_count_unscreenable<<<(unsigned)std::min<size_t>((slots + 255) / 256, 1024), 256, 0, stream>>>(
-            rowp, live, (int64_t)slots, d_count);
+            rowp, rowpn, live, (int64_t)slots, d_count);
         SVDB_LAUNCH_CHECK();
         int hc = 0;
         SVDB_CUDA(cudaMemcpyAsync(&h_nlive, d_nlive, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
@@ -493,6 +548,8 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->x64);
     cudaFree(s->xb);
     cudaFree(s->x32);
+    cudaFree(s->xbn);
+    cudaFree(s->rowpn);
     cudaFree(s->sq64);
     cudaFree(s->rowp);
     cudaFree(s->live);

@@ -24,6 +24,9 @@ struct Store {
     double* x64 = nullptr;
     __nv_bfloat16* xb = nullptr;
     float* x32 = nullptr;  // FP32 shadow (cap x ld), read by the refinement stage
+    __nv_bfloat16* xbn = nullptr;  // BF16 shadow of x / |x| (cap x ldb): the cosine screen
+    float2* rowpn = nullptr;       // {|bxn| up, |x/|x| - bxn| up} per row
+    int* d_nmax = nullptr;         // {max |x/|x| - bxn|, max |bxn|} over searchable rows (float bits)
     double* sq64 = nullptr;
     float4* rowp = nullptr;  // {|x| up (-1: dead slot), |bf16 x| up, |x - bf16 x| up (inf: unscreenable), |x|^2/2}
     uint8_t* live = nullptr;

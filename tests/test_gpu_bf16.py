@@ -158,3 +158,36 @@ def test_bf16_values_within_fp64_tolerance(S, oracle):
                 assert abs(vals[qi, j] - s) <= 1e-12 * max(1.0, abs(s))
                 assert abs(vals[qi, j] - s) <= err[qi, j] + abs(s) * 2**-52
     db.close()
+
+
+def test_bf16_cosine_dead_and_zero_rows(S, oracle):
+    """The cosine screen masks rows that are deleted, zero (cosine NaN, ranked
+    last) or tile padding; none may be emitted or lower a threshold, even while
+    the running threshold is still -inf."""
+    rng = np.random.default_rng(29)
+    X = rng.normal(size=(1000, 64))
+    X[[3, 300, 301]] = 0.0
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    host = list(X)
+    for _ in range(250):  # empty most of the first 256-row tile
+        db.delete(0)
+        host.pop(0)
+    H = np.stack(host)
+    Q = rng.normal(size=(9, 64))
+    for k in (1, 5, 32):
+        ids, vals, st = _search_both(S, db, Q, k, 0)
+        wid, wval = oracle.topk(0, H, Q, k)
+        assert np.array_equal(ids, wid) and np.array_equal(vals, wval), k
+        assert st.bound_failures == 0
+    # tiny store: 10 live rows, 2 of them zero -> the k=10 answer has NaN tails
+    small = S.VectorDatabase(0, 3)
+    Y = rng.normal(size=(10, 16))
+    Y[[2, 7]] = 0.0
+    small.insert_batch(Y)
+    ids, vals, st = _search_both(S, small, Y[:3] + 0.1, 10, 0)
+    wid, wval = oracle.topk(0, Y, Y[:3] + 0.1, 10)
+    assert np.array_equal(ids, wid)
+    assert ((vals == wval) | (np.isnan(vals) & np.isnan(wval))).all()
+    small.close()
+    db.close()
