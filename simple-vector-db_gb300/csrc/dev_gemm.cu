@@ -738,11 +738,11 @@ template <int KL>
 __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
                                                  const float4* __restrict__ rpar, const float4* __restrict__ qpar,
                                                  int k, int2* __restrict__ surv, int* __restrict__ nsurv,
-                                                 uint8_t* __restrict__ flags) {
+                                                 int* __restrict__ sig, uint8_t* __restrict__ flags) {
     extern __shared__ uint32_t vals[];  // blockDim.x * k ordered lower bounds
     __shared__ int hist[256];
     __shared__ uint32_t s_prefix, s_mask;
-    __shared__ int s_rank, s_out;
+    __shared__ int s_rank, s_out, s_sig;
     const int q = blockIdx.x;
     const float4 qp = qpar[q];
     const int n = cnt[q];
@@ -750,6 +750,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         if (threadIdx.x == 0) {
             flags[q] = qp.w == 0.f ? scr::kInvalidQuery : scr::kOverflow;
             nsurv[q] = 0;
+            sig[q] = 0x7fffffff;
         }
         return;
     }
@@ -770,6 +771,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         s_mask = 0;
         s_rank = k;
         s_out = 0;
+        s_sig = 0x7fffffff;
     }
     __syncthreads();
     const int m = bd * k;
@@ -808,13 +810,45 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         if (!isnan(U) && f2u_ord(U) >= thr_ord) {  // rows with NaN parameters never survive
             const int o = atomicAdd(&s_out, 1);
             if (o < scr::kSurvCap) sq[o] = c;
+            atomicMin(&s_sig, c.x);
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        sig[q] = s_sig;
         nsurv[q] = s_out;
         if (s_out > scr::kSurvCap) flags[q] = scr::kOverflow;
     }
+}
+
+// Order of the refinement blocks: queries sorted by their survivor signature
+// (smallest surviving row), so queries that share their survivors -- near-tie
+// clusters -- are refined by blocks that run at the same time and hit each
+// other's rows in L2.  One block, bitonic sort of (signature, query) in shared
+// memory; n is a power of two >= nq (pad keys sort last).
+__global__ void __launch_bounds__(1024) k_sort_queries(const int* __restrict__ sig, int nq, int n,
+                                                        int* __restrict__ perm) {
+    extern __shared__ unsigned long long keys[];
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        keys[i] = i < nq ? ((unsigned long long)(uint32_t)sig[i] << 32) | (uint32_t)i : ~0ull;
+    __syncthreads();
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const unsigned long long a = keys[i], b = keys[j];
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[j] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) perm[i] = (int)(keys[i] & 0xffffffffu);
 }
 
 // ---------------------------------------------------------------------------
@@ -839,7 +873,8 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
                                                         const float4* __restrict__ rpar,
                                                         const float4* __restrict__ qpar, int2* __restrict__ surv,
                                                         const int* __restrict__ nsurv, int* __restrict__ nref, int k,
-                                                        int metric, uint8_t* __restrict__ flags) {
+                                                        int metric, const int* __restrict__ perm,
+                                                        uint8_t* __restrict__ flags) {
     extern __shared__ __align__(16) uint8_t sm[];
     float* ur = reinterpret_cast<float*>(sm);  // refined upper bound per survivor
     float* qs = ur + scr::kSurvCap;            // the query in FP32 (ld floats, 16-float multiple)
@@ -847,7 +882,7 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
     __shared__ double s_tau;
     __shared__ int s_out;
     constexpr int kWarps = kRefThreads / 32;
-    const int q = blockIdx.x;
+    const int q = perm ? perm[blockIdx.x] : blockIdx.x;
     if (flags[q] != scr::kOk) {
         if (threadIdx.x == 0) nref[q] = 0;
         return;
@@ -1194,6 +1229,7 @@ struct GemmPlanCache {
     bool attr_set[4] = {false, false, false, false};
     bool refine_attr = false;
     bool select_attr = false;
+    bool sort_attr = false;
     size_t screen_smem = 0;
 };
 
@@ -1244,7 +1280,8 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, part, flags, err, alpha, total;
+    size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, part, flags, err,
+        alpha, total;
     int ntr, cap, splits;
     size_t npad;
 };
@@ -1277,6 +1314,8 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.surv = take(nq * (size_t)scr::kSurvCap * sizeof(int2));
     L.nsurv = take(nq * sizeof(int));
     L.nref = take(nq * sizeof(int));
+    L.sig = take(nq * sizeof(int));
+    L.perm = take(nq * sizeof(int));
     // re-rank splits: spread small batches over the SMs
     L.splits = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(2 * num_sms()) / std::max<size_t>(nq, 1)));
     L.part = take(nq * (size_t)L.splits * 32 * sizeof(Entry));
@@ -1315,6 +1354,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     int2* surv = reinterpret_cast<int2*>(base + L.surv);
     int* nsurv = reinterpret_cast<int*>(base + L.nsurv);
     int* nref = reinterpret_cast<int*>(base + L.nref);
+    int* sig = reinterpret_cast<int*>(base + L.sig);
+    int* perm = reinterpret_cast<int*>(base + L.perm);
     Entry* part = reinterpret_cast<Entry*>(base + L.part);
     uint8_t* flags = base + L.flags;
     int* derr = reinterpret_cast<int*>(base + L.err);
@@ -1384,10 +1425,10 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         }
         if (k <= 16)
             k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
-                                                                             nsurv, flags);
+                                                                             nsurv, sig, flags);
         else
             k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
-                                                                             nsurv, flags);
+                                                                             nsurv, sig, flags);
     }
     SVDB_LAUNCH_CHECK();
     s->prof_mark(3);
@@ -1397,8 +1438,23 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         SVDB_CUDA(cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         gc->refine_attr = true;
     }
+    // refinement order (batches of up to 16384 queries are sorted; larger ones keep index order)
+    const int* order = nullptr;
+    if (nq > 1 && nq <= 16384) {
+        int n2 = 1;
+        while (n2 < nq) n2 <<= 1;
+        if (!gc->sort_attr) {
+            SVDB_CUDA(cudaFuncSetAttribute(k_sort_queries, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           16384 * (int)sizeof(unsigned long long)));
+            gc->sort_attr = true;
+        }
+        k_sort_queries<<<1, 1024, (size_t)n2 * sizeof(unsigned long long), s->stream>>>(sig, nq, n2, perm);
+        SVDB_LAUNCH_CHECK();
+        ++kernels;
+        order = perm;
+    }
     k_refine<<<(unsigned)nq, kRefThreads, ref_smem, s->stream>>>(s->x32, s->ld, q32, a.qsq, s->sq64, s->rowp, rpar,
-                                                                 qpar, surv, nsurv, nref, k, a.metric, flags);
+                                                                 qpar, surv, nsurv, nref, k, a.metric, order, flags);
     SVDB_LAUNCH_CHECK();
     kernels += 2;
     s->prof_mark(4);
