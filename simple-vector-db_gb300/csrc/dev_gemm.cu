@@ -520,48 +520,60 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 // (the query's eq0 is folded into the threshold and the chunk maximum)
                 const float thr2 = __fsub_rd(thr, eq0);
                 float maxl = -INFINITY;
-                uint32_t mask = 0;
                 if (NORM) {
+                    // hot path: one max per element; the emission mask is built
+                    // only in the branch below, for the lanes whose chunk reaches
+                    // the threshold (the keys are the accumulator values)
                     const int rw = row0 + c * kChunk;
                     const uint32_t vb = (__ldg(P.vbits + (rw >> 5)) >> (rw & 31)) & 0xFFFFu;
-                    if (vb == 0xFFFFu) {  // every row of the chunk is searchable (warp-uniform)
+                    if (vb != 0xFFFFu) {  // warp-uniform: NaN out the rows that are not searchable
+#pragma unroll
+                        for (int i = 0; i < kChunk; ++i)
+                            if (!((vb >> i) & 1u)) v[i] = 0x7fc00000u;
+                    }
+#pragma unroll
+                    for (int i = 0; i < kChunk; ++i) maxl = fmaxf(maxl, __uint_as_float(v[i]));
+                    if (maxl >= thr2 && q < P.nq) {
+                        uint32_t mask = 0;
+#pragma unroll
+                        for (int i = 0; i < kChunk; ++i) mask |= (__uint_as_float(v[i]) >= thr2 ? 1u : 0u) << i;
+                        int slot = atomicAdd(&P.cnt[q], __popc(mask));
 #pragma unroll
                         for (int i = 0; i < kChunk; ++i) {
-                            const float g = __uint_as_float(v[i]);
-                            maxl = fmaxf(maxl, g);
-                            mask |= (g >= thr2 ? 1u : 0u) << i;
-                        }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < kChunk; ++i) {
-                            // NaN, not -inf: -inf >= thr2 holds while thr2 is still -inf
-                            const float g = ((vb >> i) & 1u) ? __uint_as_float(v[i]) : __int_as_float(0x7fc00000);
-                            maxl = fmaxf(maxl, g);
-                            mask |= (g >= thr2 ? 1u : 0u) << i;
+                            if (mask & (1u << i)) {
+                                if (slot < P.cap) cq[slot] = make_int2(rw + i, (int)v[i]);
+                                ++slot;
+                            }
                         }
                     }
                 } else {
+                    float maxu = -INFINITY;
 #pragma unroll
                     for (int i = 0; i < kChunk; ++i) {
                         const float4 p = rc[i];
                         const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
                         const float e = __fmaf_ru(eq, p.y, p.w);
                         maxl = fmaxf(maxl, __fsub_rd(key, e));
-                        mask |= (__fadd_ru(key, e) >= thr2 ? 1u : 0u) << i;
+                        maxu = fmaxf(maxu, __fadd_ru(key, e));
                         v[i] = __float_as_uint(key);
                     }
-                }
-                maxl = __fsub_rd(maxl, eq0);
-                if (mask && q < P.nq) {  // rows whose upper bound reaches the threshold
-                    int slot = atomicAdd(&P.cnt[q], __popc(mask));
+                    if (maxu >= thr2 && q < P.nq) {  // rows whose upper bound reaches the threshold
+                        uint32_t mask = 0;
 #pragma unroll
-                    for (int i = 0; i < kChunk; ++i) {
-                        if (mask & (1u << i)) {
-                            if (slot < P.cap) cq[slot] = make_int2(row0 + c * kChunk + i, (int)v[i]);
-                            ++slot;
+                        for (int i = 0; i < kChunk; ++i)
+                            mask |= (__fadd_ru(__uint_as_float(v[i]), __fmaf_ru(eq, rc[i].y, rc[i].w)) >= thr2 ? 1u : 0u)
+                                    << i;
+                        int slot = atomicAdd(&P.cnt[q], __popc(mask));
+#pragma unroll
+                        for (int i = 0; i < kChunk; ++i) {
+                            if (mask & (1u << i)) {
+                                if (slot < P.cap) cq[slot] = make_int2(row0 + c * kChunk + i, (int)v[i]);
+                                ++slot;
+                            }
                         }
                     }
                 }
+                maxl = __fsub_rd(maxl, eq0);
                 // The running threshold is the k-th best of the chunk maxima: k
                 // distinct chunks hold k distinct rows with a lower bound at
                 // least that large, so it never exceeds the k-th best lower bound.
@@ -731,6 +743,43 @@ __device__ __forceinline__ uint32_t f2u_ord(float f) {
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
+// k-th largest of m ordered values get(i) (every thread of the block calls
+// it): four 8-bit radix passes with a shared histogram
+template <class Get>
+__device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t* sh) {
+    if (threadIdx.x == 0) {
+        sh[0] = 0;  // prefix
+        sh[1] = 0;  // mask
+        sh[2] = (uint32_t)k;
+    }
+    __syncthreads();
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        const uint32_t pre = sh[0], msk = sh[1];
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const uint32_t v = get(i);
+            if ((v & msk) == pre) atomicAdd(&hist[(v >> shift) & 255u], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int cum = 0, need = (int)sh[2], dsel = 0;
+            for (int dgt = 255; dgt >= 0; --dgt) {
+                if (cum + hist[dgt] >= need) {
+                    dsel = dgt;
+                    break;
+                }
+                cum += hist[dgt];
+            }
+            sh[2] = (uint32_t)(need - cum);
+            sh[0] = pre | ((uint32_t)dsel << shift);
+            sh[1] = msk | (255u << shift);
+        }
+        __syncthreads();
+    }
+    return sh[0];
+}
+
 // Pass 1: every thread keeps the k best lower bounds of its candidates
 // (registers); their union holds the k best overall, so a radix select over
 // it in shared memory gives the exact k-th largest.  Pass 2: survivors.
@@ -741,8 +790,8 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
                                                  int* __restrict__ sig, uint8_t* __restrict__ flags) {
     extern __shared__ uint32_t vals[];  // blockDim.x * k ordered lower bounds
     __shared__ int hist[256];
-    __shared__ uint32_t s_prefix, s_mask;
-    __shared__ int s_rank, s_out, s_sig;
+    __shared__ uint32_t s_sh[3];
+    __shared__ int s_out, s_sig;
     const int q = blockIdx.x;
     const float4 qp = qpar[q];
     const int n = cnt[q];
@@ -767,42 +816,13 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     for (int j = 0; j < KL; ++j)
         if (j < k) vals[threadIdx.x * k + j] = f2u_ord(top.v[j]);
     if (threadIdx.x == 0) {
-        s_prefix = 0;
-        s_mask = 0;
-        s_rank = k;
         s_out = 0;
         s_sig = 0x7fffffff;
     }
     __syncthreads();
     const int m = bd * k;
-    uint32_t thr_ord = 0;  // fewer than k candidates: every one survives
-    if (n >= k) {
-        for (int shift = 24; shift >= 0; shift -= 8) {
-            for (int i = threadIdx.x; i < 256; i += bd) hist[i] = 0;
-            __syncthreads();
-            const uint32_t pre = s_prefix, msk = s_mask;
-            for (int i = threadIdx.x; i < m; i += bd) {
-                const uint32_t lo = vals[i];
-                if ((lo & msk) == pre) atomicAdd(&hist[(lo >> shift) & 255u], 1);
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                int cum = 0, need = s_rank, dsel = 0;
-                for (int dgt = 255; dgt >= 0; --dgt) {
-                    if (cum + hist[dgt] >= need) {
-                        dsel = dgt;
-                        break;
-                    }
-                    cum += hist[dgt];
-                }
-                s_rank = need - cum;
-                s_prefix = pre | ((uint32_t)dsel << shift);
-                s_mask = msk | (255u << shift);
-            }
-            __syncthreads();
-        }
-        thr_ord = s_prefix;  // ordered image of the k-th largest lower bound
-    }
+    // fewer than k candidates: every one survives
+    const uint32_t thr_ord = n >= k ? block_kth_largest([&](int i) { return vals[i]; }, m, k, hist, s_sh) : 0u;
     int2* sq = surv + (size_t)q * scr::kSurvCap;
     for (int i = threadIdx.x; i < n; i += bd) {
         const int2 c = cq[i];
@@ -859,27 +879,32 @@ __global__ void __launch_bounds__(1024) k_sort_queries(const int* __restrict__ s
 // with a certified bound on |S - |q - x|^2|:
 //   eta = 2^-23 (|q| + |x|) bounds the FP32 rounding of q, x and q - x,
 //   |S_exact - |q - x|^2| <= eta (2 |t| + eta), |S - S_exact| <= gamma S,
-// gamma = (chain length + 3) 2^-24 for the FP32 accumulation.  Working from
+// gamma = (chain length + 7) 2^-24 for the FP32 accumulation (16 lanes per
+// row, 4 chains per lane, then 3 + 4 additions).  Working from
 // differences keeps the error proportional to |q - x| (small for the near
 // rows that survive the screen) instead of |q| |x|.  Survivors whose upper
 // bound is below the k-th largest refined lower bound are dropped.
 // ---------------------------------------------------------------------------
-constexpr int kRefThreads = 512;
+constexpr int kRefThreads = 256;
 
-__global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict__ x32, size_t ld,
-                                                        const float* __restrict__ q32, const double* __restrict__ qsq,
-                                                        const double* __restrict__ sq64,
-                                                        const float4* __restrict__ rowp,
-                                                        const float4* __restrict__ rpar,
-                                                        const float4* __restrict__ qpar, int2* __restrict__ surv,
-                                                        const int* __restrict__ nsurv, int* __restrict__ nref, int k,
-                                                        int metric, const int* __restrict__ perm,
-                                                        uint8_t* __restrict__ flags) {
+// The per-row key and bound are interval arithmetic in FP32 with directed
+// rounding (GB300's FP64 pipe is narrow; one FP64 instruction per row per warp
+// would dominate): |q|^2 and |x|^2 enter as [rd, ru] pairs, d^2 as [S - E, S + E].
+// Each survivor's refined {L, U} goes to `lu` (the candidate list's storage,
+// dead after the select), so no per-thread state limits the occupancy.
+__global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restrict__ x32, size_t ld,
+                                                           const float* __restrict__ q32,
+                                                           const double* __restrict__ qsq,
+                                                           const float2* __restrict__ sqf,
+                                                           const float4* __restrict__ rowp,
+                                                           const float4* __restrict__ qpar, int2* __restrict__ surv,
+                                                           const int* __restrict__ nsurv, int* __restrict__ nref,
+                                                           float2* __restrict__ lu, size_t lu_stride, int k, int metric,
+                                                           const int* __restrict__ perm, uint8_t* __restrict__ flags) {
     extern __shared__ __align__(16) uint8_t sm[];
-    float* ur = reinterpret_cast<float*>(sm);  // refined upper bound per survivor
-    float* qs = ur + scr::kSurvCap;            // the query in FP32 (ld floats, 16-float multiple)
-    Entry* lists = reinterpret_cast<Entry*>(qs + ld);
-    __shared__ double s_tau;
+    float* qs = reinterpret_cast<float*>(sm);  // the query in FP32 (ld floats)
+    __shared__ int hist[256];
+    __shared__ uint32_t s_sh[3];
     __shared__ int s_out;
     constexpr int kWarps = kRefThreads / 32;
     const int q = perm ? perm[blockIdx.x] : blockIdx.x;
@@ -887,28 +912,30 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
         if (threadIdx.x == 0) nref[q] = 0;
         return;
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = q32[(size_t)q * ld + i];
     if (threadIdx.x == 0) s_out = 0;
     __syncthreads();
     const int n = nsurv[q];
     int2* sq = surv + (size_t)q * scr::kSurvCap;
+    float2* luq = lu + (size_t)q * lu_stride;
     const double qq = qsq[q];
+    const float qq_lo = __double2float_rd(qq), qq_hi = __double2float_ru(qq);
     const float qn_up = qpar[q].x;
-    // each lane: ld/16 float4 steps into 4 accumulators, then 3 + 2 additions
-    const float gamma = (float)(ld / 16 + 6) * 5.9604644775390625e-08f * 1.0001f;
-    WarpList<1> W;
-    W.init();
-    for (int base = warp * 8; base < n; base += kWarps * 8) {
-        const int i = base + g;
+    // each lane: ld/64 steps into each of 4 accumulators, then 2 + 4 additions
+    const float gamma = (float)(ld / 64 + 8) * 5.9604644775390625e-08f * 1.0001f;
+    // half a warp per row: lane h of the half reads float4 h, h+16, ...
+    const int hw = lane >> 4, h = lane & 15;
+    for (int base = warp * 2; base < n; base += kWarps * 2) {
+        const int i = base + hw;
         const bool act = i < n;
         const int row = act ? sq[i].x : 0;
         float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
         if (act) {
             const float4* x = reinterpret_cast<const float4*>(x32 + (size_t)row * ld);
             const float4* qv = reinterpret_cast<const float4*>(qs);
-#pragma unroll 4
-            for (size_t j = s; j < ld / 4; j += 4) {
+#pragma unroll 6
+            for (size_t j = h; j < ld / 4; j += 16) {
                 const float4 xv = __ldg(x + j);
                 const float4 qq4 = qv[j];
                 const float t0 = qq4.x - xv.x, t1 = qq4.y - xv.y, t2 = qq4.z - xv.z, t3 = qq4.w - xv.w;
@@ -919,94 +946,59 @@ __global__ void __launch_bounds__(kRefThreads) k_refine(const float* __restrict_
             }
         }
         float p = (a0 + a1) + (a2 + a3);
+        p += __shfl_xor_sync(0xffffffffu, p, 8);
+        p += __shfl_xor_sync(0xffffffffu, p, 4);
         p += __shfl_xor_sync(0xffffffffu, p, 2);
         p += __shfl_xor_sync(0xffffffffu, p, 1);
-        double L = -INFINITY;
-        if (act && s == 0) {
-            const double S = (double)p;
-            const double xs = sq64[row];
+        if (act && h == 0) {
+            const float2 xb = sqf[row];  // |x|^2 in [xb.x, xb.y]
             const float xn_up = rowp[row].x;
             const float sup = __fmul_ru(p, 1.0f + gamma);
             const float eta = __fmul_ru(1.1921875e-07f, __fadd_ru(qn_up, xn_up));  // 2^-23 (1 + 2^-13)
             float ed2 = __fmaf_ru(gamma, sup, __fmul_ru(eta, __fadd_ru(__fmul_ru(2.0f, __fsqrt_ru(sup)), eta)));
-            ed2 = __fmaf_ru(9.094947e-13f, __double2float_ru(qq + xs), __fmul_ru(ed2, 1.000001f));  // + 2^-40 scale
-            double key, e;
-            if (metric == SVDB_EUCLIDEAN) {
-                key = 0.5 * (qq - S);
-                e = 0.5 * (double)ed2;
-            } else if (metric == SVDB_DOT) {
-                key = 0.5 * ((qq + xs) - S);
-                e = 0.5 * (double)ed2;
-            } else {
-                // 1/|x| in FP32: relative error <= 2^-22 (conversion, sqrt, reciprocal)
-                const double mult = (double)__frcp_rn(__fsqrt_rn(__double2float_rn(xs)));
-                key = 0.5 * ((qq + xs) - S) * mult;
-                e = 0.5 * (double)ed2 * mult * (1.0 + 4.76837158203125e-07) + fabs(key) * 4.76837158203125e-07;
+            ed2 = __fmaf_ru(9.094947e-13f, __fadd_ru(qq_hi, xb.y), __fmul_ru(ed2, 1.000001f));  // + 2^-40 scale
+            const float s_hi = __fadd_ru(p, ed2), s_lo = __fsub_rd(p, ed2);  // |q - x|^2 in [s_lo, s_hi]
+            float L, U;
+            if (metric == SVDB_EUCLIDEAN) {  // key = (|q|^2 - d^2) / 2
+                L = __fmul_rd(__fsub_rd(qq_lo, s_hi), 0.5f);
+                U = __fmul_ru(__fsub_ru(qq_hi, s_lo), 0.5f);
+            } else {  // dot = (|q|^2 + |x|^2 - d^2) / 2
+                const float a_lo = __fsub_rd(__fadd_rd(qq_lo, xb.x), s_hi);
+                const float a_hi = __fsub_ru(__fadd_ru(qq_hi, xb.y), s_lo);
+                if (metric == SVDB_DOT) {
+                    L = __fmul_rd(a_lo, 0.5f);
+                    U = __fmul_ru(a_hi, 0.5f);
+                } else {  // cosine key = dot / |x|, 1/(2|x|) in [m_lo, m_hi]
+                    const float xn_lo = __fsqrt_rd(xb.x);
+                    const float m_lo = __fdiv_rd(0.5f, xn_up);
+                    const float m_hi = xn_lo > 0.f ? __fdiv_ru(0.5f, xn_lo) : INFINITY;
+                    L = a_lo >= 0.f ? __fmul_rd(a_lo, m_lo) : __fmul_rd(a_lo, m_hi);
+                    U = a_hi >= 0.f ? __fmul_ru(a_hi, m_hi) : __fmul_ru(a_hi, m_lo);
+                    if (isnan(L)) L = -INFINITY;
+                    if (isnan(U)) U = INFINITY;
+                }
             }
-            L = key - e;
-            ur[i] = __double2float_ru(key + e);
+            luq[i] = make_float2(L, U);
         }
-        // k best refined lower bounds of this warp (ascending key -L, then row)
-        double wk;
-        int wi;
-        W.worst(k, wk, wi);
-        const bool cand = act && s == 0 && key_less(-L, row, wk, wi);
-        unsigned m = __ballot_sync(0xffffffffu, cand);
-        while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1;
-            const double lv = __shfl_sync(0xffffffffu, L, src);
-            W.insert(-lv, __shfl_sync(0xffffffffu, row, src), lv, k);
-        }
-    }
-    Entry* mine = lists + warp * 32;
-    {
-        Entry e;
-        e.val = W.val[0];
-        e.id = W.id[0];
-        e.pad = 0;
-        mine[lane] = e;
     }
     __syncthreads();
-    if (warp == 0) {
-        WarpList<1> M;
-        M.init();
-        for (int w = 0; w < kWarps; ++w) {
-            const Entry e = lists[w * 32 + lane];
-            double wk;
-            int wi;
-            M.worst(k, wk, wi);
-            const bool ok = lane < k && e.id != 0x7fffffff && key_less(-e.val, e.id, wk, wi);
-            unsigned m = __ballot_sync(0xffffffffu, ok);
-            while (m) {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const double lv = __shfl_sync(0xffffffffu, e.val, src);
-                M.insert(-lv, __shfl_sync(0xffffffffu, e.id, src), lv, k);
-            }
-        }
-        double kth, dummy;
-        int kid;
-        M.at(k - 1, dummy, kid);
-        kth = __shfl_sync(0xffffffffu, M.val[0], (k - 1) & 31);
-        if (lane == 0) s_tau = kid == 0x7fffffff ? -INFINITY : kth;  // fewer than k: keep all
-    }
-    __syncthreads();
-    // compaction in two phases: every read of the list precedes every write
-    const float tau = __double2float_rd(s_tau);
+    // exact k-th largest refined lower bound; fewer than k survivors: keep all
+    const uint32_t thr_ord =
+        n >= k ? block_kth_largest([&](int i) { return f2u_ord(__ldcg(&luq[i].x)); }, n, k, hist, s_sh) : 0u;
+    // what survives is written over `lu` (as {row, screen key}) once every
+    // bound has been read; the re-rank reads it from there
     constexpr int kPer = scr::kSurvCap / kRefThreads;
-    int2 keep[kPer];
-    int nk = 0;
+    uint32_t keepbits = 0;
 #pragma unroll
     for (int m = 0; m < kPer; ++m) {
         const int i = threadIdx.x + m * kRefThreads;
-        if (i < n && ur[i] >= tau) keep[nk++] = sq[i];
+        if (i < n && f2u_ord(__ldcg(&luq[i].y)) >= thr_ord) keepbits |= 1u << m;
     }
     __syncthreads();
-    const int o = nk ? atomicAdd(&s_out, nk) : 0;
-#pragma unroll
+    int o = keepbits ? atomicAdd(&s_out, __popc(keepbits)) : 0;
+    int2* out = reinterpret_cast<int2*>(luq);
     for (int m = 0; m < kPer; ++m)
-        if (m < nk) sq[o + m] = keep[m];
+        if ((keepbits >> m) & 1u) out[o++] = sq[threadIdx.x + m * kRefThreads];
     __syncthreads();
     if (threadIdx.x == 0) nref[q] = s_out;
 }
@@ -1020,7 +1012,7 @@ template <int KS, bool EUC>
 __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, size_t ld,
                                                 const double* __restrict__ qbuf, const double* __restrict__ qsq,
                                                 const double* __restrict__ sq64, const int2* __restrict__ surv,
-                                                const int* __restrict__ nsurv, int k, int metric,
+                                                size_t surv_stride, const int* __restrict__ nsurv, int k, int metric,
                                                 const float4* __restrict__ rpar, const float4* __restrict__ qpar,
                                                 Entry* __restrict__ part, uint8_t* __restrict__ flags) {
     extern __shared__ __align__(16) uint8_t sm[];
@@ -1031,7 +1023,7 @@ __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, 
     for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = qbuf[(size_t)q * ld + i];
     __syncthreads();
     const int n = nsurv[q];
-    const int2* sq = surv + (size_t)q * scr::kSurvCap;
+    const int2* sq = surv + (size_t)q * surv_stride;
     const double qq = qsq[q];
     const double qn = sqrt(qq);
     const float4 qp = qpar[q];
@@ -1227,7 +1219,6 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     bool attr_set[4] = {false, false, false, false};
-    bool refine_attr = false;
     bool select_attr = false;
     bool sort_attr = false;
     size_t screen_smem = 0;
@@ -1432,12 +1423,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     }
     SVDB_LAUNCH_CHECK();
     s->prof_mark(3);
-    const size_t ref_smem = (size_t)scr::kSurvCap * sizeof(float) + s->ld * sizeof(float) +
-                            (size_t)(kRefThreads / 32) * 32 * sizeof(Entry);
-    if (!gc->refine_attr) {
-        SVDB_CUDA(cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        gc->refine_attr = true;
-    }
+    const size_t ref_smem = s->ld * sizeof(float);
     // refinement order (batches of up to 16384 queries are sorted; larger ones keep index order)
     const int* order = nullptr;
     if (nq > 1 && nq <= 16384) {
@@ -1453,8 +1439,11 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         ++kernels;
         order = perm;
     }
-    k_refine<<<(unsigned)nq, kRefThreads, ref_smem, s->stream>>>(s->x32, s->ld, q32, a.qsq, s->sq64, s->rowp, rpar,
-                                                                 qpar, surv, nsurv, nref, k, a.metric, order, flags);
+    // the candidate list (cap >= 8192 entries per query) is dead after the select:
+    // it holds the refined {L, U} of each survivor
+    k_refine<<<(unsigned)nq, kRefThreads, ref_smem, s->stream>>>(s->x32, s->ld, q32, a.qsq, s->sqf, s->rowp, qpar, surv,
+                                                                 nsurv, nref, reinterpret_cast<float2*>(cand),
+                                                                 (size_t)L.cap, k, a.metric, order, flags);
     SVDB_LAUNCH_CHECK();
     kernels += 2;
     s->prof_mark(4);
@@ -1462,10 +1451,10 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));
     const dim3 rgrid((unsigned)nq, (unsigned)L.splits);
     if (a.metric == SVDB_EUCLIDEAN)
-        k_rerank<1, true><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nref, k,
+        k_rerank<1, true><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k,
                                                               a.metric, rpar, qpar, part, flags);
     else
-        k_rerank<1, false><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, surv, nref, k,
+        k_rerank<1, false><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k,
                                                                a.metric, rpar, qpar, part, flags);
     SVDB_LAUNCH_CHECK();
     k_merge_rerank<1><<<(unsigned)((a.nq * 32 + 255) / 256), 256, 0, s->stream>>>(

@@ -7,6 +7,7 @@
 //   x32     C x ld   float    FP32 shadow of x64 (refinement stage)
 //   xbn     C x ldb  bf16     BF16 shadow of x64 / |x| (cosine screen)
 //   rowpn   C        float2   {|bxn| up, |x/|x| - bxn| up}
+//   sqf     C        float2   {|x|^2 down, |x|^2 up} in FP32
 //   sq64    C        double   canonical sum of squares of the master row
 //   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
 //   live    C        uint8    1 = searchable row, 2 = row of another dimension
@@ -45,7 +46,8 @@ namespace svdb {
 // One group of 4 lanes per row, canonical order for the sum of squares.
 __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bfloat16* __restrict__ xb,
                               size_t ldb, float* __restrict__ x32, __nv_bfloat16* __restrict__ xbn,
-                              float2* __restrict__ rowpn, double* __restrict__ sq64, float4* __restrict__ rowp,
+                              float2* __restrict__ rowpn, float2* __restrict__ sqf, double* __restrict__ sq64,
+                              float4* __restrict__ rowp,
                               const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
                               const int64_t* __restrict__ list) {
     const int lane = threadIdx.x & 31, s = lane & 3;
@@ -107,6 +109,7 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     if (active && s == 0) {
         // x/|x| is itself rounded (relative 2^-52 per element): the 2^-30 margin covers it
         const double up = 1.0 + 9.313225746154785e-10;
+        sqf[slot] = make_float2(__double2float_rd(sq), __double2float_ru(sq));
         rowpn[slot] = make_float2(__double2float_ru(sqrt(nbh) * up), __double2float_ru(sqrt(nres) * up + 1e-300));
         sq64[slot] = sq;
         float4 p;
@@ -333,6 +336,7 @@ int Store::grow(size_t need) {
     float* nf = nullptr;
     __nv_bfloat16* nbn = nullptr;
     float2* npn = nullptr;
+    float2* nsf = nullptr;
     double* nsq = nullptr;
     float4* np = nullptr;
     uint8_t* nl = nullptr;
@@ -343,6 +347,7 @@ int Store::grow(size_t need) {
     if (e == cudaSuccess) e = cudaMalloc(&nf, nc * ld * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&nbn, nc * ldb * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc(&npn, nc * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&nsf, nc * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nl, nc);
@@ -354,6 +359,7 @@ int Store::grow(size_t need) {
         cudaFree(nf);
         cudaFree(nbn);
         cudaFree(npn);
+        cudaFree(nsf);
         cudaFree(nsq);
         cudaFree(np);
         cudaFree(nl);
@@ -367,6 +373,7 @@ int Store::grow(size_t need) {
         SVDB_CUDA(cudaMemcpyAsync(nf, x32, slots * ld * sizeof(float), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nbn, xbn, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(npn, rowpn, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nsf, sqf, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nl, live, slots, cudaMemcpyDeviceToDevice, stream));
@@ -378,6 +385,7 @@ int Store::grow(size_t need) {
     cudaFree(x32);
     cudaFree(xbn);
     cudaFree(rowpn);
+    cudaFree(sqf);
     cudaFree(sq64);
     cudaFree(rowp);
     cudaFree(live);
@@ -387,6 +395,7 @@ int Store::grow(size_t need) {
     x32 = nf;
     xbn = nbn;
     rowpn = npn;
+    sqf = nsf;
     sq64 = nsq;
     rowp = np;
     live = nl;
@@ -479,7 +488,7 @@ int Store::sync() {
         const int64_t n = derive_hi - derive_lo;
         const int threads = 256;
         const int64_t blocks = (n * 4 + threads - 1) / threads;
-        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sq64, rowp, live, derive_lo,
+        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp, live, derive_lo,
                                                               derive_hi, nullptr);
         SVDB_LAUNCH_CHECK();
     }
@@ -491,7 +500,7 @@ int Store::sync() {
         if (rc) return rc;
         d = (int64_t*)scratch;
         SVDB_CUDA(cudaMemcpyAsync(d, dirty_list.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
-        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sq64, rowp, live, 0,
+        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp, live, 0,
                                                                          n, d);
         SVDB_LAUNCH_CHECK();
         SVDB_CUDA(cudaStreamSynchronize(stream));
@@ -550,6 +559,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->x32);
     cudaFree(s->xbn);
     cudaFree(s->rowpn);
+    cudaFree(s->sqf);
     cudaFree(s->sq64);
     cudaFree(s->rowp);
     cudaFree(s->live);
