@@ -887,6 +887,30 @@ __global__ void __launch_bounds__(1024) k_sort_queries(const int* __restrict__ s
 // ---------------------------------------------------------------------------
 constexpr int kRefThreads = 256;
 
+// k-th largest refined lower bound over a query's n survivors, then the rows
+// whose refined upper bound reaches it, written over `luq` as {row, screen
+// key} once every bound has been read (the re-rank reads them from there)
+__device__ void refine_keep(int q, int n, int k, float2* luq, const int2* sq, int* nref, int* hist, uint32_t* s_sh,
+                            int* s_out) {
+    if (threadIdx.x == 0) *s_out = 0;
+    const uint32_t thr_ord =
+        n >= k ? block_kth_largest([&](int i) { return f2u_ord(__ldcg(&luq[i].x)); }, n, k, hist, s_sh) : 0u;
+    constexpr int kPer = scr::kSurvCap / kRefThreads;
+    uint32_t keepbits = 0;
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int i = threadIdx.x + m * kRefThreads;
+        if (i < n && f2u_ord(__ldcg(&luq[i].y)) >= thr_ord) keepbits |= 1u << m;
+    }
+    __syncthreads();
+    int o = keepbits ? atomicAdd(s_out, __popc(keepbits)) : 0;
+    int2* out = reinterpret_cast<int2*>(luq);
+    for (int m = 0; m < kPer; ++m)
+        if ((keepbits >> m) & 1u) out[o++] = sq[threadIdx.x + m * kRefThreads];
+    __syncthreads();
+    if (threadIdx.x == 0) nref[q] = *s_out;
+}
+
 // The per-row key and bound are interval arithmetic in FP32 with directed
 // rounding (GB300's FP64 pipe is narrow; one FP64 instruction per row per warp
 // would dominate): |q|^2 and |x|^2 enter as [rd, ru] pairs, d^2 as [S - E, S + E].
@@ -908,13 +932,13 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
     __shared__ int s_out;
     constexpr int kWarps = kRefThreads / 32;
     const int q = perm ? perm[blockIdx.x] : blockIdx.x;
+    const int split = blockIdx.y, splits = gridDim.y;  // splits > 1: k_refine_keep finishes
     if (flags[q] != scr::kOk) {
-        if (threadIdx.x == 0) nref[q] = 0;
+        if (threadIdx.x == 0 && split == 0) nref[q] = 0;
         return;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = q32[(size_t)q * ld + i];
-    if (threadIdx.x == 0) s_out = 0;
     __syncthreads();
     const int n = nsurv[q];
     int2* sq = surv + (size_t)q * scr::kSurvCap;
@@ -926,7 +950,7 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
     const float gamma = (float)(ld / 64 + 8) * 5.9604644775390625e-08f * 1.0001f;
     // half a warp per row: lane h of the half reads float4 h, h+16, ...
     const int hw = lane >> 4, h = lane & 15;
-    for (int base = warp * 2; base < n; base += kWarps * 2) {
+    for (int base = (split * kWarps + warp) * 2; base < n; base += splits * kWarps * 2) {
         const int i = base + hw;
         const bool act = i < n;
         const int row = act ? sq[i].x : 0;
@@ -981,26 +1005,24 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
             luq[i] = make_float2(L, U);
         }
     }
-    __syncthreads();
-    // exact k-th largest refined lower bound; fewer than k survivors: keep all
-    const uint32_t thr_ord =
-        n >= k ? block_kth_largest([&](int i) { return f2u_ord(__ldcg(&luq[i].x)); }, n, k, hist, s_sh) : 0u;
-    // what survives is written over `lu` (as {row, screen key}) once every
-    // bound has been read; the re-rank reads it from there
-    constexpr int kPer = scr::kSurvCap / kRefThreads;
-    uint32_t keepbits = 0;
-#pragma unroll
-    for (int m = 0; m < kPer; ++m) {
-        const int i = threadIdx.x + m * kRefThreads;
-        if (i < n && f2u_ord(__ldcg(&luq[i].y)) >= thr_ord) keepbits |= 1u << m;
+    if (splits == 1) {
+        __syncthreads();
+        refine_keep(q, n, k, luq, sq, nref, hist, s_sh, &s_out);
     }
-    __syncthreads();
-    int o = keepbits ? atomicAdd(&s_out, __popc(keepbits)) : 0;
-    int2* out = reinterpret_cast<int2*>(luq);
-    for (int m = 0; m < kPer; ++m)
-        if ((keepbits >> m) & 1u) out[o++] = sq[threadIdx.x + m * kRefThreads];
-    __syncthreads();
-    if (threadIdx.x == 0) nref[q] = s_out;
+}
+
+// second half of a split refinement: one block per query
+__global__ void __launch_bounds__(kRefThreads) k_refine_keep(const int2* __restrict__ surv,
+                                                             const int* __restrict__ nsurv, int* __restrict__ nref,
+                                                             float2* __restrict__ lu, size_t lu_stride, int k,
+                                                             const uint8_t* __restrict__ flags) {
+    __shared__ int hist[256];
+    __shared__ uint32_t s_sh[3];
+    __shared__ int s_out;
+    const int q = blockIdx.x;
+    if (flags[q] != scr::kOk) return;  // nref already 0
+    refine_keep(q, nsurv[q], k, lu + (size_t)q * lu_stride, surv + (size_t)q * scr::kSurvCap, nref, hist, s_sh,
+                &s_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1441,10 +1463,18 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     }
     // the candidate list (cap >= 8192 entries per query) is dead after the select:
     // it holds the refined {L, U} of each survivor
-    k_refine<<<(unsigned)nq, kRefThreads, ref_smem, s->stream>>>(s->x32, s->ld, q32, a.qsq, s->sqf, s->rowp, qpar, surv,
-                                                                 nsurv, nref, reinterpret_cast<float2*>(cand),
-                                                                 (size_t)L.cap, k, a.metric, order, flags);
+    // small batches: several blocks per query score the survivors, then one keeps
+    const int rsplits = std::max(1, std::min(32, 2 * num_sms() / std::max(nq, 1)));
+    k_refine<<<dim3((unsigned)nq, (unsigned)rsplits), kRefThreads, ref_smem, s->stream>>>(
+        s->x32, s->ld, q32, a.qsq, s->sqf, s->rowp, qpar, surv, nsurv, nref, reinterpret_cast<float2*>(cand),
+        (size_t)L.cap, k, a.metric, order, flags);
     SVDB_LAUNCH_CHECK();
+    if (rsplits > 1) {
+        k_refine_keep<<<(unsigned)nq, kRefThreads, 0, s->stream>>>(surv, nsurv, nref, reinterpret_cast<float2*>(cand),
+                                                                    (size_t)L.cap, k, flags);
+        SVDB_LAUNCH_CHECK();
+        ++kernels;
+    }
     kernels += 2;
     s->prof_mark(4);
 
