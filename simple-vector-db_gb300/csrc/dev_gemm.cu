@@ -509,83 +509,73 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 tau_c = fmaxf(tau_c, fmaxf(ord2f(__ldcg(P.tau + q)), ord2f(bmin)));
             }
             float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
+            // the query's eq0 is folded into the threshold and the maxima
+            const float thr2 = __fsub_rd(thr, eq0);
+            constexpr int C = NORM ? 32 : 16;  // accumulator columns per collective load
+            float tmax = -INFINITY;            // best lower bound (less eq0) of this warp's 128 rows
 #pragma unroll 1
-            for (int c = 0; c < kBN / 2 / kChunk; ++c) {
-                uint32_t v[kChunk];
+            for (int c = 0; c < kBN / 2 / C; ++c) {
+                uint32_t v[C];
+                const int rw = row0 + c * C;
                 __syncwarp();  // converged warp for the collective load
-                tmem_ld16(tbase + (uint32_t)(c * kChunk), v);
+                if constexpr (C == 32)
+                    tmem_ld32(tbase + (uint32_t)(c * C), v);
+                else
+                    tmem_ld16(tbase + (uint32_t)(c * C), v);
                 tmem_ld_wait();
-                const float4* rc = rps + c * kChunk;
-                // branch-free pass: keys, the chunk's best lower bound, emission mask
-                // (the query's eq0 is folded into the threshold and the chunk maximum)
-                const float thr2 = __fsub_rd(thr, eq0);
-                float maxl = -INFINITY;
+                const float4* rc = rps + c * C;
+                float mu = -INFINITY;  // best upper bound (less eq0) of the chunk
                 if (NORM) {
-                    // hot path: one max per element; the emission mask is built
-                    // only in the branch below, for the lanes whose chunk reaches
-                    // the threshold (the keys are the accumulator values)
-                    const int rw = row0 + c * kChunk;
-                    const uint32_t vb = (__ldg(P.vbits + (rw >> 5)) >> (rw & 31)) & 0xFFFFu;
-                    if (vb != 0xFFFFu) {  // warp-uniform: NaN out the rows that are not searchable
+                    // keys are the accumulator values; rows that are not searchable
+                    // become NaN (every comparison with NaN is false)
+                    const uint32_t vb = __ldg(P.vbits + (rw >> 5));
+                    if (vb != 0xFFFFFFFFu) {  // warp-uniform
 #pragma unroll
-                        for (int i = 0; i < kChunk; ++i)
+                        for (int i = 0; i < C; ++i)
                             if (!((vb >> i) & 1u)) v[i] = 0x7fc00000u;
                     }
 #pragma unroll
-                    for (int i = 0; i < kChunk; ++i) maxl = fmaxf(maxl, __uint_as_float(v[i]));
-                    if (maxl >= thr2 && q < P.nq) {
-                        uint32_t mask = 0;
-#pragma unroll
-                        for (int i = 0; i < kChunk; ++i) mask |= (__uint_as_float(v[i]) >= thr2 ? 1u : 0u) << i;
-                        int slot = atomicAdd(&P.cnt[q], __popc(mask));
-#pragma unroll
-                        for (int i = 0; i < kChunk; ++i) {
-                            if (mask & (1u << i)) {
-                                if (slot < P.cap) cq[slot] = make_int2(rw + i, (int)v[i]);
-                                ++slot;
-                            }
-                        }
-                    }
+                    for (int i = 0; i < C; ++i) mu = fmaxf(mu, __uint_as_float(v[i]));
+                    tmax = fmaxf(tmax, mu);
                 } else {
-                    float maxu = -INFINITY;
 #pragma unroll
-                    for (int i = 0; i < kChunk; ++i) {
+                    for (int i = 0; i < C; ++i) {
                         const float4 p = rc[i];
                         const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
                         const float e = __fmaf_ru(eq, p.y, p.w);
-                        maxl = fmaxf(maxl, __fsub_rd(key, e));
-                        maxu = fmaxf(maxu, __fadd_ru(key, e));
+                        tmax = fmaxf(tmax, __fsub_rd(key, e));
+                        mu = fmaxf(mu, __fadd_ru(key, e));
                         v[i] = __float_as_uint(key);
                     }
-                    if (maxu >= thr2 && q < P.nq) {  // rows whose upper bound reaches the threshold
-                        uint32_t mask = 0;
+                }
+                // emission, warp-uniform: lanes reserve their slots with one atomic
+                // each, then the columns any lane emits are stored with predicates
+                const bool want = mu >= thr2 && q < P.nq;
+                if (__any_sync(0xffffffffu, want)) {
+                    uint32_t mask = 0;
 #pragma unroll
-                        for (int i = 0; i < kChunk; ++i)
-                            mask |= (__fadd_ru(__uint_as_float(v[i]), __fmaf_ru(eq, rc[i].y, rc[i].w)) >= thr2 ? 1u : 0u)
-                                    << i;
-                        int slot = atomicAdd(&P.cnt[q], __popc(mask));
+                    for (int i = 0; i < C; ++i) {
+                        const float u = NORM ? __uint_as_float(v[i])
+                                             : __fadd_ru(__uint_as_float(v[i]), __fmaf_ru(eq, rc[i].y, rc[i].w));
+                        mask |= (want && u >= thr2 ? 1u : 0u) << i;
+                    }
+                    const int base = mask ? atomicAdd(&P.cnt[q], __popc(mask)) : 0;
+                    const uint32_t any = __reduce_or_sync(0xffffffffu, mask);
 #pragma unroll
-                        for (int i = 0; i < kChunk; ++i) {
-                            if (mask & (1u << i)) {
-                                if (slot < P.cap) cq[slot] = make_int2(row0 + c * kChunk + i, (int)v[i]);
-                                ++slot;
-                            }
+                    for (int i = 0; i < C; ++i) {
+                        if ((any >> i) & 1u) {  // warp-uniform
+                            const int slot = base + __popc(mask & ((1u << i) - 1u));
+                            if (((mask >> i) & 1u) && slot < P.cap) cq[slot] = make_int2(rw + i, (int)v[i]);
                         }
                     }
                 }
-                maxl = __fsub_rd(maxl, eq0);
-                // The running threshold is the k-th best of the chunk maxima: k
-                // distinct chunks hold k distinct rows with a lower bound at
-                // least that large, so it never exceeds the k-th best lower bound.
-                if (maxl > thr && valid) {
-                    const int chunk = (row0 + c * kChunk) / kChunk;
-                    atomicMax(&P.bins[(size_t)q * P.k + chunk % P.k], f2ord(maxl));
-                }
-                if (maxl > top.mn && j > 0) {
-                    top.push(maxl);
-                    thr = fmaxf(top.mn, tau_c);
-                }
             }
+            // Running threshold: the k-th best of per-tile maxima (distinct tiles
+            // are distinct rows, so it never exceeds the k-th best lower bound);
+            // the bins take the same maxima, bin = tile half mod k.
+            const float maxl = __fsub_rd(tmax, eq0);
+            if (valid && maxl > thr) atomicMax(&P.bins[(size_t)q * P.k + (r * 2 + half) % P.k], f2ord(maxl));
+            if (valid && j > 0 && maxl > top.mn) top.push(maxl);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
