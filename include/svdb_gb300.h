@@ -102,6 +102,31 @@ int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t 
                             int metric, int precision, int64_t* d_ids, double* d_dists, double* d_err,
                             svdb_search_stats* stats);
 
+/*
+ * Exact FP64 top-k that allocates no device memory; no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc -- an allocator hook or
+ * memory pool that owns every device byte, a latency-critical path that must
+ * not take the driver's allocation lock, a host that has handed all free HBM
+ * to another component.  Same results as svdb_search_topk_device with
+ * SVDB_PREC_FP64 (ids, values, ties to the lowest index); queries, ids and
+ * dists are DEVICE buffers the caller owns, the work is queued on
+ * svdb_stream(db) and the call returns without waiting.
+ *
+ * The per-call scratch (padded queries, norms, partial top-k lists) lives in
+ * one fixed 16 MiB device array that every GPU loading this library holds
+ * until the process exits.  A call needs about 8 D bytes per query plus 16
+ * bytes per (query, result, row slice), at most 592 slices (64 queries of
+ * D = 768, top-32: about 3 MB); one that needs more is rejected with
+ * SVDB_EINVAL and a message saying how much it needed.  The store must have no pending
+ * mutations (call svdb_sync before; syncing can allocate).  The first call on
+ * a device looks up the array's device address for that device; make that
+ * first call before any stream capture.  Every call shares the array: calls
+ * whose work overlaps on the GPU (other streams, other databases) race, so
+ * order them.
+ */
+int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim, size_t k,
+                                  int metric, int64_t* d_ids, double* d_dists);
+
 /* Bulk insert of n rows (n x dim, row-major, copied): the same result as n
  * vector_db_insert calls, including the KD nodes.  uuids: n*37 bytes or
  * NULL.  Returns the first new index in *first_index. */

@@ -283,3 +283,26 @@ SVDB_API int svdb_profile_read(VectorDatabase* db, double* ms, int reset) {
     pthread_mutex_unlock(&db->mutex);
     return rc;
 }
+
+/* See include/svdb_gb300.h: the search for callers that cannot allocate. */
+SVDB_API int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim,
+                                           size_t k, int metric, int64_t* d_ids, double* d_dists) {
+    if (!db) {
+        svdb_set_error("svdb_search_topk_fp64_noalloc: NULL database");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc;
+    if (!d->dev) {
+        svdb_set_error("svdb_search_topk_fp64_noalloc: the store holds no rows");
+        rc = SVDB_EINVAL;
+    } else if (dim != d->dim) {
+        svdb_set_error("svdb_search_topk_fp64_noalloc: query dimension %zu != store dimension %zu", dim, d->dim);
+        rc = SVDB_EINVAL;
+    } else {
+        rc = svdbd_search_noalloc(d->dev, d_queries, nq, k, metric, d_ids, d_dists);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}

@@ -70,6 +70,11 @@ int svdbd_compare_vectors(int metric, const double* a, const double* b, size_t d
 int svdbd_search(svdbd_store* s, const double* q, size_t nq, size_t k, int metric, int precision,
                  int64_t* ids, double* dists, double* err, int on_device, svdb_search_stats* st);
 
+/* exact FP64 top-k with every per-call scratch byte in a fixed device array
+ * (dev_noalloc.cu); q/ids/dists in device memory; never allocates */
+int svdbd_search_noalloc(svdbd_store* s, const double* d_queries, size_t nq, size_t k, int metric, int64_t* d_ids,
+                         double* d_dists);
+
 /* ---- KD tree mirror ------------------------------------------------------ */
 svdbd_kd* svdbd_kd_create(size_t kdim);
 void svdbd_kd_destroy(svdbd_kd* t);

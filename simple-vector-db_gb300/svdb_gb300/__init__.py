@@ -91,6 +91,7 @@ def _load():
         "svdb_wait": (C.c_int, [vp]),
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
+        "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
     }
     for name, (res, args) in sig.items():
@@ -304,6 +305,13 @@ class VectorDatabase:
                                     err.ctypes.data_as(_dp) if with_err else None,
                                     C.byref(stats) if stats is not None else None), "svdb_search_topk")
         return (ids, dists, err) if with_err else (ids, dists)
+
+    def search_fp64_noalloc(self, q_ptr: int, nq: int, dim: int, k: int, metric: int, ids_ptr: int,
+                            dists_ptr: int) -> None:
+        """Exact FP64 top-k that allocates no device memory (device pointers,
+        queued on self.stream()); for callers that cannot call cudaMalloc."""
+        _check(lib.svdb_search_topk_fp64_noalloc(self.ptr, q_ptr, nq, dim, k, metric, ids_ptr, dists_ptr),
+               "svdb_search_topk_fp64_noalloc")
 
     def search_device(self, q_ptr: int, nq: int, dim: int, k: int, metric: int, precision: int, ids_ptr: int,
                       dists_ptr: int, err_ptr: int = 0, stats: SearchStats | None = None) -> None:
