@@ -42,6 +42,11 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
 METRICS = {"cosine": 0, "euclidean": 1, "dot": 2}
 N_ROWS, DIM, K_TOP, SEED = 1_000_000, 768, 10, 3
 METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GPU; p50/p99 ms"
+# DRAM bytes (read + write) of one k_screen_bf16 launch per store row, from the
+# ncu capture summarised in profiles/k_screen_bf16_200kx768_q4096.md (a 200,000-row
+# store, 4096 cosine queries; the bytes grow with the rows, so a full launch is
+# this times N).  None when no capture of the current kernel exists.
+SCREEN_DRAM_BYTES_PER_ROW = (314.145280e6 + 16.759808e6) / 200_000
 
 
 def log(*a):
@@ -257,8 +262,10 @@ def run_ours(args, ws, rank, local):
     if prec == S.PREC_BF16:
         flops = 2.0 * nq * N_ROWS * DIM
         ach = flops / (scr / 1e3) / 1e12
+        traffic = SCREEN_DRAM_BYTES_PER_ROW * N_ROWS if SCREEN_DRAM_BYTES_PER_ROW else None
         roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
-                "traffic": None, "peak_source": src, "kernel_ms": scr,
+                "traffic": traffic, "traffic_unit": "bytes per launch (ncu, scaled by rows)",
+                "algorithmic_bytes": N_ROWS * DIM * 2 + nq * DIM * 2, "peak_source": src, "kernel_ms": scr,
                 "algorithmic": f"2*Q*N*D = {flops:.3e} FLOP per launch"}
     else:
         nbytes = N_ROWS * (DIM * 8 + 1)
@@ -301,7 +308,7 @@ def main():
     global N_ROWS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp64"])
