@@ -524,7 +524,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     tmem_ld16(tbase + (uint32_t)(c * C), v);
                 tmem_ld_wait();
                 const float4* rc = rps + c * C;
-                float mu = -INFINITY;  // best upper bound (less eq0) of the chunk
+                // per 8-column group: best upper bound (less eq0); emission is
+                // handled group by group, only where some lane reaches the threshold
+                constexpr int G = C / 8;
+                float gm[G];
                 if (NORM) {
                     // keys are the accumulator values; rows that are not searchable
                     // become NaN (every comparison with NaN is false)
@@ -535,37 +538,57 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                             if (!((vb >> i) & 1u)) v[i] = 0x7fc00000u;
                     }
 #pragma unroll
-                    for (int i = 0; i < C; ++i) mu = fmaxf(mu, __uint_as_float(v[i]));
-                    tmax = fmaxf(tmax, mu);
+                    for (int g = 0; g < G; ++g) {
+                        float m = __uint_as_float(v[8 * g]);
+#pragma unroll
+                        for (int i = 1; i < 8; ++i) m = fmaxf(m, __uint_as_float(v[8 * g + i]));
+                        gm[g] = m;
+                        tmax = fmaxf(tmax, m);
+                    }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < C; ++i) {
-                        const float4 p = rc[i];
-                        const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
-                        const float e = __fmaf_ru(eq, p.y, p.w);
-                        tmax = fmaxf(tmax, __fsub_rd(key, e));
-                        mu = fmaxf(mu, __fadd_ru(key, e));
-                        v[i] = __float_as_uint(key);
+                    for (int g = 0; g < G; ++g) {
+                        float m = -INFINITY;
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const float4 p = rc[8 * g + i];
+                            const float key = __fmaf_rn(__uint_as_float(v[8 * g + i]), p.x, -p.z);
+                            const float e = __fmaf_ru(eq, p.y, p.w);
+                            tmax = fmaxf(tmax, __fsub_rd(key, e));
+                            m = fmaxf(m, __fadd_ru(key, e));
+                            v[8 * g + i] = __float_as_uint(key);
+                        }
+                        gm[g] = m;
                     }
                 }
-                // emission, warp-uniform: lanes reserve their slots with one atomic
-                // each, then the columns any lane emits are stored with predicates
+                float mu = gm[0];
+#pragma unroll
+                for (int g = 1; g < G; ++g) mu = fmaxf(mu, gm[g]);
                 const bool want = mu >= thr2 && q < P.nq;
                 if (__any_sync(0xffffffffu, want)) {
-                    uint32_t mask = 0;
 #pragma unroll
-                    for (int i = 0; i < C; ++i) {
-                        const float u = NORM ? __uint_as_float(v[i])
-                                             : __fadd_ru(__uint_as_float(v[i]), __fmaf_ru(eq, rc[i].y, rc[i].w));
-                        mask |= (want && u >= thr2 ? 1u : 0u) << i;
-                    }
-                    const int base = mask ? atomicAdd(&P.cnt[q], __popc(mask)) : 0;
-                    const uint32_t any = __reduce_or_sync(0xffffffffu, mask);
+                    for (int g = 0; g < G; ++g) {
+                        const bool wg = want && gm[g] >= thr2;
+                        if (!__any_sync(0xffffffffu, wg)) continue;  // warp-uniform
+                        // lanes reserve their slots with one atomic each; the columns
+                        // any lane emits are stored with predicates
+                        uint32_t mask = 0;
 #pragma unroll
-                    for (int i = 0; i < C; ++i) {
-                        if ((any >> i) & 1u) {  // warp-uniform
-                            const int slot = base + __popc(mask & ((1u << i) - 1u));
-                            if (((mask >> i) & 1u) && slot < P.cap) cq[slot] = make_int2(rw + i, (int)v[i]);
+                        for (int i = 0; i < 8; ++i) {
+                            const float u = NORM ? __uint_as_float(v[8 * g + i])
+                                                 : __fadd_ru(__uint_as_float(v[8 * g + i]),
+                                                             __fmaf_ru(eq, rc[8 * g + i].y, rc[8 * g + i].w));
+                            mask |= (wg && u >= thr2 ? 1u : 0u) << i;
+                        }
+                        const int base = mask ? atomicAdd(&P.cnt[q], __popc(mask)) : 0;
+                        const uint32_t any = __reduce_or_sync(0xffffffffu, mask);
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            if ((any >> i) & 1u) {  // warp-uniform
+                                const int slot = base + __popc(mask & ((1u << i) - 1u));
+                                if (((mask >> i) & 1u) && slot < P.cap)
+                                    cq[slot] = make_int2(rw + 8 * g + i, (int)v[8 * g + i]);
+                            }
                         }
                     }
                 }
