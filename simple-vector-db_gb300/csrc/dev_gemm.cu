@@ -932,7 +932,7 @@ __device__ void refine_keep(int q, int n, int k, float2* luq, const int2* sq, in
 __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restrict__ x32, size_t ld,
                                                            const float* __restrict__ q32,
                                                            const double* __restrict__ qsq,
-                                                           const float2* __restrict__ sqf,
+                                                           const float4* __restrict__ sqf,
                                                            const float4* __restrict__ rowp,
                                                            const float4* __restrict__ qpar, int2* __restrict__ surv,
                                                            const int* __restrict__ nsurv, int* __restrict__ nref,
@@ -988,7 +988,7 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
         p += __shfl_xor_sync(0xffffffffu, p, 2);
         p += __shfl_xor_sync(0xffffffffu, p, 1);
         if (act && h == 0) {
-            const float2 xb = sqf[row];  // |x|^2 in [xb.x, xb.y]
+            const float4 xb = sqf[row];  // |x|^2 in [xb.x, xb.y], 1/(2|x|) in [xb.z, xb.w]
             const float xn_up = rowp[row].x;
             const float sup = __fmul_ru(p, 1.0f + gamma);
             const float eta = __fmul_ru(1.1921875e-07f, __fadd_ru(qn_up, xn_up));  // 2^-23 (1 + 2^-13)
@@ -1005,12 +1005,9 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
                 if (metric == SVDB_DOT) {
                     L = __fmul_rd(a_lo, 0.5f);
                     U = __fmul_ru(a_hi, 0.5f);
-                } else {  // cosine key = dot / |x|, 1/(2|x|) in [m_lo, m_hi]
-                    const float xn_lo = __fsqrt_rd(xb.x);
-                    const float m_lo = __fdiv_rd(0.5f, xn_up);
-                    const float m_hi = xn_lo > 0.f ? __fdiv_ru(0.5f, xn_lo) : INFINITY;
-                    L = a_lo >= 0.f ? __fmul_rd(a_lo, m_lo) : __fmul_rd(a_lo, m_hi);
-                    U = a_hi >= 0.f ? __fmul_ru(a_hi, m_hi) : __fmul_ru(a_hi, m_lo);
+                } else {  // cosine key = dot / |x|, 1/(2|x|) in [xb.z, xb.w]
+                    L = a_lo >= 0.f ? __fmul_rd(a_lo, xb.z) : __fmul_rd(a_lo, xb.w);
+                    U = a_hi >= 0.f ? __fmul_ru(a_hi, xb.w) : __fmul_ru(a_hi, xb.z);
                     if (isnan(L)) L = -INFINITY;
                     if (isnan(U)) U = INFINITY;
                 }

@@ -7,7 +7,7 @@
 //   x32     C x ld   float    FP32 shadow of x64 (refinement stage)
 //   xbn     C x ldb  bf16     BF16 shadow of x64 / |x| (cosine screen)
 //   rowpn   C        float2   {|bxn| up, |x/|x| - bxn| up}
-//   sqf     C        float2   {|x|^2 down, |x|^2 up} in FP32
+//   sqf     C        float4   {|x|^2 down, |x|^2 up, 1/(2|x|) down, 1/(2|x|) up} in FP32
 //   sq64    C        double   canonical sum of squares of the master row
 //   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
 //   live    C        uint8    1 = searchable row, 2 = row of another dimension
@@ -46,7 +46,7 @@ namespace svdb {
 // One group of 4 lanes per row, canonical order for the sum of squares.
 __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bfloat16* __restrict__ xb,
                               size_t ldb, float* __restrict__ x32, __nv_bfloat16* __restrict__ xbn,
-                              float2* __restrict__ rowpn, float2* __restrict__ sqf, double* __restrict__ sq64,
+                              float2* __restrict__ rowpn, float4* __restrict__ sqf, double* __restrict__ sq64,
                               float4* __restrict__ rowp,
                               const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
                               const int64_t* __restrict__ list) {
@@ -109,7 +109,13 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     if (active && s == 0) {
         // x/|x| is itself rounded (relative 2^-52 per element): the 2^-30 margin covers it
         const double up = 1.0 + 9.313225746154785e-10;
-        sqf[slot] = make_float2(__double2float_rd(sq), __double2float_ru(sq));
+        {
+            // |x| to within 2^-50 relative either way (FP64 sum and square root)
+            const double xn = sqrt(sq);
+            const double lo = xn * (1.0 - 8.881784197001252e-16), hi = xn * (1.0 + 8.881784197001252e-16);
+            sqf[slot] = make_float4(__double2float_rd(sq), __double2float_ru(sq), __double2float_rd(0.5 / hi),
+                                    lo > 0.0 ? __double2float_ru(0.5 / lo) : __int_as_float(0x7f800000));
+        }
         rowpn[slot] = make_float2(__double2float_ru(sqrt(nbh) * up), __double2float_ru(sqrt(nres) * up + 1e-300));
         sq64[slot] = sq;
         float4 p;
@@ -336,7 +342,7 @@ int Store::grow(size_t need) {
     float* nf = nullptr;
     __nv_bfloat16* nbn = nullptr;
     float2* npn = nullptr;
-    float2* nsf = nullptr;
+    float4* nsf = nullptr;
     double* nsq = nullptr;
     float4* np = nullptr;
     uint8_t* nl = nullptr;
@@ -347,7 +353,7 @@ int Store::grow(size_t need) {
     if (e == cudaSuccess) e = cudaMalloc(&nf, nc * ld * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&nbn, nc * ldb * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc(&npn, nc * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMalloc(&nsf, nc * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&nsf, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nl, nc);
@@ -373,7 +379,7 @@ int Store::grow(size_t need) {
         SVDB_CUDA(cudaMemcpyAsync(nf, x32, slots * ld * sizeof(float), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nbn, xbn, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(npn, rowpn, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
-        SVDB_CUDA(cudaMemcpyAsync(nsf, sqf, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nsf, sqf, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nl, live, slots, cudaMemcpyDeviceToDevice, stream));

@@ -26,7 +26,8 @@ struct Store {
     float* x32 = nullptr;  // FP32 shadow (cap x ld), read by the refinement stage
     __nv_bfloat16* xbn = nullptr;  // BF16 shadow of x / |x| (cap x ldb): the cosine screen
     float2* rowpn = nullptr;       // {|bxn| up, |x/|x| - bxn| up} per row
-    float2* sqf = nullptr;         // {|x|^2 rounded down, |x|^2 rounded up} in FP32 (refinement)
+    float4* sqf = nullptr;         // FP32 intervals for the refinement: {|x|^2 down, |x|^2 up,
+                                   //  1/(2|x|) down, 1/(2|x|) up}
     int* d_nmax = nullptr;         // {max |x/|x| - bxn|, max |bxn|} over searchable rows (float bits)
     double* sq64 = nullptr;
     float4* rowp = nullptr;  // {|x| up (-1: dead slot), |bf16 x| up, |x - bf16 x| up (inf: unscreenable), |x|^2/2}
