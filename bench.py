@@ -180,9 +180,9 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     st = S.SearchStats()
 
-    def step(b):
+    def step(b, stats=None):
         q = Qd[b % nbatch]
-        db.search_device(q.data_ptr(), nq, DIM, k, metric, prec, ids.data_ptr(), dists.data_ptr(), 0, st)
+        db.search_device(q.data_ptr(), nq, DIM, k, metric, prec, ids.data_ptr(), dists.data_ptr(), 0, stats)
 
     # correctness guard on a slice of the first batch: ids equal the device FP64 scan
     ids_ref, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP64)
@@ -192,6 +192,8 @@ def run_ours(args, ws, rank, local):
 
     for w in range(args.warmup):
         step(w)
+    step(0, st)  # the candidate funnel and launch count of one search (statistics cost a host round trip)
+    launches_per_step = st.kernels
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -209,7 +211,7 @@ def run_ours(args, ws, rank, local):
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
         step(s)
-        kernels += st.kernels
+        kernels += launches_per_step
         b.record(stream)
         per_step.append((a, b))
     ev1.record(stream)

@@ -733,7 +733,8 @@ __global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ r
     }
 }
 
-__global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int nq, int k, int* err, int* alpha) {
+__global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int nq, int k, int* alpha, int* redo_n,
+                              unsigned long long* stats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nq) {
         tau[i] = f2ord(-INFINITY);
@@ -742,9 +743,10 @@ __global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int
         flags[i] = scr::kOk;
     }
     if (i == 0) {
-        *err = 0;
         *alpha = 0;
+        *redo_n = 0;
     }
+    if (i < 5) stats[i] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1036,40 +1038,64 @@ __global__ void __launch_bounds__(kRefThreads) k_refine_keep(const int2* __restr
 }
 
 // ---------------------------------------------------------------------------
-// stage 3: FP64 re-rank of the survivors in the canonical order.  Block
-// (q, split) scores survivors split, split + splits, ... (64 rows at a time,
-// 4 lanes per row) and writes its best k as a partial list.
+// stage 3: FP64 re-rank of what the refinement keeps
 // ---------------------------------------------------------------------------
-template <int KS, bool EUC>
-__global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, size_t ld,
-                                                const double* __restrict__ qbuf, const double* __restrict__ qsq,
-                                                const double* __restrict__ sq64, const int2* __restrict__ surv,
-                                                size_t surv_stride, const int* __restrict__ nsurv, int k, int metric,
-                                                const float4* __restrict__ rpar, const float4* __restrict__ qpar,
-                                                Entry* __restrict__ part, uint8_t* __restrict__ flags) {
+// The common case: at most kSmallRerank rows left per query.  One block per
+// query scores them (4 lanes per row, canonical order) and ranks them by
+// counting, on order-preserving 64-bit integer images of the ranking key (the
+// FP64 pipe is narrow; -0.0 is folded into +0.0 and NaN ranks as +inf, exactly
+// as double comparisons order them), ties to the lowest row.  Queries with
+// more rows are answered by the exact scan.
+constexpr int kSmallRerank = 512;
+
+__device__ __forceinline__ long long rank_ord(int metric, double v) {
+    double kk = metric == SVDB_EUCLIDEAN ? v : -v;
+    if (isnan(kk)) kk = __longlong_as_double(0x7ff0000000000000ll);
+    if (kk == 0.0) kk = 0.0;
+    const long long b = __double_as_longlong(kk);
+    return b >= 0 ? b : b ^ 0x7fffffffffffffffll;
+}
+
+template <bool EUC>
+__global__ void __launch_bounds__(256) k_rerank_small(const double* __restrict__ x64, size_t ld,
+                                                      const double* __restrict__ qbuf, const double* __restrict__ qsq,
+                                                      const double* __restrict__ sq64, const int2* __restrict__ surv,
+                                                      size_t surv_stride, const int* __restrict__ nsurv, int k,
+                                                      int metric, int d, const float4* __restrict__ rpar,
+                                                      const float4* __restrict__ qpar,
+                                                      const int64_t* __restrict__ logical, int64_t* __restrict__ ids,
+                                                      double* __restrict__ dists, double* __restrict__ err,
+                                                      uint8_t* __restrict__ flags) {
     extern __shared__ __align__(16) uint8_t sm[];
     double* qs = reinterpret_cast<double*>(sm);
-    const int q = blockIdx.x, split = blockIdx.y, splits = gridDim.y;
-    if (flags[q] != scr::kOk) return;  // answered by the exact scan
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
-    for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = qbuf[(size_t)q * ld + i];
-    __syncthreads();
+    long long* skey = reinterpret_cast<long long*>(qs + ld);
+    double* sval = reinterpret_cast<double*>(skey + kSmallRerank);
+    int* srow = reinterpret_cast<int*>(sval + kSmallRerank);
+    int* spos = srow + kSmallRerank;  // candidate index at each output position
+    __shared__ int s_bad;
+    const int q = blockIdx.x;
+    if (flags[q] != scr::kOk) return;
     const int n = nsurv[q];
+    if (n > kSmallRerank) {
+        if (threadIdx.x == 0) flags[q] = scr::kOverflow;  // the exact scan answers it
+        return;
+    }
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 2, s = lane & 3;
+    for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = qbuf[(size_t)q * ld + i];
+    if (threadIdx.x == 0) s_bad = 0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) spos[i] = -1;
+    __syncthreads();
     const int2* sq = surv + (size_t)q * surv_stride;
     const double qq = qsq[q];
     const double qn = sqrt(qq);
     const float4 qp = qpar[q];
-    bool bound_ok = true;
-    WarpList<KS> Lw;
-    Lw.init();
-    for (int base = (split * 8 + warp) * 8; base < n; base += splits * 64) {
+    for (int base = 0; base < n; base += 64) {
         const int i = base + g;
         const bool act = i < n;
         const int2 c = act ? sq[i] : make_int2(0, 0);
-        const int row = c.x;
         double p = 0.0;
         if (act) {
-            const double* x = x64 + (size_t)row * ld;
+            const double* x = x64 + (size_t)c.x * ld;
             for (size_t j = 2 * s; j < ld; j += 8) {
                 const double2 v = *reinterpret_cast<const double2*>(x + j);
                 const double2 qv = *reinterpret_cast<const double2*>(qs + j);
@@ -1084,10 +1110,9 @@ __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, 
             }
         }
         p = group4_sum(p);
-        double val = 0.0;
-        if (act) {
-            const double xs = sq64[row];
-            double kex;
+        if (act && s == 0) {
+            const double xs = sq64[c.x];
+            double val, kex;
             if (EUC) {
                 val = sqrt(p);
                 kex = 0.5 * (qq - p);
@@ -1100,144 +1125,87 @@ __global__ void __launch_bounds__(256) k_rerank(const double* __restrict__ x64, 
             }
             // the screen's bound must hold against the exact value
             const float key = __int_as_float(c.y);
-            const float e = screen_bound(rpar[row], qp.x, qp.y, qp.z);
-            if (s == 0 && !(fabs(kex - (double)key) <= (double)e)) bound_ok = false;
+            if (!(fabs(kex - (double)key) <= (double)screen_bound(rpar[c.x], qp.x, qp.y, qp.z))) s_bad = 1;
+            skey[i] = rank_ord(metric, val);
+            sval[i] = val;
+            srow[i] = c.x;
         }
-        const double kk = rank_key(metric, val);
-        double wk;
-        int wi;
-        Lw.worst(k, wk, wi);
-        const bool cand_ok = act && s == 0 && key_less(kk, row, wk, wi);
-        unsigned m = __ballot_sync(0xffffffffu, cand_ok);
-        while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1;
-            Lw.insert(__shfl_sync(0xffffffffu, kk, src), __shfl_sync(0xffffffffu, row, src),
-                      __shfl_sync(0xffffffffu, val, src), k);
-        }
-    }
-    if (!__all_sync(0xffffffffu, bound_ok) && lane == 0) flags[q] = scr::kBoundFail;
-    __syncthreads();  // query row no longer needed: reuse shared memory for the block merge
-    constexpr int KP = 32 * KS;
-    Entry* lists = reinterpret_cast<Entry*>(sm);
-#pragma unroll
-    for (int t = 0; t < KS; ++t) {
-        Entry e;
-        e.val = Lw.val[t];
-        e.id = Lw.id[t];
-        e.pad = 0;
-        lists[warp * KP + t * 32 + lane] = e;
     }
     __syncthreads();
-    if (warp == 0) {
-        WarpList<KS> M;
-        M.init();
-        for (int w = 0; w < 8; ++w) {
-            for (int c0 = 0; c0 < k; c0 += 32) {
-                const int pp = c0 + lane;
-                const Entry e = lists[w * KP + min(pp, KP - 1)];
-                const double key = rank_key(metric, e.val);
-                double wk;
-                int wi;
-                M.worst(k, wk, wi);
-                const bool ok = pp < k && e.id != 0x7fffffff && key_less(key, e.id, wk, wi);
-                unsigned m = __ballot_sync(0xffffffffu, ok);
-                while (m) {
-                    const int src = __ffs(m) - 1;
-                    m &= m - 1;
-                    M.insert(__shfl_sync(0xffffffffu, key, src), __shfl_sync(0xffffffffu, e.id, src),
-                             __shfl_sync(0xffffffffu, e.val, src), k);
-                }
-            }
-        }
-        Entry* out = part + ((size_t)q * splits + split) * k;
-#pragma unroll
-        for (int t = 0; t < KS; ++t) {
-            const int pp = t * 32 + lane;
-            if (pp < k) {
-                Entry e;
-                e.val = M.val[t];
-                e.id = M.id[t];
-                e.pad = 0;
-                out[pp] = e;
-            }
-        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const long long ki = skey[i];
+        const int ri = srow[i];
+        int pos = 0;
+        for (int j = 0; j < n; ++j) pos += (skey[j] < ki || (skey[j] == ki && srow[j] < ri)) ? 1 : 0;
+        if (pos < k) spos[pos] = i;
     }
-}
-
-// one warp per query: merge the partial lists of the re-rank; the result is
-// exact only if all k entries are finite (NaN-valued rows, which the screen
-// never emits, could otherwise belong in the list)
-template <int KS>
-__global__ void k_merge_rerank(const Entry* __restrict__ part, int splits, int nq, int k, int metric, int d,
-                               const int64_t* __restrict__ logical, const double* __restrict__ qsq,
-                               const double* __restrict__ sq64, int64_t* __restrict__ ids,
-                               double* __restrict__ dists, double* __restrict__ err, uint8_t* __restrict__ flags) {
-    const int q = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (q >= nq || flags[q] != scr::kOk) return;
-    WarpList<KS> M;
-    M.init();
-    const Entry* src = part + (size_t)q * splits * k;
-    const int total = splits * k;
-    for (int c = 0; c < total; c += 32) {
-        const int p = c + lane;
-        Entry e;
-        e.val = 0.0;
-        e.id = 0x7fffffff;
-        if (p < total) e = src[p];
-        const double key = rank_key(metric, e.val);
-        double wk;
-        int wi;
-        M.worst(k, wk, wi);
-        const bool cand = p < total && e.id != 0x7fffffff && key_less(key, e.id, wk, wi);
-        unsigned m = __ballot_sync(0xffffffffu, cand);
-        while (m) {
-            const int sl = __ffs(m) - 1;
-            m &= m - 1;
-            M.insert(__shfl_sync(0xffffffffu, key, sl), __shfl_sync(0xffffffffu, e.id, sl),
-                     __shfl_sync(0xffffffffu, e.val, sl), k);
-        }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_bad) flags[q] = scr::kBoundFail;
+    if (s_bad) return;
+    // exact only with k finite results: NaN-valued rows, which the screen never
+    // emits, could otherwise belong in the list
+    int fin = 1;
+    for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        const int i = spos[t];
+        if (i < 0 || isnan(sval[i])) fin = 0;
     }
-    bool fin = true;
-#pragma unroll
-    for (int t = 0; t < KS; ++t) {
-        const int pp = t * 32 + lane;
-        if (pp < k && (M.id[t] == 0x7fffffff || isnan(M.val[t]))) fin = false;
-    }
-    if (!__all_sync(0xffffffffu, fin)) {
-        if (lane == 0) flags[q] = scr::kTooFew;
+    if (!__syncthreads_and(fin)) {
+        if (threadIdx.x == 0) flags[q] = scr::kTooFew;
         return;
     }
-#pragma unroll
-    for (int t = 0; t < KS; ++t) {
-        const int pp = t * 32 + lane;
-        if (pp < k) {
-            const int slot = M.id[t];
-            const size_t o = (size_t)q * k + pp;
-            ids[o] = logical[slot];
-            dists[o] = M.val[t];
-            if (err) err[o] = result_err_bound(metric, d, M.val[t], qsq[q], sq64[slot]);
-        }
+    for (int t = threadIdx.x; t < k; t += blockDim.x) {
+        const int i = spos[t];
+        const size_t o = (size_t)q * k + t;
+        ids[o] = logical[srow[i]];
+        dists[o] = sval[i];
+        if (err) err[o] = result_err_bound(metric, d, sval[i], qq, sq64[srow[i]]);
     }
 }
 
 // gather query rows (padded FP64) of the queries to re-answer; scatter back
+// queries the screen could not certify, compacted on the device, with the
+// batch's statistics {candidates, survivors, re-ranked, widened, bound failures}
+__global__ void k_collect_redo(const uint8_t* __restrict__ flags, const int* __restrict__ cnt,
+                               const int* __restrict__ nsurv, const int* __restrict__ nref, int nq,
+                               int* __restrict__ list, int* __restrict__ count,
+                               unsigned long long* __restrict__ stats) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long v[5] = {0, 0, 0, 0, 0};
+    if (q < nq) {
+        const uint8_t f = flags[q];
+        if (f != scr::kOk) list[atomicAdd(count, 1)] = q;
+        v[0] = (unsigned)cnt[q];
+        v[1] = (unsigned)nsurv[q];
+        v[2] = (unsigned)nref[q];
+        v[3] = f != scr::kOk;
+        v[4] = f == scr::kBoundFail;
+    }
+#pragma unroll
+    for (int t = 0; t < 5; ++t) {
+        unsigned long long x = v[t];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(stats + t, x);
+    }
+}
+
+// gather query rows (padded FP64) of the queries to re-answer; scatter back
+// (the count lives on the device: with nothing to re-answer these exit at once)
 __global__ void k_gather_queries(const double* __restrict__ qbuf, const double* __restrict__ qsq, size_t ld,
-                                 const int* __restrict__ list, int n, double* __restrict__ qout,
-                                 double* __restrict__ qsq_out) {
+                                 const int* __restrict__ list, const int* __restrict__ n_dev,
+                                 double* __restrict__ qout, double* __restrict__ qsq_out) {
     const int i = blockIdx.x;
-    if (i >= n) return;
+    if (i >= *n_dev) return;
     const int q = list[i];
     for (size_t j = threadIdx.x; j < ld; j += blockDim.x) qout[(size_t)i * ld + j] = qbuf[(size_t)q * ld + j];
     if (threadIdx.x == 0) qsq_out[i] = qsq[q];
 }
 
 __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const double* __restrict__ d_in,
-                                  const double* __restrict__ e_in, const int* __restrict__ list, int n, int k,
-                                  int64_t* __restrict__ ids, double* __restrict__ dists, double* __restrict__ err) {
+                                  const double* __restrict__ e_in, const int* __restrict__ list,
+                                  const int* __restrict__ n_dev, int k, int64_t* __restrict__ ids,
+                                  double* __restrict__ dists, double* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n * k) return;
+    if (i >= *n_dev * k) return;
     const int qi = i / k, j = i % k;
     const size_t o = (size_t)list[qi] * k + j;
     ids[o] = ids_in[i];
@@ -1253,6 +1221,7 @@ struct GemmPlanCache {
     bool attr_set[4] = {false, false, false, false};
     bool select_attr = false;
     bool sort_attr = false;
+    bool rerank_attr = false;
     size_t screen_smem = 0;
 };
 
@@ -1303,11 +1272,12 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 }
 
 struct Bf16Layout {
-    size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, part, flags, err,
-        alpha, total;
-    int ntr, cap, splits;
+    size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
+    int ntr, cap;
     size_t npad;
 };
+
+constexpr size_t k_max_bf16 = 32;  // the screen's running top-k holds at most 32
 
 static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     Bf16Layout L;
@@ -1339,12 +1309,16 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.nref = take(nq * sizeof(int));
     L.sig = take(nq * sizeof(int));
     L.perm = take(nq * sizeof(int));
-    // re-rank splits: spread small batches over the SMs
-    L.splits = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(2 * num_sms()) / std::max<size_t>(nq, 1)));
-    L.part = take(nq * (size_t)L.splits * 32 * sizeof(Entry));
     L.flags = take(nq);
-    L.err = take(sizeof(int));
     L.alpha = take(sizeof(int));
+    // the exact-scan fallback, sized for the whole batch (its count is on the device)
+    L.redo = take(nq * sizeof(int));
+    L.redo_n = take(sizeof(int));
+    L.stats = take(5 * sizeof(unsigned long long));
+    L.rq = take(nq * s->ld * sizeof(double));
+    L.rsq = take(nq * sizeof(double));
+    L.rres = take(nq * (size_t)k_max_bf16 * (sizeof(int64_t) + 2 * sizeof(double)));
+    L.rscr = take(search_fp64_scratch(s, nq, k_max_bf16));
     L.total = off;
     return L;
 }
@@ -1379,16 +1353,17 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     int* nref = reinterpret_cast<int*>(base + L.nref);
     int* sig = reinterpret_cast<int*>(base + L.sig);
     int* perm = reinterpret_cast<int*>(base + L.perm);
-    Entry* part = reinterpret_cast<Entry*>(base + L.part);
     uint8_t* flags = base + L.flags;
-    int* derr = reinterpret_cast<int*>(base + L.err);
+    int* redo = reinterpret_cast<int*>(base + L.redo);
+    int* redo_n = reinterpret_cast<int*>(base + L.redo_n);
+    unsigned long long* dstats = reinterpret_cast<unsigned long long*>(base + L.stats);
     const int nq = (int)a.nq, k = (int)a.k;
     uint32_t kernels = 0;
 
     k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
                                                                           qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
-    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, flags, nq, k, derr, alpha);
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, flags, nq, k, alpha, redo_n, dstats);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
@@ -1413,7 +1388,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.bins = bins;
     P.cnt = cnt;
     P.cand = cand;
-    P.err = derr;
+    P.err = s->d_err;  // persistent: read at the next synchronous point
     P.nq = nq;
     P.k = k;
     P.cap = L.cap;
@@ -1488,88 +1463,64 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     kernels += 2;
     s->prof_mark(4);
 
-    const size_t rr_smem = std::max(s->ld * sizeof(double), (size_t)8 * 32 * sizeof(Entry));
-    const dim3 rgrid((unsigned)nq, (unsigned)L.splits);
-    if (a.metric == SVDB_EUCLIDEAN)
-        k_rerank<1, true><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k,
-                                                              a.metric, rpar, qpar, part, flags);
-    else
-        k_rerank<1, false><<<rgrid, 256, rr_smem, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k,
-                                                               a.metric, rpar, qpar, part, flags);
-    SVDB_LAUNCH_CHECK();
-    k_merge_rerank<1><<<(unsigned)((a.nq * 32 + 255) / 256), 256, 0, s->stream>>>(
-        part, L.splits, nq, k, a.metric, (int)s->dim, s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err, flags);
-    SVDB_LAUNCH_CHECK();
-    kernels += 2;
+    {
+        const size_t rr_smem = s->ld * sizeof(double) + (size_t)kSmallRerank * (8 + 8 + 4 + 4);
+        if (!gc->rerank_attr) {
+            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           200 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           200 * 1024));
+            gc->rerank_attr = true;
+        }
+        if (a.metric == SVDB_EUCLIDEAN)
+            k_rerank_small<true><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
+                s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k, a.metric, (int)s->dim, rpar, qpar,
+                s->logical, a.ids, a.dists, a.err, flags);
+        else
+            k_rerank_small<false><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
+                s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k, a.metric, (int)s->dim, rpar, qpar,
+                s->logical, a.ids, a.dists, a.err, flags);
+        SVDB_LAUNCH_CHECK();
+        ++kernels;
+    }
 
-    // queries the screen could not certify: exact FP64 scan
-    std::vector<uint8_t> hflags(a.nq);
-    std::vector<int> hcnt(3 * a.nq);
-    int herr = 0;
-    SVDB_CUDA(cudaMemcpyAsync(hflags.data(), flags, a.nq, cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaMemcpyAsync(hcnt.data(), cnt, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaMemcpyAsync(hcnt.data() + a.nq, nsurv, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaMemcpyAsync(hcnt.data() + 2 * a.nq, nref, a.nq * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    SVDB_CUDA(cudaStreamSynchronize(s->stream));
-    if (herr) {
-        svdb_set_error("search_bf16: the screen kernel's bounded wait ran out");
-        return SVDB_ETIMEOUT;
-    }
-    std::vector<int> redo;
-    uint64_t c0 = 0, c1 = 0, c2 = 0;
-    uint32_t bound_fail = 0;
-    for (size_t i = 0; i < a.nq; ++i) {
-        if (hflags[i] != scr::kOk) redo.push_back((int)i);
-        if (hflags[i] == scr::kBoundFail) ++bound_fail;
-        c0 += (uint64_t)hcnt[i];
-        c1 += (uint64_t)hcnt[a.nq + i];
-        c2 += (uint64_t)hcnt[2 * a.nq + i];
-    }
-    if (st) {
-        st->candidates += c0;
-        st->survivors += c1;
-        st->reranked += c2;
-        st->widened += (uint32_t)redo.size();
-        st->bound_failures += bound_fail;
-    }
-    if (!redo.empty()) {
-        const size_t nr = redo.size();
-        const size_t need = round_up(nr * s->ld * sizeof(double), 256) + round_up(nr * sizeof(double), 256) +
-                            round_up(nr * sizeof(int), 256) +
-                            round_up(nr * a.k * (sizeof(int64_t) + 2 * sizeof(double)), 256) +
-                            search_fp64_scratch(s, nr, a.k);
-        rc = s->scratch2_reserve(need);
-        if (rc) return rc;
-        uint8_t* b2 = reinterpret_cast<uint8_t*>(s->scratch2);
-        double* rq = reinterpret_cast<double*>(b2);
-        b2 += round_up(nr * s->ld * sizeof(double), 256);
-        double* rsq = reinterpret_cast<double*>(b2);
-        b2 += round_up(nr * sizeof(double), 256);
-        int* rlist = reinterpret_cast<int*>(b2);
-        b2 += round_up(nr * sizeof(int), 256);
-        int64_t* rids = reinterpret_cast<int64_t*>(b2);
-        double* rd = reinterpret_cast<double*>(rids + nr * a.k);
-        double* re = rd + nr * a.k;
-        b2 += round_up(nr * a.k * (sizeof(int64_t) + 2 * sizeof(double)), 256);
-        SVDB_CUDA(cudaMemcpyAsync(rlist, redo.data(), nr * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-        k_gather_queries<<<(unsigned)nr, 256, 0, s->stream>>>(a.q, a.qsq, s->ld, rlist, (int)nr, rq, rsq);
+    // queries the screen could not certify: exact FP64 scan, entirely on the
+    // device (no host round trip; with nothing to redo the kernels exit at once)
+    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, nsurv, nref, nq, redo, redo_n,
+                                                                          dstats);
+    SVDB_LAUNCH_CHECK();
+    {
+        double* rq = reinterpret_cast<double*>(base + L.rq);
+        double* rsq = reinterpret_cast<double*>(base + L.rsq);
+        int64_t* rids = reinterpret_cast<int64_t*>(base + L.rres);
+        double* rd = reinterpret_cast<double*>(rids + a.nq * a.k);
+        double* re = rd + a.nq * a.k;
+        k_gather_queries<<<(unsigned)nq, 256, 0, s->stream>>>(a.q, a.qsq, s->ld, redo, redo_n, rq, rsq);
         SVDB_LAUNCH_CHECK();
         SearchArgs b = a;
         b.q = rq;
         b.qsq = rsq;
-        b.nq = nr;
         b.ids = rids;
         b.dists = rd;
         b.err = re;
+        b.nq_dev = redo_n;
         uint32_t kk = 0;
-        rc = search_fp64(s, b, b2, search_fp64_scratch(s, nr, a.k), &kk, false);
+        rc = search_fp64(s, b, base + L.rscr, search_fp64_scratch(s, a.nq, a.k), &kk, false);
         if (rc) return rc;
-        k_scatter_results<<<(unsigned)((nr * a.k + 255) / 256), 256, 0, s->stream>>>(rids, rd, re, rlist, (int)nr,
-                                                                                  (int)a.k, a.ids, a.dists, a.err);
+        k_scatter_results<<<(unsigned)((a.nq * a.k + 255) / 256), 256, 0, s->stream>>>(rids, rd, re, redo, redo_n,
+                                                                                    (int)a.k, a.ids, a.dists, a.err);
         SVDB_LAUNCH_CHECK();
-        SVDB_CUDA(cudaStreamSynchronize(s->stream));  // redo (host vector) and the pinned lists go out of scope
-        kernels += kk + 2;
+        kernels += kk + 3;
+    }
+    if (st) {  // statistics cost a host round trip: only when asked for
+        unsigned long long h[5];
+        SVDB_CUDA(cudaMemcpyAsync(h, dstats, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+        SVDB_CUDA(cudaStreamSynchronize(s->stream));
+        st->candidates += h[0];
+        st->survivors += h[1];
+        st->reranked += h[2];
+        st->widened += (uint32_t)h[3];
+        st->bound_failures += (uint32_t)h[4];
     }
     s->prof_mark(5);
     if (st) st->kernels += kernels;

@@ -66,8 +66,11 @@ __global__ void __launch_bounds__(256) k_scan_fp64(const double* __restrict__ x6
                                                    const double* __restrict__ sq64, int64_t nslots,
                                                    int64_t rows_per_slice, const double* __restrict__ qbuf,
                                                    const double* __restrict__ qsq, int nq, int metric, int k,
-                                                   Entry* __restrict__ part, int nslices) {
+                                                   Entry* __restrict__ part, int nslices,
+                                                   const int* __restrict__ nq_dev) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (nq_dev) nq = min(nq, *nq_dev);
+    if ((int)blockIdx.y * QB >= nq) return;  // whole block beyond the answered queries
     double* qs = reinterpret_cast<double*>(smem_raw);
     const int qb0 = blockIdx.y * QB;
     const int slice = blockIdx.x;
@@ -192,12 +195,14 @@ __global__ void __launch_bounds__(256) k_scan_fp64(const double* __restrict__ x6
 
 // one warp per query: merge nslices x k partial lists, write logical ids
 template <int KS>
-__global__ void k_merge_fp64(const Entry* __restrict__ part, int nslices, int nq, int k, int metric, int d,
+__global__ void k_merge_fp64(const Entry* __restrict__ part, int nslices, int nq, const int* __restrict__ nq_dev, int k,
+                             int metric, int d,
                              const int64_t* __restrict__ logical, const double* __restrict__ qsq,
                              const double* __restrict__ sq64, int64_t* __restrict__ ids, double* __restrict__ dists,
                              double* __restrict__ err) {
     const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
+    if (nq_dev) nq = min(nq, *nq_dev);
     if (qi >= nq) return;
     WarpList<KS> M;
     M.init();
@@ -276,7 +281,7 @@ static int launch_scan(Store* s, const ScanPlan& p, const SearchArgs& a, Entry* 
     if (p.smem > 48 * 1024) SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
     dim3 grid((unsigned)p.nslices, (unsigned)p.nqb);
     kern<<<grid, 256, p.smem, s->stream>>>(s->x64, s->ld, s->live, s->sq64, (int64_t)s->slots, p.rows_per_slice, a.q,
-                                          a.qsq, (int)a.nq, a.metric, (int)a.k, part, p.nslices);
+                                          a.qsq, (int)a.nq, a.metric, (int)a.k, part, p.nslices, a.nq_dev);
     SVDB_LAUNCH_CHECK();
     return SVDB_OK;
 }
@@ -312,15 +317,15 @@ int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     const unsigned blocks = (unsigned)((a.nq * 32 + 255) / 256);
     switch (p.ks) {
         case 1:
-            k_merge_fp64<1><<<blocks, 256, 0, s->stream>>>(part, p.nslices, (int)a.nq, (int)a.k, a.metric, (int)s->dim,
+            k_merge_fp64<1><<<blocks, 256, 0, s->stream>>>(part, p.nslices, (int)a.nq, a.nq_dev, (int)a.k, a.metric, (int)s->dim,
                                                           s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err);
             break;
         case 2:
-            k_merge_fp64<2><<<blocks, 256, 0, s->stream>>>(part, p.nslices, (int)a.nq, (int)a.k, a.metric, (int)s->dim,
+            k_merge_fp64<2><<<blocks, 256, 0, s->stream>>>(part, p.nslices, (int)a.nq, a.nq_dev, (int)a.k, a.metric, (int)s->dim,
                                                           s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err);
             break;
         default:
-            k_merge_fp64<4><<<blocks, 256, 0, s->stream>>>(part, p.nslices, (int)a.nq, (int)a.k, a.metric, (int)s->dim,
+            k_merge_fp64<4><<<blocks, 256, 0, s->stream>>>(part, p.nslices, (int)a.nq, a.nq_dev, (int)a.k, a.metric, (int)s->dim,
                                                           s->logical, a.qsq, s->sq64, a.ids, a.dists, a.err);
     }
     SVDB_LAUNCH_CHECK();
@@ -425,6 +430,8 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
         SVDB_CUDA(cudaMemcpyAsync(hp, outp, out_n * (sizeof(int64_t) + 2 * sizeof(double)), cudaMemcpyDeviceToHost,
                                   s->stream));
         SVDB_CUDA(cudaStreamSynchronize(s->stream));
+        rc = s->check_error();
+        if (rc) return rc;
         std::memcpy(ids, hp, out_n * sizeof(int64_t));
         std::memcpy(dists, hp + out_n * sizeof(int64_t), out_n * sizeof(double));
         if (err) std::memcpy(err, hp + out_n * (sizeof(int64_t) + sizeof(double)), out_n * sizeof(double));

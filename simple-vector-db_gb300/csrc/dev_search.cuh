@@ -23,6 +23,7 @@ struct SearchArgs {
     int64_t* ids;        // nq x k (device)
     double* dists;       // nq x k (device)
     double* err;         // nq x k (device) or null
+    const int* nq_dev = nullptr;  // if set: only the first *nq_dev queries are answered (device-side count)
 };
 
 // FP64 bound on |computed - exact| for one result (see dev_search.cu)

@@ -321,7 +321,8 @@ int Store::ensure() {
     }
     cudaStream_t st = nullptr;
     SVDB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, 4 * sizeof(int)) != cudaSuccess) {
+    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, 4 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&d_err, sizeof(int)) != cudaSuccess || cudaMemset(d_err, 0, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         cudaStreamDestroy(st);
         svdb_set_error("device store: cannot allocate a counter");
@@ -427,6 +428,18 @@ int Store::scratch_reserve(size_t bytes) {
     }
     scratch_bytes = nb;
     return SVDB_OK;
+}
+
+// After the stream is idle: a device kernel's bounded wait that ran out shows
+// here as SVDB_ETIMEOUT (once; the word is cleared).
+int Store::check_error() {
+    if (!d_err) return SVDB_OK;
+    int h = 0;
+    SVDB_CUDA(cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!h) return SVDB_OK;
+    SVDB_CUDA(cudaMemset(d_err, 0, sizeof(int)));
+    svdb_set_error("a search kernel's bounded wait ran out (its results are not valid)");
+    return SVDB_ETIMEOUT;
 }
 
 int Store::scratch2_reserve(size_t bytes) {
@@ -573,6 +586,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->scratch);
     cudaFree(s->d_nlive);
     cudaFree(s->d_count);
+    cudaFree(s->d_err);
     cudaFree(s->scratch2);
     cudaFreeHost(s->pin);
     if (s->prof_events)
@@ -713,7 +727,7 @@ int svdbd_store_wait(svdbd_store* hs) {
     Store* s = reinterpret_cast<Store*>(hs);
     if (!s->stream) return SVDB_OK;
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
-    return SVDB_OK;
+    return s->check_error();
 }
 
 int svdbd_compare_slots(svdbd_store* hs, int metric, const int64_t* slot1, const int64_t* slot2, size_t n,

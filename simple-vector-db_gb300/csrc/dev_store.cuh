@@ -49,6 +49,8 @@ struct Store {
     // live rows the BF16 screen cannot bound (|x| >= 1e15 or non-finite); as of the last sync
     int64_t n_unscreen = 0;
     int* d_count = nullptr;
+    int* d_err = nullptr;  // set by a kernel whose bounded wait ran out; read and cleared at sync points
+    int check_error();
 
     // per-call scratch (device) and staging (pinned host); scratch2 serves a
     // stage's fallback while scratch is still in use
