@@ -270,6 +270,19 @@ struct TopL {
     }
 };
 
+// k > 32: no per-thread running top-k (it would not fit in registers); the
+// thresholds come from the shared bins and the published maxima alone
+template <>
+struct TopL<0> {
+    float v[1];
+    float mn;
+    __device__ __forceinline__ void init(int k) {
+        mn = k > 0 ? -INFINITY : INFINITY;
+        v[0] = mn;
+    }
+    __device__ __forceinline__ void push(float) {}
+};
+
 struct ScreenParams {
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
     const float4* spar;  // per row {mult, b, m, 2^-19 m}: the screen's one-FMA form of the bound
@@ -820,24 +833,31 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     }
     const int2* cq = cand + (size_t)q * cap;
     const int bd = blockDim.x;
-    TopL<KL> top;
-    top.init(k);
-    for (int i = threadIdx.x; i < n; i += bd) {
+    auto lower = [&](int i) {
         const int2 c = cq[i];
-        const float L = __fsub_rd(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
-        if (L > top.mn) top.push(L);
-    }
-#pragma unroll
-    for (int j = 0; j < KL; ++j)
-        if (j < k) vals[threadIdx.x * k + j] = f2u_ord(top.v[j]);
+        return f2u_ord(__fsub_rd(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z)));
+    };
     if (threadIdx.x == 0) {
         s_out = 0;
         s_sig = 0x7fffffff;
     }
-    __syncthreads();
-    const int m = bd * k;
-    // fewer than k candidates: every one survives
-    const uint32_t thr_ord = n >= k ? block_kth_largest([&](int i) { return vals[i]; }, m, k, hist, s_sh) : 0u;
+    uint32_t thr_ord = 0;  // fewer than k candidates: every one survives
+    if constexpr (KL > 0) {
+        TopL<KL> top;
+        top.init(k);
+        for (int i = threadIdx.x; i < n; i += bd) {
+            const float L = __fsub_rd(__int_as_float(cq[i].y), screen_bound(__ldg(rpar + cq[i].x), qp.x, qp.y, qp.z));
+            if (L > top.mn) top.push(L);
+        }
+#pragma unroll
+        for (int j = 0; j < KL; ++j)
+            if (j < k) vals[threadIdx.x * k + j] = f2u_ord(top.v[j]);
+        __syncthreads();
+        if (n >= k) thr_ord = block_kth_largest([&](int i) { return vals[i]; }, bd * k, k, hist, s_sh);
+    } else {
+        __syncthreads();
+        if (n >= k) thr_ord = block_kth_largest(lower, n, k, hist, s_sh);
+    }
     int2* sq = surv + (size_t)q * scr::kSurvCap;
     for (int i = threadIdx.x; i < n; i += bd) {
         const int2 c = cq[i];
@@ -1218,7 +1238,7 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 // ---------------------------------------------------------------------------
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    bool attr_set[4] = {false, false, false, false};
+    bool attr_set[6] = {false, false, false, false, false, false};
     bool select_attr = false;
     bool sort_attr = false;
     bool rerank_attr = false;
@@ -1277,7 +1297,7 @@ struct Bf16Layout {
     size_t npad;
 };
 
-constexpr size_t k_max_bf16 = 32;  // the screen's running top-k holds at most 32
+constexpr size_t k_max_bf16 = 128;  // largest k the screen certifies
 
 static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     Bf16Layout L;
@@ -1296,7 +1316,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.spar = take(L.npad * sizeof(float4));
     L.vbits = take(L.npad / 8);
     L.tau = take(nq * sizeof(int));
-    L.bins = take(nq * 32 * sizeof(int));
+    L.bins = take(nq * k_max_bf16 * sizeof(int));
     L.cnt = take(nq * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
     // per query before the running thresholds settle)
@@ -1325,7 +1345,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
 
 size_t search_bf16_scratch(const Store* s, size_t nq, size_t k) { return bf16_layout(s, nq).total; }
 
-bool bf16_supported(const Store* s, size_t k) { return k <= 32 && s->n_unscreen == 0 && s->nlive > 0; }
+bool bf16_supported(const Store* s, size_t k) { return k <= k_max_bf16 && s->n_unscreen == 0 && s->nlive > 0; }
 
 int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st) {
     GemmPlanCache* gc = nullptr;
@@ -1399,9 +1419,10 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.rgroups = std::max(1, std::min(G / std::max(P.ntq, 1), P.ntr));
     const unsigned grid = (unsigned)(P.ntq * P.rgroups);
     {
-        auto kern = k <= 16 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
-                            : (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>);
-        const int v = (k <= 16 ? 0 : 2) + (norm ? 1 : 0);
+        auto kern = k <= 16   ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
+                    : k <= 32 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
+                              : (norm ? k_screen_bf16<0, true> : k_screen_bf16<0, false>);
+        const int v = (k <= 16 ? 0 : (k <= 32 ? 2 : 4)) + (norm ? 1 : 0);
         if (!gc->attr_set[v]) {
             SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
             gc->attr_set[v] = true;
@@ -1415,7 +1436,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     {
         // small batches carry many candidates per query: wider blocks
         const int sel_threads = nq >= 256 ? 256 : 1024;
-        const size_t sel_smem = (size_t)sel_threads * k * sizeof(uint32_t);
+        const size_t sel_smem = k <= 32 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;
         if (!gc->select_attr) {
             SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
             SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
@@ -1424,9 +1445,12 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         if (k <= 16)
             k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
                                                                              nsurv, sig, flags);
-        else
+        else if (k <= 32)
             k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
                                                                              nsurv, sig, flags);
+        else
+            k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
+                                                                            nsurv, sig, flags);
     }
     SVDB_LAUNCH_CHECK();
     s->prof_mark(3);

@@ -363,7 +363,7 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     const size_t qbytes = round_up(nq * s->ld * sizeof(double), 256);
     const size_t sqbytes = round_up(nq * sizeof(double), 256);
     const size_t obytes = on_device ? 0 : round_up(out_n * (sizeof(int64_t) + 2 * sizeof(double)), 256);
-    // the screen certifies k <= 32 on stores without unscreenable rows; the
+    // the screen certifies k <= 128 on stores without unscreenable rows; the
     // rest is answered by the exact scan
     const bool use_bf16 = precision == SVDB_PREC_BF16 && bf16_supported(s, k);
     size_t kbytes = 0;
