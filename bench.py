@@ -41,6 +41,7 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
 
 METRICS = {"cosine": 0, "euclidean": 1, "dot": 2}
 N_ROWS, DIM, K_TOP, SEED = 1_000_000, 768, 10, 3
+N_ROWS_DEFAULT = N_ROWS
 METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GPU; p50/p99 ms"
 # DRAM bytes (read + write) of one k_screen_bf16 launch per store row, from the
 # ncu capture summarised in profiles/k_screen_bf16_200kx768_q4096.md (a 200,000-row
@@ -306,6 +307,113 @@ def run_ours(args, ws, rank, local):
         dist.destroy_process_group()
 
 
+def run_scan128(args, ws, rank, local):
+    """Plain FP64 single-query scan at scale: 1M x 128 L2-normalised N(0,1)
+    rows (seed 2), queries issued one at a time, top-1 and top-10 for each
+    metric.  Reported against the FP64 pipe (the scan's bound on GB300) and as
+    HBM bytes per second."""
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    n, d = args.rows if args.rows != N_ROWS_DEFAULT else 1_000_000, 128
+    X, Q = W.config2(n, d, max(args.steps, 1) + args.warmup)
+    db = S.VectorDatabase(n, 3)
+    db.insert_batch(X)
+    db.sync()
+    Qd = torch.from_numpy(Q).cuda()
+    stream = torch.cuda.ExternalStream(db.stream())
+    results = {}
+    for metric_name, metric in METRICS.items():
+        for k in (1, 10):
+            ids = torch.empty((1, k), dtype=torch.int64, device="cuda")
+            dists = torch.empty((1, k), dtype=torch.float64, device="cuda")
+            for w in range(args.warmup):
+                db.search_device(Qd[w].data_ptr(), 1, d, k, metric, S.PREC_FP64, ids.data_ptr(), dists.data_ptr())
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for s_ in range(args.steps):
+                q = Qd[args.warmup + s_]
+                db.search_device(q.data_ptr(), 1, d, k, metric, S.PREC_FP64, ids.data_ptr(), dists.data_ptr())
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b) / args.steps
+            results[f"{metric_name}_top{k}"] = {"queries_per_s": 1e3 / ms, "ms_per_query": ms,
+                                               "hbm_gbs": n * d * 8 / (ms / 1e3) / 1e9,
+                                               "fp64_tflops": 2.0 * n * d / (ms / 1e3) / 1e12}
+    hbm, _, src = peaks()
+    best = max(results.values(), key=lambda r: r["queries_per_s"])
+    line = {"metric": "plain FP64 single-query scan, 1M x 128, queries/s", "value": best["queries_per_s"],
+            "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": best["ms_per_query"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "1M x 128 L2-normalised N(0,1) FP64 (seed 2), one query per step, FP64 scan"},
+            "per_case": results,
+            "roofline": {"bound": "fp64 pipe (HBM figure for reference)", "achieved": best["hbm_gbs"], "peak": hbm,
+                         "unit": "GB/s", "frac": best["hbm_gbs"] / hbm, "traffic": None, "peak_source": src}}
+    print(json.dumps(line), flush=True)
+    db.close()
+
+
+def run_ragged(args, ws, rank, local):
+    """Uneven batched multi-collection search: 5 collections (D, N) =
+    (64, 2M), (128, 1M), (384, 500k), (768, 200k), (1536, 50k), uniform[-1,1]
+    float64 (seed 4); a ragged batch of 8,192 queries split 40/25/15/12/8 %,
+    k per query uniform in [1, 100], cosine.  One step issues each
+    collection's share as one search (k = the share's largest k; each query
+    keeps its own first k) on that collection's stream, all five in flight
+    together."""
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    prec = S.PREC_BF16 if args.precision == "bf16" else S.PREC_FP64
+    cols = W.config4(8192)
+    dbs, bufs = [], []
+    for X, Q, ks in cols:
+        db = S.VectorDatabase(X.shape[0], 3)
+        db.insert_batch(X)
+        db.sync()
+        kmax = int(ks.max())
+        qd = torch.from_numpy(Q).cuda()
+        ids = torch.empty((Q.shape[0], kmax), dtype=torch.int64, device="cuda")
+        dd = torch.empty((Q.shape[0], kmax), dtype=torch.float64, device="cuda")
+        dbs.append(db)
+        bufs.append((qd, ids, dd, kmax, X.shape[1]))
+    torch.cuda.synchronize()
+
+    def step():
+        for db, (qd, ids, dd, kmax, d) in zip(dbs, bufs):
+            db.search_device(qd.data_ptr(), qd.shape[0], d, kmax, 0, prec, ids.data_ptr(), dd.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    for db in dbs:
+        db.wait()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    for db in dbs:
+        db.wait()
+    dt = time.perf_counter() - t
+    nq = sum(b[0].shape[0] for b in bufs)
+    line = {"metric": "exact top-k queries/s, ragged batch over 5 collections (k in [1,100])",
+            "value": nq * args.steps / dt, "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f64" if prec == S.PREC_BF16 else "f64",
+            "data": "synthetic",
+            "config": {"workload": "5 collections (D,N) = (64,2M) (128,1M) (384,500k) (768,200k) (1536,50k), "
+                                   "uniform[-1,1] seed 4, 8192 queries split 40/25/15/12/8 %, k ~ U[1,100], cosine",
+                       "precision": args.precision}}
+    print(json.dumps(line), flush=True)
+    for db in dbs:
+        db.close()
+
+
 def main():
     global N_ROWS
     ap = argparse.ArgumentParser()
@@ -319,6 +427,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged"],
+                    help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
+                         "ragged: one batch over 5 collections of different dimensions")
     args = ap.parse_args()
     N_ROWS = args.rows
     if args.q is None:
@@ -326,6 +437,10 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.workload == "scan128":
+        run_scan128(args, ws, rank, local)
+    elif args.workload == "ragged":
+        run_ragged(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 

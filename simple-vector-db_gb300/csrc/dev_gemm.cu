@@ -64,7 +64,7 @@ constexpr uint32_t kStageB = kBN * kBK * 2;  // 32 KB
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitimate wait
 constexpr int kCapMin = 8192, kCapMax = 65536;   // candidates kept per query (adaptive)
 constexpr int kSurvCap = 8192;                    // survivors re-ranked per query
-constexpr size_t kCandBudget = size_t(512) << 20; // bytes of candidate lists per search
+constexpr size_t kCandBudget = size_t(4) << 30;   // bytes of candidate lists per search (HBM is plentiful)
 constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key and m, per unit of m
 // flags
 constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4;

@@ -92,3 +92,26 @@ def config3(n: int = 1_000_000, d: int = 768, seed: int = 3):
     """Mixed-precision batched search store: 1,024-centre mixture, sigma 0.05."""
     m = Mixture(d, seed)
     return m, m.sample(n, 0)
+
+
+# Uneven batched multi-collection workload: (dimension, rows) per collection and
+# the share of the ragged query batch that goes to it.
+CONFIG4_COLLECTIONS = ((64, 2_000_000), (128, 1_000_000), (384, 500_000), (768, 200_000), (1536, 50_000))
+CONFIG4_SHARES = (0.40, 0.25, 0.15, 0.12, 0.08)
+
+
+def config4(total_queries: int = 8192, scale: float = 1.0):
+    """Five collections of uniform[-1,1] float64 rows (seed 4), a ragged batch
+    of `total_queries` split 40/25/15/12/8 % across them, k per query uniform
+    in [1, 100].  `scale` shrinks the collections (tests)."""
+    rng = np.random.default_rng(4)
+    out = []
+    counts = [int(round(total_queries * f)) for f in CONFIG4_SHARES]
+    counts[0] += total_queries - sum(counts)
+    for c, ((d, n), nq) in enumerate(zip(CONFIG4_COLLECTIONS, counts)):
+        n = max(1, int(n * scale))
+        X = uniform(n, d, [4, c])
+        Q = uniform(nq, d, [4, 100 + c])
+        ks = rng.integers(1, 101, nq)
+        out.append((X, Q, ks))
+    return out
