@@ -127,6 +127,17 @@ int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t 
 int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim, size_t k,
                                   int metric, int64_t* d_ids, double* d_dists);
 
+/*
+ * Merge of per-shard top-k lists (host only, no GPU; no reference
+ * counterpart).  A store split by row ranges over several GPUs or processes
+ * answers a query with one exact top-k per shard; this combines nshards such
+ * lists (ids already global, layout [shard][query][k]) into the exact global
+ * top-k: order by value (Euclidean ascending, cosine / dot descending, NaN
+ * last), ties to the lowest global id; missing entries are id -1 / NaN.
+ */
+int svdb_merge_topk(int metric, const int64_t* ids, const double* vals, size_t nshards, size_t nq, size_t k,
+                    int64_t* out_ids, double* out_vals);
+
 /* Bulk insert of n rows (n x dim, row-major, copied): the same result as n
  * vector_db_insert calls, including the KD nodes.  uuids: n*37 bytes or
  * NULL.  Returns the first new index in *first_index. */

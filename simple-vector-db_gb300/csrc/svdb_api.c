@@ -306,3 +306,55 @@ SVDB_API int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_q
     pthread_mutex_unlock(&db->mutex);
     return rc;
 }
+
+/* ---- merge of per-shard top-k lists (host) ------------------------------ */
+typedef struct {
+    double key;
+    int64_t id;
+    double val;
+} merge_ent;
+
+static double merge_key(int metric, double v) {
+    if (isnan(v)) return INFINITY;
+    return metric == SVDB_EUCLIDEAN ? v : -v;
+}
+
+static int merge_less(const merge_ent* a, const merge_ent* b) {
+    return a->key < b->key || (a->key == b->key && a->id < b->id);
+}
+
+SVDB_API int svdb_merge_topk(int metric, const int64_t* ids, const double* vals, size_t nshards, size_t nq, size_t k,
+                             int64_t* out_ids, double* out_vals) {
+    if (metric < 0 || metric > 2 || k == 0 || (nq && (!ids || !vals || !out_ids || !out_vals))) {
+        svdb_set_error("svdb_merge_topk: bad argument");
+        return SVDB_EINVAL;
+    }
+    merge_ent* best = (merge_ent*)malloc(k * sizeof(merge_ent));
+    if (!best) {
+        svdb_set_error("svdb_merge_topk: out of host memory");
+        return SVDB_ENOMEM;
+    }
+    for (size_t q = 0; q < nq; ++q) {
+        size_t cnt = 0;
+        for (size_t sh = 0; sh < nshards; ++sh) {
+            const size_t base = (sh * nq + q) * k;
+            for (size_t j = 0; j < k; ++j) {
+                if (ids[base + j] < 0) continue;
+                merge_ent e = {merge_key(metric, vals[base + j]), ids[base + j], vals[base + j]};
+                if (cnt == k && !merge_less(&e, &best[k - 1])) continue;
+                size_t pos = cnt < k ? cnt++ : k - 1;
+                while (pos > 0 && merge_less(&e, &best[pos - 1])) {
+                    best[pos] = best[pos - 1];
+                    --pos;
+                }
+                best[pos] = e;
+            }
+        }
+        for (size_t j = 0; j < k; ++j) {
+            out_ids[q * k + j] = j < cnt ? best[j].id : -1;
+            out_vals[q * k + j] = j < cnt ? best[j].val : NAN;
+        }
+    }
+    free(best);
+    return SVDB_OK;
+}

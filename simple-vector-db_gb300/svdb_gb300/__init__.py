@@ -91,6 +91,7 @@ def _load():
         "svdb_wait": (C.c_int, [vp]),
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
+        "svdb_merge_topk": (C.c_int, [C.c_int, _i64p, _dp, sz, sz, sz, _i64p, _dp]),
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
     }
@@ -319,6 +320,19 @@ class VectorDatabase:
         _check(lib.svdb_search_topk_device(self.ptr, q_ptr, nq, dim, k, metric, precision, ids_ptr, dists_ptr,
                                            err_ptr or None, C.byref(stats) if stats is not None else None),
                "svdb_search_topk_device")
+
+
+def merge_topk(metric: int, ids, vals):
+    """Exact global top-k from per-shard lists ([shard, query, k], global ids);
+    ties to the lowest global id (svdb_merge_topk)."""
+    ids = np.ascontiguousarray(ids, np.int64)
+    vals = np.ascontiguousarray(vals, np.float64)
+    nsh, nq, k = ids.shape
+    oi = np.empty((nq, k), np.int64)
+    ov = np.empty((nq, k), np.float64)
+    _check(lib.svdb_merge_topk(metric, ids.ctypes.data_as(_i64p), vals.ctypes.data_as(_dp), nsh, nq, k,
+                               oi.ctypes.data_as(_i64p), ov.ctypes.data_as(_dp)), "svdb_merge_topk")
+    return oi, ov
 
 
 class KDTree:
