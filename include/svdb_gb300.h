@@ -128,6 +128,18 @@ int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_queries, s
                                   int metric, int64_t* d_ids, double* d_dists);
 
 /*
+ * Health check of the kernels' failure path (no reference counterpart).  Runs
+ * one CTA of the screen's bounded-wait sequence on mbarriers that nothing
+ * arrives on: one role gives up after limit_us microseconds (1 .. 10^6), the
+ * other role, holding tensor memory, leaves through the shared abort flag,
+ * the tensor memory is released and the store's error word is raised.  A
+ * working path returns SVDB_ETIMEOUT with *gave_up == 3 (both roles left
+ * their waits) and leaves the GPU context and the store usable; any other
+ * result means a search could not report a stalled pipeline.  Synchronous.
+ */
+int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, uint32_t* gave_up);
+
+/*
  * Merge of per-shard top-k lists (host only, no GPU; no reference
  * counterpart).  A store split by row ranges over several GPUs or processes
  * answers a query with one exact top-k per shard; this combines nshards such

@@ -1551,4 +1551,61 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     return SVDB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// self-test of the bounded waits (no fault, no hang)
+// ---------------------------------------------------------------------------
+// The screen's roles wait on mbarriers through mbar_wait: a wait that runs out
+// raises the CTA's abort flag, every other role leaves its own wait when it
+// sees the flag, the TMEM allocation is released and the kernel reports
+// through the store's error word.  This kernel runs that same sequence on
+// mbarriers that nothing ever arrives on: warp 0 waits with `limit_ns`, warp 1
+// holds TMEM and waits with the full limit, so it can only leave through the
+// abort flag.  `gave_up` gets bit w for each warp whose wait returned false.
+__global__ void __launch_bounds__(64, 1) k_selftest_wait(uint64_t limit_ns, int* err, uint32_t* gave_up) {
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        abort_flag = 0;
+    }
+    if (warp == 1) tmem_alloc(&tmem_base, 32);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    volatile int* ab = &abort_flag;
+    if (lane == 0) {
+        const bool ok = mbar_wait(&bar[warp], 0, ab, warp == 0 ? limit_ns : scr::kWaitLimitNs);
+        if (!ok) atomicOr(gave_up, 1u << warp);
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x == 0 && abort_flag) atomicExch(err, 1);
+    if (warp == 1) tmem_dealloc(tmem_base, 32);
+}
+
+int selftest_wait(Store* s, uint32_t limit_us, uint32_t* gave_up) {
+    int rc = s->ensure();
+    if (!rc) rc = s->scratch_reserve(sizeof(uint32_t));
+    if (rc) return rc;
+    uint32_t* d_gave = reinterpret_cast<uint32_t*>(s->scratch);
+    SVDB_CUDA(cudaMemsetAsync(d_gave, 0, sizeof(uint32_t), s->stream));
+    const uint64_t lim = (uint64_t)std::min<uint32_t>(std::max<uint32_t>(limit_us, 1u), 1000000u) * 1000ull;
+    k_selftest_wait<<<1, 64, 0, s->stream>>>(lim, s->d_err, d_gave);
+    SVDB_LAUNCH_CHECK();
+    uint32_t h = 0;
+    SVDB_CUDA(cudaMemcpyAsync(&h, d_gave, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    if (gave_up) *gave_up = h;
+    return s->check_error();
+}
+
 }  // namespace svdb
+
+extern "C" int svdbd_selftest_wait(svdbd_store* hs, uint32_t limit_us, uint32_t* gave_up) {
+    return svdb::selftest_wait(reinterpret_cast<svdb::Store*>(hs), limit_us, gave_up);
+}

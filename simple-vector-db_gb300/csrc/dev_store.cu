@@ -336,6 +336,12 @@ int Store::grow(size_t need) {
     int erc = ensure();
     if (erc) return erc;
     if (need <= cap) return SVDB_OK;
+    // the largest row count whose FP64 rows fit in the address space, halved
+    // so the doubling below cannot wrap
+    if (need > (SIZE_MAX / (ld * sizeof(double) + 64)) / 2) {
+        svdb_set_error("device store: %zu rows of dim %zu exceed any device's memory", need, dim);
+        return SVDB_ENOMEM;
+    }
     size_t nc = cap ? cap : 1024;
     while (nc < need) nc *= 2;
     double* nx = nullptr;

@@ -307,6 +307,24 @@ SVDB_API int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_q
     return rc;
 }
 
+SVDB_API int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, uint32_t* gave_up) {
+    if (!db) {
+        svdb_set_error("svdb_selftest_bounded_wait: NULL database");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc;
+    if (!d->dev) {
+        svdb_set_error("svdb_selftest_bounded_wait: the store holds no rows (no device store yet)");
+        rc = SVDB_EINVAL;
+    } else {
+        rc = svdbd_selftest_wait(d->dev, limit_us, gave_up);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
 /* ---- merge of per-shard top-k lists (host) ------------------------------ */
 typedef struct {
     double key;

@@ -72,6 +72,7 @@ int svdbd_search(svdbd_store* s, const double* q, size_t nq, size_t k, int metri
 
 /* exact FP64 top-k with every per-call scratch byte in a fixed device array
  * (dev_noalloc.cu); q/ids/dists in device memory; never allocates */
+int svdbd_selftest_wait(svdbd_store* s, uint32_t limit_us, uint32_t* gave_up);
 int svdbd_search_noalloc(svdbd_store* s, const double* d_queries, size_t nq, size_t k, int metric, int64_t* d_ids,
                          double* d_dists);
 

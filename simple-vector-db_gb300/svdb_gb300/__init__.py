@@ -21,6 +21,8 @@ LIB_PATH = os.environ.get("SVDB_LIB", os.path.join(_PKG, "_build", "libsvdb_gb30
 
 COSINE, EUCLIDEAN, DOT = 0, 1, 2
 PREC_FP64, PREC_BF16 = 0, 1
+# status codes (include/svdb_gb300.h)
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENODEV = 0, -1, -2, -3, -4, -5
 METRIC_URLS = {"/compare/cosine_similarity": COSINE, "/compare/euclidean_distance": EUCLIDEAN,
                "/compare/dot_product": DOT}
 CMP_OK, CMP_OUT_OF_BOUNDS, CMP_NOT_FOUND, CMP_DIFF_DIM, CMP_SIZE_MISMATCH, CMP_UNKNOWN_METHOD = range(6)
@@ -91,6 +93,7 @@ def _load():
         "svdb_wait": (C.c_int, [vp]),
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
+        "svdb_selftest_bounded_wait": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_uint32)]),
         "svdb_merge_topk": (C.c_int, [C.c_int, _i64p, _dp, sz, sz, sz, _i64p, _dp]),
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
@@ -313,6 +316,13 @@ class VectorDatabase:
         queued on self.stream()); for callers that cannot call cudaMalloc."""
         _check(lib.svdb_search_topk_fp64_noalloc(self.ptr, q_ptr, nq, dim, k, metric, ids_ptr, dists_ptr),
                "svdb_search_topk_fp64_noalloc")
+
+    def selftest_bounded_wait(self, limit_us: int = 20000):
+        """(status, gave_up bits, message) of svdb_selftest_bounded_wait; a
+        working failure path gives (ETIMEOUT, 3, ...)."""
+        g = C.c_uint32(0)
+        rc = lib.svdb_selftest_bounded_wait(self.ptr, limit_us, C.byref(g))
+        return rc, g.value, last_error()
 
     def search_device(self, q_ptr: int, nq: int, dim: int, k: int, metric: int, precision: int, ids_ptr: int,
                       dists_ptr: int, err_ptr: int = 0, stats: SearchStats | None = None) -> None:
