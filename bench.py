@@ -414,6 +414,74 @@ def run_ragged(args, ws, rank, local):
         db.close()
 
 
+def run_serve(args, ws, rank, local):
+    """Serving loop: a server store (rows only in HBM) of the D=768 mixture
+    (1,024 centres, sigma 0.05, seed 5) grown from 1M to 5M rows; at each
+    size a seeded Poisson trace at --rate requests/s (70 % /nearest top-10
+    Euclidean, 10 % /compare with a uniform metric, 15 % insert, 3 % update,
+    2 % delete) is served open-loop in real time by svdb_server_execute
+    batches (BF16 screen + FP64 re-rank), then a second trace at the same
+    offered load through the plain FP64 path, cut off after --fp64-seconds.
+    Latency = completion - arrival per request, queueing included; the rows
+    of every request come from pageable host memory and every answer goes
+    back to it."""
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import serve, workloads as W
+
+    torch.cuda.set_device(local)
+    m = W.Mixture(DIM, 5)
+    sizes = [int(x) for x in args.serve_sizes.split(",")]
+    nreq = int(args.rate * args.serve_seconds)
+    reserve = max(sizes) + 2 * nreq
+    t = time.perf_counter()
+    srv = serve.Server(DIM, reserve)  # admission: the whole capacity must fit in free HBM now
+    log(f"[bench] server store reserved for {reserve} rows ({time.perf_counter() - t:.1f}s)")
+    phases, chunk, stream = [], 1 << 18, 1000
+    clocks = Clocks(local)
+    for si, size in enumerate(sizes):
+        t = time.perf_counter()
+        while srv.size < size:
+            srv.insert_block(m.sample(min(chunk, size - srv.size), stream))
+            stream += 1
+        log(f"[bench] store at {srv.size} rows ({time.perf_counter() - t:.1f}s)")
+        warm = serve.make_trace(m.sample, srv.size, max(1000, nreq // 10), args.rate, seed=50 + si)
+        serve.replay(srv, warm, S.PREC_BF16)
+        tr = serve.make_trace(m.sample, srv.size, nreq, args.rate, seed=5 + si)
+        n_at_start = srv.size
+        res = serve.replay(srv, tr, S.PREC_BF16)
+        log(f"[bench] bf16 served {res['requests']}/{res['offered']} p50 {res['p50_ms']:.2f} p99 "
+            f"{res['p99_ms']:.2f} ms, mean batch {res['mean_batch']:.1f}")
+        trf = serve.make_trace(m.sample, srv.size, nreq, args.rate, seed=500 + si)
+        resf = serve.replay(srv, trf, S.PREC_FP64, max_batch=256, time_limit=args.fp64_seconds)
+        log(f"[bench] fp64 served {resf['requests']}/{resf['offered']} in {resf['wall_s']:.1f}s, p99 "
+            f"{resf['p99_ms']:.1f} ms")
+        phases.append({
+            "store_rows": n_at_start, "offered_per_s": args.rate, "requests": res["requests"],
+            "served_per_s": res["served_per_s"], "p50_ms": res["p50_ms"], "p99_ms": res["p99_ms"],
+            "max_ms": res["max_ms"], "mean_batch": res["mean_batch"], "widened": res["widened"],
+            "bound_failures": res["bound_failures"], "statuses": res["statuses"], "mix": tr.counts(),
+            "plain_fp64": {"requests": resf["requests"], "offered": resf["offered"],
+                           "served_per_s": resf["served_per_s"], "p50_ms": resf["p50_ms"],
+                           "p99_ms": resf["p99_ms"], "cut_off_s": args.fp64_seconds}})
+    clk = clocks.stop()
+    total = sum(p["requests"] for p in phases)
+    wall = sum(p["requests"] / p["served_per_s"] for p in phases)
+    line = {"metric": f"served requests/s at {args.rate:.0f} req/s offered (70% /nearest top-10, 10% /compare, "
+                      "15% insert, 3% update, 2% delete), store 1M->5M x 768; p50/p99 ms",
+            "value": total / wall, "unit": "requests/s", "n_gpus": 1, "steps": len(phases), "warmup": len(phases),
+            "ms_per_step": 1e3 * wall / len(phases), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16+f64", "data": "synthetic",
+            "config": {"workload": "serving loop: D=768 mixture (1024 centres, sigma 0.05, seed 5), Poisson "
+                                   f"arrivals at {args.rate:.0f}/s, {args.serve_seconds:.1f}s of trace per store "
+                                   "size", "store_sizes": sizes, "precision": "bf16",
+                       "l2": "store larger than L2"},
+            "latency_ms": {"p50": max(p["p50_ms"] for p in phases), "p99": max(p["p99_ms"] for p in phases)},
+            "phases": phases, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    srv.close()
+
+
 def main():
     global N_ROWS
     ap = argparse.ArgumentParser()
@@ -427,9 +495,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged"],
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve"],
                     help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
-                         "ragged: one batch over 5 collections of different dimensions")
+                         "ragged: one batch over 5 collections of different dimensions; serve: the serving loop")
+    ap.add_argument("--rate", type=float, default=20000.0, help="serve: offered requests/s")
+    ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
+    ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
+    ap.add_argument("--fp64-seconds", type=float, default=2.0, help="serve: cut-off of the plain FP64 trace")
     args = ap.parse_args()
     N_ROWS = args.rows
     if args.q is None:
@@ -441,6 +513,8 @@ def main():
         run_scan128(args, ws, rank, local)
     elif args.workload == "ragged":
         run_ragged(args, ws, rank, local)
+    elif args.workload == "serve":
+        run_serve(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 

@@ -127,6 +127,65 @@ int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t 
 int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim, size_t k,
                                   int metric, int64_t* d_ids, double* d_dists);
 
+/* ---- serving: batches of mixed requests on a device-resident store -------
+ *
+ * A server store keeps its rows only in HBM (no host copies, no KD tree): the
+ * request path of a server that batches requests as they arrive.  Positional
+ * semantics are the reference's: rows are numbered 0..size-1 in insertion
+ * order, an insert appends (src/vector_database.c:99-125), an update
+ * overwrites in place (:160-175) and a delete shifts every later row down by
+ * one (:185-195).  Deleted rows become tombstones in the device store and an
+ * order-statistic tree maps positions to slots, so no mutation moves rows.
+ *
+ * svdb_server_execute runs one batch: every INSERT / UPDATE / DELETE in
+ * request order first, then every NEAREST and COMPARE against the resulting
+ * state -- one serial order of requests that were all waiting at the same
+ * time.  NEARESTs with the same (metric, k) share one top-k search and
+ * COMPAREs with the same metric one pair kernel.
+ */
+#define SVDB_REQ_NEAREST 0 /* exact top-k of vec (POST /nearest?number=k, README.md:287) */
+#define SVDB_REQ_COMPARE 1 /* metric of rows a and b (GET /compare/..., src/compare_handler.c:86-170) */
+#define SVDB_REQ_INSERT 2  /* append vec (POST /vector, src/post_handler.c:333) */
+#define SVDB_REQ_UPDATE 3  /* overwrite row a with vec (PUT /vector, src/put_handler.c:155,247) */
+#define SVDB_REQ_DELETE 4  /* delete row a (DELETE /vector, src/delete_handler.c:84,96) */
+
+typedef struct svdb_request {
+    int32_t op;        /* SVDB_REQ_* */
+    int32_t metric;    /* NEAREST, COMPARE: SVDB_COSINE / SVDB_EUCLIDEAN / SVDB_DOT */
+    uint32_t k;        /* NEAREST: 1..128 */
+    uint32_t reserved; /* 0 */
+    uint64_t a, b;     /* COMPARE: positions of the two rows; UPDATE, DELETE: a */
+    const double* vec; /* NEAREST, INSERT, UPDATE: dim doubles in host memory */
+} svdb_request;
+
+typedef struct svdb_response {
+    int32_t status; /* 0; SVDB_CMP_OUT_OF_BOUNDS (COMPARE, UPDATE, DELETE past the end);
+                       SVDB_CMP_UNKNOWN_METHOD; SVDB_ENOMEM (INSERT refused: no HBM left);
+                       SVDB_EINVAL (bad op, k or vec) */
+    float value;    /* COMPARE: the reference's float metric */
+    uint64_t index; /* INSERT: position of the new row */
+} svdb_response;
+
+typedef struct svdb_server svdb_server;
+
+/* A server store of dimension dim with room for reserve_rows rows allocated
+ * up front; NULL (message in svdb_last_error) when that does not fit in the
+ * device's free memory. */
+svdb_server* svdb_server_create(size_t dim, size_t reserve_rows);
+void svdb_server_destroy(svdb_server* s);
+size_t svdb_server_size(svdb_server* s);
+/* bulk load: append n rows (n x dim, row-major); *first_index = position of the first */
+int svdb_server_insert_block(svdb_server* s, const double* rows, size_t n, size_t* first_index);
+/* GET /vector?index= (src/get_handler.c:88-101): copy row `index` to out[dim] */
+int svdb_server_read(svdb_server* s, size_t index, double* out);
+/* One batch (see above).  NEAREST results of request i go to ids/dists +
+ * i * stride (stride >= its k; -1 / NaN past the number of rows).  The
+ * return value is SVDB_OK unless the batch as a whole failed (a CUDA error);
+ * per-request outcomes are in resp[i].status.  stats (optional) adds up the
+ * searches' statistics. */
+int svdb_server_execute(svdb_server* s, const svdb_request* req, size_t n, svdb_response* resp, int precision,
+                        int64_t* ids, double* dists, size_t stride, svdb_search_stats* stats);
+
 /*
  * Health check of the kernels' failure path (no reference counterpart).  Runs
  * one CTA of the screen's bounded-wait sequence on mbarriers that nothing

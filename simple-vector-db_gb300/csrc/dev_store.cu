@@ -133,51 +133,103 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
 
 // Single-block exclusive scan of live flags -> slot->logical map, done in
 // chunks of 1024*4 slots carrying the running count.
-__global__ void k_logical_map(const uint8_t* __restrict__ live, int64_t n, int64_t* __restrict__ logical,
-                              int64_t* __restrict__ nlive_out) {
-    __shared__ int64_t warp_tot[32];
+// slot -> logical rank (positional index) of every slot, -1 for deleted ones;
+// nlive_out = number of occupied positions.  Three passes so the map scales
+// with the store: per-chunk counts (one 1024-thread block per kMapChunk
+// slots), an exclusive scan of the chunk counts, and a per-chunk block scan
+// that writes the ranks.
+constexpr int kMapChunk = 4096;
+
+__global__ void __launch_bounds__(1024) k_map_count(const uint8_t* __restrict__ live, int64_t n,
+                                                    int64_t* __restrict__ blk) {
+    __shared__ int ws[32];
+    const int64_t base = (int64_t)blockIdx.x * kMapChunk;
+    int c = 0;
+    for (int u = threadIdx.x; u < kMapChunk; u += 1024) c += (base + u < n && live[base + u] != 0) ? 1 : 0;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int v = __reduce_add_sync(0xffffffffu, ws[threadIdx.x]);
+        if (threadIdx.x == 0) blk[blockIdx.x] = v;
+    }
+}
+
+// exclusive scan of nb chunk counts in place (one block), total to *nlive_out
+__global__ void __launch_bounds__(1024) k_map_scan(int64_t* __restrict__ blk, int64_t nb,
+                                                   int64_t* __restrict__ nlive_out) {
+    __shared__ int64_t wt[32];
     __shared__ int64_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int64_t base = 0; base < n; base += 4096) {
-        int64_t i0 = base + threadIdx.x * 4;
-        int c[4], tot = 0;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            c[u] = (i0 + u < n) ? (live[i0 + u] != 0 ? 1 : 0) : 0;
-            tot += c[u];
-        }
-        int incl = tot;
+    for (int64_t b0 = 0; b0 < nb; b0 += 1024) {
+        const int64_t i = b0 + threadIdx.x;
+        const int64_t v = i < nb ? blk[i] : 0;
+        int64_t incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            const int64_t t = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += t;
         }
-        if (lane == 31) warp_tot[warp] = incl;
+        if (lane == 31) wt[warp] = incl;
         __syncthreads();
         if (warp == 0) {
-            int64_t w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+            const int64_t w = wt[lane];
             int64_t wi = w;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+                const int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
                 if (lane >= o) wi += t;
             }
-            warp_tot[lane] = wi - w;  // exclusive
+            wt[lane] = wi - w;
         }
         __syncthreads();
-        int64_t run = carry + warp_tot[warp] + (incl - tot);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (i0 + u < n) logical[i0 + u] = c[u] ? run : -1;
-            run += c[u];
-        }
+        const int64_t c0 = carry;
+        if (i < nb) blk[i] = c0 + wt[warp] + incl - v;
         __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = run;
+        if (threadIdx.x == 1023) carry = c0 + wt[warp] + incl;
         __syncthreads();
     }
     if (threadIdx.x == 0) *nlive_out = carry;
+}
+
+__global__ void __launch_bounds__(1024) k_map_write(const uint8_t* __restrict__ live, int64_t n,
+                                                    const int64_t* __restrict__ blk, int64_t* __restrict__ logical) {
+    __shared__ int64_t wt[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t i0 = (int64_t)blockIdx.x * kMapChunk + threadIdx.x * 4;
+    int c[4], tot = 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        c[u] = (i0 + u < n && live[i0 + u] != 0) ? 1 : 0;
+        tot += c[u];
+    }
+    int incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wt[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int64_t w = wt[lane];
+        int64_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        wt[lane] = wi - w;
+    }
+    __syncthreads();
+    int64_t run = blk[blockIdx.x] + wt[warp] + (incl - tot);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if (i0 + u < n) logical[i0 + u] = c[u] ? run : -1;
+        run += c[u];
+    }
 }
 
 // live rows whose BF16 screen terms are unbounded (marked +inf by k_derive_rows)
@@ -354,6 +406,7 @@ int Store::grow(size_t need) {
     float4* np = nullptr;
     uint8_t* nl = nullptr;
     int64_t* nlog = nullptr;
+    int64_t* nblk = nullptr;
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = cudaMalloc(&nx, nc * ld * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&nb, nc * ldb * sizeof(__nv_bfloat16));
@@ -365,6 +418,7 @@ int Store::grow(size_t need) {
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nl, nc);
     if (e == cudaSuccess) e = cudaMalloc(&nlog, nc * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&nblk, ((nc + kMapChunk - 1) / kMapChunk) * sizeof(int64_t));
     if (e != cudaSuccess) {
         cudaGetLastError();
         cudaFree(nx);
@@ -377,6 +431,7 @@ int Store::grow(size_t need) {
         cudaFree(np);
         cudaFree(nl);
         cudaFree(nlog);
+        cudaFree(nblk);
         svdb_set_error("device store: cannot grow to %zu rows of dim %zu: %s", nc, dim, cudaGetErrorString(e));
         return SVDB_ENOMEM;
     }
@@ -403,6 +458,7 @@ int Store::grow(size_t need) {
     cudaFree(rowp);
     cudaFree(live);
     cudaFree(logical);
+    cudaFree(mapblk);
     x64 = nx;
     xb = nb;
     x32 = nf;
@@ -413,6 +469,7 @@ int Store::grow(size_t need) {
     rowp = np;
     live = nl;
     logical = nlog;
+    mapblk = nblk;
     cap = nc;
     return SVDB_OK;
 }
@@ -532,7 +589,12 @@ int Store::sync() {
         dirty_list.clear();
     }
     if (map_dirty && slots) {
-        k_logical_map<<<1, 1024, 0, stream>>>(live, (int64_t)slots, logical, d_nlive);
+        const int64_t nb = ((int64_t)slots + kMapChunk - 1) / kMapChunk;
+        k_map_count<<<(unsigned)nb, 1024, 0, stream>>>(live, (int64_t)slots, mapblk);
+        SVDB_LAUNCH_CHECK();
+        k_map_scan<<<1, 1024, 0, stream>>>(mapblk, nb, d_nlive);
+        SVDB_LAUNCH_CHECK();
+        k_map_write<<<(unsigned)nb, 1024, 0, stream>>>(live, (int64_t)slots, mapblk, logical);
         SVDB_LAUNCH_CHECK();
         SVDB_CUDA(cudaMemsetAsync(d_count, 0, 3 * sizeof(int), stream));
         k_count_unscreenable<<<(unsigned)std::min<size_t>((slots + 255) / 256, 1024), 256, 0, stream>>>(
@@ -589,6 +651,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->rowp);
     cudaFree(s->live);
     cudaFree(s->logical);
+    cudaFree(s->mapblk);
     cudaFree(s->scratch);
     cudaFree(s->d_nlive);
     cudaFree(s->d_count);
@@ -718,6 +781,21 @@ int svdbd_store_kill(svdbd_store* hs, int64_t slot) {
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     s->dirty_list.push_back(slot);  // its row error term becomes +inf (never screened)
     s->map_dirty = true;
+    return SVDB_OK;
+}
+
+int svdbd_store_read_row(svdbd_store* hs, int64_t slot, double* out) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if (slot >= 0 && (size_t)slot >= s->slots && (size_t)slot < s->slots + s->stage_rows) {
+        std::memcpy(out, s->stage.data() + ((size_t)slot - s->slots) * s->dim, s->dim * sizeof(double));
+        return SVDB_OK;
+    }
+    if (slot < 0 || (size_t)slot >= s->slots) {
+        svdb_set_error("read_row: slot %lld out of range", (long long)slot);
+        return SVDB_EINVAL;
+    }
+    SVDB_CUDA(cudaMemcpyAsync(out, s->x64 + slot * s->ld, s->dim * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
     return SVDB_OK;
 }
 

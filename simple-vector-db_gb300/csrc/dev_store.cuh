@@ -33,6 +33,7 @@ struct Store {
     float4* rowp = nullptr;  // {|x| up (-1: dead slot), |bf16 x| up, |x - bf16 x| up (inf: unscreenable), |x|^2/2}
     uint8_t* live = nullptr;
     int64_t* logical = nullptr;
+    int64_t* mapblk = nullptr;  // per-chunk offsets of the slot->logical map
     int64_t* d_nlive = nullptr;
     int64_t h_nlive = 0;
 

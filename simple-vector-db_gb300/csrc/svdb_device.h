@@ -52,6 +52,8 @@ int svdbd_store_append(svdbd_store* s, const double* const* rows, const uint8_t*
 int svdbd_store_append_block(svdbd_store* s, const double* rows, size_t n);
 int svdbd_store_overwrite(svdbd_store* s, int64_t slot, const double* row, int live);
 int svdbd_store_kill(svdbd_store* s, int64_t slot);
+/* copy one row (device or still staged) to host memory */
+int svdbd_store_read_row(svdbd_store* s, int64_t slot, double* out);
 /* flush staged mutations, rebuild derived arrays and the slot->logical map */
 int svdbd_store_sync(svdbd_store* s);
 int svdbd_store_wait(svdbd_store* s);

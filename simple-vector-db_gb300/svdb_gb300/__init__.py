@@ -94,6 +94,12 @@ def _load():
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
         "svdb_selftest_bounded_wait": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_uint32)]),
+        "svdb_server_create": (vp, [sz, sz]),
+        "svdb_server_destroy": (None, [vp]),
+        "svdb_server_size": (sz, [vp]),
+        "svdb_server_insert_block": (C.c_int, [vp, _dp, sz, C.POINTER(C.c_size_t)]),
+        "svdb_server_read": (C.c_int, [vp, sz, _dp]),
+        "svdb_server_execute": (C.c_int, [vp, vp, sz, vp, C.c_int, _i64p, _dp, sz, C.POINTER(SearchStats)]),
         "svdb_merge_topk": (C.c_int, [C.c_int, _i64p, _dp, sz, sz, sz, _i64p, _dp]),
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
