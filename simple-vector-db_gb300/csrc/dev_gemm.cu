@@ -63,6 +63,8 @@ constexpr uint32_t kStageA = kBM * kBK * 2;  // 16 KB
 constexpr uint32_t kStageB = kBN * kBK * 2;  // 32 KB
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitimate wait
 constexpr int kCapMin = 8192, kCapMax = 65536;   // candidates kept per query (adaptive)
+constexpr int kSubMin = 4096;                     // slots per sub-list when the budget allows
+constexpr int kMaxSub = 512;                      // sub-lists per query: 2 per row group
 constexpr int kSurvCap = 8192;                    // survivors re-ranked per query
 constexpr size_t kCandBudget = size_t(4) << 30;   // bytes of candidate lists per search (HBM is plentiful)
 constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key and m, per unit of m
@@ -292,10 +294,11 @@ struct ScreenParams {
     const float4* qpar;  // per query {qn, eqq, eq0, valid}
     int* tau;            // per query: shared lower bound of the k-th best key (ordered int)
     int* bins;           // per query, k bins: best chunk maximum of the chunks whose index % k is the bin
-    int* cnt;            // per query candidate count (may exceed cap: overflow)
-    int2* cand;          // per query: cap x {row slot, key bits}
+    int* cnt;            // per (query, sub-list) candidate count (may exceed subcap: overflow)
+    int2* cand;          // per query: nsub sub-lists of subcap x {row slot, key bits}, stride cap
     int* err;            // set to 1 when a wait timed out
     int nq, k, cap;
+    int nsub, subcap;    // sub-list = (row group, column half): one emitting thread each
     int ntq;      // query tiles
     int ntr;      // row tiles
     int rgroups;  // row groups per query tile
@@ -457,13 +460,21 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         TopL<KL> top;
         top.init(valid ? P.k : 0);  // invalid queries: threshold +inf, never emit, never push
         float tau_c = -INFINITY, published = -INFINITY;
-        int2* cq = P.cand + (size_t)(q < P.nq ? q : 0) * P.cap;
+        // this thread's own sub-list of the query's candidates: emission needs no
+        // atomic, the count stays in a register and is stored once at the end
+        const int sub = grp * 2 + half;
+        int2* cq = P.cand + (size_t)(q < P.nq ? q : 0) * P.cap + (size_t)sub * P.subcap;
+        int nemit = 0;
         const int col0 = half * (kBN / 2);
         int j = 0;
         for (int r = r0; r < r1; ++r, ++j) {
             const int b = j & 1;
             const uint32_t use = (uint32_t)j >> 1;
             const float4* rps = S.rp[b] + col0;  // this warp's 128 rows, staged by the producer
+            // cosine: validity words of this warp's 128 rows (lane c holds the word
+            // of chunk c), loaded before the wait so their latency is hidden
+            uint32_t vbl = 0;
+            if (NORM && lane < kBN / 2 / 32) vbl = __ldg(P.vbits + ((r * kBN + col0) >> 5) + lane);
             // tcgen05.ld is warp-collective (.sync.aligned): every branch that
             // leads to one must be taken by the whole warp, including this wait
             bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
@@ -544,7 +555,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 if (NORM) {
                     // keys are the accumulator values; rows that are not searchable
                     // become NaN (every comparison with NaN is false)
-                    const uint32_t vb = __ldg(P.vbits + (rw >> 5));
+                    const uint32_t vb = __shfl_sync(0xffffffffu, vbl, c);
                     if (vb != 0xFFFFFFFFu) {  // warp-uniform
 #pragma unroll
                         for (int i = 0; i < C; ++i)
@@ -593,13 +604,14 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                                                              __fmaf_ru(eq, rc[8 * g + i].y, rc[8 * g + i].w));
                             mask |= (wg && u >= thr2 ? 1u : 0u) << i;
                         }
-                        const int base = mask ? atomicAdd(&P.cnt[q], __popc(mask)) : 0;
+                        const int base = nemit;
+                        nemit += __popc(mask);
                         const uint32_t any = __reduce_or_sync(0xffffffffu, mask);
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
                             if ((any >> i) & 1u) {  // warp-uniform
                                 const int slot = base + __popc(mask & ((1u << i) - 1u));
-                                if (((mask >> i) & 1u) && slot < P.cap)
+                                if (((mask >> i) & 1u) && slot < P.subcap)
                                     cq[slot] = make_int2(rw + 8 * g + i, (int)v[8 * g + i]);
                             }
                         }
@@ -623,6 +635,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 published = top.mn;
             }
         }
+        if (q < P.nq) P.cnt[(size_t)q * P.nsub + sub] = nemit;
     }
 
     __syncthreads();
@@ -746,13 +759,13 @@ __global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ r
     }
 }
 
-__global__ void k_init_search(int* tau, int* bins, int* cnt, uint8_t* flags, int nq, int k, int* alpha, int* redo_n,
-                              unsigned long long* stats) {
+__global__ void k_init_search(int* tau, int* bins, int* cnt, int nsub, uint8_t* flags, int nq, int k, int* alpha,
+                              int* redo_n, unsigned long long* stats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nq) {
         tau[i] = f2ord(-INFINITY);
         for (int t = 0; t < k; ++t) bins[(size_t)i * k + t] = f2ord(-INFINITY);
-        cnt[i] = 0;
+        for (int t = 0; t < nsub; ++t) cnt[(size_t)i * nsub + t] = 0;
         flags[i] = scr::kOk;
     }
     if (i == 0) {
@@ -811,19 +824,49 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
 // Pass 1: every thread keeps the k best lower bounds of its candidates
 // (registers); their union holds the k best overall, so a radix select over
 // it in shared memory gives the exact k-th largest.  Pass 2: survivors.
+//
+// The query's candidates sit in nsub sub-lists (one per emitting thread of the
+// screen); candidate i of the concatenation is found by a binary search over
+// the exclusive prefix of the sub-list counts (shared memory).
 template <int KL>
 __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
-                                                 const float4* __restrict__ rpar, const float4* __restrict__ qpar,
-                                                 int k, int2* __restrict__ surv, int* __restrict__ nsurv,
-                                                 int* __restrict__ sig, uint8_t* __restrict__ flags) {
+                                                 int nsub, int subcap, const float4* __restrict__ rpar,
+                                                 const float4* __restrict__ qpar, int k, int2* __restrict__ surv,
+                                                 int* __restrict__ nsurv, int* __restrict__ sig,
+                                                 uint8_t* __restrict__ flags) {
     extern __shared__ uint32_t vals[];  // blockDim.x * k ordered lower bounds
     __shared__ int hist[256];
     __shared__ uint32_t s_sh[3];
-    __shared__ int s_out, s_sig;
+    __shared__ int s_out, s_sig, s_over;
+    __shared__ int s_pre[scr::kMaxSub + 1];
     const int q = blockIdx.x;
     const float4 qp = qpar[q];
-    const int n = cnt[q];
-    if (qp.w == 0.f || n > cap) {
+    if (threadIdx.x < 32) {  // warp 0: prefix of the sub-list counts
+        const int lane = threadIdx.x;
+        int run = 0;
+        bool over = false;
+        for (int s0 = 0; s0 < nsub; s0 += 32) {
+            const int s = s0 + lane;
+            const int c = s < nsub ? cnt[(size_t)q * nsub + s] : 0;
+            over = over || c > subcap;
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (s < nsub) s_pre[s] = run + incl - c;
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        over = __any_sync(0xffffffffu, over);
+        if (lane == 0) {
+            s_pre[nsub] = run;
+            s_over = over ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    const int n = s_pre[nsub];
+    if (qp.w == 0.f || s_over) {
         if (threadIdx.x == 0) {
             flags[q] = qp.w == 0.f ? scr::kInvalidQuery : scr::kOverflow;
             nsurv[q] = 0;
@@ -831,10 +874,21 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         }
         return;
     }
-    const int2* cq = cand + (size_t)q * cap;
+    const int2* cbase = cand + (size_t)q * cap;
+    auto at = [&](int i) {  // the largest sub-list s with prefix <= i holds candidate i
+        int lo = 0, hi = nsub - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_pre[mid] <= i)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        return cbase[(size_t)lo * subcap + (i - s_pre[lo])];
+    };
     const int bd = blockDim.x;
     auto lower = [&](int i) {
-        const int2 c = cq[i];
+        const int2 c = at(i);
         return f2u_ord(__fsub_rd(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z)));
     };
     if (threadIdx.x == 0) {
@@ -846,7 +900,8 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         TopL<KL> top;
         top.init(k);
         for (int i = threadIdx.x; i < n; i += bd) {
-            const float L = __fsub_rd(__int_as_float(cq[i].y), screen_bound(__ldg(rpar + cq[i].x), qp.x, qp.y, qp.z));
+            const int2 c = at(i);
+            const float L = __fsub_rd(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
             if (L > top.mn) top.push(L);
         }
 #pragma unroll
@@ -860,7 +915,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     }
     int2* sq = surv + (size_t)q * scr::kSurvCap;
     for (int i = threadIdx.x; i < n; i += bd) {
-        const int2 c = cq[i];
+        const int2 c = at(i);
         const float U = __fadd_ru(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
         if (!isnan(U) && f2u_ord(U) >= thr_ord) {  // rows with NaN parameters never survive
             const int o = atomicAdd(&s_out, 1);
@@ -1185,7 +1240,7 @@ __global__ void __launch_bounds__(256) k_rerank_small(const double* __restrict__
 // gather query rows (padded FP64) of the queries to re-answer; scatter back
 // queries the screen could not certify, compacted on the device, with the
 // batch's statistics {candidates, survivors, re-ranked, widened, bound failures}
-__global__ void k_collect_redo(const uint8_t* __restrict__ flags, const int* __restrict__ cnt,
+__global__ void k_collect_redo(const uint8_t* __restrict__ flags, const int* __restrict__ cnt, int nsub,
                                const int* __restrict__ nsurv, const int* __restrict__ nref, int nq,
                                int* __restrict__ list, int* __restrict__ count,
                                unsigned long long* __restrict__ stats) {
@@ -1194,7 +1249,7 @@ __global__ void k_collect_redo(const uint8_t* __restrict__ flags, const int* __r
     if (q < nq) {
         const uint8_t f = flags[q];
         if (f != scr::kOk) list[atomicAdd(count, 1)] = q;
-        v[0] = (unsigned)cnt[q];
+        for (int t = 0; t < nsub; ++t) v[0] += (unsigned)cnt[(size_t)q * nsub + t];
         v[1] = (unsigned)nsurv[q];
         v[2] = (unsigned)nref[q];
         v[3] = f != scr::kOk;
@@ -1294,8 +1349,16 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 struct Bf16Layout {
     size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     int ntr, cap;
+    int rgroups, nsub, subcap;
     size_t npad;
 };
+
+// row groups of the screen grid: query tiles x row groups CTAs, about one per SM
+static int screen_rgroups(size_t nq, int ntr) {
+    const int ntq = (int)((nq + scr::kBM - 1) / scr::kBM);
+    int rg = std::max(1, std::min(num_sms() / std::max(ntq, 1), ntr));
+    return std::min(rg, scr::kMaxSub / 2);
+}
 
 constexpr size_t k_max_bf16 = 128;  // largest k the screen certifies
 
@@ -1317,13 +1380,20 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.vbits = take(L.npad / 8);
     L.tau = take(nq * sizeof(int));
     L.bins = take(nq * k_max_bf16 * sizeof(int));
-    L.cnt = take(nq * sizeof(int));
+    L.rgroups = screen_rgroups(nq, L.ntr);
+    L.nsub = 2 * L.rgroups;
+    L.cnt = take(nq * (size_t)L.nsub * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
-    // per query before the running thresholds settle)
-    size_t cap = scr::kCapMax;
+    // per query before the running thresholds settle), split into one
+    // sub-list per emitting thread; at least the survivor cap in all, since
+    // the refinement reuses the storage
+    size_t cap = std::max<size_t>(scr::kCapMax, (size_t)L.nsub * scr::kSubMin);
     while (cap > (size_t)scr::kCapMin && nq * cap * sizeof(int2) > scr::kCandBudget) cap >>= 1;
-    L.cap = (int)cap;
-    L.cand = take(nq * cap * sizeof(int2));
+    size_t subcap = cap / L.nsub;
+    if (subcap * L.nsub < (size_t)scr::kSurvCap) subcap = (scr::kSurvCap + L.nsub - 1) / L.nsub;
+    L.subcap = (int)subcap;
+    L.cap = (int)(subcap * L.nsub);
+    L.cand = take(nq * (size_t)L.cap * sizeof(int2));
     L.surv = take(nq * (size_t)scr::kSurvCap * sizeof(int2));
     L.nsurv = take(nq * sizeof(int));
     L.nref = take(nq * sizeof(int));
@@ -1383,7 +1453,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
                                                                           qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
-    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, flags, nq, k, alpha, redo_n, dstats);
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, L.nsub, flags, nq, k, alpha, redo_n,
+                                                                         dstats);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
@@ -1412,11 +1483,12 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.nq = nq;
     P.k = k;
     P.cap = L.cap;
+    P.nsub = L.nsub;
+    P.subcap = L.subcap;
     P.ntq = (nq + scr::kBM - 1) / scr::kBM;
     P.ntr = L.ntr;
     P.kblocks = (int)(s->ldb / scr::kBK);
-    const int G = num_sms();
-    P.rgroups = std::max(1, std::min(G / std::max(P.ntq, 1), P.ntr));
+    P.rgroups = L.rgroups;
     const unsigned grid = (unsigned)(P.ntq * P.rgroups);
     {
         auto kern = k <= 16   ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
@@ -1443,13 +1515,13 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
             gc->select_attr = true;
         }
         if (k <= 16)
-            k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
+            k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, L.nsub, L.subcap, rpar, qpar, k, surv,
                                                                              nsurv, sig, flags);
         else if (k <= 32)
-            k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
+            k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, L.nsub, L.subcap, rpar, qpar, k, surv,
                                                                              nsurv, sig, flags);
         else
-            k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, rpar, qpar, k, surv,
+            k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, L.nsub, L.subcap, rpar, qpar, k, surv,
                                                                             nsurv, sig, flags);
     }
     SVDB_LAUNCH_CHECK();
@@ -1510,7 +1582,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     // queries the screen could not certify: exact FP64 scan, entirely on the
     // device (no host round trip; with nothing to redo the kernels exit at once)
-    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, nsurv, nref, nq, redo, redo_n,
+    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, L.nsub, nsurv, nref, nq, redo, redo_n,
                                                                           dstats);
     SVDB_LAUNCH_CHECK();
     {
