@@ -64,7 +64,7 @@ constexpr uint32_t kStageB = kBN * kBK * 2;  // 32 KB
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitimate wait
 constexpr int kCapMin = 8192, kCapMax = 65536;   // candidates kept per query (adaptive)
 constexpr int kSubMin = 4096;                     // slots per sub-list when the budget allows
-constexpr int kMaxSub = 512;                      // sub-lists per query: 2 per row group
+constexpr int kMaxSub = 512;                      // sub-lists per query: 2 per segment of its query tile
 constexpr int kSurvCap = 8192;                    // survivors re-ranked per query
 constexpr size_t kCandBudget = size_t(4) << 30;   // bytes of candidate lists per search (HBM is plentiful)
 constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key and m, per unit of m
@@ -285,6 +285,27 @@ struct TopL<0> {
     __device__ __forceinline__ void push(float) {}
 };
 
+// Work of one CTA: up to kMaxSeg segments, each a range of store tiles
+// [lo, hi) against one query tile; `sub` numbers the segment among those of
+// its query tile (it selects the candidate sub-lists the segment writes).
+constexpr int kMaxCtas = 160;
+constexpr int kMaxSeg = 4;
+struct ScreenSeg {
+    int32_t lo, hi;
+    uint16_t qt, sub;
+};
+struct ScreenSched {
+    ScreenSeg seg[kMaxCtas][kMaxSeg];
+    uint8_t nseg[kMaxCtas];
+    int direct;  // 1: no table; CTA i takes query tile i against every store tile
+    int ntr;
+};
+
+__device__ __forceinline__ ScreenSeg sched_seg(const ScreenSched& S, int sg) {
+    if (S.direct) return ScreenSeg{0, S.ntr, (uint16_t)blockIdx.x, 0};
+    return S.seg[blockIdx.x][sg];
+}
+
 struct ScreenParams {
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
     const float4* spar;  // per row {mult, b, m, 2^-19 m}: the screen's one-FMA form of the bound
@@ -299,10 +320,8 @@ struct ScreenParams {
     int* err;            // set to 1 when a wait timed out
     int nq, k, cap;
     int nsub, subcap;    // sub-list = (row group, column half): one emitting thread each
-    int ntq;      // query tiles
-    int ntr;      // row tiles
-    int rgroups;  // row groups per query tile
     int kblocks;  // ldb / 64
+    ScreenSched sched;
 };
 
 // NORM (cosine): the B operand is the unit-norm shadow, so the key is the
@@ -318,10 +337,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int qt = blockIdx.x % P.ntq;
-    const int grp = blockIdx.x / P.ntq;
-    const int r0 = (int)((int64_t)grp * P.ntr / P.rgroups);
-    const int r1 = (int)((int64_t)(grp + 1) * P.ntr / P.rgroups);
+    const int nseg = P.sched.direct ? 1 : P.sched.nseg[blockIdx.x];
     const int KB = P.kblocks;
     volatile int* abort = &S.abort;
 
@@ -361,10 +377,17 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             uint32_t issued = 0;  // loads issued (for draining on abort)
             uint32_t rp_issued = 0;
             bool ok = true;
-            for (int r = r0; r < r1 && ok; ++r) {
+            uint32_t jt = 0;  // tiles so far (all segments)
+            for (int sg = 0; sg < nseg && ok; ++sg) {
+            const ScreenSeg seg = sched_seg(P.sched, sg);
+            const int qt = seg.qt;
+            for (int r = seg.lo; r < seg.hi && ok; ++r, ++jt) {
                 if (!NORM) {  // the tile's screen parameters into the 2-slot ring (freed by the epilogue)
-                    const uint32_t jt = (uint32_t)(r - r0), slot = jt & 1u;
-                    if (!mbar_wait(&S.rp_empty[slot], ((jt >> 1) & 1u) ^ 1u, abort, kWaitLimitNs)) break;
+                    const uint32_t slot = jt & 1u;
+                    if (!mbar_wait(&S.rp_empty[slot], ((jt >> 1) & 1u) ^ 1u, abort, kWaitLimitNs)) {
+                        ok = false;
+                        break;
+                    }
                     mbar_expect_tx(&S.rp_full[slot], kBN * sizeof(float4));
                     bulk_load(S.rp[slot], P.spar + (size_t)r * kBN, kBN * sizeof(float4), &S.rp_full[slot]);
                     ++rp_issued;
@@ -383,6 +406,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         phase ^= 1;
                     }
                 }
+            }
             }
             // every issued load must have landed before the CTA may exit:
             // wait (bounded) for the completion of the last kStages loads
@@ -406,7 +430,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             uint32_t phase = 0;
             bool ok = true;
             int j = 0;
-            for (int r = r0; r < r1 && ok; ++r, ++j) {
+            for (int sg = 0; sg < nseg && ok; ++sg)
+            for (int r = sched_seg(P.sched, sg).lo, rh = sched_seg(P.sched, sg).hi; r < rh && ok; ++r, ++j) {
                 const int b = j & 1;
                 const uint32_t use = (uint32_t)j >> 1;
                 if (!mbar_wait(&S.accempty[b], (use & 1u) ^ 1u, abort, kWaitLimitNs)) break;
@@ -443,7 +468,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         const int quad = warp & 3;
         const int half = (warp - 2) >> 2;
         const int qi = quad * 32 + lane;
-        const int q = qt * kBM + qi;
+        const int col0 = half * (kBN / 2);
+        int j = 0;  // tiles so far (all segments): accumulator buffer and phase
+        bool alive = true;
+        for (int sg = 0; sg < nseg && alive; ++sg) {
+        // every segment starts afresh: its query tile, running top-k, warm-up
+        const ScreenSeg seg = sched_seg(P.sched, sg);
+        const int q = seg.qt * kBM + qi;
         float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0 (NORM: eq0 = E)
         bool valid = false;
         if (q < P.nq) {
@@ -462,12 +493,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         float tau_c = -INFINITY, published = -INFINITY;
         // this thread's own sub-list of the query's candidates: emission needs no
         // atomic, the count stays in a register and is stored once at the end
-        const int sub = grp * 2 + half;
+        const int sub = 2 * seg.sub + half;
         int2* cq = P.cand + (size_t)(q < P.nq ? q : 0) * P.cap + (size_t)sub * P.subcap;
         int nemit = 0;
-        const int col0 = half * (kBN / 2);
-        int j = 0;
-        for (int r = r0; r < r1; ++r, ++j) {
+        for (int r = seg.lo, js = 0; r < seg.hi; ++r, ++j, ++js) {
             const int b = j & 1;
             const uint32_t use = (uint32_t)j >> 1;
             const float4* rps = S.rp[b] + col0;  // this warp's 128 rows, staged by the producer
@@ -479,12 +508,15 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // leads to one must be taken by the whole warp, including this wait
             bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
             if (!NORM) got = got && mbar_wait(&S.rp_full[b], use & 1u, abort, kWaitLimitNs);
-            if (!__all_sync(0xffffffffu, got)) break;
+            if (!__all_sync(0xffffffffu, got)) {
+                alive = false;
+                break;
+            }
             tc_fence_after();
             const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN + col0);
             const int row0 = r * kBN + col0;
-            if (j == 0) {  // warp-uniform: lanes of invalid queries load and discard
-                // Warm-up on the first tile, before anything is emitted: fold the
+            if (js == 0) {  // warp-uniform: lanes of invalid queries load and discard
+                // Warm-up on the segment's first tile, before anything is emitted: fold the
                 // lower bound of every row into the running k best (rows, not chunk
                 // maxima, so k values exist after one tile) and publish the chunk
                 // maxima to the bins.  The emitting pass below then skips its pushes
@@ -523,7 +555,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     }
                 }
             }
-            if (valid && (j < 8 || (j & 7) == 0)) {
+            if (valid && (js < 8 || (js & 7) == 0)) {
                 // The k bins hold lower bounds of k distinct rows (chunks of different
                 // bins are different rows), so their minimum is a valid threshold; it
                 // reflects what every CTA has seen of this query, not only this one.
@@ -623,7 +655,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // the bins take the same maxima, bin = tile half mod k.
             const float maxl = __fsub_rd(tmax, eq0);
             if (valid && maxl > thr) atomicMax(&P.bins[(size_t)q * P.k + (r * 2 + half) % P.k], f2ord(maxl));
-            if (valid && j > 0 && maxl > top.mn) top.push(maxl);
+            if (valid && js > 0 && maxl > top.mn) top.push(maxl);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -636,6 +668,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
         }
         if (q < P.nq) P.cnt[(size_t)q * P.nsub + sub] = nemit;
+        }
     }
 
     __syncthreads();
@@ -1349,15 +1382,72 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
 struct Bf16Layout {
     size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     int ntr, cap;
-    int rgroups, nsub, subcap;
+    int nctas, nsub, subcap;
     size_t npad;
+    ScreenSched sched;
 };
 
-// row groups of the screen grid: query tiles x row groups CTAs, about one per SM
-static int screen_rgroups(size_t nq, int ntr) {
-    const int ntq = (int)((nq + scr::kBM - 1) / scr::kBM);
-    int rg = std::max(1, std::min(num_sms() / std::max(ntq, 1), ntr));
-    return std::min(rg, scr::kMaxSub / 2);
+// The screen's work, query tiles x store tiles, over G = one CTA per SM.  With
+// G = base * ntq + ea, query tiles [0, ea) get base + 1 CTAs that split the
+// store tiles evenly, the others base CTAs of T = ceil(ntq * ntr / G) tiles
+// each; what those leave at the end of the store (ntr - base * T tiles per
+// query tile) is shared out among the first family's CTAs, whose own share is
+// shorter.  Every CTA then has ~T tiles; CTAs that cover the same store rows
+// do so at the same time (a row is read from HBM about once per family).
+// Returns the number of CTAs; *maxsub = most segments of one query tile.
+static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub) {
+    std::memset(&S, 0, sizeof(S));
+    S.ntr = ntr;
+    const int G = std::min(num_sms(), kMaxCtas);
+    if (ntq >= G) {
+        S.direct = 1;
+        *maxsub = 1;
+        return ntq;
+    }
+    std::vector<int> ord(ntq, 0);
+    bool fits = true;
+    auto add = [&](int c, int qt, int lo, int hi) {
+        if (hi <= lo) return;
+        if (S.nseg[c] >= kMaxSeg) {
+            fits = false;
+            return;
+        }
+        S.seg[c][S.nseg[c]++] = ScreenSeg{lo, hi, (uint16_t)qt, (uint16_t)ord[qt]++};
+    };
+    const int base = G / ntq, ea = G % ntq;
+    const int T = (int)(((int64_t)ntq * ntr + G - 1) / G);
+    int c = 0;
+    for (int qt = 0; qt < ea; ++qt)
+        for (int jj = 0; jj <= base; ++jj, ++c)
+            add(c, qt, (int)((int64_t)jj * ntr / (base + 1)), (int)((int64_t)(jj + 1) * ntr / (base + 1)));
+    const int helpers = c;
+    for (int qt = ea; qt < ntq; ++qt)
+        for (int jj = 0; jj < base; ++jj, ++c)
+            add(c, qt, (int)std::min<int64_t>((int64_t)jj * T, ntr), (int)std::min<int64_t>((int64_t)(jj + 1) * T, ntr));
+    const int64_t Rq = std::max<int64_t>(0, (int64_t)ntr - (int64_t)base * T);
+    const int64_t R = (int64_t)(ntq - ea) * Rq;
+    for (int h = 0; h < helpers && R > 0; ++h) {
+        int64_t s0 = h * R / helpers;
+        const int64_t e0 = (h + 1) * R / helpers;
+        while (s0 < e0) {
+            const int64_t qb = s0 / Rq, qe = std::min(e0, (qb + 1) * Rq);
+            add(h, ea + (int)qb, (int)((int64_t)base * T + s0 - qb * Rq), (int)((int64_t)base * T + qe - qb * Rq));
+            s0 = qe;
+        }
+    }
+    if (fits && 2 * *std::max_element(ord.begin(), ord.end()) > scr::kMaxSub) fits = false;
+    if (!fits) {  // plain row groups: query tile x row range, one segment each
+        std::memset(&S, 0, sizeof(S));
+        S.ntr = ntr;
+        std::fill(ord.begin(), ord.end(), 0);
+        c = 0;
+        for (int g = 0; g < base; ++g)
+            for (int qt = 0; qt < ntq; ++qt, ++c)
+                S.seg[c][S.nseg[c]++] = ScreenSeg{(int)((int64_t)g * ntr / base), (int)((int64_t)(g + 1) * ntr / base),
+                                                  (uint16_t)qt, (uint16_t)ord[qt]++};
+    }
+    *maxsub = std::max(1, *std::max_element(ord.begin(), ord.end()));
+    return c;
 }
 
 constexpr size_t k_max_bf16 = 128;  // largest k the screen certifies
@@ -1380,8 +1470,9 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.vbits = take(L.npad / 8);
     L.tau = take(nq * sizeof(int));
     L.bins = take(nq * k_max_bf16 * sizeof(int));
-    L.rgroups = screen_rgroups(nq, L.ntr);
-    L.nsub = 2 * L.rgroups;
+    int maxsub = 1;
+    L.nctas = screen_schedule((int)((nq + scr::kBM - 1) / scr::kBM), L.ntr, L.sched, &maxsub);
+    L.nsub = 2 * maxsub;
     L.cnt = take(nq * (size_t)L.nsub * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
     // per query before the running thresholds settle), split into one
@@ -1485,11 +1576,9 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.cap = L.cap;
     P.nsub = L.nsub;
     P.subcap = L.subcap;
-    P.ntq = (nq + scr::kBM - 1) / scr::kBM;
-    P.ntr = L.ntr;
     P.kblocks = (int)(s->ldb / scr::kBK);
-    P.rgroups = L.rgroups;
-    const unsigned grid = (unsigned)(P.ntq * P.rgroups);
+    P.sched = L.sched;
+    const unsigned grid = (unsigned)L.nctas;
     {
         auto kern = k <= 16   ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
                     : k <= 32 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
