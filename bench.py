@@ -47,7 +47,7 @@ METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GP
 # ncu capture summarised in profiles/k_screen_bf16_200kx768_q4096.md (a 200,000-row
 # store, 4096 cosine queries; the bytes grow with the rows, so a full launch is
 # this times N).  None when no capture of the current kernel exists.
-SCREEN_DRAM_BYTES_PER_ROW = (316.354304e6 + 17.259520e6) / 200_000
+SCREEN_DRAM_BYTES_PER_ROW = (420.257536e6 + 19.836416e6) / 200_000
 
 
 def log(*a):
