@@ -1034,6 +1034,35 @@ __device__ void refine_keep(int q, int n, int k, float2* luq, const int2* sq, in
     if (threadIdx.x == 0) nref[q] = *s_out;
 }
 
+// Refined {L, U} of one survivor from p = S (see above): the key's interval.
+// xb = sqf[row]: |x|^2 in [xb.x, xb.y], 1/(2|x|) in [xb.z, xb.w].
+__device__ __forceinline__ float2 refine_interval(float p, float gamma, float qq_lo, float qq_hi, float qn_up,
+                                                  float4 xb, float xn_up, int metric) {
+    const float sup = __fmul_ru(p, 1.0f + gamma);
+    const float eta = __fmul_ru(1.1921875e-07f, __fadd_ru(qn_up, xn_up));  // 2^-23 (1 + 2^-13)
+    float ed2 = __fmaf_ru(gamma, sup, __fmul_ru(eta, __fadd_ru(__fmul_ru(2.0f, __fsqrt_ru(sup)), eta)));
+    ed2 = __fmaf_ru(9.094947e-13f, __fadd_ru(qq_hi, xb.y), __fmul_ru(ed2, 1.000001f));  // + 2^-40 scale
+    const float s_hi = __fadd_ru(p, ed2), s_lo = __fsub_rd(p, ed2);  // |q - x|^2 in [s_lo, s_hi]
+    float L, U;
+    if (metric == SVDB_EUCLIDEAN) {  // key = (|q|^2 - d^2) / 2
+        L = __fmul_rd(__fsub_rd(qq_lo, s_hi), 0.5f);
+        U = __fmul_ru(__fsub_ru(qq_hi, s_lo), 0.5f);
+    } else {  // dot = (|q|^2 + |x|^2 - d^2) / 2
+        const float a_lo = __fsub_rd(__fadd_rd(qq_lo, xb.x), s_hi);
+        const float a_hi = __fsub_ru(__fadd_ru(qq_hi, xb.y), s_lo);
+        if (metric == SVDB_DOT) {
+            L = __fmul_rd(a_lo, 0.5f);
+            U = __fmul_ru(a_hi, 0.5f);
+        } else {  // cosine key = dot / |x|, 1/(2|x|) in [xb.z, xb.w]
+            L = a_lo >= 0.f ? __fmul_rd(a_lo, xb.z) : __fmul_rd(a_lo, xb.w);
+            U = a_hi >= 0.f ? __fmul_ru(a_hi, xb.w) : __fmul_ru(a_hi, xb.z);
+            if (isnan(L)) L = -INFINITY;
+            if (isnan(U)) U = INFINITY;
+        }
+    }
+    return make_float2(L, U);
+}
+
 // The per-row key and bound are interval arithmetic in FP32 with directed
 // rounding (GB300's FP64 pipe is narrow; one FP64 instruction per row per warp
 // would dominate): |q|^2 and |x|^2 enter as [rd, ru] pairs, d^2 as [S - E, S + E].
@@ -1072,11 +1101,27 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
     // each lane: ld/64 steps into each of 4 accumulators, then 2 + 4 additions
     const float gamma = (float)(ld / 64 + 8) * 5.9604644775390625e-08f * 1.0001f;
     // half a warp per row: lane h of the half reads float4 h, h+16, ...
+    // Software-pipelined: the next row's index and norm intervals are fetched
+    // while this row's 3 KB are read and reduced, so a row costs one memory
+    // round trip instead of three dependent ones.
     const int hw = lane >> 4, h = lane & 15;
-    for (int base = (split * kWarps + warp) * 2; base < n; base += splits * kWarps * 2) {
+    const int stride = splits * kWarps * 2;
+    int base = (split * kWarps + warp) * 2;
+    int row_n = base + hw < n ? sq[base + hw].x : 0;
+    float4 xb_n = make_float4(0.f, 0.f, 0.f, 0.f);
+    float xn_n = 0.f;
+    if (base + hw < n && h == 0) {
+        xb_n = sqf[row_n];
+        xn_n = rowp[row_n].x;
+    }
+    for (; base < n; base += stride) {
         const int i = base + hw;
         const bool act = i < n;
-        const int row = act ? sq[i].x : 0;
+        const int row = row_n;
+        const float4 xb = xb_n;
+        const float xn_up = xn_n;
+        const int in = i + stride;
+        row_n = in < n ? sq[in].x : 0;
         float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
         if (act) {
             const float4* x = reinterpret_cast<const float4*>(x32 + (size_t)row * ld);
@@ -1097,33 +1142,11 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
         p += __shfl_xor_sync(0xffffffffu, p, 4);
         p += __shfl_xor_sync(0xffffffffu, p, 2);
         p += __shfl_xor_sync(0xffffffffu, p, 1);
-        if (act && h == 0) {
-            const float4 xb = sqf[row];  // |x|^2 in [xb.x, xb.y], 1/(2|x|) in [xb.z, xb.w]
-            const float xn_up = rowp[row].x;
-            const float sup = __fmul_ru(p, 1.0f + gamma);
-            const float eta = __fmul_ru(1.1921875e-07f, __fadd_ru(qn_up, xn_up));  // 2^-23 (1 + 2^-13)
-            float ed2 = __fmaf_ru(gamma, sup, __fmul_ru(eta, __fadd_ru(__fmul_ru(2.0f, __fsqrt_ru(sup)), eta)));
-            ed2 = __fmaf_ru(9.094947e-13f, __fadd_ru(qq_hi, xb.y), __fmul_ru(ed2, 1.000001f));  // + 2^-40 scale
-            const float s_hi = __fadd_ru(p, ed2), s_lo = __fsub_rd(p, ed2);  // |q - x|^2 in [s_lo, s_hi]
-            float L, U;
-            if (metric == SVDB_EUCLIDEAN) {  // key = (|q|^2 - d^2) / 2
-                L = __fmul_rd(__fsub_rd(qq_lo, s_hi), 0.5f);
-                U = __fmul_ru(__fsub_ru(qq_hi, s_lo), 0.5f);
-            } else {  // dot = (|q|^2 + |x|^2 - d^2) / 2
-                const float a_lo = __fsub_rd(__fadd_rd(qq_lo, xb.x), s_hi);
-                const float a_hi = __fsub_ru(__fadd_ru(qq_hi, xb.y), s_lo);
-                if (metric == SVDB_DOT) {
-                    L = __fmul_rd(a_lo, 0.5f);
-                    U = __fmul_ru(a_hi, 0.5f);
-                } else {  // cosine key = dot / |x|, 1/(2|x|) in [xb.z, xb.w]
-                    L = a_lo >= 0.f ? __fmul_rd(a_lo, xb.z) : __fmul_rd(a_lo, xb.w);
-                    U = a_hi >= 0.f ? __fmul_ru(a_hi, xb.w) : __fmul_ru(a_hi, xb.z);
-                    if (isnan(L)) L = -INFINITY;
-                    if (isnan(U)) U = INFINITY;
-                }
-            }
-            luq[i] = make_float2(L, U);
+        if (in < n && h == 0) {
+            xb_n = sqf[row_n];
+            xn_n = rowp[row_n].x;
         }
+        if (act && h == 0) luq[i] = refine_interval(p, gamma, qq_lo, qq_hi, qn_up, xb, xn_up, metric);
     }
     if (splits == 1) {
         __syncthreads();

@@ -207,3 +207,29 @@ def test_bf16_cosine_dead_and_zero_rows(S, oracle):
     assert ((vals == wval) | (np.isnan(vals) & np.isnan(wval))).all()
     small.close()
     db.close()
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_bf16_grouped_refinement(S, oracle, metric):
+    """Batches larger than two queries per SM: one refinement block per query,
+    in the order of the sorted survivor signatures.  Uneven clusters (a few
+    hundred to 2,600 near-ties) and queries between two centres (survivors
+    from two clusters) on the same batch."""
+    rng = np.random.default_rng(700 + metric)
+    d = 60
+    C = rng.normal(size=(40, d))
+    sizes = np.concatenate([rng.integers(100, 900, 34), rng.integers(1500, 2600, 6)])
+    X = np.concatenate([C[c] + 0.05 * rng.normal(size=(n, d)) for c, n in enumerate(sizes)])
+    X = X[rng.permutation(len(X))]
+    which = rng.integers(0, 40, 600)
+    Q = C[which] + 0.05 * rng.normal(size=(600, d))
+    Q[::7] = 0.5 * (C[which[::7]] + C[(which[::7] + 1) % 40]) + 0.05 * rng.normal(size=(len(Q[::7]), d))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for k in (1, 10, 32):
+        ids, vals, st = _search_both(S, db, Q, k, metric)
+        wid, wval = oracle.topk(metric, X, Q, k)
+        assert np.array_equal(ids, wid), k
+        assert np.array_equal(vals, wval), k
+        assert st.bound_failures == 0 and st.widened == 0, k
+    db.close()
