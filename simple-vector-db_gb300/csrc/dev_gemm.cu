@@ -1068,7 +1068,7 @@ __device__ __forceinline__ float2 refine_interval(float p, float gamma, float qq
 // would dominate): |q|^2 and |x|^2 enter as [rd, ru] pairs, d^2 as [S - E, S + E].
 // Each survivor's refined {L, U} goes to `lu` (the candidate list's storage,
 // dead after the select), so no per-thread state limits the occupancy.
-__global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restrict__ x32, size_t ld,
+__global__ void __launch_bounds__(kRefThreads, 3) k_refine(const float* __restrict__ x32, size_t ld,
                                                            const float* __restrict__ q32,
                                                            const double* __restrict__ qsq,
                                                            const float4* __restrict__ sqf,
@@ -1126,7 +1126,7 @@ __global__ void __launch_bounds__(kRefThreads, 4) k_refine(const float* __restri
         if (act) {
             const float4* x = reinterpret_cast<const float4*>(x32 + (size_t)row * ld);
             const float4* qv = reinterpret_cast<const float4*>(qs);
-#pragma unroll 6
+#pragma unroll 12
             for (size_t j = h; j < ld / 4; j += 16) {
                 const float4 xv = __ldg(x + j);
                 const float4 qq4 = qv[j];
