@@ -30,6 +30,18 @@ namespace svdb {
 constexpr int kRowAlign = 16;  // FP64 master row stride: multiple of 16 doubles (128 B)
 constexpr int kBf16Align = 64; // BF16 shadow row stride: multiple of 64 (one 128-B swizzle row)
 
+// The BF16 shadows are stored the way the tensor-core screen consumes them:
+// tiles of 256 rows x 64 columns (32 KB), the tiles of one 256-row group
+// consecutive in column order, each tile in the 128-byte-swizzled layout
+// (16-byte chunk c of row r at chunk c ^ (r & 7) of the row's 128 bytes).  A
+// screen stage is then one contiguous 32 KB bulk copy, and HBM is read in
+// whole tiles rather than 128 bytes from each of 256 rows.  Index of element
+// e of row `slot`; ldb is a multiple of 64.
+__host__ __device__ inline size_t bf16_tile_index(int64_t slot, size_t e, size_t ldb) {
+    const size_t t = (size_t)slot >> 8, r = (size_t)slot & 255u, kb = e >> 6, c = (e >> 3) & 7u, w = e & 7u;
+    return (((t * (ldb >> 6) + kb) << 8) + r) * 64u + ((c ^ (r & 7u)) << 3) + w;
+}
+
 static inline size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
 
 // ---------------------------------------------------------------------------

@@ -307,6 +307,7 @@ __device__ __forceinline__ ScreenSeg sched_seg(const ScreenSched& S, int sg) {
 }
 
 struct ScreenParams {
+    const __nv_bfloat16* xblk;  // the BF16 shadow being screened, in 256 x 64 swizzled tiles
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
     const float4* spar;  // per row {mult, b, m, 2^-19 m}: the screen's one-FMA form of the bound
     const int* alpha;    // max over rows of a/b (float bits): |q| a <= |q| alpha b
@@ -331,8 +332,7 @@ struct ScreenParams {
 // bit per row keeps dead, zero and padding rows out of the lower bounds.
 template <int KL, bool NORM>
 __global__ void __launch_bounds__(scr::kThreads, 1)
-    k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
-                  const ScreenParams P) {
+    k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const ScreenParams P) {
     using namespace scr;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -361,7 +361,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
     }
     if (warp == 0 && lane == 0) {
         tma_prefetch_desc(&tmq);
-        tma_prefetch_desc(&tmx);
     }
     if (warp == 1) tmem_alloc(&S.tmem_base, kTmemCols);
     tc_fence_before();
@@ -399,7 +398,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     }
                     mbar_expect_tx(&S.full[stage], kStageA + kStageB);
                     tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * kBK, qt * kBM);
-                    tma_load_2d(S.b[stage], &tmx, &S.full[stage], kb * kBK, r * kBN);
+                    // the store tile: one contiguous 32 KB block, already swizzled
+                    bulk_load(S.b[stage], P.xblk + ((size_t)r * KB + kb) * (kBN * kBK), kStageB, &S.full[stage]);
                     ++issued;
                     if (++stage == kStages) {
                         stage = 0;
@@ -1576,13 +1576,13 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
-    CUtensorMap tmq, tmx;
+    CUtensorMap tmq;
     rc = make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
     const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
-    if (!rc) rc = make_map(gc, &tmx, norm ? s->xbn : s->xb, s->slots, s->ldb, scr::kBN);
     if (rc) return rc;
 
     ScreenParams P;
+    P.xblk = norm ? s->xbn : s->xb;
     P.rpar = rpar;
     P.spar = spar;
     P.alpha = alpha;
@@ -1611,7 +1611,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
             SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
             gc->attr_set[v] = true;
         }
-        kern<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, tmx, P);
+        kern<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, P);
     }
     SVDB_LAUNCH_CHECK();
     ++kernels;

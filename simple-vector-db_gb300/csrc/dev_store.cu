@@ -56,7 +56,6 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     const bool active = gid < nrow;
     const int64_t slot = active ? (list ? list[gid] : lo + gid) : 0;
     const double* x = x64 + slot * ld;
-    __nv_bfloat16* xh = xb + slot * ldb;
     float* xf = x32 + slot * ld;
     double sq = 0.0, bh = 0.0, res = 0.0;
     if (active) {
@@ -70,14 +69,11 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
             bh = fma(fy, fy, bh);
             res = fma(v.x - fx, v.x - fx, res);
             res = fma(v.y - fy, v.y - fy, res);
-            xh[j] = hx;
-            xh[j + 1] = hy;
+            *reinterpret_cast<__nv_bfloat162*>(xb + bf16_tile_index(slot, j, ldb)) = __halves2bfloat162(hx, hy);
             *reinterpret_cast<float2*>(xf + j) = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
         }
-        for (size_t j = ld + 2 * s; j < ldb; j += 8) {  // zero the BF16 tail beyond ld
-            xh[j] = __float2bfloat16(0.0f);
-            xh[j + 1] = __float2bfloat16(0.0f);
-        }
+        for (size_t j = ld + 2 * s; j < ldb; j += 8)  // zero the BF16 tail beyond ld
+            *reinterpret_cast<__nv_bfloat162*>(xb + bf16_tile_index(slot, j, ldb)) = __floats2bfloat162_rn(0.f, 0.f);
     }
     sq = group4_sum(sq);
     bh = group4_sum(bh);
@@ -86,7 +82,6 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     double nbh = 0.0, nres = 0.0;
     if (active) {
         const double ixn = sq > 0.0 ? 1.0 / sqrt(sq) : 0.0;
-        __nv_bfloat16* xn = xbn + slot * ldb;
         for (size_t j = 2 * s; j < ld; j += 8) {
             const double2 v = *reinterpret_cast<const double2*>(x + j);
             const double ux = v.x * ixn, uy = v.y * ixn;
@@ -96,13 +91,10 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
             nbh = fma(fy, fy, nbh);
             nres = fma(ux - fx, ux - fx, nres);
             nres = fma(uy - fy, uy - fy, nres);
-            xn[j] = hx;
-            xn[j + 1] = hy;
+            *reinterpret_cast<__nv_bfloat162*>(xbn + bf16_tile_index(slot, j, ldb)) = __halves2bfloat162(hx, hy);
         }
-        for (size_t j = ld + 2 * s; j < ldb; j += 8) {
-            xn[j] = __float2bfloat16(0.0f);
-            xn[j + 1] = __float2bfloat16(0.0f);
-        }
+        for (size_t j = ld + 2 * s; j < ldb; j += 8)
+            *reinterpret_cast<__nv_bfloat162*>(xbn + bf16_tile_index(slot, j, ldb)) = __floats2bfloat162_rn(0.f, 0.f);
     }
     nbh = group4_sum(nbh);
     nres = group4_sum(nres);
@@ -435,11 +427,15 @@ int Store::grow(size_t need) {
         svdb_set_error("device store: cannot grow to %zu rows of dim %zu: %s", nc, dim, cudaGetErrorString(e));
         return SVDB_ENOMEM;
     }
+    // BF16 shadows: whole 256-row tiles; rows never written stay zero
+    SVDB_CUDA(cudaMemsetAsync(nb, 0, nc * ldb * sizeof(__nv_bfloat16), stream));
+    SVDB_CUDA(cudaMemsetAsync(nbn, 0, nc * ldb * sizeof(__nv_bfloat16), stream));
     if (slots) {
+        const size_t tile_rows = round_up(slots, 256);
         SVDB_CUDA(cudaMemcpyAsync(nx, x64, slots * ld * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-        SVDB_CUDA(cudaMemcpyAsync(nb, xb, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nb, xb, tile_rows * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nf, x32, slots * ld * sizeof(float), cudaMemcpyDeviceToDevice, stream));
-        SVDB_CUDA(cudaMemcpyAsync(nbn, xbn, slots * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nbn, xbn, tile_rows * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(npn, rowpn, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsf, sqf, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
