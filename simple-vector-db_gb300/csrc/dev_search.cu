@@ -347,6 +347,17 @@ __global__ void k_fill_empty(int64_t* ids, double* dists, double* err, size_t n)
 
 using namespace svdb;
 
+// Host memory the DMA engines can read directly (cudaHostAlloc'd or registered).
+static bool host_pinned(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
 extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t k, int metric, int precision,
                             int64_t* ids, double* dists, double* err, int on_device, svdb_search_stats* st) {
     Store* s = reinterpret_cast<Store*>(hs);
@@ -378,13 +389,26 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     unsigned char* kscr = outp + obytes;
     const double* qsrc = q;
     s->prof_begin();
+    // host buffers: page-locked ones are read and written by DMA directly,
+    // pageable ones go through the store's pinned staging buffer
+    const bool pin_out = !on_device && host_pinned(ids) && host_pinned(dists) && (!err || host_pinned(err));
     if (!on_device) {
         double* qraw = (double*)(kscr + kbytes);
-        rc = s->pinned_reserve(std::max(nq * s->dim * sizeof(double), out_n * (sizeof(int64_t) + 2 * sizeof(double))));
-        if (rc) return rc;
-        std::memcpy(s->pin, q, nq * s->dim * sizeof(double));
-        SVDB_CUDA(cudaMemcpyAsync(qraw, s->pin, nq * s->dim * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        if (host_pinned(q)) {
+            SVDB_CUDA(cudaMemcpyAsync(qraw, q, nq * s->dim * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        } else {
+            rc = s->pinned_reserve(
+                std::max(nq * s->dim * sizeof(double), out_n * (sizeof(int64_t) + 2 * sizeof(double))));
+            if (rc) return rc;
+            std::memcpy(s->pin, q, nq * s->dim * sizeof(double));
+            SVDB_CUDA(cudaMemcpyAsync(qraw, s->pin, nq * s->dim * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        }
         qsrc = qraw;
+        if (!pin_out) {
+            rc = s->pinned_reserve(
+                std::max(nq * s->dim * sizeof(double), out_n * (sizeof(int64_t) + 2 * sizeof(double))));
+            if (rc) return rc;
+        }
     }
     SearchArgs a;
     a.q = qbuf;
@@ -425,7 +449,16 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     s->prof_end();
     if (rc) return rc;
     if (st) st->kernels += kernels;
-    if (!on_device) {
+    if (!on_device && pin_out && !st) {
+        SVDB_CUDA(cudaMemcpyAsync(ids, a.ids, out_n * sizeof(int64_t), cudaMemcpyDeviceToHost, s->stream));
+        SVDB_CUDA(cudaMemcpyAsync(dists, a.dists, out_n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        if (err) SVDB_CUDA(cudaMemcpyAsync(err, a.err, out_n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        SVDB_CUDA(cudaStreamSynchronize(s->stream));
+        rc = s->check_error();
+        if (rc) return rc;
+    } else if (!on_device) {
+        rc = s->pinned_reserve(std::max(nq * s->dim * sizeof(double), out_n * (sizeof(int64_t) + 2 * sizeof(double))));
+        if (rc) return rc;
         unsigned char* hp = (unsigned char*)s->pin;
         SVDB_CUDA(cudaMemcpyAsync(hp, outp, out_n * (sizeof(int64_t) + 2 * sizeof(double)), cudaMemcpyDeviceToHost,
                                   s->stream));

@@ -303,12 +303,20 @@ class VectorDatabase:
 
     # -- top-k ---------------------------------------------------------------
     def search(self, queries, k: int, metric: int = COSINE, precision: int = PREC_FP64, with_err: bool = False,
-               stats: SearchStats | None = None):
+               stats: SearchStats | None = None, out=None):
+        """Exact top-k (svdb_search_topk).  `out` = (ids, dists) preallocated
+        [nq, k] int64 / float64 arrays; page-locked host buffers (queries and
+        outputs) are read and written by DMA without a staging copy."""
         q = _f64(queries)
         q = q.reshape(-1, q.shape[-1])
         nq = q.shape[0]
-        ids = np.empty((nq, k), np.int64)
-        dists = np.empty((nq, k), np.float64)
+        if out is not None:
+            ids, dists = out
+            assert ids.shape == (nq, k) and dists.shape == (nq, k) and ids.dtype == np.int64
+            assert dists.dtype == np.float64 and ids.flags.c_contiguous and dists.flags.c_contiguous
+        else:
+            ids = np.empty((nq, k), np.int64)
+            dists = np.empty((nq, k), np.float64)
         err = np.empty((nq, k), np.float64) if with_err else None
         _check(lib.svdb_search_topk(self.ptr, q.ctypes.data_as(_dp), nq, q.shape[1], k, metric, precision,
                                     ids.ctypes.data_as(_i64p), dists.ctypes.data_as(_dp),

@@ -240,3 +240,31 @@ def test_topk_rejects_bad_arguments(S):
     with pytest.raises(S.SvdbError):
         db.search(np.ones(8), 1, metric=7)
     db.close()
+
+
+def test_search_host_buffers_pinned_and_pageable(svdb, oracle):
+    """Host-buffer searches give the same answers whether the queries and the
+    result arrays are page-locked (DMA straight to and from them) or pageable
+    (staged through the library's buffer)."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    rng = np.random.default_rng(12)
+    X = rng.normal(size=(5000, 96))
+    Q = rng.normal(size=(70, 96))
+    db = svdb.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    Qp = torch.from_numpy(Q).pin_memory().numpy()
+    for prec in (svdb.PREC_FP64, svdb.PREC_BF16):
+        wid, wval = oracle.topk(1, X, Q, 10)
+        a_ids, a_vals = db.search(Q, 10, 1, prec)
+        ids_h = torch.empty((70, 10), dtype=torch.int64).pin_memory().numpy()
+        dists_h = torch.empty((70, 10), dtype=torch.float64).pin_memory().numpy()
+        for _ in range(2):  # reuse of the same page-locked buffers
+            db.search(Qp, 10, 1, prec, out=(ids_h, dists_h))
+            assert np.array_equal(ids_h, wid) and np.array_equal(dists_h, wval)
+        assert np.array_equal(a_ids, wid) and np.array_equal(a_vals, wval)
+        ids_m, dists_m = np.empty((70, 10), np.int64), np.empty((70, 10))  # pinned queries, pageable results
+        db.search(Qp, 10, 1, prec, out=(ids_m, dists_m))
+        assert np.array_equal(ids_m, wid) and np.array_equal(dists_m, wval)
+    db.close()
