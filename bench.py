@@ -366,10 +366,10 @@ def run_ragged(args, ws, rank, local):
     """Uneven batched multi-collection search: 5 collections (D, N) =
     (64, 2M), (128, 1M), (384, 500k), (768, 200k), (1536, 50k), uniform[-1,1]
     float64 (seed 4); a ragged batch of 8,192 queries split 40/25/15/12/8 %,
-    k per query uniform in [1, 100], cosine.  One step issues each
-    collection's share as one search (k = the share's largest k; each query
-    keeps its own first k) on that collection's stream, all five in flight
-    together."""
+    k per query uniform in [1, 100], cosine.  The batch is one ragged plan
+    (svdb_ragged_*): bound once, autotuned, captured as one CUDA graph; one
+    step is one run of the plan (one graph launch) over all five collections,
+    each query answered with its own k."""
     import torch
     import svdb_gb300 as S
     from svdb_gb300 import workloads as W
@@ -377,33 +377,47 @@ def run_ragged(args, ws, rank, local):
     torch.cuda.set_device(local)
     prec = S.PREC_BF16 if args.precision == "bf16" else S.PREC_FP64
     cols = W.config4(8192)
-    dbs, bufs = [], []
+    dbs, bufs, parts = [], [], []
     for X, Q, ks in cols:
         db = S.VectorDatabase(X.shape[0], 3)
         db.insert_batch(X)
         db.sync()
-        kmax = int(ks.max())
+        stride = int(ks.max())
         qd = torch.from_numpy(Q).cuda()
-        ids = torch.empty((Q.shape[0], kmax), dtype=torch.int64, device="cuda")
-        dd = torch.empty((Q.shape[0], kmax), dtype=torch.float64, device="cuda")
+        ids = torch.empty((Q.shape[0], stride), dtype=torch.int64, device="cuda")
+        dd = torch.empty((Q.shape[0], stride), dtype=torch.float64, device="cuda")
         dbs.append(db)
-        bufs.append((qd, ids, dd, kmax, X.shape[1]))
+        bufs.append((qd, ids, dd))
+        parts.append((db, qd.data_ptr(), Q.shape[0], Q.shape[1], ks, ids.data_ptr(), dd.data_ptr(), stride))
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = S.RaggedPlan(parts, S.COSINE, prec, S.RAGGED_AUTOTUNE)
+    tune_s = time.perf_counter() - t0
+    info = plan.info()
 
-    def step():
-        for db, (qd, ids, dd, kmax, d) in zip(dbs, bufs):
-            db.search_device(qd.data_ptr(), qd.shape[0], d, kmax, 0, prec, ids.data_ptr(), dd.data_ptr())
+    # correctness guard: a few queries of every collection against the device FP64 scan
+    plan.run()
+    plan.wait()
+    for (X, Q, ks), db, (_, ids, dd) in zip(cols, dbs, bufs):
+        for i in (0, Q.shape[0] // 2, Q.shape[0] - 1):
+            k = int(ks[i])
+            ref_ids, _ = db.search(Q[i:i + 1], k, S.COSINE, S.PREC_FP64)
+            if not np.array_equal(ids[i, :k].cpu().numpy(), ref_ids[0]):
+                raise SystemExit("bench: ragged plan ids differ from the FP64 scan")
 
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.ExternalStream(plan.stream())
     for _ in range(args.warmup):
-        step()
-    for db in dbs:
-        db.wait()
-    t = time.perf_counter()
+        plan.run()
+    plan.wait()
+    clk = Clocks(local)
+    ev0.record(stream)
     for _ in range(args.steps):
-        step()
-    for db in dbs:
-        db.wait()
-    dt = time.perf_counter() - t
+        plan.run()
+    ev1.record(stream)
+    plan.wait()
+    clocks = clk.stop()
+    dt = ev0.elapsed_time(ev1) / 1e3
     nq = sum(b[0].shape[0] for b in bufs)
     line = {"metric": "exact top-k queries/s, ragged batch over 5 collections (k in [1,100])",
             "value": nq * args.steps / dt, "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
@@ -412,8 +426,16 @@ def run_ragged(args, ws, rank, local):
             "data": "synthetic",
             "config": {"workload": "5 collections (D,N) = (64,2M) (128,1M) (384,500k) (768,200k) (1536,50k), "
                                    "uniform[-1,1] seed 4, 8192 queries split 40/25/15/12/8 %, k ~ U[1,100], cosine",
-                       "precision": args.precision}}
+                       "precision": args.precision, "l2": "stores (5.4 GB FP64) larger than L2; no flush needed"},
+            "plan": {"grouping": info["grouping"], "concurrent": info["concurrent"], "graph": info["graph"],
+                     "searches_per_run": info["searches"], "graph_launches_per_step": 1,
+                     "autotune_ms_per_run": {"(grouping 0, concurrent 1)": info["tuned_ms"][0],
+                                             "(1, 1)": info["tuned_ms"][1], "(0, 0)": info["tuned_ms"][2],
+                                             "(1, 0)": info["tuned_ms"][3]},
+                     "autotune_s": tune_s, "captures": info["captures"]},
+            "clocks": clocks}
     print(json.dumps(line), flush=True)
+    plan.close()
     for db in dbs:
         db.close()
 

@@ -127,6 +127,62 @@ int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t 
 int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_queries, size_t nq, size_t dim, size_t k,
                                   int metric, int64_t* d_ids, double* d_dists);
 
+/* ---- ragged batches over several collections -----------------------------
+ *
+ * No reference counterpart (the reference serves one collection, one query
+ * per request).  A plan binds one uneven batch of top-k queries over several
+ * stores, possibly of different dimensions, each query with its own k; one
+ * svdb_ragged_run answers all of it with one CUDA graph launch.  Per part:
+ * the store, nq queries (DEVICE, nq x dim, row-major), the k of each query
+ * (HOST, nq values in 1..128, read at creation), and DEVICE outputs of nq x
+ * stride (stride >= every k of the part): ids[i*stride + j] and
+ * dists[i*stride + j] are exactly what svdb_search_topk_device gives for
+ * query i with its own k, and -1 / NaN for j >= that k.
+ *
+ * The buffers are bound at creation: a run reads the queries' current
+ * contents and overwrites the outputs (creation itself runs the plan, several
+ * times with SVDB_RAGGED_AUTOTUNE).  Stores may change between runs (pending
+ * mutations are applied at the start of a run, and a change the captured
+ * graph depends on makes the run capture it again).  A run is queued on
+ * svdb_ragged_stream and returns without waiting; later calls on the same
+ * stores are ordered after it.  Destroy a plan before its stores.
+ */
+typedef struct svdb_ragged_part {
+    VectorDatabase* db;
+    size_t nq;
+    size_t dim;               /* must equal the store's dimension */
+    const double* d_queries;  /* device, nq x dim */
+    const uint32_t* k;        /* host, nq entries */
+    int64_t* d_ids;           /* device, nq x stride */
+    double* d_dists;          /* device, nq x stride */
+    size_t stride;
+} svdb_ragged_part;
+
+#define SVDB_RAGGED_AUTOTUNE 1u /* time every execution choice on these inputs, keep the fastest */
+#define SVDB_RAGGED_NO_GRAPH 2u /* enqueue the kernels directly at each run (no graph) */
+
+typedef struct svdb_ragged_info {
+    int32_t grouping;   /* 0: one search per part with its largest k; 1: one per k class (<=16, <=32, <=128) */
+    int32_t concurrent; /* 1: different stores' searches run at the same time; 0: one after another */
+    int32_t graph;      /* 1: runs replay a captured CUDA graph */
+    int32_t searches;   /* searches per run */
+    float tuned_ms[4];  /* autotuner's ms per run of (grouping, concurrent) = (0,1) (1,1) (0,0) (1,0); 0: not tried */
+    uint32_t captures;  /* graph captures so far */
+    uint32_t reserved;
+} svdb_ragged_info;
+
+typedef struct svdb_ragged svdb_ragged;
+/* NULL on failure (message in svdb_last_error) */
+svdb_ragged* svdb_ragged_create(const svdb_ragged_part* parts, size_t nparts, int metric, int precision,
+                                unsigned flags);
+int svdb_ragged_run(svdb_ragged* plan);
+/* block until the plan's last run is done; SVDB_ETIMEOUT if a kernel's bounded wait ran out */
+int svdb_ragged_wait(svdb_ragged* plan);
+/* the CUDA stream (cudaStream_t) runs are queued on */
+void* svdb_ragged_stream(svdb_ragged* plan);
+int svdb_ragged_get_info(svdb_ragged* plan, svdb_ragged_info* info);
+void svdb_ragged_destroy(svdb_ragged* plan);
+
 /* ---- serving: batches of mixed requests on a device-resident store -------
  *
  * A server store keeps its rows only in HBM (no host copies, no KD tree): the

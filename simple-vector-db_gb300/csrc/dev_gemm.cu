@@ -65,8 +65,9 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitim
 constexpr int kCapMin = 8192, kCapMax = 65536;   // candidates kept per query (adaptive)
 constexpr int kSubMin = 4096;                     // slots per sub-list when the budget allows
 constexpr int kMaxSub = 512;                      // sub-lists per query: 2 per segment of its query tile
+constexpr int kWarmUnits = kBN / 2 / kChunk;       // chunks one epilogue thread publishes in a warm-up
 constexpr int kSurvCap = 8192;                    // survivors re-ranked per query
-constexpr size_t kCandBudget = size_t(4) << 30;   // bytes of candidate lists per search (HBM is plentiful)
+constexpr size_t kCandBudget = size_t(16) << 30;  // bytes of candidate lists per search (HBM is plentiful)
 constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key and m, per unit of m
 // flags
 constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4;
@@ -297,6 +298,7 @@ struct ScreenSeg {
 struct ScreenSched {
     ScreenSeg seg[kMaxCtas][kMaxSeg];
     uint8_t nseg[kMaxCtas];
+    uint16_t nsq[kMaxCtas];  // segments of query tile qt (the `sub` values 0..nsq-1)
     int direct;  // 1: no table; CTA i takes query tile i against every store tile
     int ntr;
 };
@@ -490,6 +492,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         }
         TopL<KL> top;
         top.init(valid ? P.k : 0);  // invalid queries: threshold +inf, never emit, never push
+        const int nsq = P.sched.direct ? 1 : (int)P.sched.nsq[seg.qt];
         float tau_c = -INFINITY, published = -INFINITY;
         // this thread's own sub-list of the query's candidates: emission needs no
         // atomic, the count stays in a register and is stored once at the end
@@ -519,8 +522,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 // Warm-up on the segment's first tile, before anything is emitted: fold the
                 // lower bound of every row into the running k best (rows, not chunk
                 // maxima, so k values exist after one tile) and publish the chunk
-                // maxima to the bins.  The emitting pass below then skips its pushes
-                // for this tile, so no row is counted twice.
+                // maxima to the bins (unit = the chunk's place among the warm-up
+                // chunks of the query tile's segments, so segments fill disjoint
+                // bins).  The emitting pass below then skips its pushes and its bin
+                // update for this tile, so no row is counted twice.
 #pragma unroll 1
                 for (int c = 0; c < kBN / 2 / kChunk; ++c) {
                     uint32_t v[kChunk];
@@ -549,10 +554,9 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                             if (valid && l > top.mn) top.push(l);
                         }
                     }
-                    if (valid && maxl > -INFINITY) {
-                        const int chunk = (row0 + c * kChunk) / kChunk;
-                        atomicMax(&P.bins[(size_t)q * P.k + chunk % P.k], f2ord(maxl));
-                    }
+                    if (valid && maxl > -INFINITY)
+                        atomicMax(&P.bins[(size_t)q * P.k + ((2 * seg.sub + half) * kWarmUnits + c) % P.k],
+                                  f2ord(maxl));
                 }
             }
             if (valid && (js < 8 || (js & 7) == 0)) {
@@ -651,10 +655,19 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 }
             }
             // Running threshold: the k-th best of per-tile maxima (distinct tiles
-            // are distinct rows, so it never exceeds the k-th best lower bound);
-            // the bins take the same maxima, bin = tile half mod k.
+            // are distinct rows, so it never exceeds the k-th best lower bound).
+            // The bins take the same maxima, one unit (tile half) per bin.  Units
+            // are numbered round by round over the query tile's segments, after
+            // the warm-up's chunks (unit_id below), so the bins fill after about
+            // k / (2 x segments) tiles of every segment whatever the segments'
+            // offsets; the warm-up tile's rows are already in the bins as chunks
+            // and are not published a second time (a row in two bins would make
+            // their minimum exceed the k-th best lower bound).
             const float maxl = __fsub_rd(tmax, eq0);
-            if (valid && maxl > thr) atomicMax(&P.bins[(size_t)q * P.k + (r * 2 + half) % P.k], f2ord(maxl));
+            if (valid && js > 0 && maxl > thr) {
+                const int unit = 2 * kWarmUnits * nsq + (js - 1) * 2 * nsq + 2 * seg.sub + half;
+                atomicMax(&P.bins[(size_t)q * P.k + unit % P.k], f2ord(maxl));
+            }
             if (valid && js > 0 && maxl > top.mn) top.push(maxl);
             tc_fence_before();
             __syncwarp();
@@ -1469,6 +1482,7 @@ static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub) {
                 S.seg[c][S.nseg[c]++] = ScreenSeg{(int)((int64_t)g * ntr / base), (int)((int64_t)(g + 1) * ntr / base),
                                                   (uint16_t)qt, (uint16_t)ord[qt]++};
     }
+    for (int qt = 0; qt < ntq; ++qt) S.nsq[qt] = (uint16_t)std::max(1, ord[qt]);
     *maxsub = std::max(1, *std::max_element(ord.begin(), ord.end()));
     return c;
 }

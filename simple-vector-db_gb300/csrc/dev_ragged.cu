@@ -1,0 +1,441 @@
+// dev_ragged.cu -- one ragged batch of top-k queries over several stores of
+// different dimensions, replayed as one CUDA graph.
+//
+// A plan binds, per part, a store, its queries (device, nq x dim), a k per
+// query (1..128) and the output buffers (device, nq x stride).  One run
+// answers every part: the part's queries are searched on its store's stream
+// (the same BF16 screen + certified re-rank or FP64 scan as a single search),
+// and the results are scattered into the caller's layout, entries past a
+// query's own k set to -1 / NaN.  The whole run is captured once into a CUDA
+// graph and replayed with one launch; it is captured again when a store
+// changes in a way the graph bakes in (the store's epoch).
+//
+// Two choices change the speed but not the results, and the autotuner times
+// every combination on the plan's own inputs at creation:
+//   grouping   0: one search per part, k = the part's largest k;
+//              1: one search per k class (k <= 16, <= 32, <= 128: the screen's
+//                 register-resident running top-k, and the bins-only form),
+//                 so small-k queries do not pay for the part's largest k;
+//   concurrent 1: the parts of different stores run on their stores' streams
+//                 at the same time (a screen fills the SMs another part's
+//                 screen leaves idle at its tail); 0: one part after another.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "dev_store.cuh"
+
+namespace svdb {
+
+// queries of one k class, gathered from the part's buffer (rows idx[i])
+__global__ void k_ragged_gather(const double* __restrict__ src, size_t dim, const int* __restrict__ idx, int n,
+                                double* __restrict__ dst) {
+    const size_t total = (size_t)n * dim;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = t / dim, e = t - i * dim;
+        dst[t] = src[(size_t)idx[i] * dim + e];
+    }
+}
+
+// results of one search (n x kg, best first) -> the caller's rows idx[i] (or
+// i) of stride `stride`; entries at or past the query's own k are -1 / NaN
+__global__ void k_ragged_scatter(const int64_t* __restrict__ gids, const double* __restrict__ gd, int kg,
+                                 const int* __restrict__ idx, int n, const uint32_t* __restrict__ kq, size_t stride,
+                                 int64_t* __restrict__ ids, double* __restrict__ dists) {
+    const size_t total = (size_t)n * stride;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = t / stride, j = t - i * stride;
+        const size_t q = idx ? (size_t)idx[i] : i;
+        const bool keep = j < (size_t)kq[q] && j < (size_t)kg;
+        ids[q * stride + j] = keep ? gids[i * kg + j] : -1;
+        dists[q * stride + j] = keep ? gd[i * kg + j] : __longlong_as_double(0x7ff8000000000000ll);
+    }
+}
+
+namespace {
+
+struct Part {
+    Store* s = nullptr;
+    size_t nq = 0, stride = 0;
+    const double* q = nullptr;
+    int64_t* ids = nullptr;
+    double* dists = nullptr;
+    std::vector<uint32_t> hk;
+    uint32_t* d_k = nullptr;
+};
+
+// one search of a run: `n` queries of part `part` with k = kg
+struct Group {
+    int part = 0, n = 0, kg = 0;
+    int* d_idx = nullptr;   // rows of the part (nullptr: all of them, in order)
+    double* d_q = nullptr;  // gathered queries (nullptr: the part's own buffer)
+    int64_t* d_ids = nullptr;
+    double* d_dists = nullptr;
+};
+
+struct Plan {
+    std::vector<Part> parts;
+    std::vector<Store*> stores;  // distinct, in first-use order
+    int metric = 0, precision = 0;
+    bool graph_on = true;
+    int grouping = 0, concurrent = 1;
+    std::vector<Group> groups;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_done = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
+    std::vector<cudaEvent_t> ev_store;  // per store: its part of a run is done / its earlier work is done
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> epochs;
+    float tuned_ms[4] = {0, 0, 0, 0};
+    uint32_t captures = 0;
+};
+
+int k_class(uint32_t k) { return k <= 16 ? 0 : (k <= 32 ? 1 : 2); }
+
+void free_groups(Plan* p) {
+    for (Group& g : p->groups) {
+        cudaFree(g.d_idx);
+        cudaFree(g.d_q);
+        cudaFree(g.d_ids);
+        cudaFree(g.d_dists);
+    }
+    p->groups.clear();
+}
+
+void drop_graph(Plan* p) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->exec = nullptr;
+    p->graph = nullptr;
+}
+
+// the searches of a run for the current grouping, with their device buffers
+int make_groups(Plan* p) {
+    free_groups(p);
+    for (size_t pi = 0; pi < p->parts.size(); ++pi) {
+        const Part& P = p->parts[pi];
+        if (P.nq == 0) continue;
+        std::vector<std::vector<int>> cls(p->grouping ? 3 : 1);
+        for (size_t i = 0; i < P.nq; ++i) cls[p->grouping ? k_class(P.hk[i]) : 0].push_back((int)i);
+        for (auto& rows : cls) {
+            if (rows.empty()) continue;
+            Group g;
+            g.part = (int)pi;
+            g.n = (int)rows.size();
+            uint32_t kg = 0;
+            for (int r : rows) kg = std::max(kg, P.hk[r]);
+            g.kg = (int)kg;
+            const bool all = rows.size() == P.nq;  // the whole part, in order: no gather
+            cudaError_t e = cudaSuccess;
+            if (!all) {
+                e = cudaMalloc(&g.d_idx, rows.size() * sizeof(int));
+                if (e == cudaSuccess) e = cudaMalloc(&g.d_q, rows.size() * P.s->dim * sizeof(double));
+                if (e == cudaSuccess)
+                    e = cudaMemcpy(g.d_idx, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice);
+            }
+            if (e == cudaSuccess) e = cudaMalloc(&g.d_ids, rows.size() * kg * sizeof(int64_t));
+            if (e == cudaSuccess) e = cudaMalloc(&g.d_dists, rows.size() * kg * sizeof(double));
+            p->groups.push_back(g);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                svdb_set_error("ragged plan: cannot allocate group buffers: %s", cudaGetErrorString(e));
+                return e == cudaErrorMemoryAllocation ? SVDB_ENOMEM : SVDB_ECUDA;
+            }
+        }
+    }
+    return SVDB_OK;
+}
+
+// the searches of one part's store, on that store's stream
+int enqueue_store(Plan* p, Store* s) {
+    for (const Group& g : p->groups) {
+        const Part& P = p->parts[g.part];
+        if (P.s != s) continue;
+        const double* q = P.q;
+        if (g.d_idx) {
+            const size_t total = (size_t)g.n * s->dim;
+            k_ragged_gather<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s->stream>>>(
+                P.q, s->dim, g.d_idx, g.n, g.d_q);
+            SVDB_LAUNCH_CHECK();
+            q = g.d_q;
+        }
+        int rc = svdbd_search(reinterpret_cast<svdbd_store*>(s), q, (size_t)g.n, (size_t)g.kg, p->metric,
+                              p->precision, g.d_ids, g.d_dists, nullptr, 1, nullptr);
+        if (rc) return rc;
+        const size_t total = (size_t)g.n * P.stride;
+        k_ragged_scatter<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s->stream>>>(
+            g.d_ids, g.d_dists, g.kg, g.d_idx, g.n, P.d_k, P.stride, P.ids, P.dists);
+        SVDB_LAUNCH_CHECK();
+    }
+    return SVDB_OK;
+}
+
+// one run, forked from and joined back to the origin stream (captured or not)
+int enqueue(Plan* p) {
+    SVDB_CUDA(cudaEventRecord(p->ev_fork, p->origin));
+    cudaEvent_t prev = p->ev_fork;
+    for (size_t i = 0; i < p->stores.size(); ++i) {
+        Store* s = p->stores[i];
+        SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->concurrent ? p->ev_fork : prev, 0));
+        int rc = enqueue_store(p, s);
+        if (rc) return rc;
+        SVDB_CUDA(cudaEventRecord(p->ev_store[i], s->stream));
+        prev = p->ev_store[i];
+    }
+    for (size_t i = 0; i < p->stores.size(); ++i) SVDB_CUDA(cudaStreamWaitEvent(p->origin, p->ev_store[i], 0));
+    return SVDB_OK;
+}
+
+bool epochs_current(const Plan* p) {
+    if (p->epochs.size() != p->stores.size()) return false;
+    for (size_t i = 0; i < p->stores.size(); ++i)
+        if (p->stores[i]->epoch != p->epochs[i]) return false;
+    return true;
+}
+
+int check_stores(Plan* p) {
+    for (Store* s : p->stores) {
+        int rc = s->check_error();
+        if (rc) return rc;
+    }
+    return SVDB_OK;
+}
+
+// A direct run first (it sizes every store's scratch for this plan and makes
+// the one-time kernel set-up), then the capture of a second run.
+int capture(Plan* p) {
+    drop_graph(p);
+    int rc = enqueue(p);
+    if (rc) return rc;
+    SVDB_CUDA(cudaStreamSynchronize(p->origin));
+    rc = check_stores(p);
+    if (rc) return rc;
+    p->epochs.clear();
+    for (Store* s : p->stores) p->epochs.push_back(s->epoch);
+    std::vector<char> prof(p->stores.size());
+    for (size_t i = 0; i < p->stores.size(); ++i) {  // stage timing is not recorded inside a graph
+        prof[i] = p->stores[i]->prof;
+        p->stores[i]->prof = false;
+    }
+    SVDB_CUDA(cudaStreamBeginCapture(p->origin, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue(p);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(p->origin, &g);
+    for (size_t i = 0; i < p->stores.size(); ++i) p->stores[i]->prof = prof[i] != 0;
+    if (rc || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (!rc) {
+            svdb_set_error("ragged plan: graph capture failed: %s", cudaGetErrorString(e));
+            rc = SVDB_ECUDA;
+        }
+        return rc;
+    }
+    p->graph = g;
+    SVDB_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
+    if (!epochs_current(p)) {  // nothing may move between the direct run and the capture
+        drop_graph(p);
+        svdb_set_error("ragged plan: a store changed during capture");
+        return SVDB_ECUDA;
+    }
+    ++p->captures;
+    return SVDB_OK;
+}
+
+int run(Plan* p) {
+    for (Store* s : p->stores) {  // pending mutations are applied first (outside any capture)
+        int rc = s->sync();
+        if (rc) return rc;
+    }
+    if (!p->graph_on) return enqueue(p);
+    if (!p->exec || !epochs_current(p)) {
+        int rc = capture(p);
+        if (rc) return rc;
+    }
+    // earlier work on the stores' streams comes first; later work on them
+    // (mutations, searches) waits for this run
+    for (size_t i = 0; i < p->stores.size(); ++i) {
+        SVDB_CUDA(cudaEventRecord(p->ev_store[i], p->stores[i]->stream));
+        SVDB_CUDA(cudaStreamWaitEvent(p->origin, p->ev_store[i], 0));
+    }
+    SVDB_CUDA(cudaGraphLaunch(p->exec, p->origin));
+    SVDB_CUDA(cudaEventRecord(p->ev_done, p->origin));
+    for (Store* s : p->stores) SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->ev_done, 0));
+    return SVDB_OK;
+}
+
+int configure(Plan* p, int grouping, int concurrent) {
+    drop_graph(p);
+    const bool regroup = p->groups.empty() || grouping != p->grouping;
+    p->grouping = grouping;
+    p->concurrent = concurrent;
+    return regroup ? make_groups(p) : SVDB_OK;
+}
+
+// ms per run of the current configuration: one untimed run (capture
+// included), then the best of `reps` timed runs
+int time_config(Plan* p, int reps, float* ms) {
+    int rc = run(p);
+    if (rc) return rc;
+    SVDB_CUDA(cudaStreamSynchronize(p->origin));
+    float best = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+        SVDB_CUDA(cudaEventRecord(p->ev_t0, p->origin));
+        rc = run(p);
+        if (rc) return rc;
+        SVDB_CUDA(cudaEventRecord(p->ev_t1, p->origin));
+        SVDB_CUDA(cudaEventSynchronize(p->ev_t1));
+        float t = 0;
+        SVDB_CUDA(cudaEventElapsedTime(&t, p->ev_t0, p->ev_t1));
+        best = std::min(best, t);
+    }
+    *ms = best;
+    return check_stores(p);
+}
+
+int autotune(Plan* p) {
+    bool mixed = false;  // does any part hold queries of more than one k class?
+    for (const Part& P : p->parts)
+        for (size_t i = 1; i < P.nq && !mixed; ++i) mixed = k_class(P.hk[i]) != k_class(P.hk[0]);
+    const int cfg[4][2] = {{0, 1}, {1, 1}, {0, 0}, {1, 0}};
+    int best = -1;
+    for (int c = 0; c < 4; ++c) {
+        if (cfg[c][0] && !mixed) continue;
+        if (!cfg[c][1] && p->stores.size() < 2) continue;
+        int rc = configure(p, cfg[c][0], cfg[c][1]);
+        if (!rc) rc = time_config(p, 3, &p->tuned_ms[c]);
+        if (rc) return rc;
+        if (best < 0 || p->tuned_ms[c] < p->tuned_ms[best]) best = c;
+    }
+    return configure(p, cfg[best][0], cfg[best][1]);
+}
+
+void destroy(Plan* p) {
+    if (p->origin) cudaStreamSynchronize(p->origin);
+    drop_graph(p);
+    free_groups(p);
+    for (Part& P : p->parts) cudaFree(P.d_k);
+    for (cudaEvent_t e : p->ev_store) cudaEventDestroy(e);
+    for (cudaEvent_t e : {p->ev_fork, p->ev_done, p->ev_t0, p->ev_t1})
+        if (e) cudaEventDestroy(e);
+    if (p->origin) cudaStreamDestroy(p->origin);
+    delete p;
+}
+
+}  // namespace
+}  // namespace svdb
+
+using svdb::Plan;
+using svdb::Store;
+
+extern "C" {
+
+svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts, int metric, int precision,
+                                  unsigned flags) {
+    Plan* p = new (std::nothrow) Plan();
+    if (!p) {
+        svdb_set_error("ragged plan: out of host memory");
+        return nullptr;
+    }
+    p->metric = metric;
+    p->precision = precision;
+    p->graph_on = !(flags & SVDB_RAGGED_NO_GRAPH);
+    int rc = SVDB_OK;
+    auto fail = [&](int code) {
+        (void)code;
+        svdb::destroy(p);
+        return (svdbd_ragged*)nullptr;
+    };
+    for (size_t i = 0; i < nparts; ++i) {
+        Store* s = reinterpret_cast<Store*>(parts[i].store);
+        rc = s->ensure();
+        if (rc) return fail(rc);
+        svdb::Part P;
+        P.s = s;
+        P.nq = parts[i].nq;
+        P.stride = parts[i].stride;
+        P.q = parts[i].d_queries;
+        P.ids = parts[i].d_ids;
+        P.dists = parts[i].d_dists;
+        P.hk.assign(parts[i].k, parts[i].k + parts[i].nq);
+        if (P.nq) {
+            cudaError_t e = cudaMalloc(&P.d_k, P.nq * sizeof(uint32_t));
+            if (e == cudaSuccess) e = cudaMemcpy(P.d_k, P.hk.data(), P.nq * sizeof(uint32_t), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                svdb_set_error("ragged plan: cannot allocate per-query k: %s", cudaGetErrorString(e));
+                p->parts.push_back(P);
+                return fail(SVDB_ENOMEM);
+            }
+        }
+        p->parts.push_back(P);
+        if (std::find(p->stores.begin(), p->stores.end(), s) == p->stores.end()) p->stores.push_back(s);
+    }
+    // stores with more work first: in the one-after-another order the longest
+    // work starts first (rows x padded dimension x queries)
+    {
+        std::vector<std::pair<double, Store*>> w;
+        for (Store* s : p->stores) {
+            double q = 0;
+            for (const svdb::Part& P : p->parts)
+                if (P.s == s) q += (double)P.nq;
+            w.push_back({-(double)s->slots * (double)s->ldb * q, s});
+        }
+        std::stable_sort(w.begin(), w.end(),
+                         [](const std::pair<double, Store*>& a, const std::pair<double, Store*>& b) { return a.first < b.first; });
+        for (size_t i = 0; i < w.size(); ++i) p->stores[i] = w[i].second;
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&p->origin, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->ev_t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->ev_t1);
+    for (size_t i = 0; i < p->stores.size() && e == cudaSuccess; ++i) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) p->ev_store.push_back(ev);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        svdb_set_error("ragged plan: cannot create streams/events: %s", cudaGetErrorString(e));
+        return fail(SVDB_ECUDA);
+    }
+    for (Store* s : p->stores) {
+        rc = s->sync();
+        if (rc) return fail(rc);
+    }
+    rc = (flags & SVDB_RAGGED_AUTOTUNE) ? svdb::autotune(p) : svdb::configure(p, 0, 1);
+    if (rc) return fail(rc);
+    return reinterpret_cast<svdbd_ragged*>(p);
+}
+
+int svdbd_ragged_run(svdbd_ragged* hp) { return svdb::run(reinterpret_cast<Plan*>(hp)); }
+
+int svdbd_ragged_wait(svdbd_ragged* hp) {
+    Plan* p = reinterpret_cast<Plan*>(hp);
+    SVDB_CUDA(cudaStreamSynchronize(p->origin));
+    return svdb::check_stores(p);
+}
+
+void* svdbd_ragged_stream(svdbd_ragged* hp) { return reinterpret_cast<Plan*>(hp)->origin; }
+
+int svdbd_ragged_info(svdbd_ragged* hp, svdb_ragged_info* out) {
+    Plan* p = reinterpret_cast<Plan*>(hp);
+    std::memset(out, 0, sizeof(*out));
+    out->grouping = p->grouping;
+    out->concurrent = p->concurrent;
+    out->graph = p->graph_on ? 1 : 0;
+    out->searches = (int32_t)p->groups.size();
+    for (int i = 0; i < 4; ++i) out->tuned_ms[i] = p->tuned_ms[i];
+    out->captures = p->captures;
+    return SVDB_OK;
+}
+
+void svdbd_ragged_destroy(svdbd_ragged* hp) {
+    if (hp) svdb::destroy(reinterpret_cast<Plan*>(hp));
+}
+
+}  // extern "C"

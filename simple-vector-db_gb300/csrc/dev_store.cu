@@ -467,6 +467,7 @@ int Store::grow(size_t need) {
     logical = nlog;
     mapblk = nblk;
     cap = nc;
+    ++epoch;
     return SVDB_OK;
 }
 
@@ -486,6 +487,7 @@ int Store::scratch_reserve(size_t bytes) {
         return SVDB_ENOMEM;
     }
     scratch_bytes = nb;
+    ++epoch;
     return SVDB_OK;
 }
 
@@ -515,6 +517,7 @@ int Store::scratch2_reserve(size_t bytes) {
         return SVDB_ENOMEM;
     }
     scratch2_bytes = nb;
+    ++epoch;
     return SVDB_OK;
 }
 
@@ -548,6 +551,7 @@ int Store::flush() {
     SVDB_CUDA(cudaMemcpyAsync(live + first, stage_live.data(), n, cudaMemcpyHostToDevice, stream));
     SVDB_CUDA(cudaStreamSynchronize(stream));  // stage_live is pageable and cleared below
     slots += n;
+    ++epoch;
     stage.clear();
     stage_live.clear();
     stage_rows = 0;
@@ -603,6 +607,7 @@ int Store::sync() {
         nlive = (size_t)h_nlive;
         n_unscreen = hc;
         map_dirty = false;
+        ++epoch;
     } else if (!slots) {
         nlive = 0;
         map_dirty = false;
@@ -723,6 +728,7 @@ int svdbd_store_append_block(svdbd_store* hs, const double* rows, size_t n) {
     }
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     s->slots += n;
+    ++s->epoch;
     if (s->derive_lo < 0 || (int64_t)first < s->derive_lo) s->derive_lo = (int64_t)first;
     s->derive_hi = (int64_t)s->slots;
     s->map_dirty = true;

@@ -64,6 +64,12 @@ struct Store {
 
     GemmPlanCache* gemm = nullptr;
 
+    // Bumped whenever something a captured CUDA graph bakes in changes: an
+    // array moves (growth, scratch reallocation), the slot count, the live
+    // count or the unscreenable count changes.  A ragged plan compares it
+    // with the value at capture time and captures again when it differs.
+    uint64_t epoch = 0;
+
     // stage timing (svdb_profile): a ring of per-search event sets, resolved
     // lazily so profiling adds no host synchronisation to a search
     static constexpr int kProfRing = 64;

@@ -307,6 +307,143 @@ SVDB_API int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_q
     return rc;
 }
 
+/* ---- ragged batches over several collections ---------------------------- */
+struct svdb_ragged {
+    svdbd_ragged* dev;
+    VectorDatabase** dbs; /* distinct, in address order (the order their locks are taken) */
+    size_t ndb;
+};
+
+static int db_addr_cmp(const void* a, const void* b) {
+    const uintptr_t x = (uintptr_t) * (VectorDatabase* const*)a, y = (uintptr_t) * (VectorDatabase* const*)b;
+    return x < y ? -1 : (x > y);
+}
+
+static void ragged_lock(svdb_ragged* r, int lock) {
+    for (size_t i = 0; i < r->ndb; ++i) {
+        if (lock)
+            pthread_mutex_lock(&r->dbs[i]->mutex);
+        else
+            pthread_mutex_unlock(&r->dbs[r->ndb - 1 - i]->mutex);
+    }
+}
+
+SVDB_API svdb_ragged* svdb_ragged_create(const svdb_ragged_part* parts, size_t nparts, int metric, int precision,
+                                         unsigned flags) {
+    if (!parts || nparts == 0 || metric < 0 || metric > 2 ||
+        (precision != SVDB_PREC_FP64 && precision != SVDB_PREC_BF16)) {
+        svdb_set_error("svdb_ragged_create: bad argument (parts, metric or precision)");
+        return NULL;
+    }
+    svdb_ragged* r = (svdb_ragged*)calloc(1, sizeof(svdb_ragged));
+    svdbd_ragged_part* dp = (svdbd_ragged_part*)calloc(nparts, sizeof(svdbd_ragged_part));
+    if (r) r->dbs = (VectorDatabase**)calloc(nparts, sizeof(VectorDatabase*));
+    if (!r || !dp || !r->dbs) {
+        svdb_set_error("svdb_ragged_create: out of host memory");
+        if (r) free(r->dbs);
+        free(r);
+        free(dp);
+        return NULL;
+    }
+    for (size_t i = 0; i < nparts; ++i) {
+        const svdb_ragged_part* p = &parts[i];
+        if (!p->db || (p->nq && (!p->d_queries || !p->k || !p->d_ids || !p->d_dists))) {
+            svdb_set_error("svdb_ragged_create: part %zu: NULL argument", i);
+            goto fail;
+        }
+        size_t j = 0;
+        while (j < r->ndb && r->dbs[j] != p->db) ++j;
+        if (j == r->ndb) r->dbs[r->ndb++] = p->db;
+    }
+    qsort(r->dbs, r->ndb, sizeof(VectorDatabase*), db_addr_cmp);
+    ragged_lock(r, 1);
+    for (size_t i = 0; i < nparts; ++i) {
+        const svdb_ragged_part* p = &parts[i];
+        svdb_db* d = svdb_of(p->db);
+        if (!d->dev) {
+            svdb_set_error("svdb_ragged_create: part %zu: the store holds no rows", i);
+            break;
+        }
+        if (p->dim != d->dim) {
+            svdb_set_error("svdb_ragged_create: part %zu: query dimension %zu != store dimension %zu", i, p->dim,
+                           d->dim);
+            break;
+        }
+        size_t bad = p->nq;
+        for (size_t q = 0; q < p->nq && bad == p->nq; ++q)
+            if (p->k[q] == 0 || p->k[q] > 128 || p->k[q] > p->stride) bad = q;
+        if (bad != p->nq) {
+            svdb_set_error("svdb_ragged_create: part %zu query %zu: k = %u (must be 1..128 and <= stride %zu)", i,
+                           bad, p->k[bad], p->stride);
+            break;
+        }
+        dp[i].store = d->dev;
+        dp[i].nq = p->nq;
+        dp[i].stride = p->stride;
+        dp[i].d_queries = p->d_queries;
+        dp[i].k = p->k;
+        dp[i].d_ids = p->d_ids;
+        dp[i].d_dists = p->d_dists;
+    }
+    if (!dp[nparts - 1].store && parts[nparts - 1].db) {
+        /* a part failed validation above (message already set) */
+    } else {
+        size_t ok = 0;
+        while (ok < nparts && dp[ok].store) ++ok;
+        if (ok == nparts) r->dev = svdbd_ragged_create(dp, nparts, metric, precision, flags);
+    }
+    ragged_lock(r, 0);
+    if (!r->dev) goto fail;
+    free(dp);
+    return r;
+fail:
+    free(dp);
+    free(r->dbs);
+    free(r);
+    return NULL;
+}
+
+SVDB_API int svdb_ragged_run(svdb_ragged* r) {
+    if (!r) {
+        svdb_set_error("svdb_ragged_run: NULL plan");
+        return SVDB_EINVAL;
+    }
+    ragged_lock(r, 1);
+    int rc = svdbd_ragged_run(r->dev);
+    ragged_lock(r, 0);
+    return rc;
+}
+
+SVDB_API int svdb_ragged_wait(svdb_ragged* r) {
+    if (!r) {
+        svdb_set_error("svdb_ragged_wait: NULL plan");
+        return SVDB_EINVAL;
+    }
+    ragged_lock(r, 1);
+    int rc = svdbd_ragged_wait(r->dev);
+    ragged_lock(r, 0);
+    return rc;
+}
+
+SVDB_API void* svdb_ragged_stream(svdb_ragged* r) { return r ? svdbd_ragged_stream(r->dev) : NULL; }
+
+SVDB_API int svdb_ragged_get_info(svdb_ragged* r, svdb_ragged_info* info) {
+    if (!r || !info) {
+        svdb_set_error("svdb_ragged_get_info: NULL argument");
+        return SVDB_EINVAL;
+    }
+    return svdbd_ragged_info(r->dev, info);
+}
+
+SVDB_API void svdb_ragged_destroy(svdb_ragged* r) {
+    if (!r) return;
+    ragged_lock(r, 1);
+    svdbd_ragged_destroy(r->dev);
+    ragged_lock(r, 0);
+    free(r->dbs);
+    free(r);
+}
+
 SVDB_API int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, uint32_t* gave_up) {
     if (!db) {
         svdb_set_error("svdb_selftest_bounded_wait: NULL database");

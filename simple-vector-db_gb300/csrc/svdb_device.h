@@ -78,6 +78,24 @@ int svdbd_selftest_wait(svdbd_store* s, uint32_t limit_us, uint32_t* gave_up);
 int svdbd_search_noalloc(svdbd_store* s, const double* d_queries, size_t nq, size_t k, int metric, int64_t* d_ids,
                          double* d_dists);
 
+/* ragged batch over several stores, replayed as one CUDA graph (dev_ragged.cu) */
+typedef struct svdbd_ragged svdbd_ragged;
+typedef struct svdbd_ragged_part {
+    svdbd_store* store;
+    size_t nq, stride;
+    const double* d_queries; /* nq x dim, device */
+    const uint32_t* k;       /* host, nq entries (1..128) */
+    int64_t* d_ids;          /* nq x stride, device */
+    double* d_dists;
+} svdbd_ragged_part;
+svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts, int metric, int precision,
+                                  unsigned flags);
+int svdbd_ragged_run(svdbd_ragged* p);
+int svdbd_ragged_wait(svdbd_ragged* p);
+void* svdbd_ragged_stream(svdbd_ragged* p);
+int svdbd_ragged_info(svdbd_ragged* p, svdb_ragged_info* out);
+void svdbd_ragged_destroy(svdbd_ragged* p);
+
 /* ---- KD tree mirror ------------------------------------------------------ */
 svdbd_kd* svdbd_kd_create(size_t kdim);
 void svdbd_kd_destroy(svdbd_kd* t);

@@ -53,6 +53,22 @@ class SearchStats(C.Structure):
                 ("reserved", C.c_uint32), ("max_err_bound", C.c_double)]
 
 
+class RaggedPart(C.Structure):
+    """svdb_ragged_part (include/svdb_gb300.h)."""
+    _fields_ = [("db", C.c_void_p), ("nq", C.c_size_t), ("dim", C.c_size_t), ("d_queries", C.c_void_p),
+                ("k", C.POINTER(C.c_uint32)), ("d_ids", C.c_void_p), ("d_dists", C.c_void_p),
+                ("stride", C.c_size_t)]
+
+
+class RaggedInfo(C.Structure):
+    """svdb_ragged_info (include/svdb_gb300.h)."""
+    _fields_ = [("grouping", C.c_int32), ("concurrent", C.c_int32), ("graph", C.c_int32), ("searches", C.c_int32),
+                ("tuned_ms", C.c_float * 4), ("captures", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+RAGGED_AUTOTUNE, RAGGED_NO_GRAPH = 1, 2
+
+
 class SvdbError(RuntimeError):
     pass
 
@@ -103,6 +119,12 @@ def _load():
         "svdb_merge_topk": (C.c_int, [C.c_int, _i64p, _dp, sz, sz, sz, _i64p, _dp]),
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
+        "svdb_ragged_create": (vp, [C.POINTER(RaggedPart), sz, C.c_int, C.c_int, C.c_uint]),
+        "svdb_ragged_run": (C.c_int, [vp]),
+        "svdb_ragged_wait": (C.c_int, [vp]),
+        "svdb_ragged_stream": (vp, [vp]),
+        "svdb_ragged_get_info": (C.c_int, [vp, C.POINTER(RaggedInfo)]),
+        "svdb_ragged_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -344,6 +366,55 @@ class VectorDatabase:
         _check(lib.svdb_search_topk_device(self.ptr, q_ptr, nq, dim, k, metric, precision, ids_ptr, dists_ptr,
                                            err_ptr or None, C.byref(stats) if stats is not None else None),
                "svdb_search_topk_device")
+
+
+class RaggedPlan:
+    """svdb_ragged_create / _run / _wait / _destroy: one uneven batch of
+    top-k queries over several stores (different dimensions allowed), each
+    query with its own k, answered by one CUDA-graph launch per run.
+
+    ``parts`` is a list of (db, q_ptr, nq, dim, ks, ids_ptr, dists_ptr,
+    stride): device pointers (torch tensors' data_ptr()), ks a host sequence
+    of nq ints.  The buffers stay bound to the plan."""
+
+    def __init__(self, parts, metric: int, precision: int, flags: int = RAGGED_AUTOTUNE):
+        arr = (RaggedPart * len(parts))()
+        self._ks = []
+        for i, (db, q_ptr, nq, dim, ks, ids_ptr, dists_ptr, stride) in enumerate(parts):
+            k = np.ascontiguousarray(ks, dtype=np.uint32)
+            assert k.shape == (nq,)
+            self._ks.append(k)
+            arr[i] = RaggedPart(db.ptr, nq, dim, q_ptr, k.ctypes.data_as(C.POINTER(C.c_uint32)), ids_ptr,
+                                dists_ptr, stride)
+        self.ptr = lib.svdb_ragged_create(arr, len(parts), metric, precision, flags)
+        if not self.ptr:
+            raise SvdbError(f"svdb_ragged_create failed: {last_error()}")
+
+    def run(self) -> None:
+        _check(lib.svdb_ragged_run(self.ptr), "svdb_ragged_run")
+
+    def wait(self) -> None:
+        _check(lib.svdb_ragged_wait(self.ptr), "svdb_ragged_wait")
+
+    def stream(self) -> int:
+        return lib.svdb_ragged_stream(self.ptr) or 0
+
+    def info(self) -> dict:
+        inf = RaggedInfo()
+        _check(lib.svdb_ragged_get_info(self.ptr, C.byref(inf)), "svdb_ragged_get_info")
+        return {"grouping": inf.grouping, "concurrent": inf.concurrent, "graph": inf.graph,
+                "searches": inf.searches, "tuned_ms": [float(x) for x in inf.tuned_ms], "captures": inf.captures}
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            lib.svdb_ragged_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def merge_topk(metric: int, ids, vals):
