@@ -233,3 +233,28 @@ def test_bf16_grouped_refinement(S, oracle, metric):
         assert np.array_equal(vals, wval), k
         assert st.bound_failures == 0 and st.widened == 0, k
     db.close()
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_bf16_separated_top_rows_in_first_tiles(S, oracle, metric):
+    """Well-separated best rows (gaps far wider than the screen's bound) in the
+    first tile and further on, a small store whose segments are single tiles
+    (every tile is a warm-up tile): the shared running thresholds must never
+    count one row twice, or the second-best row would be cut."""
+    rng = np.random.default_rng(11 + metric)
+    X = rng.normal(size=(5000, 128))
+    q = rng.normal(size=128)
+    X[16] = q
+    X[3000] = 0.9 * q + 0.05 * rng.normal(size=128)
+    X[4900] = 0.8 * q + 0.05 * rng.normal(size=128)
+    Q = np.stack([q, q + 1e-3 * rng.normal(size=128)])
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for k in (2, 3, 5):
+        wid, wval = oracle.topk(metric, X, Q, k)
+        for _ in range(10):
+            ids, vals, st = _search_both(S, db, Q, k, metric)
+            assert np.array_equal(ids, wid), (k, ids, wid)
+            assert np.array_equal(vals, wval)
+            assert st.bound_failures == 0
+    db.close()
