@@ -212,6 +212,8 @@ typedef struct svdb_request {
     uint32_t reserved; /* 0 */
     uint64_t a, b;     /* COMPARE: positions of the two rows; UPDATE, DELETE: a */
     const double* vec; /* NEAREST, INSERT, UPDATE: dim doubles in host memory */
+    const char* uuid;  /* INSERT: the row's uuid (NULL: ""); UPDATE: its new uuid (NULL: unchanged);
+                          a C string of which the first 37 bytes count, as char uuid[37] stores it */
 } svdb_request;
 
 typedef struct svdb_response {
@@ -232,8 +234,28 @@ void svdb_server_destroy(svdb_server* s);
 size_t svdb_server_size(svdb_server* s);
 /* bulk load: append n rows (n x dim, row-major); *first_index = position of the first */
 int svdb_server_insert_block(svdb_server* s, const double* rows, size_t n, size_t* first_index);
+/* bulk load with uuids: uuids is n x 37 bytes (char uuid[37] per row) or NULL */
+int svdb_server_insert_rows(svdb_server* s, const double* rows, const char* uuids, size_t n, size_t* first_index);
 /* GET /vector?index= (src/get_handler.c:88-101): copy row `index` to out[dim] */
 int svdb_server_read(svdb_server* s, size_t index, double* out);
+/* GET /vector?uuid= (src/get_handler.c:99-118, src/vector_database.c:145-158)
+ * for n uuids (n x 37 bytes): out_index[i] = position of the first row whose
+ * uuid equals uuid i under strncmp(.., 37), -1 if none.  Answered by the
+ * device's uuid index. */
+int svdb_server_find_uuid(svdb_server* s, const char* uuids, size_t n, int64_t* out_index);
+/* vector_db_save's file format (src/vector_database.c:203-228): size_t n, then
+ * per row uuid[37], size_t dim, double[dim], rows in positional order, read
+ * back from HBM in blocks.  The reference counts rows it then skips (rows
+ * without data); a server store has none, so n is always the rows written. */
+int svdb_server_save(svdb_server* s, const char* filename);
+/* A server store of dimension dim loaded from a file in that format
+ * (vector_db_load, src/vector_database.c:237-292): the file's bytes are copied
+ * to the device as they are, in blocks, and unpacked there into the FP64 rows
+ * and the uuid index.  Every row must have dimension dim; a file that ends
+ * early keeps the rows before the cut (message on stderr), as the drop-in
+ * vector_db_load does.  reserve_rows: extra room beyond the file's rows.
+ * NULL on failure (message in svdb_last_error). */
+svdb_server* svdb_server_load(const char* filename, size_t dim, size_t reserve_rows);
 /* One batch (see above).  NEAREST results of request i go to ids/dists +
  * i * stride (stride >= its k; -1 / NaN past the number of rows).  The
  * return value is SVDB_OK unless the batch as a whole failed (a CUDA error);
@@ -264,6 +286,13 @@ int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, uint32_t* 
  */
 int svdb_merge_topk(int metric, const int64_t* ids, const double* vals, size_t nshards, size_t nq, size_t k,
                     int64_t* out_ids, double* out_vals);
+
+/* GET /vector?uuid= for n uuids (n x 37 bytes) on the drop-in store
+ * (src/vector_database.c:145-158, src/get_handler.c:99-118): out_index[i] =
+ * position of the first row whose uuid equals uuid i under strncmp(.., 37),
+ * -1 if none.  vector_db_read_by_uuid is this with n = 1.  Answered by the
+ * device's uuid index (a hash table of the stored uuids); no row is scanned. */
+int svdb_find_uuid_batch(VectorDatabase* db, const char* uuids, size_t n, int64_t* out_index);
 
 /* Bulk insert of n rows (n x dim, row-major, copied): the same result as n
  * vector_db_insert calls, including the KD nodes.  uuids: n*37 bytes or

@@ -195,6 +195,8 @@ class RefLib:
         L.vector_db_read.restype = C.POINTER(RefVector)
         L.vector_db_read.argtypes = [C.c_void_p, C.c_size_t]
         L.vector_db_update.argtypes = [C.c_void_p, C.c_size_t, RefVector]
+        L.vector_db_read_by_uuid.restype = C.POINTER(RefVector)
+        L.vector_db_read_by_uuid.argtypes = [C.c_void_p, C.c_char_p]
         L.vector_db_delete.argtypes = [C.c_void_p, C.c_size_t]
         for n in ("cosine_similarity", "euclidean_distance", "dot_product"):
             getattr(L, n).restype = C.c_float
@@ -254,8 +256,18 @@ class RefStore:
         r = self.r.L.vector_db_insert(self.db, self.r.make_vector(v, uuid))
         return -1 if r == 2**64 - 1 else int(r)
 
-    def update(self, i, v):
-        self.r.L.vector_db_update(self.db, i, self.r.make_vector(v))
+    def update(self, i, v, uuid=b""):
+        self.r.L.vector_db_update(self.db, i, self.r.make_vector(v, uuid))
+
+    def find_uuid(self, key: bytes) -> int:
+        """vector_db_read_by_uuid (src/vector_database.c:145-158) -> the row's
+        position (pointer minus the array base over sizeof(Vector) = 56), -1
+        for NULL."""
+        p = self.r.L.vector_db_read_by_uuid(self.db, key)
+        if not p:
+            return -1
+        base = C.cast(self.db, C.POINTER(C.c_void_p))[0]
+        return (C.cast(p, C.c_void_p).value - base) // C.sizeof(RefVector)
 
     def delete(self, i):
         self.r.L.vector_db_delete(self.db, i)
@@ -276,3 +288,23 @@ class RefStore:
         if self.db:
             self.r.L.vector_db_free(self.db)
             self.db = None
+
+
+# ---------------------------------------------------------------------------
+# uuid lookup (numpy restatement of src/vector_database.c:145-158)
+# ---------------------------------------------------------------------------
+def uuid_record(u: bytes) -> np.ndarray:
+    """char uuid[37] as strncmp(.., 37) sees it: the bytes up to the first NUL
+    (at most 37), zero padded to 37."""
+    b = bytes(u)[:37]
+    b = b.split(b"\0", 1)[0]
+    return np.frombuffer(b.ljust(37, b"\0"), np.uint8)
+
+
+def uuid_first(table: np.ndarray, key: bytes) -> int:
+    """Position of the first row of `table` (n x 37 records) whose uuid equals
+    `key` under strncmp(.., 37) -- the reference's linear scan -- or -1."""
+    if table.shape[0] == 0:
+        return -1
+    hit = np.flatnonzero((table == uuid_record(key)).all(axis=1))
+    return int(hit[0]) if hit.size else -1

@@ -566,6 +566,8 @@ int Store::sync() {
     if (rc) return rc;
     rc = flush();
     if (rc) return rc;
+    rc = uuid_flush();
+    if (rc) return rc;
     if (derive_lo >= 0 && derive_hi > derive_lo) {
         const int64_t n = derive_hi - derive_lo;
         const int threads = 256;
@@ -638,6 +640,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
     Store* s = reinterpret_cast<Store*>(hs);
     if (!s) return;
     if (!s->stream) {  // never touched the GPU
+        s->uuid_free();
         delete s;
         return;
     }
@@ -663,6 +666,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
         for (int i = 0; i < Store::kProfRing; ++i)
             for (int j = 0; j < Store::kProfMarks; ++j) cudaEventDestroy(s->pev[i][j]);
     s->release_extra();
+    s->uuid_free();
     cudaStreamDestroy(s->stream);
     delete s;
 }

@@ -13,6 +13,7 @@
 namespace svdb {
 
 struct GemmPlanCache;  // dev_gemm.cu
+struct UuidIndex;      // dev_uuid.cu
 
 struct Store {
     size_t dim = 0, ld = 0, ldb = 0;
@@ -86,6 +87,15 @@ struct Store {
     void prof_end() { prof_cur = -1; }
     int prof_resolve_one();
     int prof_read(double* ms, bool reset);
+
+    // uuid -> position index (dev_uuid.cu); created by the first uuid set
+    UuidIndex* uid = nullptr;
+    int uuid_set(int64_t slot, const char* uuid37);  // staged; applied at sync
+    int uuid_flush();
+    void uuid_free();
+    int uuid_find(const char* uuids37, size_t n, int64_t* out_pos);
+    int append_raw(const void* rows, size_t n, size_t rowbytes);
+    int read_block(int64_t first, size_t n, double* rows, char* uuids37, uint8_t* live);
 
     int ensure();
     int grow(size_t need);

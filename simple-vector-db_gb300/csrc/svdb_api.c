@@ -205,6 +205,8 @@ SVDB_API int svdb_insert_batch(VectorDatabase* db, const double* rows, size_t n,
                 r = svdbd_store_append(d->dev, &none, &flag, 1);
             }
         }
+        for (size_t i = 0; i < n && !r && uuids; ++i)
+            if (uuids[i * UUID_SIZE]) r = svdbd_store_set_uuid(d->dev, (int64_t)(slot0 + i), uuids + i * UUID_SIZE);
         if (r) {
             for (size_t i = 0; i < n; ++i) free(db->vectors[db->size + i].data);
             pthread_mutex_unlock(&db->mutex);
@@ -302,6 +304,31 @@ SVDB_API int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_q
         rc = SVDB_EINVAL;
     } else {
         rc = svdbd_search_noalloc(d->dev, d_queries, nq, k, metric, d_ids, d_dists);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+/* ---- GET /vector?uuid= in batches ---------------------------------------- */
+SVDB_API int svdb_find_uuid_batch(VectorDatabase* db, const char* uuids, size_t n, int64_t* out_index) {
+    if (!db || (n && (!uuids || !out_index))) {
+        svdb_set_error("svdb_find_uuid_batch: NULL argument");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = SVDB_OK;
+    if (d->dev) {
+        rc = svdbd_uuid_find(d->dev, uuids, n, out_index);
+    } else { /* no row of nonzero dimension yet: nothing on the device */
+        for (size_t q = 0; q < n; ++q) {
+            out_index[q] = -1;
+            for (size_t i = 0; i < db->size; ++i)
+                if (strncmp(db->vectors[i].uuid, uuids + q * UUID_SIZE, UUID_SIZE) == 0) {
+                    out_index[q] = (int64_t)i;
+                    break;
+                }
+        }
     }
     pthread_mutex_unlock(&db->mutex);
     return rc;

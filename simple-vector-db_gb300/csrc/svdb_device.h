@@ -78,6 +78,15 @@ int svdbd_selftest_wait(svdbd_store* s, uint32_t limit_us, uint32_t* gave_up);
 int svdbd_search_noalloc(svdbd_store* s, const double* d_queries, size_t nq, size_t k, int metric, int64_t* d_ids,
                          double* d_dists);
 
+/* uuid of a slot (char[37] as the reference stores it; staged, applied at
+ * sync), batched lookup of positions by uuid (-1: none), rows of the
+ * reference's file format appended straight into the device store, and a
+ * block of slots read back (dev_uuid.cu) */
+int svdbd_store_set_uuid(svdbd_store* s, int64_t slot, const char* uuid37);
+int svdbd_uuid_find(svdbd_store* s, const char* uuids37, size_t n, int64_t* out_pos);
+int svdbd_store_append_raw(svdbd_store* s, const void* rows, size_t n, size_t rowbytes);
+int svdbd_store_read_block(svdbd_store* s, int64_t first, size_t n, double* rows, char* uuids37, uint8_t* live);
+
 /* ragged batch over several stores, replayed as one CUDA graph (dev_ragged.cu) */
 typedef struct svdbd_ragged svdbd_ragged;
 typedef struct svdbd_ragged_part {

@@ -14,6 +14,7 @@
  */
 #include <math.h>
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -120,14 +121,21 @@ SVDB_API size_t svdb_server_size(svdb_server* s) {
 }
 
 SVDB_API int svdb_server_insert_block(svdb_server* s, const double* rows, size_t n, size_t* first_index) {
+    return svdb_server_insert_rows(s, rows, NULL, n, first_index);
+}
+
+SVDB_API int svdb_server_insert_rows(svdb_server* s, const double* rows, const char* uuids, size_t n,
+                                     size_t* first_index) {
     if (!s || (n && !rows)) {
-        svdb_set_error("svdb_server_insert_block: NULL argument");
+        svdb_set_error("svdb_server_insert_rows: NULL argument");
         return SVDB_EINVAL;
     }
     pthread_mutex_lock(&s->mu);
     if (first_index) *first_index = s->nlive;
     int rc = fen_reserve(s, s->nslots + n);
     if (!rc && n) rc = svdbd_store_append_block(s->st, rows, n);
+    for (size_t i = 0; i < n && !rc && uuids; ++i)
+        if (uuids[i * 37]) rc = svdbd_store_set_uuid(s->st, (int64_t)(s->nslots + i), uuids + i * 37);
     if (!rc) {
         for (size_t i = 0; i < n; ++i) fen_add(s, s->nslots + i, 1);
         s->nslots += n;
@@ -253,6 +261,7 @@ SVDB_API int svdb_server_execute(svdb_server* s, const svdb_request* req, size_t
                 o->status = SVDB_ENOMEM;
             } else {
                 rc = svdbd_store_append(s->st, &r->vec, NULL, 1);
+                if (!rc && r->uuid && r->uuid[0]) rc = svdbd_store_set_uuid(s->st, (int64_t)s->nslots, r->uuid);
                 if (!rc) {
                     fen_add(s, s->nslots++, 1);
                     o->index = s->nlive++;
@@ -267,6 +276,7 @@ SVDB_API int svdb_server_execute(svdb_server* s, const svdb_request* req, size_t
                 const int64_t slot = fen_slot(s, (size_t)r->a);
                 if (r->op == SVDB_REQ_UPDATE) {
                     rc = svdbd_store_overwrite(s->st, slot, r->vec, 1);
+                    if (!rc && r->uuid) rc = svdbd_store_set_uuid(s->st, slot, r->uuid);
                 } else {
                     rc = svdbd_store_kill(s->st, slot);
                     if (!rc) {
@@ -338,4 +348,143 @@ SVDB_API int svdb_server_execute(svdb_server* s, const svdb_request* req, size_t
                                                                              : SVDB_CMP_UNKNOWN_METHOD;
     pthread_mutex_unlock(&s->mu);
     return rc;
+}
+
+/* ---- uuid lookups and persistence --------------------------------------- */
+SVDB_API int svdb_server_find_uuid(svdb_server* s, const char* uuids, size_t n, int64_t* out_index) {
+    if (!s || (n && (!uuids || !out_index))) {
+        svdb_set_error("svdb_server_find_uuid: NULL argument");
+        return SVDB_EINVAL;
+    }
+    pthread_mutex_lock(&s->mu);
+    int rc = svdbd_uuid_find(s->st, uuids, n, out_index);
+    pthread_mutex_unlock(&s->mu);
+    return rc;
+}
+
+/* rows read back from HBM in blocks of this many slots */
+#define SERVER_IO_BLOCK 16384
+
+SVDB_API int svdb_server_save(svdb_server* s, const char* filename) {
+    if (!s || !filename) {
+        svdb_set_error("svdb_server_save: NULL argument");
+        return SVDB_EINVAL;
+    }
+    pthread_mutex_lock(&s->mu);
+    int rc = SVDB_OK;
+    const size_t blk = SERVER_IO_BLOCK;
+    double* rows = (double*)malloc(blk * s->dim * sizeof(double));
+    char* uu = (char*)malloc(blk * 37);
+    uint8_t* lv = (uint8_t*)malloc(blk);
+    FILE* f = fopen(filename, "wb");
+    if (!rows || !uu || !lv || !f) {
+        svdb_set_error(f ? "svdb_server_save: out of host memory" : "svdb_server_save: cannot open the file");
+        rc = f ? SVDB_ENOMEM : SVDB_EINVAL;
+    }
+    if (!rc) {
+        const size_t n = s->nlive, dim = s->dim;
+        size_t written = 0;
+        if (fwrite(&n, sizeof(size_t), 1, f) != 1) rc = SVDB_EINVAL;
+        for (size_t first = 0; first < s->nslots && !rc; first += blk) {
+            const size_t m = s->nslots - first < blk ? s->nslots - first : blk;
+            rc = svdbd_store_read_block(s->st, (int64_t)first, m, rows, uu, lv);
+            for (size_t i = 0; i < m && !rc; ++i) {
+                if (!lv[i]) continue;
+                if (fwrite(uu + i * 37, 1, 37, f) != 37 || fwrite(&dim, sizeof(size_t), 1, f) != 1 ||
+                    fwrite(rows + i * dim, sizeof(double), dim, f) != dim)
+                    rc = SVDB_EINVAL;
+                written++;
+            }
+        }
+        if (!rc && written != n) {
+            svdb_set_error("svdb_server_save: %zu rows written, %zu expected", written, n);
+            rc = SVDB_ECUDA;
+        } else if (rc == SVDB_EINVAL) {
+            svdb_set_error("svdb_server_save: write error");
+        }
+    }
+    if (f && fclose(f) != 0 && !rc) {
+        svdb_set_error("svdb_server_save: write error");
+        rc = SVDB_EINVAL;
+    }
+    free(rows);
+    free(uu);
+    free(lv);
+    pthread_mutex_unlock(&s->mu);
+    return rc;
+}
+
+SVDB_API svdb_server* svdb_server_load(const char* filename, size_t dim, size_t reserve_rows) {
+    if (!filename || dim == 0) {
+        svdb_set_error("svdb_server_load: NULL file name or dimension 0");
+        return NULL;
+    }
+    FILE* f = fopen(filename, "rb");
+    if (!f) {
+        svdb_set_error("svdb_server_load: cannot open the file");
+        return NULL;
+    }
+    size_t n = 0;
+    if (fread(&n, sizeof(size_t), 1, f) != 1) n = 0;
+    const size_t rowbytes = 37 + sizeof(size_t) + dim * sizeof(double);
+    long long avail = -1; /* rows the file can hold at most (a bad count cannot reserve absurd memory) */
+    if (fseek(f, 0, SEEK_END) == 0) {
+        const long end = ftell(f);
+        if (end >= 8) avail = (long long)((size_t)(end - 8) / rowbytes);
+        fseek(f, 8, SEEK_SET);
+    }
+    if (avail >= 0 && (size_t)avail < n) {
+        fprintf(stderr, "svdb_server_load: the file counts %zu rows but holds %lld (truncated file)\n", n, avail);
+        n = (size_t)avail;
+    }
+    svdb_server* s = svdb_server_create(dim, n + reserve_rows);
+    if (!s) {
+        fclose(f);
+        return NULL;
+    }
+    /* blocks of about 64 MB of file bytes */
+    size_t blk = ((size_t)64 << 20) / rowbytes;
+    if (blk == 0) blk = 1;
+    uint8_t* buf = (uint8_t*)malloc(blk * rowbytes);
+    int rc = buf ? SVDB_OK : SVDB_ENOMEM;
+    if (rc) svdb_set_error("svdb_server_load: out of host memory");
+    size_t done = 0;
+    while (!rc && done < n) {
+        const size_t want = n - done < blk ? n - done : blk;
+        const size_t got = fread(buf, rowbytes, want, f);
+        size_t m = 0;
+        for (; m < got; ++m) { /* every row must have the store's dimension */
+            size_t d = 0;
+            memcpy(&d, buf + m * rowbytes + 37, sizeof(size_t));
+            if (d != dim) break;
+        }
+        if (m < got) {
+            svdb_set_error("svdb_server_load: row %zu has dimension != %zu", done + m, dim);
+            rc = SVDB_EINVAL;
+        }
+        if (m) {
+            pthread_mutex_lock(&s->mu);
+            int r = fen_reserve(s, s->nslots + m);
+            if (!r) r = svdbd_store_append_raw(s->st, buf, m, rowbytes);
+            if (!r) {
+                for (size_t i = 0; i < m; ++i) fen_add(s, s->nslots + i, 1);
+                s->nslots += m;
+                s->nlive += m;
+            }
+            pthread_mutex_unlock(&s->mu);
+            if (r && !rc) rc = r;
+        }
+        done += m;
+        if (!rc && got < want) {
+            fprintf(stderr, "svdb_server_load: truncated file at row %zu\n", done);
+            break;
+        }
+    }
+    free(buf);
+    fclose(f);
+    if (rc) {
+        svdb_server_destroy(s);
+        return NULL;
+    }
+    return s;
 }

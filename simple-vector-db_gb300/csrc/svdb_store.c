@@ -115,6 +115,7 @@ int svdb_db_ensure_dev(svdb_db* d, size_t dim) {
         uint8_t flag = 2;
         d->slot_of[i] = (int64_t)svdbd_store_slots(d->dev);
         int rc = svdbd_store_append(d->dev, &none, &flag, 1);
+        if (!rc && d->pub.vectors[i].uuid[0]) rc = svdbd_store_set_uuid(d->dev, d->slot_of[i], d->pub.vectors[i].uuid);
         if (rc) return rc;
     }
     return SVDB_OK;
@@ -140,7 +141,8 @@ static size_t insert_locked(svdb_db* d, Vector vec) {
         const double* row = vec.data;
         uint8_t live = row_flag(d, &vec);
         slot = (int64_t)svdbd_store_slots(d->dev);
-        if (svdbd_store_append(d->dev, &row, &live, 1) != SVDB_OK) {
+        if (svdbd_store_append(d->dev, &row, &live, 1) != SVDB_OK ||
+            (vec.uuid[0] && svdbd_store_set_uuid(d->dev, slot, vec.uuid) != SVDB_OK)) {
             fprintf(stderr, "vector_db_insert: %s\n", svdb_last_error());
             return (size_t)-1;
         }
@@ -167,16 +169,32 @@ SVDB_API Vector* vector_db_read(VectorDatabase* db, size_t index) {
     return v;
 }
 
-/* linear uuid scan, src/vector_database.c:145-158 (not on the GPU path) */
+/* src/vector_database.c:145-158: the first row in positional order whose
+ * uuid equals `uuid` under strncmp(.., 37).  The reference scans the array;
+ * here the device's uuid index answers (dev_uuid.cu).  A store that has never
+ * held a row of nonzero dimension has no device store -- nothing to index --
+ * and its (dimensionless) rows are scanned. */
 SVDB_API Vector* vector_db_read_by_uuid(VectorDatabase* db, const char* uuid) {
     if (!db || !uuid) return NULL;
+    svdb_db* d = svdb_of(db);
     pthread_mutex_lock(&db->mutex);
     Vector* v = NULL;
-    for (size_t i = 0; i < db->size; ++i)
-        if (strncmp(db->vectors[i].uuid, uuid, UUID_SIZE) == 0) {
-            v = &db->vectors[i];
-            break;
-        }
+    if (d->dev) {
+        char key[UUID_SIZE];
+        memset(key, 0, sizeof(key));
+        for (size_t i = 0; i < UUID_SIZE && uuid[i]; ++i) key[i] = uuid[i];
+        int64_t pos = -1;
+        if (svdbd_uuid_find(d->dev, key, 1, &pos) != SVDB_OK)
+            fprintf(stderr, "vector_db_read_by_uuid: %s\n", svdb_last_error());
+        else if (pos >= 0 && (size_t)pos < db->size)
+            v = &db->vectors[pos];
+    } else {
+        for (size_t i = 0; i < db->size; ++i)
+            if (strncmp(db->vectors[i].uuid, uuid, UUID_SIZE) == 0) {
+                v = &db->vectors[i];
+                break;
+            }
+    }
     pthread_mutex_unlock(&db->mutex);
     return v;
 }
@@ -189,7 +207,8 @@ SVDB_API void vector_db_update(VectorDatabase* db, size_t index, Vector vec) {
         if (svdb_db_ensure_dev(d, vec.dimension) != SVDB_OK)
             fprintf(stderr, "vector_db_update: %s\n", svdb_last_error());
         else if (d->dev &&
-                 svdbd_store_overwrite(d->dev, d->slot_of[index], vec.data, row_flag(d, &vec)) != SVDB_OK)
+                 (svdbd_store_overwrite(d->dev, d->slot_of[index], vec.data, row_flag(d, &vec)) != SVDB_OK ||
+                  svdbd_store_set_uuid(d->dev, d->slot_of[index], vec.uuid) != SVDB_OK))
             fprintf(stderr, "vector_db_update: %s\n", svdb_last_error());
         free(db->vectors[index].data);
         db->vectors[index] = vec;

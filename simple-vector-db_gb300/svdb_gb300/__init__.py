@@ -119,6 +119,11 @@ def _load():
         "svdb_merge_topk": (C.c_int, [C.c_int, _i64p, _dp, sz, sz, sz, _i64p, _dp]),
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
+        "svdb_find_uuid_batch": (C.c_int, [vp, C.c_char_p, sz, _i64p]),
+        "svdb_server_insert_rows": (C.c_int, [vp, _dp, C.c_char_p, sz, C.POINTER(C.c_size_t)]),
+        "svdb_server_find_uuid": (C.c_int, [vp, C.c_char_p, sz, _i64p]),
+        "svdb_server_save": (C.c_int, [vp, C.c_char_p]),
+        "svdb_server_load": (vp, [C.c_char_p, sz, sz]),
         "svdb_ragged_create": (vp, [C.POINTER(RaggedPart), sz, C.c_int, C.c_int, C.c_uint]),
         "svdb_ragged_run": (C.c_int, [vp]),
         "svdb_ragged_wait": (C.c_int, [vp]),
@@ -171,6 +176,16 @@ def make_vector(data, uuid: bytes | str = b"", owned: bool = True) -> Vector:
         v.data = a.ctypes.data_as(_dp)
         v._keep = a
     return v
+
+
+def uuid_block(uuids) -> bytes:
+    """n uuids (str or bytes) as n x 37 bytes, each NUL-padded the way
+    char uuid[37] holds a shorter string (longer ones keep 37 bytes)."""
+    out = bytearray()
+    for u in uuids:
+        b = u.encode() if isinstance(u, str) else bytes(u)
+        out += b[:37].ljust(37, b"\0")
+    return bytes(out)
 
 
 def cosine_similarity(a, b) -> np.float32:
@@ -246,6 +261,15 @@ class VectorDatabase:
         p = lib.vector_db_read(self.ptr, index)
         return bytes(p.contents.uuid).split(b"\0")[0] if p else None
 
+    def find_uuid(self, uuids) -> np.ndarray:
+        """svdb_find_uuid_batch: position of the first row with each uuid
+        (strncmp over 37 bytes, as the reference compares), -1 if none."""
+        keys = uuid_block(uuids)
+        out = np.empty(len(uuids), np.int64)
+        _check(lib.svdb_find_uuid_batch(self.ptr, keys, len(uuids), out.ctypes.data_as(_i64p)),
+               "svdb_find_uuid_batch")
+        return out
+
     def read_by_uuid(self, uuid: bytes | str):
         if isinstance(uuid, str):
             uuid = uuid.encode()
@@ -255,8 +279,8 @@ class VectorDatabase:
         v = p.contents
         return np.ctypeslib.as_array(v.data, shape=(v.dimension,)).copy()
 
-    def update(self, index: int, data) -> None:
-        lib.vector_db_update(self.ptr, index, make_vector(data))
+    def update(self, index: int, data, uuid: bytes | str = b"") -> None:
+        lib.vector_db_update(self.ptr, index, make_vector(data, uuid))
 
     def delete(self, index: int) -> None:
         lib.vector_db_delete(self.ptr, index)

@@ -16,16 +16,16 @@ import time
 
 import numpy as np
 
-from . import EUCLIDEAN, PREC_BF16, SearchStats, _check, _dp, _f64, _i64p, last_error, lib
+from . import EUCLIDEAN, PREC_BF16, SearchStats, SvdbError, _check, _dp, _f64, _i64p, last_error, lib, uuid_block
 
 REQ_NEAREST, REQ_COMPARE, REQ_INSERT, REQ_UPDATE, REQ_DELETE = range(5)
 REQ_NAMES = ("nearest", "compare", "insert", "update", "delete")
 
 # struct svdb_request / svdb_response (include/svdb_gb300.h)
 REQ_DTYPE = np.dtype([("op", "<i4"), ("metric", "<i4"), ("k", "<u4"), ("reserved", "<u4"), ("a", "<u8"),
-                      ("b", "<u8"), ("vec", "<u8")])
+                      ("b", "<u8"), ("vec", "<u8"), ("uuid", "<u8")])
 RESP_DTYPE = np.dtype([("status", "<i4"), ("value", "<f4"), ("index", "<u8")])
-assert REQ_DTYPE.itemsize == 40 and RESP_DTYPE.itemsize == 16
+assert REQ_DTYPE.itemsize == 48 and RESP_DTYPE.itemsize == 16
 
 # /nearest 70 %, /compare 10 %, insert 15 %, update 3 %, delete 2 %
 DEFAULT_MIX = (0.70, 0.10, 0.15, 0.03, 0.02)
@@ -34,12 +34,37 @@ DEFAULT_MIX = (0.70, 0.10, 0.15, 0.03, 0.02)
 class Server:
     """svdb_server_*: rows only in HBM; `reserve_rows` allocated up front."""
 
-    def __init__(self, dim: int, reserve_rows: int):
+    def __init__(self, dim: int, reserve_rows: int, _ptr=None):
         self.dim = dim
-        self.ptr = lib.svdb_server_create(dim, reserve_rows)
+        self.ptr = _ptr or lib.svdb_server_create(dim, reserve_rows)
         if not self.ptr:
-            from . import SvdbError
             raise SvdbError(f"svdb_server_create failed: {last_error()}")
+
+    @classmethod
+    def load(cls, filename: str, dim: int, reserve_rows: int = 0) -> "Server":
+        """svdb_server_load: a reference-format file straight into HBM."""
+        p = lib.svdb_server_load(filename.encode(), dim, reserve_rows)
+        if not p:
+            raise SvdbError(f"svdb_server_load failed: {last_error()}")
+        return cls(dim, 0, _ptr=p)
+
+    def save(self, filename: str) -> None:
+        _check(lib.svdb_server_save(self.ptr, filename.encode()), "svdb_server_save")
+
+    def insert_rows(self, rows, uuids=None) -> int:
+        r = _f64(rows).reshape(-1, self.dim)
+        keys = uuid_block(uuids) if uuids is not None else None
+        first = C.c_size_t(0)
+        _check(lib.svdb_server_insert_rows(self.ptr, r.ctypes.data_as(_dp), keys, r.shape[0], C.byref(first)),
+               "svdb_server_insert_rows")
+        return first.value
+
+    def find_uuid(self, uuids) -> np.ndarray:
+        keys = uuid_block(uuids)
+        out = np.empty(len(uuids), np.int64)
+        _check(lib.svdb_server_find_uuid(self.ptr, keys, len(uuids), out.ctypes.data_as(_i64p)),
+               "svdb_server_find_uuid")
+        return out
 
     def close(self) -> None:
         if self.ptr:

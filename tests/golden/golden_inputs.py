@@ -91,3 +91,49 @@ def mutation_trace():
             if idx < size:
                 size -= 1
     return ops, D
+
+
+def uuid_pool():
+    """uuid strings for the uuid trace: 36-character uuid-like strings, a
+    family sharing a 30-character prefix, short ones, duplicates by reuse,
+    and the empty uuid."""
+    r = np.random.default_rng(21)
+    hexd = np.array(list("0123456789abcdef"))
+
+    def u36():
+        h = "".join(r.choice(hexd, 32))
+        return f"{h[:8]}-{h[8:12]}-{h[12:16]}-{h[16:20]}-{h[20:]}".encode()
+
+    pool = [u36() for _ in range(120)]
+    stem = u36()[:30]
+    pool += [stem + f"{i:06d}".encode() for i in range(40)]
+    pool += [bytes(r.choice(list(b"abcxyz"), int(r.integers(1, 6))).tolist()) for _ in range(40)]
+    pool += [b""]
+    return pool
+
+
+def uuid_trace():
+    """2,000 operations on a D=8 store: 55 % insert with a uuid drawn from the
+    pool (so uuids repeat), 20 % update with a new uuid (sometimes empty), 20 %
+    delete, indices sometimes out of range; then every pool uuid and a few
+    absent ones are looked up."""
+    D = 8
+    r = np.random.default_rng(22)
+    pool = uuid_pool()
+    ops = []
+    size = 0
+    for _ in range(2_000):
+        u = r.random()
+        if u < 0.55 or size == 0:
+            ops.append((0, 0, r.uniform(-1, 1, D), pool[int(r.integers(0, len(pool)))]))
+            size += 1
+        elif u < 0.75:
+            idx = int(r.integers(0, size + 3))
+            ops.append((1, idx, r.uniform(-1, 1, D), pool[int(r.integers(0, len(pool)))]))
+        else:
+            idx = int(r.integers(0, size + 3))
+            ops.append((2, idx, None, b""))
+            if idx < size:
+                size -= 1
+    keys = pool + [b"absent", pool[0][:35], pool[120][:31] + b"x"]
+    return ops, D, keys

@@ -22,7 +22,7 @@ sys.path.insert(0, HERE)
 
 import oracle as O  # noqa: E402
 from golden_inputs import (compare_inputs, kd_inputs, mutation_trace, addvec_pairs,  # noqa: E402
-                           sha)
+                           sha, uuid_trace)
 
 
 def main() -> None:
@@ -64,12 +64,26 @@ def main() -> None:
     size_mut = st2.size
     rows_sha = sha(np.stack([st2.read(i) for i in range(size_mut)]))
 
+    # -- GET /vector?uuid= (vector_db_read_by_uuid) after a uuid trace ----------
+    uops, _, ukeys = uuid_trace()
+    st3 = O.RefStore(ref, 3)
+    for op, idx, v, u in uops:
+        if op == 0:
+            st3.insert(v, u)
+        elif op == 1:
+            st3.update(idx, v, u)
+        else:
+            st3.delete(idx)
+    uuid_found = np.array([st3.find_uuid(k) for k in ukeys], np.int64)
+    uuid_size = st3.size
+
     np.savez_compressed(
         os.path.join(HERE, "golden_reference.npz"),
         compare_x_sha=sha(X), compare_pairs_sha=sha(pairs), compare_vals=vals,
         adv_sha=sha(np.concatenate([np.concatenate(A), np.concatenate(B)])), adv_vals=adv,
         kd_x_sha=sha(Xk), kd_q_sha=sha(Qk), kd_nearest=near,
         mut_nearest=near_mut, mut_size=np.int64(size_mut), mut_rows_sha=np.frombuffer(rows_sha.encode(), np.uint8),
+        uuid_found=uuid_found, uuid_size=np.int64(uuid_size),
     )
     print("wrote golden_reference.npz:", vals.shape, adv.shape, near.shape, near_mut.shape, size_mut)
 

@@ -47,8 +47,9 @@ def test_struct_layout_matches_reference(svdb):
 
 
 def test_positional_store_semantics_host(svdb):
-    """insert / read / update / delete / read_by_uuid as
-    src/vector_database.c:81-195 (host side; no GPU call is made)."""
+    """insert / read / update / delete as src/vector_database.c:81-195 (host
+    side; no GPU call is made).  read_by_uuid is answered by the device's
+    uuid index (tests/test_gpu_uuid.py)."""
     db = svdb.VectorDatabase(0, 3)
     rows = [np.full(8, float(i)) for i in range(6)]
     for i, r in enumerate(rows):
@@ -64,8 +65,6 @@ def test_positional_store_semantics_host(svdb):
     db.update(0, np.full(8, 42.0))
     assert np.array_equal(db.read(0), np.full(8, 42.0))
     assert db.read(5) is None
-    assert np.array_equal(db.read_by_uuid("uuid-4"), rows[4])
-    assert db.read_by_uuid("nope") is None
     db.close()
 
 
@@ -140,4 +139,7 @@ def test_library_fails_loudly_without_gpu(svdb):
         db.search(np.ones(4), 1)
     assert db.kdtree_nearest(np.ones(4)) == -1
     assert np.isnan(svdb.cosine_similarity(np.ones(4), np.ones(4)))
+    assert db.read_by_uuid("") is None
+    with pytest.raises(svdb.SvdbError):
+        db.find_uuid(["a"])
     db.close()

@@ -122,3 +122,59 @@ def test_oracle_matches_compiled_reference(oracle, refstore):
     Q = r.uniform(-1, 1, (300, 32))
     assert [rs.nearest(q) for q in Q] == [os_.nearest(q) for q in Q]
     rs.free()
+
+
+def _replay_uuid_trace(ops):
+    """The positional store's uuids after the trace (reference semantics:
+    insert appends, update replaces the row's uuid, delete shifts; indices
+    past the end are ignored), as an n x 37 record table."""
+    import oracle as O
+    recs = []
+    for op, idx, _, u in ops:
+        if op == 0:
+            recs.append(O.uuid_record(u))
+        elif op == 1 and idx < len(recs):
+            recs[idx] = O.uuid_record(u)
+        elif op == 2 and idx < len(recs):
+            del recs[idx]
+    return np.stack(recs) if recs else np.zeros((0, 37), np.uint8)
+
+
+def test_uuid_restatement_matches_golden(golden):
+    """vector_db_read_by_uuid (src/vector_database.c:145-158) after a trace of
+    inserts with repeated, prefix-sharing, short and empty uuids, updates that
+    change uuids and deletes: the numpy restatement finds the same rows the
+    compiled reference found."""
+    import oracle as O
+    from golden_inputs import uuid_trace
+    ops, _, keys = uuid_trace()
+    table = _replay_uuid_trace(ops)
+    assert table.shape[0] == int(golden["uuid_size"])
+    found = np.array([O.uuid_first(table, k) for k in keys])
+    assert np.array_equal(found, golden["uuid_found"])
+    assert (found >= 0).sum() > 150 and (found < 0).sum() >= 3
+
+
+def test_uuid_restatement_matches_compiled_reference(refstore):
+    import oracle as O
+    r = np.random.default_rng(3)
+    st = O.RefStore(refstore, 3)
+    recs = []
+    pool = [b"", b"a", b"ab", b"x" * 36, b"x" * 35 + b"y"] + [f"{i:036d}".encode() for i in range(20)]
+    for _ in range(400):
+        u = pool[int(r.integers(0, len(pool)))]
+        if r.random() < 0.7 or not recs:
+            st.insert(r.uniform(-1, 1, 4), u)
+            recs.append(O.uuid_record(u))
+        else:
+            i = int(r.integers(0, len(recs)))
+            if r.random() < 0.5:
+                st.update(i, r.uniform(-1, 1, 4), u)
+                recs[i] = O.uuid_record(u)
+            else:
+                st.delete(i)
+                del recs[i]
+    table = np.stack(recs)
+    for k in pool + [b"x" * 37, b"zz"]:
+        assert st.find_uuid(k) == O.uuid_first(table, k), k
+    st.free()

@@ -12,8 +12,9 @@ ROWS_D = 48
 
 def test_request_layouts_match_the_c_structs(svdb):
     from svdb_gb300 import serve
-    assert serve.REQ_DTYPE.itemsize == 40 and serve.RESP_DTYPE.itemsize == 16
-    assert [serve.REQ_DTYPE.fields[f][1] for f in ("op", "metric", "k", "a", "b", "vec")] == [0, 4, 8, 16, 24, 32]
+    assert serve.REQ_DTYPE.itemsize == 48 and serve.RESP_DTYPE.itemsize == 16
+    assert [serve.REQ_DTYPE.fields[f][1] for f in ("op", "metric", "k", "a", "b", "vec", "uuid")] == \
+        [0, 4, 8, 16, 24, 32, 40]
     assert [serve.RESP_DTYPE.fields[f][1] for f in ("status", "value", "index")] == [0, 4, 8]
 
 
