@@ -24,6 +24,7 @@ queries of all ranks over the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -508,6 +509,112 @@ def run_serve(args, ws, rank, local):
     srv.close()
 
 
+def run_uuid(args, ws, rank, local):
+    """GET /vector?uuid= and persistence on a server store of 1,000,000 x 128
+    FP64 rows (N(0,1), seed 6) with unique 36-character uuids: batches of
+    4,096 lookups (90 % present, 10 % absent) through svdb_server_find_uuid
+    (host keys in, host positions out: copies inside the timed region), then
+    the store saved to and loaded from the reference's file format through
+    HBM.  CPU baseline: the reference's linear strncmp scan (oracle port) on
+    all host cores over a bounded sample of keys."""
+    import tempfile
+
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import serve
+
+    torch.cuda.set_device(local)
+    n, d, nb = 1_000_000, 128, 4096
+    rng = np.random.default_rng(6)
+    X = rng.normal(size=(n, d))
+    hexd = np.frombuffer(b"0123456789abcdef", np.uint8)
+    h = hexd[rng.integers(0, 16, (n, 32))]
+    U = np.zeros((n, 37), np.uint8)
+    U[:, 0:8], U[:, 9:13], U[:, 14:18], U[:, 19:23], U[:, 24:36] = h[:, 0:8], h[:, 8:12], h[:, 12:16], h[:, 16:20], h[:, 20:32]
+    U[:, [8, 13, 18, 23]] = ord("-")
+    table = U.tobytes()
+    srv = serve.Server(d, n)
+    t0 = time.perf_counter()
+    first = C.c_size_t(0)
+    S._check(S.lib.svdb_server_insert_rows(srv.ptr, X.ctypes.data_as(S._dp), table, n, C.byref(first)),
+             "svdb_server_insert_rows")
+    log(f"[bench] store + uuids {time.perf_counter() - t0:.1f}s")
+    batches = []
+    for b in range(4):
+        pick = rng.integers(0, n, nb)
+        keys = U[pick].copy()
+        absent = rng.random(nb) < 0.1
+        keys[absent, 0] = ord("z")  # no stored uuid starts with z
+        batches.append((keys.tobytes(), np.where(absent, -1, pick)))
+    out = np.empty(nb, np.int64)
+
+    def step(b):
+        keys, _ = batches[b % len(batches)]
+        S._check(S.lib.svdb_server_find_uuid(srv.ptr, keys, nb, out.ctypes.data_as(S._i64p)), "find_uuid")
+
+    for b, (keys, want) in enumerate(batches):  # correctness guard: positions equal the generator's
+        step(b)
+        if not np.array_equal(out, want):
+            raise SystemExit("bench: uuid lookups differ from the stored positions")
+    for w in range(args.warmup):
+        step(w)
+    clk = Clocks(local)
+    t = time.perf_counter()
+    for s_ in range(args.steps):
+        step(s_)
+    dt = time.perf_counter() - t
+    clocks = clk.stop()
+    lookups_s = nb * args.steps / dt
+
+    # persistence through HBM (file of 8 + n x (45 + 8 d) bytes)
+    tmpdir = tempfile.mkdtemp(prefix="svdb_bench_")
+    fpath = os.path.join(tmpdir, "store.db")
+    t = time.perf_counter()
+    srv.save(fpath)
+    save_s = time.perf_counter() - t
+    fbytes = os.path.getsize(fpath)
+    t = time.perf_counter()
+    srv2 = serve.Server.load(fpath, d)
+    srv2.find_uuid([b"warm"])
+    load_s = time.perf_counter() - t
+    keys, want = batches[0]
+    got = np.empty(nb, np.int64)
+    S._check(S.lib.svdb_server_find_uuid(srv2.ptr, keys, nb, got.ctypes.data_as(S._i64p)), "find_uuid")
+    if srv2.size != n or not np.array_equal(got, want) or not np.array_equal(srv2.read(n - 1), X[n - 1]):
+        raise SystemExit("bench: the loaded store differs from the saved one")
+    srv2.close()
+    os.remove(fpath)
+    os.rmdir(tmpdir)
+
+    cpu = None
+    if args.cpu_sample > 0:
+        import oracle as O
+        cores = os.cpu_count() or 1
+        o = O.Oracle()
+        m = max(cores, min(args.cpu_sample * 512, 32768))
+        t = time.perf_counter()
+        res = o.find_uuid(table, batches[0][0][: m * 37], cores)
+        cpu_dt = time.perf_counter() - t
+        if not np.array_equal(res, batches[0][1][:m]):
+            raise SystemExit("bench: oracle uuid scan disagrees")
+        cpu = {"value": m / cpu_dt, "unit": "lookups/s", "cores": cores, "kind": "port",
+               "sample": f"{m} lookups, each a linear strncmp scan of the 1M-row uuid array ({cpu_dt:.1f} s)"}
+    line = {"metric": "GET /vector?uuid= lookups/s, 1M rows (batches of 4096, host buffers)", "value": lookups_s,
+            "unit": "lookups/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8 keys, i64 positions", "data": "synthetic",
+            "config": {"workload": "server store 1M x 128 FP64 N(0,1) seed 6, unique 36-char uuids; lookups 90 % "
+                                   "present / 10 % absent; persistence in the reference's file format",
+                       "l2": "uuid records (40 MB) and table (68 MB) fit in L2: lookups are latency-bound"},
+            "e2e": {"value": lookups_s, "unit": "lookups/s", "h2d_bytes_per_step": nb * 40,
+                    "d2h_bytes_per_step": nb * 8},
+            "persistence": {"file_bytes": fbytes, "save_s": save_s, "save_gbs": fbytes / save_s / 1e9,
+                            "load_s": load_s, "load_gbs": fbytes / load_s / 1e9},
+            "cpu_baseline": cpu, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    srv.close()
+
+
 def main():
     global N_ROWS
     ap = argparse.ArgumentParser()
@@ -521,9 +628,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve"],
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid"],
                     help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
-                         "ragged: one batch over 5 collections of different dimensions; serve: the serving loop")
+                         "ragged: one batch over 5 collections of different dimensions; serve: the serving loop; "
+                         "uuid: GET /vector?uuid= lookups and persistence")
     ap.add_argument("--rate", type=float, default=20000.0, help="serve: offered requests/s")
     ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
@@ -541,6 +649,8 @@ def main():
         run_ragged(args, ws, rank, local)
     elif args.workload == "serve":
         run_serve(args, ws, rank, local)
+    elif args.workload == "uuid":
+        run_uuid(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 

@@ -82,6 +82,22 @@ int svdb_nearest_batch(VectorDatabase* db, const double* queries, size_t nq, siz
                        int64_t* out_index);
 
 /*
+ * POST /nearest over a MEDIAN-split KD tree (opt-in; README.md:3,34 describes
+ * one, src/kdtree.c builds an insertion-order tree instead).  The tree holds
+ * the store's current rows of the store's dimension, split on the first
+ * kd-dimension coordinates, and is built on the device whenever the rows
+ * changed since the last call.  out_index[i] is the position of the row
+ * nearest to query i over those coordinates (the same unfused FP64 distance
+ * as src/kdtree.c:134-137), ties to the lowest position; -1 for an empty
+ * store.  It differs from svdb_nearest_batch (the reference's /nearest) in
+ * two ways: no stale nodes from updates and deletes (src/vector_database.c:
+ * 169-195), and ties to the lowest position instead of the first node
+ * visited.
+ */
+int svdb_nearest_batch_median(VectorDatabase* db, const double* queries, size_t nq, size_t dim,
+                              int64_t* out_index);
+
+/*
  * Exact top-k (no reference counterpart: /nearest is top-1 and documents an
  * unimplemented `number` parameter, README.md:287).  For each of nq queries
  * (nq x dim, row-major), ids[i*k + j] is the logical index of the j-th

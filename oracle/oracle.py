@@ -82,7 +82,18 @@ class Oracle:
         L.orc_store_rows.argtypes = [C.c_void_p]
         L.orc_store_nearest.restype = C.c_size_t
         L.orc_store_nearest.argtypes = [C.c_void_p, _dp]
+        L.orc_find_uuid.restype = C.c_int
+        L.orc_find_uuid.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t, _i64p, C.c_int]
         self.L = L
+
+    # -- GET /vector?uuid=: the reference's linear strncmp scan -------------
+    def find_uuid(self, table: bytes, keys: bytes, threads: int = 1) -> np.ndarray:
+        """table, keys: n x 37 and nk x 37 bytes (char uuid[37] each)."""
+        n, nk = len(table) // 37, len(keys) // 37
+        out = np.empty(nk, np.int64)
+        if self.L.orc_find_uuid(table, n, keys, nk, _ptr(out, _i64p), threads) != 0:
+            raise RuntimeError("orc_find_uuid: thread start failed")
+        return out
 
     # -- /compare metrics, reference-exact (float accumulation) -------------
     def ref_metric(self, metric: int, a: np.ndarray, b: np.ndarray) -> np.float32:

@@ -37,6 +37,11 @@
  *       top-1 only); order = (key ascending, id ascending) where key is the
  *       distance for Euclidean and the negated value for cosine/dot, NaN
  *       ranked last.
+ *
+ *   orc_find_uuid src/vector_database.c:145-158 -- the linear scan of
+ *       vector_db_read_by_uuid: first row whose uuid[37] equals the key
+ *       under strncmp(.., 37); n keys, each scanned independently, spread
+ *       over `threads` threads.
  */
 #include <math.h>
 #include <pthread.h>
@@ -384,3 +389,39 @@ const double* orc_store_rows(const orc_store* s) { return s->rows; }
  * (size_t)-1 for "No nearest neighbor found"; an index >= size is the
  * "Nearest neighbor not found" outcome (the row was deleted). */
 size_t orc_store_nearest(const orc_store* s, const double* q) { return orc_kd_nearest(s->kd, q); }
+
+/* ---- uuid lookup (src/vector_database.c:145-158) ------------------------ */
+typedef struct {
+    const char* table; /* n x 37 */
+    size_t n;
+    const char* keys; /* nk x 37 */
+    size_t nk;
+    int64_t* out;
+    int threads, t;
+} uuid_job;
+
+static void* uuid_worker(void* arg) {
+    uuid_job* J = (uuid_job*)arg;
+    for (size_t q = (size_t)J->t; q < J->nk; q += (size_t)J->threads) {
+        J->out[q] = -1;
+        for (size_t i = 0; i < J->n; ++i)
+            if (strncmp(J->table + i * 37, J->keys + q * 37, 37) == 0) {
+                J->out[q] = (int64_t)i;
+                break;
+            }
+    }
+    return NULL;
+}
+
+int orc_find_uuid(const char* table, size_t n, const char* keys, size_t nk, int64_t* out, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t th[256];
+    uuid_job J[256];
+    for (int t = 0; t < threads; ++t) {
+        J[t] = (uuid_job){table, n, keys, nk, out, threads, t};
+        if (pthread_create(&th[t], NULL, uuid_worker, &J[t]) != 0) return -1;
+    }
+    for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    return 0;
+}

@@ -552,6 +552,7 @@ int Store::flush() {
     SVDB_CUDA(cudaStreamSynchronize(stream));  // stage_live is pageable and cleared below
     slots += n;
     ++epoch;
+    ++version;
     stage.clear();
     stage_live.clear();
     stage_rows = 0;
@@ -641,6 +642,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
     if (!s) return;
     if (!s->stream) {  // never touched the GPU
         s->uuid_free();
+        s->kdm_free();
         delete s;
         return;
     }
@@ -667,6 +669,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
             for (int j = 0; j < Store::kProfMarks; ++j) cudaEventDestroy(s->pev[i][j]);
     s->release_extra();
     s->uuid_free();
+    s->kdm_free();
     cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -733,6 +736,7 @@ int svdbd_store_append_block(svdbd_store* hs, const double* rows, size_t n) {
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     s->slots += n;
     ++s->epoch;
+    ++s->version;
     if (s->derive_lo < 0 || (int64_t)first < s->derive_lo) s->derive_lo = (int64_t)first;
     s->derive_hi = (int64_t)s->slots;
     s->map_dirty = true;
@@ -749,6 +753,7 @@ int svdbd_store_overwrite(svdbd_store* hs, int64_t slot, const double* row, int 
         else
             std::memset(s->stage.data() + st * s->dim, 0, s->dim * sizeof(double));
         s->stage_live[st] = ok ? 1 : 2;
+        ++s->version;
         return SVDB_OK;
     }
     int rc = s->flush();
@@ -766,6 +771,7 @@ int svdbd_store_overwrite(svdbd_store* hs, int64_t slot, const double* row, int 
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     s->dirty_list.push_back(slot);
     s->map_dirty = true;
+    ++s->version;
     return SVDB_OK;
 }
 
@@ -778,6 +784,7 @@ int svdbd_store_kill(svdbd_store* hs, int64_t slot) {
             return SVDB_EINVAL;
         }
         s->stage_live[st] = 0;
+        ++s->version;
         return SVDB_OK;
     }
     int rc = s->ensure();
@@ -787,6 +794,7 @@ int svdbd_store_kill(svdbd_store* hs, int64_t slot) {
     SVDB_CUDA(cudaStreamSynchronize(s->stream));
     s->dirty_list.push_back(slot);  // its row error term becomes +inf (never screened)
     s->map_dirty = true;
+    ++s->version;
     return SVDB_OK;
 }
 

@@ -14,6 +14,7 @@ namespace svdb {
 
 struct GemmPlanCache;  // dev_gemm.cu
 struct UuidIndex;      // dev_uuid.cu
+struct KdmTree;        // dev_kdm.cu
 
 struct Store {
     size_t dim = 0, ld = 0, ldb = 0;
@@ -70,6 +71,9 @@ struct Store {
     // count or the unscreenable count changes.  A ragged plan compares it
     // with the value at capture time and captures again when it differs.
     uint64_t epoch = 0;
+    // Bumped by every change of the rows' contents or liveness (derived
+    // structures built from the rows, like the median KD tree, compare it).
+    uint64_t version = 0;
 
     // stage timing (svdb_profile): a ring of per-search event sets, resolved
     // lazily so profiling adds no host synchronisation to a search
@@ -96,6 +100,11 @@ struct Store {
     int uuid_find(const char* uuids37, size_t n, int64_t* out_pos);
     int append_raw(const void* rows, size_t n, size_t rowbytes);
     int read_block(int64_t first, size_t n, double* rows, char* uuids37, uint8_t* live);
+
+    // median-split KD tree over the searchable rows (dev_kdm.cu), rebuilt on demand
+    KdmTree* kdm = nullptr;
+    int kdm_nearest(size_t kdim, const double* q, size_t nq, size_t qstride, int64_t* out_pos);
+    void kdm_free();
 
     int ensure();
     int grow(size_t need);

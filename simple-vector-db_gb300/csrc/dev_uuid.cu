@@ -433,6 +433,7 @@ int Store::append_raw(const void* rows, size_t n, size_t rowbytes) {
     SVDB_LAUNCH_CHECK();
     slots += n;
     ++epoch;
+    ++version;
     rc = uid_put(this, uid, dst, n);
     if (rc) return rc;
     SVDB_CUDA(cudaStreamSynchronize(stream));

@@ -109,6 +109,29 @@ SVDB_API int svdb_nearest_batch(VectorDatabase* db, const double* queries, size_
     return svdb_kd_nearest_batch(db->kdtree, queries, nq, dim, out_index);
 }
 
+SVDB_API int svdb_nearest_batch_median(VectorDatabase* db, const double* queries, size_t nq, size_t dim,
+                                       int64_t* out_index) {
+    if (!db || (nq && (!queries || !out_index))) {
+        svdb_set_error("svdb_nearest_batch_median: NULL argument");
+        return SVDB_EINVAL;
+    }
+    const size_t kdim = db->kdtree->dimension;
+    if (nq && dim < kdim) {
+        svdb_set_error("svdb_nearest_batch_median: query dimension %zu < KD dimension %zu", dim, kdim);
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = SVDB_OK;
+    if (!d->dev) { /* no row of nonzero dimension: an empty tree */
+        for (size_t i = 0; i < nq; ++i) out_index[i] = -1;
+    } else {
+        rc = svdbd_kdm_nearest(d->dev, kdim, queries, nq, dim, out_index);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
 static int search_common(VectorDatabase* db, const double* q, size_t nq, size_t dim, size_t k, int metric,
                          int precision, int64_t* ids, double* dists, double* err, int on_device,
                          svdb_search_stats* stats) {

@@ -87,6 +87,11 @@ int svdbd_uuid_find(svdbd_store* s, const char* uuids37, size_t n, int64_t* out_
 int svdbd_store_append_raw(svdbd_store* s, const void* rows, size_t n, size_t rowbytes);
 int svdbd_store_read_block(svdbd_store* s, int64_t first, size_t n, double* rows, char* uuids37, uint8_t* live);
 
+/* exact 1-NN over the first kdim coordinates by a median-split KD tree of the
+ * store's searchable rows, built on the device when the rows changed
+ * (dev_kdm.cu); q: nq host rows of qstride doubles; out: positions (-1: none) */
+int svdbd_kdm_nearest(svdbd_store* s, size_t kdim, const double* q, size_t nq, size_t qstride, int64_t* out_pos);
+
 /* ragged batch over several stores, replayed as one CUDA graph (dev_ragged.cu) */
 typedef struct svdbd_ragged svdbd_ragged;
 typedef struct svdbd_ragged_part {

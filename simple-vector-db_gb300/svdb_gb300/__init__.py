@@ -120,6 +120,7 @@ def _load():
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
         "svdb_find_uuid_batch": (C.c_int, [vp, C.c_char_p, sz, _i64p]),
+        "svdb_nearest_batch_median": (C.c_int, [vp, _dp, sz, sz, _i64p]),
         "svdb_server_insert_rows": (C.c_int, [vp, _dp, C.c_char_p, sz, C.POINTER(C.c_size_t)]),
         "svdb_server_find_uuid": (C.c_int, [vp, C.c_char_p, sz, _i64p]),
         "svdb_server_save": (C.c_int, [vp, C.c_char_p]),
@@ -325,6 +326,16 @@ class VectorDatabase:
         out = np.empty(q.shape[0], np.int64)
         _check(lib.svdb_nearest_batch(self.ptr, q.ctypes.data_as(_dp), q.shape[0], q.shape[1],
                                       out.ctypes.data_as(_i64p)), "svdb_nearest_batch")
+        return out
+
+    def nearest_batch_median(self, queries) -> np.ndarray:
+        """svdb_nearest_batch_median: exact 1-NN over the KD prefix by a
+        median-split tree of the current rows, ties to the lowest position."""
+        q = _f64(queries)
+        q = q.reshape(-1, q.shape[-1])
+        out = np.empty(q.shape[0], np.int64)
+        _check(lib.svdb_nearest_batch_median(self.ptr, q.ctypes.data_as(_dp), q.shape[0], q.shape[1],
+                                             out.ctypes.data_as(_i64p)), "svdb_nearest_batch_median")
         return out
 
     # -- /compare ------------------------------------------------------------
