@@ -615,6 +615,110 @@ def run_uuid(args, ws, rank, local):
     srv.close()
 
 
+def run_nearest(args, ws, rank, local):
+    """The reference's own CPU-runnable case and /nearest at scale.
+
+    Part 1 (N=10,000 x 128 U[-1,1] seed 0, KD dimension 3; 1,000 queries seed
+    1): per query, POST /nearest (the reference's insertion-order KD tree,
+    svdb_nearest_batch) plus GET /compare against 10 random stored ids with
+    cosine, Euclidean and dot (svdb_compare_batch, 30 pairs); one step = all
+    1,000 queries.  Part 2 (N=1,000,000 x 128 N(0,1) seed 2, KD dimension 3;
+    10,000 queries): /nearest through the insertion-order tree, and through
+    the opt-in median tree (device build time reported apart).  CPU baseline:
+    the oracle's restatement of kdtree_nearest and the float metrics, one
+    thread, on part 1."""
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    X, Q, kd = W.config1()
+    db = S.VectorDatabase(X.shape[0], kd)
+    db.insert_batch(X)
+    db.sync()
+    r = np.random.default_rng(1)
+    i1 = r.integers(0, X.shape[0], Q.shape[0] * 10)  # per query: 10 pairs of random stored ids
+    i2 = r.integers(0, X.shape[0], Q.shape[0] * 10)
+
+    def step():
+        near = db.nearest_batch(Q)
+        vals = [db.compare_batch(m, i1, i2)[0] for m in range(3)]
+        return near, vals
+
+    near, vals = step()  # correctness guard: the oracle's tree and metrics on a sample
+    import oracle as O
+    o = O.Oracle()
+    okd = O.OracleKD(o, kd)
+    for i in range(X.shape[0]):
+        okd.insert(X[i], i)
+    for qi in range(0, Q.shape[0], 97):
+        if okd.nearest(Q[qi]) != near[qi]:
+            raise SystemExit("bench: /nearest differs from the oracle")
+    for j in range(0, i1.size, 331):
+        for m in range(3):
+            if np.float32(o.ref_metric(m, X[i1[j]], X[i2[j]])).tobytes() != vals[m][j].tobytes():
+                raise SystemExit("bench: /compare differs from the oracle")
+    for _ in range(args.warmup):
+        step()
+    clk = Clocks(local)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t
+    clocks = clk.stop()
+    qps = Q.shape[0] * args.steps / dt
+
+    cpu = None
+    if args.cpu_sample > 0:
+        t = time.perf_counter()
+        nq_cpu = 0
+        while time.perf_counter() - t < 3.0 and nq_cpu < Q.shape[0]:
+            okd.nearest(Q[nq_cpu])
+            for j in range(10):
+                for m in range(3):
+                    o.ref_metric(m, X[i1[nq_cpu * 10 + j]], X[i2[nq_cpu * 10 + j]])
+            nq_cpu += 1
+        cpu_dt = time.perf_counter() - t
+        cpu = {"value": nq_cpu / cpu_dt, "unit": "queries/s", "cores": 1, "kind": "port",
+               "sample": f"{nq_cpu} queries (/nearest + 30 /compare each) through the oracle's restatement, "
+                         f"one thread, called per request as the handlers do ({cpu_dt:.1f} s)"}
+    db.close()
+
+    # part 2: /nearest at 1M rows
+    X2, Q2 = W.config2(1_000_000, 128, 10_000)
+    db2 = S.VectorDatabase(X2.shape[0], 3)
+    db2.insert_batch(X2)
+    db2.sync()
+    db2.nearest_batch(Q2[:16])
+    t = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        db2.nearest_batch(Q2)
+    ins_qps = Q2.shape[0] * reps / (time.perf_counter() - t)
+    t = time.perf_counter()
+    a = db2.nearest_batch_median(Q2[:16])  # the first call builds the tree
+    build_s = time.perf_counter() - t
+    t = time.perf_counter()
+    for _ in range(reps):
+        b = db2.nearest_batch_median(Q2)
+    med_qps = Q2.shape[0] * reps / (time.perf_counter() - t)
+    db2.close()
+    line = {"metric": "config-1 queries/s: /nearest + /compare x 10 ids x 3 metrics per query (N=10k x 128, kd 3)",
+            "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (float accumulation in /compare, as the reference)", "data": "synthetic",
+            "config": {"workload": "N=10,000 x 128 U[-1,1] seed 0, kd 3, 1,000 queries seed 1; per query /nearest "
+                                   "+ 30 /compare pairs; one step = the 1,000 queries as one batch of each",
+                       "l2": "store (10 MB) fits in L2: latency-bound"},
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": int(Q.nbytes + 3 * 2 * i1.nbytes),
+                    "d2h_bytes_per_step": int(Q.shape[0] * 8 + 3 * i1.size * 5)},
+            "nearest_1M": {"rows": 1_000_000, "kd_dim": 3, "queries": int(Q2.shape[0]),
+                           "insertion_order_tree_qps": ins_qps, "median_tree_qps": med_qps,
+                           "median_tree_build_s": build_s},
+            "cpu_baseline": cpu, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global N_ROWS
     ap = argparse.ArgumentParser()
@@ -628,10 +732,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid"],
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest"],
                     help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
                          "ragged: one batch over 5 collections of different dimensions; serve: the serving loop; "
-                         "uuid: GET /vector?uuid= lookups and persistence")
+                         "uuid: GET /vector?uuid= lookups and persistence; nearest: the CPU-runnable config-1 "
+                         "case (/nearest + /compare) and /nearest at 1M rows")
     ap.add_argument("--rate", type=float, default=20000.0, help="serve: offered requests/s")
     ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
@@ -651,6 +756,8 @@ def main():
         run_serve(args, ws, rank, local)
     elif args.workload == "uuid":
         run_uuid(args, ws, rank, local)
+    elif args.workload == "nearest":
+        run_nearest(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 
