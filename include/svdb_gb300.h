@@ -82,6 +82,28 @@ int svdb_nearest_batch(VectorDatabase* db, const double* queries, size_t nq, siz
                        int64_t* out_index);
 
 /*
+ * Request bodies of POST /nearest decoded on the device, in batches: the
+ * JSON text of nearest_handler_callback (src/compare_handler.c:300-390) --
+ * an array of exactly dim numbers -- to the doubles cJSON gives the
+ * reference (each number the correctly rounded value of the decimal strtod
+ * accepts).  Body i is text[offsets[i] .. offsets[i+1]) (a NUL byte ends it
+ * early, as cJSON_Parse reads a C string); out[i*dim + j] is its j-th
+ * number (NaN when status[i] != SVDB_DEC_OK).  Statuses follow the handler's
+ * checks in its order.  The grammar is cJSON's (published 1.7 sources; the
+ * reference does not pin a version): any byte <= 32 is whitespace, a UTF-8
+ * byte-order mark is skipped, content after the value is ignored, nesting up
+ * to 1000, and the children of a top-level object count like an array's.
+ */
+#define SVDB_DEC_OK 0
+#define SVDB_DEC_INVALID_JSON 1   /* 400 {"error": "Invalid JSON"} (:300-313) */
+#define SVDB_DEC_SIZE_MISMATCH 2  /* 400 {"error": "Vector size mismatch"} (:318-341) */
+#define SVDB_DEC_INVALID_DATA 3   /* 400 {"error": "Invalid vector data"} (:366-384): a child is not a number */
+#define SVDB_DEC_UNSUPPORTED 4    /* a number of more than 19 significant digits whose first 19 leave its
+                                     rounding open (not decoded; never produced by printf-style %.17g text) */
+int svdb_decode_vectors(const char* text, const uint64_t* offsets, size_t n, size_t dim, double* out,
+                        int32_t* status);
+
+/*
  * POST /nearest over a MEDIAN-split KD tree (opt-in; README.md:3,34 describes
  * one, src/kdtree.c builds an insertion-order tree instead).  The tree holds
  * the store's current rows of the store's dimension, split on the first

@@ -82,9 +82,19 @@ class Oracle:
         L.orc_store_rows.argtypes = [C.c_void_p]
         L.orc_store_nearest.restype = C.c_size_t
         L.orc_store_nearest.argtypes = [C.c_void_p, _dp]
+        L.orc_decode_body.restype = C.c_int
+        L.orc_decode_body.argtypes = [C.c_char_p, C.c_size_t, C.c_size_t, _dp]
         L.orc_find_uuid.restype = C.c_int
         L.orc_find_uuid.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t, _i64p, C.c_int]
         self.L = L
+
+    # -- POST /nearest body: cJSON_Parse + the handler's checks -------------
+    def decode_body(self, body: bytes, dim: int):
+        """(status, values): 0 ok, 1 Invalid JSON, 2 Vector size mismatch,
+        3 Invalid vector data (src/compare_handler.c:300-390)."""
+        out = np.full(max(dim, 1), np.nan)
+        st = self.L.orc_decode_body(body, len(body), dim, _ptr(out))
+        return st, out[:dim]
 
     # -- GET /vector?uuid=: the reference's linear strncmp scan -------------
     def find_uuid(self, table: bytes, keys: bytes, threads: int = 1) -> np.ndarray:

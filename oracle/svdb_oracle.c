@@ -38,6 +38,16 @@
  *       distance for Euclidean and the negated value for cosine/dot, NaN
  *       ranked last.
  *
+ *   orc_decode_body  src/compare_handler.c:300-390 -- the checks the /nearest
+ *       handler makes on its body through cJSON (the third-party JSON
+ *       library the reference links; version not pinned, restated from the
+ *       published cJSON 1.7 sources): cJSON_Parse of the text (whitespace =
+ *       bytes <= 32, a UTF-8 BOM skipped, content after the value ignored,
+ *       nesting up to 1000, cJSON's string escapes, numbers = strtod on the
+ *       run of [0-9+-eE.] characters, at most 63), then the child count
+ *       against dim, then every child a number.  Numbers come from the C
+ *       library's strtod itself, as in cJSON.
+ *
  *   orc_find_uuid src/vector_database.c:145-158 -- the linear scan of
  *       vector_db_read_by_uuid: first row whose uuid[37] equals the key
  *       under strncmp(.., 37); n keys, each scanned independently, spread
@@ -423,5 +433,185 @@ int orc_find_uuid(const char* table, size_t n, const char* keys, size_t nk, int6
         if (pthread_create(&th[t], NULL, uuid_worker, &J[t]) != 0) return -1;
     }
     for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    return 0;
+}
+
+/* ---- /nearest body decode (cJSON_Parse + the handler's checks) ----------- */
+#include <stdio.h>
+
+typedef struct {
+    const unsigned char* p;
+    size_t n; /* bytes before the first NUL */
+    size_t i;
+    int depth;
+} jcur;
+
+static void jws(jcur* c) {
+    while (c->i < c->n && c->p[c->i] <= 32) c->i++;
+}
+
+static int jhex(unsigned char ch) {
+    if (ch >= '0' && ch <= '9') return ch - '0';
+    if (ch >= 'A' && ch <= 'F') return ch - 'A' + 10;
+    if (ch >= 'a' && ch <= 'f') return ch - 'a' + 10;
+    return -1;
+}
+
+static unsigned jhex4(const unsigned char* s) {
+    unsigned h = 0;
+    for (int k = 0; k < 4; ++k) {
+        int v = jhex(s[k]);
+        if (v < 0) return 0;
+        h = (h << 4) | (unsigned)v;
+    }
+    return h;
+}
+
+static int jstring(jcur* c) {
+    if (c->i >= c->n || c->p[c->i] != '"') return 0;
+    size_t e = c->i + 1;
+    while (e < c->n && c->p[e] != '"') {
+        if (c->p[e] == '\\') {
+            if (e + 1 >= c->n) return 0;
+            e++;
+        }
+        e++;
+    }
+    if (e >= c->n) return 0;
+    for (size_t k = c->i + 1; k < e;) {
+        if (c->p[k] != '\\') {
+            k++;
+            continue;
+        }
+        unsigned char x = c->p[k + 1];
+        if (strchr("bfnrt\"\\/", x) && x) {
+            k += 2;
+        } else if (x == 'u') {
+            if (e - k < 6) return 0;
+            unsigned a = jhex4(c->p + k + 2);
+            if (a >= 0xDC00 && a <= 0xDFFF) return 0;
+            if (a >= 0xD800 && a <= 0xDBFF) {
+                if (e - (k + 6) < 6 || c->p[k + 6] != '\\' || c->p[k + 7] != 'u') return 0;
+                unsigned b = jhex4(c->p + k + 8);
+                if (b < 0xDC00 || b > 0xDFFF) return 0;
+                k += 12;
+            } else {
+                k += 6;
+            }
+        } else {
+            return 0;
+        }
+    }
+    c->i = e + 1;
+    return 1;
+}
+
+/* one value; *is_num: it was a number, *num: its value */
+static int jvalue(jcur* c, int* is_num, double* num, size_t* nchild, size_t dim, double* out, int* bad, int top);
+
+static int jnumber(jcur* c, double* v) {
+    char buf[64];
+    size_t k = 0;
+    while (k < 63 && c->i + k < c->n && strchr("0123456789+-eE.", c->p[c->i + k]) && c->p[c->i + k]) {
+        buf[k] = (char)c->p[c->i + k];
+        k++;
+    }
+    buf[k] = 0;
+    char* end = NULL;
+    *v = strtod(buf, &end);
+    if (end == buf) return 0;
+    c->i += (size_t)(end - buf);
+    return 1;
+}
+
+static int jcontainer(jcur* c, int obj, size_t* nchild, size_t dim, double* out, int* bad, int top) {
+    if (c->depth >= 1000) return 0;
+    c->depth++;
+    c->i++;
+    jws(c);
+    if (c->i < c->n && c->p[c->i] == (obj ? '}' : ']')) {
+        c->i++;
+        c->depth--;
+        return 1;
+    }
+    for (;;) {
+        jws(c);
+        if (obj) {
+            if (!jstring(c)) return 0;
+            jws(c);
+            if (c->i >= c->n || c->p[c->i] != ':') return 0;
+            c->i++;
+            jws(c);
+        }
+        int isn = 0;
+        double v = 0;
+        if (!jvalue(c, &isn, &v, NULL, 0, NULL, NULL, 0)) return 0;
+        if (top) {
+            if (*nchild < dim) {
+                out[*nchild] = v;
+                if (!isn) *bad = 1;
+            }
+            (*nchild)++;
+        }
+        jws(c);
+        if (c->i < c->n && c->p[c->i] == ',') {
+            c->i++;
+            continue;
+        }
+        if (c->i < c->n && c->p[c->i] == (obj ? '}' : ']')) {
+            c->i++;
+            c->depth--;
+            return 1;
+        }
+        return 0;
+    }
+}
+
+static int jvalue(jcur* c, int* is_num, double* num, size_t* nchild, size_t dim, double* out, int* bad, int top) {
+    *is_num = 0;
+    if (c->i >= c->n) return 0;
+    unsigned char ch = c->p[c->i];
+    if (c->n - c->i >= 4 && memcmp(c->p + c->i, "null", 4) == 0) {
+        c->i += 4;
+        return 1;
+    }
+    if (c->n - c->i >= 5 && memcmp(c->p + c->i, "false", 5) == 0) {
+        c->i += 5;
+        return 1;
+    }
+    if (c->n - c->i >= 4 && memcmp(c->p + c->i, "true", 4) == 0) {
+        c->i += 4;
+        return 1;
+    }
+    if (ch == '"') return jstring(c);
+    if (ch == '-' || (ch >= '0' && ch <= '9')) {
+        *is_num = 1;
+        return jnumber(c, num);
+    }
+    if (ch == '[' || ch == '{') return jcontainer(c, ch == '{', nchild, dim, out, bad, top);
+    return 0;
+}
+
+/* status as the /nearest handler decides it: 0 ok, 1 "Invalid JSON",
+ * 2 "Vector size mismatch", 3 "Invalid vector data"; out: dim values */
+int orc_decode_body(const char* text, size_t len, size_t dim, double* out) {
+    jcur c;
+    c.p = (const unsigned char*)text;
+    c.n = len;
+    for (size_t k = 0; k < len; ++k)
+        if (text[k] == 0) {
+            c.n = k;
+            break;
+        }
+    c.i = 0;
+    c.depth = 0;
+    if (c.n >= 4 && c.p[0] == 0xEF && c.p[1] == 0xBB && c.p[2] == 0xBF) c.i = 3;
+    jws(&c);
+    size_t nchild = 0;
+    int bad = 0, isn = 0;
+    double v = 0;
+    if (!jvalue(&c, &isn, &v, &nchild, dim, out, &bad, 1)) return 1;
+    if (nchild != dim) return 2;
+    if (bad) return 3;
     return 0;
 }

@@ -332,6 +332,21 @@ SVDB_API int svdb_search_topk_fp64_noalloc(VectorDatabase* db, const double* d_q
     return rc;
 }
 
+/* ---- POST /nearest bodies decoded on the device --------------------------- */
+SVDB_API int svdb_decode_vectors(const char* text, const uint64_t* offsets, size_t n, size_t dim, double* out,
+                                 int32_t* status) {
+    if (n && (!text || !offsets || !out || !status)) {
+        svdb_set_error("svdb_decode_vectors: NULL argument");
+        return SVDB_EINVAL;
+    }
+    for (size_t i = 0; i < n; ++i)
+        if (offsets[i + 1] < offsets[i]) {
+            svdb_set_error("svdb_decode_vectors: offsets must not decrease (body %zu)", i);
+            return SVDB_EINVAL;
+        }
+    return svdbd_decode_bodies(text, offsets, n, dim, out, status);
+}
+
 /* ---- GET /vector?uuid= in batches ---------------------------------------- */
 SVDB_API int svdb_find_uuid_batch(VectorDatabase* db, const char* uuids, size_t n, int64_t* out_index) {
     if (!db || (n && (!uuids || !out_index))) {

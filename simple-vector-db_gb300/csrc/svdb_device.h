@@ -92,6 +92,10 @@ int svdbd_store_read_block(svdbd_store* s, int64_t first, size_t n, double* rows
  * (dev_kdm.cu); q: nq host rows of qstride doubles; out: positions (-1: none) */
 int svdbd_kdm_nearest(svdbd_store* s, size_t kdim, const double* q, size_t nq, size_t qstride, int64_t* out_pos);
 
+/* POST /nearest bodies decoded on the device (dev_decode.cu): n bodies at
+ * text[off[i] .. off[i+1]) -> n x dim doubles and a SVDB_DEC_* status each */
+int svdbd_decode_bodies(const char* text, const uint64_t* off, size_t n, size_t dim, double* out, int32_t* status);
+
 /* ragged batch over several stores, replayed as one CUDA graph (dev_ragged.cu) */
 typedef struct svdbd_ragged svdbd_ragged;
 typedef struct svdbd_ragged_part {

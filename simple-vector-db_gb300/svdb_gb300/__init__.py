@@ -120,6 +120,7 @@ def _load():
         "svdb_search_topk_fp64_noalloc": (C.c_int, [vp, vp, sz, sz, sz, C.c_int, vp, vp]),
         "svdb_profile_read": (C.c_int, [vp, _dp, C.c_int]),
         "svdb_find_uuid_batch": (C.c_int, [vp, C.c_char_p, sz, _i64p]),
+        "svdb_decode_vectors": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint64), sz, sz, _dp, C.POINTER(C.c_int32)]),
         "svdb_nearest_batch_median": (C.c_int, [vp, _dp, sz, sz, _i64p]),
         "svdb_server_insert_rows": (C.c_int, [vp, _dp, C.c_char_p, sz, C.POINTER(C.c_size_t)]),
         "svdb_server_find_uuid": (C.c_int, [vp, C.c_char_p, sz, _i64p]),
@@ -187,6 +188,23 @@ def uuid_block(uuids) -> bytes:
         b = u.encode() if isinstance(u, str) else bytes(u)
         out += b[:37].ljust(37, b"\0")
     return bytes(out)
+
+
+def decode_vectors(bodies, dim: int):
+    """svdb_decode_vectors: POST /nearest bodies (bytes each) decoded on the
+    device -> (values [n, dim] float64, status [n] int32, SVDB_DEC_*)."""
+    text = b"".join(bodies)
+    off = np.zeros(len(bodies) + 1, np.uint64)
+    off[1:] = np.cumsum([len(b) for b in bodies])
+    out = np.empty((len(bodies), dim), np.float64)
+    st = np.empty(len(bodies), np.int32)
+    _check(lib.svdb_decode_vectors(text, off.ctypes.data_as(C.POINTER(C.c_uint64)), len(bodies), dim,
+                                   out.ctypes.data_as(_dp), st.ctypes.data_as(C.POINTER(C.c_int32))),
+           "svdb_decode_vectors")
+    return out, st
+
+
+DEC_OK, DEC_INVALID_JSON, DEC_SIZE_MISMATCH, DEC_INVALID_DATA, DEC_UNSUPPORTED = range(5)
 
 
 def cosine_similarity(a, b) -> np.float32:
