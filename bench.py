@@ -719,6 +719,68 @@ def run_nearest(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_decode(args, ws, rank, local):
+    """POST /nearest request bodies decoded on the device: batches of 4,096
+    bodies, each a JSON array of 768 numbers written with %.17g (N(0,1) x
+    10^U[-8,8), seed 7; ~18 MB of text per batch), through svdb_decode_vectors
+    (host text in, host doubles out: copies inside the timed region).  CPU
+    baseline: the oracle's restatement of cJSON_Parse + strtod, one thread."""
+    import svdb_gb300 as S
+    import torch
+
+    torch.cuda.set_device(local)
+    nb, dim = 4096, 768
+    rng = np.random.default_rng(7)
+    X = rng.normal(size=(nb, dim)) * 10.0 ** rng.integers(-8, 8, (nb, 1))
+    bodies = [("[" + ",".join("%.17g" % x for x in row) + "]").encode() for row in X]
+    text = b"".join(bodies)
+    off = np.zeros(nb + 1, np.uint64)
+    off[1:] = np.cumsum([len(b) for b in bodies])
+    out = np.empty((nb, dim), np.float64)
+    st = np.empty(nb, np.int32)
+
+    def step():
+        S._check(S.lib.svdb_decode_vectors(text, off.ctypes.data_as(C.POINTER(C.c_uint64)), nb, dim,
+                                           out.ctypes.data_as(S._dp), st.ctypes.data_as(C.POINTER(C.c_int32))),
+                 "svdb_decode_vectors")
+
+    step()
+    if not (st == 0).all() or out.tobytes() != X.tobytes():  # %.17g round-trips every double
+        raise SystemExit("bench: decoded values differ from the encoded doubles")
+    for _ in range(args.warmup):
+        step()
+    clk = Clocks(local)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t
+    clocks = clk.stop()
+    cpu = None
+    if args.cpu_sample > 0:
+        import oracle as O
+        o = O.Oracle()
+        t = time.perf_counter()
+        m = 0
+        while m < nb and time.perf_counter() - t < 3.0:
+            s_, v = o.decode_body(bodies[m], dim)
+            if s_ != 0 or v.tobytes() != X[m].tobytes():
+                raise SystemExit("bench: the oracle's decode disagrees")
+            m += 1
+        cdt = time.perf_counter() - t
+        cpu = {"value": m / cdt, "unit": "bodies/s", "cores": 1, "kind": "port",
+               "sample": f"{m} bodies through the oracle's cJSON_Parse + strtod restatement, one thread ({cdt:.1f} s)"}
+    line = {"metric": "POST /nearest bodies decoded per second (768 numbers each, %.17g text)", "value": nb * args.steps / dt,
+            "unit": "bodies/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8 text -> f64", "data": "synthetic",
+            "config": {"workload": f"4096 bodies x 768 numbers (%.17g), {len(text) / 1e6:.1f} MB of JSON text per batch",
+                       "l2": "text larger than L2 per batch; no flush needed"},
+            "e2e": {"value": nb * args.steps / dt, "unit": "bodies/s", "h2d_bytes_per_step": int(len(text) + off.nbytes),
+                    "d2h_bytes_per_step": int(out.nbytes + st.nbytes)},
+            "text_gbs": len(text) * args.steps / dt / 1e9, "cpu_baseline": cpu, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global N_ROWS
     ap = argparse.ArgumentParser()
@@ -732,11 +794,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest"],
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest", "decode"],
                     help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
                          "ragged: one batch over 5 collections of different dimensions; serve: the serving loop; "
                          "uuid: GET /vector?uuid= lookups and persistence; nearest: the CPU-runnable config-1 "
-                         "case (/nearest + /compare) and /nearest at 1M rows")
+                         "case (/nearest + /compare) and /nearest at 1M rows; decode: /nearest bodies decoded on the GPU")
     ap.add_argument("--rate", type=float, default=20000.0, help="serve: offered requests/s")
     ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
@@ -758,6 +820,8 @@ def main():
         run_uuid(args, ws, rank, local)
     elif args.workload == "nearest":
         run_nearest(args, ws, rank, local)
+    elif args.workload == "decode":
+        run_decode(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 
