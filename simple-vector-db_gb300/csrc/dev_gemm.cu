@@ -1076,43 +1076,16 @@ __device__ __forceinline__ float2 refine_interval(float p, float gamma, float qq
     return make_float2(L, U);
 }
 
-// The per-row key and bound are interval arithmetic in FP32 with directed
-// rounding (GB300's FP64 pipe is narrow; one FP64 instruction per row per warp
-// would dominate): |q|^2 and |x|^2 enter as [rd, ru] pairs, d^2 as [S - E, S + E].
-// Each survivor's refined {L, U} goes to `lu` (the candidate list's storage,
-// dead after the select), so no per-thread state limits the occupancy.
-__global__ void __launch_bounds__(kRefThreads, 3) k_refine(const float* __restrict__ x32, size_t ld,
-                                                           const float* __restrict__ q32,
-                                                           const double* __restrict__ qsq,
-                                                           const float4* __restrict__ sqf,
-                                                           const float4* __restrict__ rowp,
-                                                           const float4* __restrict__ qpar, int2* __restrict__ surv,
-                                                           const int* __restrict__ nsurv, int* __restrict__ nref,
-                                                           float2* __restrict__ lu, size_t lu_stride, int k, int metric,
-                                                           const int* __restrict__ perm, uint8_t* __restrict__ flags) {
-    extern __shared__ __align__(16) uint8_t sm[];
-    float* qs = reinterpret_cast<float*>(sm);  // the query in FP32 (ld floats)
-    __shared__ int hist[256];
-    __shared__ uint32_t s_sh[3];
-    __shared__ int s_out;
+// Scores the survivors of query q in FP32 (one half warp per row, the
+// query's FP32 copy `qs` in shared memory) and writes each survivor's refined
+// {L, U} to luq.  Rows base = (split * warps + warp) * 2 + half, stepping by
+// splits * warps * 2.
+__device__ __forceinline__ void refine_rows(const float* __restrict__ x32, size_t ld, const float* qs,
+                                            const float4* __restrict__ sqf, const float4* __restrict__ rowp,
+                                            const int2* sq, int n, float2* luq, float gamma, float qq_lo,
+                                            float qq_hi, float qn_up, int metric, int split, int splits) {
     constexpr int kWarps = kRefThreads / 32;
-    const int q = perm ? perm[blockIdx.x] : blockIdx.x;
-    const int split = blockIdx.y, splits = gridDim.y;  // splits > 1: k_refine_keep finishes
-    if (flags[q] != scr::kOk) {
-        if (threadIdx.x == 0 && split == 0) nref[q] = 0;
-        return;
-    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = q32[(size_t)q * ld + i];
-    __syncthreads();
-    const int n = nsurv[q];
-    int2* sq = surv + (size_t)q * scr::kSurvCap;
-    float2* luq = lu + (size_t)q * lu_stride;
-    const double qq = qsq[q];
-    const float qq_lo = __double2float_rd(qq), qq_hi = __double2float_ru(qq);
-    const float qn_up = qpar[q].x;
-    // each lane: ld/64 steps into each of 4 accumulators, then 2 + 4 additions
-    const float gamma = (float)(ld / 64 + 8) * 5.9604644775390625e-08f * 1.0001f;
     // half a warp per row: lane h of the half reads float4 h, h+16, ...
     // Software-pipelined: the next row's index and norm intervals are fetched
     // while this row's 3 KB are read and reduced, so a row costs one memory
@@ -1161,6 +1134,43 @@ __global__ void __launch_bounds__(kRefThreads, 3) k_refine(const float* __restri
         }
         if (act && h == 0) luq[i] = refine_interval(p, gamma, qq_lo, qq_hi, qn_up, xb, xn_up, metric);
     }
+}
+
+// The per-row key and bound are interval arithmetic in FP32 with directed
+// rounding (GB300's FP64 pipe is narrow; one FP64 instruction per row per warp
+// would dominate): |q|^2 and |x|^2 enter as [rd, ru] pairs, d^2 as [S - E, S + E].
+// Each survivor's refined {L, U} goes to `lu` (the candidate list's storage,
+// dead after the select), so no per-thread state limits the occupancy.
+__global__ void __launch_bounds__(kRefThreads, 3) k_refine(const float* __restrict__ x32, size_t ld,
+                                                           const float* __restrict__ q32,
+                                                           const double* __restrict__ qsq,
+                                                           const float4* __restrict__ sqf,
+                                                           const float4* __restrict__ rowp,
+                                                           const float4* __restrict__ qpar, int2* __restrict__ surv,
+                                                           const int* __restrict__ nsurv, int* __restrict__ nref,
+                                                           float2* __restrict__ lu, size_t lu_stride, int k, int metric,
+                                                           const int* __restrict__ perm, uint8_t* __restrict__ flags) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    float* qs = reinterpret_cast<float*>(sm);  // the query in FP32 (ld floats)
+    __shared__ int hist[256];
+    __shared__ uint32_t s_sh[3];
+    __shared__ int s_out;
+    const int q = perm ? perm[blockIdx.x] : blockIdx.x;
+    const int split = blockIdx.y, splits = gridDim.y;  // splits > 1: k_refine_keep finishes
+    if (flags[q] != scr::kOk) {
+        if (threadIdx.x == 0 && split == 0) nref[q] = 0;
+        return;
+    }
+    for (size_t i = threadIdx.x; i < ld; i += blockDim.x) qs[i] = q32[(size_t)q * ld + i];
+    const int n = nsurv[q];
+    int2* sq = surv + (size_t)q * scr::kSurvCap;
+    __syncthreads();
+    float2* luq = lu + (size_t)q * lu_stride;
+    const double qq = qsq[q];
+    // each lane: ld/64 steps into each of 4 accumulators, then 2 + 4 additions
+    const float gamma = (float)(ld / 64 + 8) * 5.9604644775390625e-08f * 1.0001f;
+    refine_rows(x32, ld, qs, sqf, rowp, sq, n, luq, gamma, __double2float_rd(qq), __double2float_ru(qq), qpar[q].x,
+                metric, split, splits);
     if (splits == 1) {
         __syncthreads();
         refine_keep(q, n, k, luq, sq, nref, hist, s_sh, &s_out);
@@ -1176,7 +1186,10 @@ __global__ void __launch_bounds__(kRefThreads) k_refine_keep(const int2* __restr
     __shared__ uint32_t s_sh[3];
     __shared__ int s_out;
     const int q = blockIdx.x;
-    if (flags[q] != scr::kOk) return;  // nref already 0
+    if (flags[q] != scr::kOk) {
+        if (threadIdx.x == 0) nref[q] = 0;
+        return;
+    }
     refine_keep(q, nsurv[q], k, lu + (size_t)q * lu_stride, surv + (size_t)q * scr::kSurvCap, nref, hist, s_sh,
                 &s_out);
 }
@@ -1366,6 +1379,7 @@ struct GemmPlanCache {
     bool select_attr = false;
     bool sort_attr = false;
     bool rerank_attr = false;
+    bool refine_attr = false;
     size_t screen_smem = 0;
 };
 
@@ -1653,6 +1667,10 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     SVDB_LAUNCH_CHECK();
     s->prof_mark(3);
     const size_t ref_smem = s->ld * sizeof(float);
+    if (!gc->refine_attr) {
+        SVDB_CUDA(cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        gc->refine_attr = true;
+    }
     // refinement order (batches of up to 16384 queries are sorted; larger ones keep index order)
     const int* order = nullptr;
     if (nq > 1 && nq <= 16384) {

@@ -211,10 +211,12 @@ def test_bf16_cosine_dead_and_zero_rows(S, oracle):
 
 @pytest.mark.parametrize("metric", [0, 1, 2])
 def test_bf16_grouped_refinement(S, oracle, metric):
-    """Batches larger than two queries per SM: one refinement block per query,
-    in the order of the sorted survivor signatures.  Uneven clusters (a few
-    hundred to 2,600 near-ties) and queries between two centres (survivors
-    from two clusters) on the same batch."""
+    """Batches larger than two queries per SM: queries sorted by survivor
+    signature and refined in groups of up to 4 sharing a signature (each
+    distinct row read once per group).  Uneven clusters (a few hundred to
+    2,600 near-ties: groups past 4,096 survivor entries take the one-query-
+    at-a-time path) and queries between two centres (survivors from two
+    clusters, so group members' survivor sets differ) on the same batch."""
     rng = np.random.default_rng(700 + metric)
     d = 60
     C = rng.normal(size=(40, d))
@@ -257,4 +259,25 @@ def test_bf16_separated_top_rows_in_first_tiles(S, oracle, metric):
             assert np.array_equal(ids, wid), (k, ids, wid)
             assert np.array_equal(vals, wval)
             assert st.bound_failures == 0
+    db.close()
+
+
+@pytest.mark.parametrize("d", [768, 1000])
+def test_bf16_grouped_refinement_wide_rows(S, oracle, d):
+    """Grouped refinement at wide rows (768: 12 float4 per lane; 1000: rows
+    padded to 1008, 16 per lane): 400 queries over 20 clusters, ids and
+    values identical to the oracle for k = 10 and 100."""
+    rng = np.random.default_rng(900 + d)
+    C = rng.normal(size=(20, d))
+    X = C[rng.integers(0, 20, 6000)] + 0.05 * rng.normal(size=(6000, d))
+    Q = C[rng.integers(0, 20, 400)] + 0.05 * rng.normal(size=(400, d))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for metric in (0, 1):
+        for k in (10, 100):
+            ids, vals, st = _search_both(S, db, Q, k, metric)
+            wid, wval = oracle.topk(metric, X, Q, k)
+            assert np.array_equal(ids, wid), (metric, k)
+            assert np.array_equal(vals, wval), (metric, k)
+            assert st.bound_failures == 0 and st.widened == 0, (metric, k)
     db.close()
