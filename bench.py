@@ -3,7 +3,7 @@
 3), query batches drawn from the same mixture.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision bf16|fp64] [--q Q] [--metric cosine|euclidean|dot]
+                    [--precision bf16|fp8|fp64] [--q Q] [--metric cosine|euclidean|dot]
 
 One step = one batch of Q queries answered end to end by the library's
 top-k search.  `value` is queries/s with queries and results resident in HBM
@@ -160,7 +160,7 @@ def run_ours(args, ws, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     metric = METRICS[args.metric]
-    prec = S.PREC_BF16 if args.precision == "bf16" else S.PREC_FP64
+    prec = {"bf16": S.PREC_BF16, "fp8": S.PREC_FP8, "fp64": S.PREC_FP64}[args.precision]
     nq, k = args.q, K_TOP
 
     t0 = time.perf_counter()
@@ -275,6 +275,13 @@ def run_ours(args, ws, rank, local):
                 "traffic": traffic, "traffic_unit": "bytes per launch (ncu, scaled by rows)",
                 "algorithmic_bytes": N_ROWS * DIM * 2 + nq * DIM * 2, "peak_source": src, "kernel_ms": scr,
                 "algorithmic": f"2*Q*N*D = {flops:.3e} FLOP per launch"}
+    elif prec == S.PREC_FP8:
+        # dense FP8 runs at twice the BF16 rate on this part; the measured BF16 peak x 2 is the denominator
+        flops = 2.0 * nq * N_ROWS * DIM
+        ach = flops / (scr / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": 2 * bf16, "unit": "TFLOP/s", "frac": ach / (2 * bf16),
+                "traffic": None, "algorithmic_bytes": N_ROWS * DIM + nq * DIM, "peak_source": src + " bf16 x 2",
+                "kernel_ms": scr, "algorithmic": f"2*Q*N*D = {flops:.3e} FLOP per launch (E4M3)"}
     else:
         nbytes = N_ROWS * (DIM * 8 + 1)
         ach = nbytes / (scr / 1e3) / 1e9
@@ -291,7 +298,8 @@ def run_ours(args, ws, rank, local):
     if rank == 0:
         line = {"metric": METRIC_NAME, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "bf16+f64" if prec == S.PREC_BF16 else "f64", "data": "synthetic",
+                "vs_baseline": None, "dtype": {S.PREC_BF16: "bf16+f64", S.PREC_FP8: "e4m3+f32+f64"}.get(prec, "f64"),
+                "data": "synthetic",
                 "config": {"workload": f"1M x 768 FP64 Gaussian mixture (1024 centres, sigma 0.05, seed 3), "
                                        f"exact top-{k} {args.metric}, {args.precision}",
                            "query_batch": nq, "precision": args.precision, "parallelism": f"replicas{ws}",
@@ -788,7 +796,7 @@ def main():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp64"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp8", "fp64"])
     ap.add_argument("--q", type=int, default=None, help="queries per step")
     ap.add_argument("--metric", default="cosine", choices=list(METRICS))
     ap.add_argument("--cpu-sample", type=int, default=64)
@@ -806,7 +814,7 @@ def main():
     args = ap.parse_args()
     N_ROWS = args.rows
     if args.q is None:
-        args.q = 4096 if args.precision == "bf16" else 64
+        args.q = 64 if args.precision == "fp64" else 4096
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)

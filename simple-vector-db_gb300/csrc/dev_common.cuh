@@ -42,6 +42,18 @@ __host__ __device__ inline size_t bf16_tile_index(int64_t slot, size_t e, size_t
     return (((t * (ldb >> 6) + kb) << 8) + r) * 64u + ((c ^ (r & 7u)) << 3) + w;
 }
 
+// The FP8 (E4M3) cosine shadow uses the same tiles in bytes: 256 rows x 128
+// elements (one 128-byte swizzle row each), 16-element chunks swizzled; ldb8
+// is a multiple of 128.  Byte index of element e of row `slot`.
+__host__ __device__ inline size_t f8_tile_index(int64_t slot, size_t e, size_t ldb8) {
+    const size_t t = (size_t)slot >> 8, r = (size_t)slot & 255u, kb = e >> 7, c = (e >> 4) & 7u, w = e & 15u;
+    return (((t * (ldb8 >> 7) + kb) << 8) + r) * 128u + ((c ^ (r & 7u)) << 4) + w;
+}
+
+// Power-of-two scale of the FP8 unit-norm shadow: |x/|x|| <= 1 per element,
+// so 256 x/|x| stays inside E4M3's 448 and the key's rescaling is exact.
+constexpr double kF8RowScale = 256.0;
+
 static inline size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
 
 // ---------------------------------------------------------------------------

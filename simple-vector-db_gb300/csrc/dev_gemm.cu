@@ -48,6 +48,8 @@
 
 #include "dev_search.cuh"
 
+#include <cuda_fp8.h>
+
 namespace svdb {
 
 namespace scr {
@@ -177,6 +179,16 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// D[tmem] (+)= A[smem] . B[smem]^T, both K-major E4M3 (32 per K step), FP32 accumulate
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
 // arrive on `bar` once every tcgen05 op issued so far by this thread has completed
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -223,6 +235,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
     return (1u << 4)                     // D format: F32
            | (1u << 7)                   // A format: BF16
            | (1u << 10)                  // B format: BF16
+           | ((uint32_t)(n >> 3) << 17)  // N / 8
+           | ((uint32_t)(m >> 4) << 24); // M / 16
+}
+// instruction descriptor, kind::f8f6f4: E4M3 x E4M3 -> FP32, both K-major
+__host__ __device__ constexpr uint32_t idesc_e4m3(int m, int n) {
+    return (1u << 4)                     // D format: F32
+           | (0u << 7)                   // A format: E4M3
+           | (0u << 10)                  // B format: E4M3
            | ((uint32_t)(n >> 3) << 17)  // N / 8
            | ((uint32_t)(m >> 4) << 24); // M / 16
 }
@@ -309,7 +329,8 @@ __device__ __forceinline__ ScreenSeg sched_seg(const ScreenSched& S, int sg) {
 }
 
 struct ScreenParams {
-    const __nv_bfloat16* xblk;  // the BF16 shadow being screened, in 256 x 64 swizzled tiles
+    const uint8_t* xblk;  // the shadow being screened, in swizzled 256-row x 128-byte tiles (BF16 or E4M3)
+    const float* qscale;  // FP8: per query, the exact power of two from accumulator units to key units
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
     const float4* spar;  // per row {mult, b, m, 2^-19 m}: the screen's one-FMA form of the bound
     const int* alpha;    // max over rows of a/b (float bits): |q| a <= |q| alpha b
@@ -332,9 +353,14 @@ struct ScreenParams {
 //   E = |q| max|x/|x| - bxn| + eqq max|bxn| + eq0;
 // the epilogue is a max, a compare and a mask per element, and a validity
 // bit per row keeps dead, zero and padding rows out of the lower bounds.
-template <int KL, bool NORM>
+// F8 (cosine only): E4M3 operands, kind::f8f6f4 with 128 elements per stage;
+// the accumulator is in units of 2^e times the key (query scale x 256), so
+// thresholds are scaled into accumulator units once per tile and emitted
+// keys back once per candidate, both exactly (powers of two).
+template <int KL, bool NORM, bool F8 = false>
 __global__ void __launch_bounds__(scr::kThreads, 1)
     k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const ScreenParams P) {
+    static_assert(!F8 || NORM, "the FP8 screen is the cosine screen");
     using namespace scr;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -399,9 +425,9 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         break;
                     }
                     mbar_expect_tx(&S.full[stage], kStageA + kStageB);
-                    tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * kBK, qt * kBM);
+                    tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * (F8 ? 2 * kBK : kBK), qt * kBM);
                     // the store tile: one contiguous 32 KB block, already swizzled
-                    bulk_load(S.b[stage], P.xblk + ((size_t)r * KB + kb) * (kBN * kBK), kStageB, &S.full[stage]);
+                    bulk_load(S.b[stage], P.xblk + ((size_t)r * KB + kb) * kStageB, kStageB, &S.full[stage]);
                     ++issued;
                     if (++stage == kStages) {
                         stage = 0;
@@ -427,7 +453,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
     } else if (warp == 1) {
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(kBM, kBN);
+            constexpr uint32_t idesc = F8 ? idesc_e4m3(kBM, kBN) : idesc_bf16(kBM, kBN);
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
@@ -448,8 +474,12 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     const uint64_t ad = sdesc_sw128(smem_u32(S.a[stage]));
                     const uint64_t bd = sdesc_sw128(smem_u32(S.b[stage]));
 #pragma unroll
-                    for (int kk = 0; kk < kBK / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle row
-                        mma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
+                    for (int kk = 0; kk < kBK / 16; ++kk) {  // +32 bytes per K step (16 BF16 or 32 E4M3)
+                        if constexpr (F8)
+                            mma_f8(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
+                        else
+                            mma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
+                    }
                     mma_commit(&S.empty[stage]);
                     if (++stage == kStages) {
                         stage = 0;
@@ -479,6 +509,12 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         const int q = seg.qt * kBM + qi;
         float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0 (NORM: eq0 = E)
         bool valid = false;
+        // F8: key = accumulator x cs, cs a power of two (so both directions are exact)
+        float cs = 1.f, ics = 1.f;
+        if (F8 && q < P.nq) {
+            cs = P.qscale[q];
+            ics = __frcp_rn(cs);
+        }
         if (q < P.nq) {
             const float4 qp = P.qpar[q];
             if (NORM) {
@@ -540,7 +576,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
 #pragma unroll
                         for (int i = 0; i < kChunk; ++i) {
                             // masked rows are NaN: every comparison with them is false
-                            const float l = ((vb >> i) & 1u) ? __fsub_rd(__uint_as_float(v[i]), eq0) : __int_as_float(0x7fc00000);
+                            const float l = ((vb >> i) & 1u) ? __fsub_rd(F8 ? __uint_as_float(v[i]) * cs : __uint_as_float(v[i]), eq0) : __int_as_float(0x7fc00000);
                             maxl = fmaxf(maxl, l);
                             if (valid && l > top.mn) top.push(l);
                         }
@@ -570,7 +606,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
             // the query's eq0 is folded into the threshold and the maxima
-            const float thr2 = __fsub_rd(thr, eq0);
+            // in accumulator units (F8: exact rescale by a power of two)
+            const float thr2 = F8 ? __fsub_rd(thr, eq0) * ics : __fsub_rd(thr, eq0);
             constexpr int C = NORM ? 32 : 16;  // accumulator columns per collective load
             float tmax = -INFINITY;            // best lower bound (less eq0) of this warp's 128 rows
 #pragma unroll 1
@@ -648,7 +685,9 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                             if ((any >> i) & 1u) {  // warp-uniform
                                 const int slot = base + __popc(mask & ((1u << i) - 1u));
                                 if (((mask >> i) & 1u) && slot < P.subcap)
-                                    cq[slot] = make_int2(rw + 8 * g + i, (int)v[8 * g + i]);
+                                    cq[slot] = make_int2(rw + 8 * g + i,
+                                                         F8 ? __float_as_int(__uint_as_float(v[8 * g + i]) * cs)
+                                                            : (int)v[8 * g + i]);
                             }
                         }
                     }
@@ -663,7 +702,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // offsets; the warm-up tile's rows are already in the bins as chunks
             // and are not published a second time (a row in two bins would make
             // their minimum exceed the k-th best lower bound).
-            const float maxl = __fsub_rd(tmax, eq0);
+            const float maxl = __fsub_rd(F8 ? tmax * cs : tmax, eq0);
             if (valid && js > 0 && maxl > thr) {
                 const int unit = 2 * kWarmUnits * nsq + (js - 1) * 2 * nsq + 2 * seg.sub + half;
                 atomicMax(&P.bins[(size_t)q * P.k + unit % P.k], f2ord(maxl));
@@ -752,6 +791,85 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
         p.z = __double2float_ru(eq0);
         p.w = ok && isfinite(p.x) && isfinite(p.y) ? 1.0f : 0.0f;
         qpar[qi] = p;
+    }
+}
+
+// The FP8 (cosine) form of k_prep_bf16: the query scaled by a power of two
+// 2^e (the largest with max |q_i| 2^e <= 448, E4M3's largest finite value),
+// its E4M3 copy (nq x ldb8 bytes, zero padded), the FP32 copy for the
+// refinement, the bound terms and qscale = 2^-(e+8): key = accumulator x
+// qscale exactly (the store's shadow carries 256 x/|x|).  The tensor core's
+// accumulation of E4M3 products is modelled pessimistically, as if each K=32
+// step kept only 13 bits: c_acc = (ldb8/32 + 1) x 40 x 2^-13 of |bq| |bx|
+// (for D = 768 about 0.12; the E4M3 rounding itself is ~0.04 per vector).
+__global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
+                          size_t ldb8, uint8_t* __restrict__ q8, float* __restrict__ q32, float4* __restrict__ qpar,
+                          float* __restrict__ qscale) {
+    const int lane = threadIdx.x & 31, s = lane & 3;
+    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
+    const bool active = qi < nq;
+    const double* src = qbuf + (size_t)(active ? qi : 0) * ld;
+    double m = 0.0;
+    bool finite = true;
+    if (active)
+        for (size_t j = s; j < ld; j += 4) {
+            const double a = src[j];
+            finite = finite && isfinite(a);
+            m = fmax(m, fabs(a));
+        }
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 1));
+    int e = 0;
+    if (m > 0.0 && isfinite(m)) {
+        e = (int)floor(log2(448.0 / m));
+        while (m * ldexp(1.0, e) > 448.0) --e;
+    }
+    const double sc = ldexp(1.0, e);
+    double res = 0.0, bsq = 0.0;
+    if (active) {
+        uint8_t* dst = q8 + (size_t)qi * ldb8;
+        float* dst32 = q32 + (size_t)qi * ld;
+        for (size_t j = 2 * s; j < ld; j += 8) {
+            const double a = src[j], c = src[j + 1];
+            const __nv_fp8_storage_t ea = __nv_cvt_double_to_fp8(a * sc, __NV_SATFINITE, __NV_E4M3);
+            const __nv_fp8_storage_t ec = __nv_cvt_double_to_fp8(c * sc, __NV_SATFINITE, __NV_E4M3);
+            const double fa = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(ea, __NV_E4M3))) / sc;
+            const double fc = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(ec, __NV_E4M3))) / sc;
+            bsq = fma(fa, fa, bsq);
+            bsq = fma(fc, fc, bsq);
+            res = fma(a - fa, a - fa, res);
+            res = fma(c - fc, c - fc, res);
+            dst[j] = ea;
+            dst[j + 1] = ec;
+            *reinterpret_cast<float2*>(dst32 + j) = make_float2(__double2float_rn(a), __double2float_rn(c));
+        }
+        for (size_t j = ld + 2 * s; j < ldb8; j += 8) {
+            dst[j] = 0;
+            dst[j + 1] = 0;
+        }
+    }
+    res = group4_sum(res);
+    bsq = group4_sum(bsq);
+    const unsigned all_finite = __all_sync(0xffffffffu, finite);
+    if (active && s == 0) {
+        const double sq = qsq[qi];
+        const double up = 1.0 + 9.313225746154785e-10;
+        const double qn = sqrt(sq) * up;
+        const double eq = sqrt(res) * up;
+        const double bqn = sqrt(bsq) * up;
+        const double cacc = (double)(ldb8 / 32 + 1) * 40.0 * 1.220703125e-04;
+        const double eqq = (eq + cacc * bqn) * (1.0 + 9.5367431640625e-07) + 3.637978807091713e-12 * qn +
+                           9.5367431640625e-07 * (1.0 + cacc) * 1.02 * bqn;
+        const double eq0 = 9.094947017729282e-13 * qn + 1e-30;
+        // the key's rescale 2^-(e+8) stays a normal FP32 power of two
+        const bool ok = all_finite && isfinite(sq) && sq < 1e30 && sq > 0.0 && e > -100 && e < 100;
+        float4 p;
+        p.x = __double2float_ru(qn);
+        p.y = __double2float_ru(eqq);
+        p.z = __double2float_ru(eq0);
+        p.w = ok && isfinite(p.x) && isfinite(p.y) ? 1.0f : 0.0f;
+        qpar[qi] = p;
+        qscale[qi] = (float)ldexp(1.0, -(e + 8));
     }
 }
 
@@ -1375,7 +1493,7 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 // ---------------------------------------------------------------------------
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    bool attr_set[6] = {false, false, false, false, false, false};
+    bool attr_set[9] = {false, false, false, false, false, false, false, false, false};
     bool select_attr = false;
     bool sort_attr = false;
     bool rerank_attr = false;
@@ -1429,8 +1547,24 @@ static int make_map(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t r
     return SVDB_OK;
 }
 
+// E4M3 queries: the tensor map of make_map over bytes (128-element boxes)
+static int make_map8(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t rows, size_t ldb8, int box_rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)ldb8, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ldb8};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * scr::kBK), (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = c->encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        svdb_set_error("search_fp8: cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return SVDB_ECUDA;
+    }
+    return SVDB_OK;
+}
+
 struct Bf16Layout {
-    size_t qb, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
+    size_t qb, qscale, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     int ntr, cap;
     int nctas, nsub, subcap;
     size_t npad;
@@ -1513,7 +1647,8 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     };
     L.ntr = (int)((std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN);
     L.npad = (size_t)L.ntr * scr::kBN;
-    L.qb = take(nq * s->ldb * 2);
+    L.qb = take(std::max(nq * s->ldb * 2, nq * s->ldb8));  // BF16 queries, or the E4M3 ones
+    L.qscale = take(nq * sizeof(float));
     L.q32 = take(nq * s->ld * sizeof(float));
     L.qpar = take(nq * sizeof(float4));
     L.rpar = take(L.npad * sizeof(float4));
@@ -1559,7 +1694,7 @@ size_t search_bf16_scratch(const Store* s, size_t nq, size_t k) { return bf16_la
 
 bool bf16_supported(const Store* s, size_t k) { return k <= k_max_bf16 && s->n_unscreen == 0 && s->nlive > 0; }
 
-int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st) {
+int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st, bool f8) {
     GemmPlanCache* gc = nullptr;
     int rc = gemm_cache(s, &gc);
     if (rc) return rc;
@@ -1592,30 +1727,38 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     const int nq = (int)a.nq, k = (int)a.k;
     uint32_t kernels = 0;
 
-    k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
-                                                                          qb, q32, qpar);
+    float* qscale = reinterpret_cast<float*>(base + L.qscale);
+    f8 = f8 && a.metric == SVDB_COSINE;  // the E4M3 shadow is the unit-norm (cosine) one
+    if (f8)
+        k_prep_f8<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(
+            a.q, a.qsq, nq, s->ld, s->ldb8, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
+    else
+        k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
+                                                                              a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
     k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, L.nsub, flags, nq, k, alpha, redo_n,
                                                                          dstats);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
-                                                                          a.metric, s->rowpn, rpar, spar, alpha, vbits);
+                                                                          a.metric, f8 ? s->rowpn8 : s->rowpn, rpar, spar,
+                                                                          alpha, vbits);
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
     CUtensorMap tmq;
-    rc = make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
+    rc = f8 ? make_map8(gc, &tmq, qb, a.nq, s->ldb8, scr::kBM) : make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
     const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
     if (rc) return rc;
 
     ScreenParams P;
-    P.xblk = norm ? s->xbn : s->xb;
+    P.xblk = reinterpret_cast<const uint8_t*>(f8 ? (const void*)s->xbn8 : norm ? (const void*)s->xbn : (const void*)s->xb);
+    P.qscale = qscale;
     P.rpar = rpar;
     P.spar = spar;
     P.alpha = alpha;
     P.vbits = vbits;
-    P.nmax = s->d_count + 1;
+    P.nmax = s->d_count + (f8 ? 3 : 1);
     P.qpar = qpar;
     P.tau = tau;
     P.bins = bins;
@@ -1627,14 +1770,17 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.cap = L.cap;
     P.nsub = L.nsub;
     P.subcap = L.subcap;
-    P.kblocks = (int)(s->ldb / scr::kBK);
+    P.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
     P.sched = L.sched;
     const unsigned grid = (unsigned)L.nctas;
     {
-        auto kern = k <= 16   ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
+        auto kern = f8        ? (k <= 16 ? k_screen_bf16<16, true, true>
+                                 : k <= 32 ? k_screen_bf16<32, true, true>
+                                           : k_screen_bf16<0, true, true>)
+                    : k <= 16 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
                     : k <= 32 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
                               : (norm ? k_screen_bf16<0, true> : k_screen_bf16<0, false>);
-        const int v = (k <= 16 ? 0 : (k <= 32 ? 2 : 4)) + (norm ? 1 : 0);
+        const int v = f8 ? 6 + (k <= 16 ? 0 : (k <= 32 ? 1 : 2)) : (k <= 16 ? 0 : (k <= 32 ? 2 : 4)) + (norm ? 1 : 0);
         if (!gc->attr_set[v]) {
             SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
             gc->attr_set[v] = true;

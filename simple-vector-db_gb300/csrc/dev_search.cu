@@ -361,7 +361,8 @@ static bool host_pinned(const void* p) {
 extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t k, int metric, int precision,
                             int64_t* ids, double* dists, double* err, int on_device, svdb_search_stats* st) {
     Store* s = reinterpret_cast<Store*>(hs);
-    if (k == 0 || k > 128 || metric < 0 || metric > 2 || (precision != SVDB_PREC_FP64 && precision != SVDB_PREC_BF16)) {
+    if (k == 0 || k > 128 || metric < 0 || metric > 2 ||
+        (precision != SVDB_PREC_FP64 && precision != SVDB_PREC_BF16 && precision != SVDB_PREC_FP8)) {
         svdb_set_error("search: bad argument (k=%zu metric=%d precision=%d; k must be 1..128)", k, metric, precision);
         return SVDB_EINVAL;
     }
@@ -376,7 +377,7 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     const size_t obytes = on_device ? 0 : round_up(out_n * (sizeof(int64_t) + 2 * sizeof(double)), 256);
     // the screen certifies k <= 128 on stores without unscreenable rows; the
     // rest is answered by the exact scan
-    const bool use_bf16 = precision == SVDB_PREC_BF16 && bf16_supported(s, k);
+    const bool use_bf16 = (precision == SVDB_PREC_BF16 || precision == SVDB_PREC_FP8) && bf16_supported(s, k);
     size_t kbytes = 0;
     if (s->nlive) kbytes = use_bf16 ? search_bf16_scratch(s, nq, k) : search_fp64_scratch(s, nq, k);
     const size_t qin = on_device ? 0 : round_up(nq * s->dim * sizeof(double), 256);
@@ -437,13 +438,13 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     } else if (!use_bf16) {
         rc = search_fp64(s, a, kscr, kbytes, &kernels);
         if (st) {
-            if (precision == SVDB_PREC_BF16) st->widened += (uint32_t)nq;
+            if (precision != SVDB_PREC_FP64) st->widened += (uint32_t)nq;
             st->candidates += (uint64_t)nq * s->nlive;
             st->survivors += (uint64_t)nq * s->nlive;
             st->reranked += (uint64_t)nq * s->nlive;
         }
     } else {
-        rc = search_bf16(s, a, kscr, kbytes, st);
+        rc = search_bf16(s, a, kscr, kbytes, st, precision == SVDB_PREC_FP8);
     }
     s->prof_mark(SVDB_NSTAGES);
     s->prof_end();

@@ -45,7 +45,9 @@ int search_fp64(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 size_t search_fp64_scratch(const Store* s, size_t nq, size_t k);
 
 // BF16 screen + certified FP64 re-rank (dev_gemm.cu)
-int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st);
+// f8: the cosine screen on the E4M3 shadow (other metrics keep BF16)
+int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st,
+                bool f8 = false);
 size_t search_bf16_scratch(const Store* s, size_t nq, size_t k);
 // the screen certifies k <= 128 on stores without unscreenable rows
 bool bf16_supported(const Store* s, size_t k);

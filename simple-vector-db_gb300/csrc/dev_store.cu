@@ -7,6 +7,8 @@
 //   x32     C x ld   float    FP32 shadow of x64 (refinement stage)
 //   xbn     C x ldb  bf16     BF16 shadow of x64 / |x| (cosine screen)
 //   rowpn   C        float2   {|bxn| up, |x/|x| - bxn| up}
+//   xbn8    C x ldb8 e4m3     FP8 shadow of 256 x / |x| (FP8 cosine screen), ldb8 = D rounded up to 128
+//   rowpn8  C        float2   {|bxn8|/256 up, |x/|x| - bxn8/256| up}
 //   sqf     C        float4   {|x|^2 down, |x|^2 up, 1/(2|x|) down, 1/(2|x|) up} in FP32
 //   sq64    C        double   canonical sum of squares of the master row
 //   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
@@ -22,6 +24,8 @@
 
 #include "dev_common.cuh"
 #include "dev_store.cuh"
+
+#include <cuda_fp8.h>
 
 namespace {
 thread_local char g_err[512];
@@ -47,8 +51,8 @@ namespace svdb {
 __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bfloat16* __restrict__ xb,
                               size_t ldb, float* __restrict__ x32, __nv_bfloat16* __restrict__ xbn,
                               float2* __restrict__ rowpn, float4* __restrict__ sqf, double* __restrict__ sq64,
-                              float4* __restrict__ rowp,
-                              const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
+                              float4* __restrict__ rowp, uint8_t* __restrict__ xbn8, size_t ldb8,
+                              float2* __restrict__ rowpn8, const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
                               const int64_t* __restrict__ list) {
     const int lane = threadIdx.x & 31, s = lane & 3;
     const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
@@ -78,8 +82,9 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     sq = group4_sum(sq);
     bh = group4_sum(bh);
     res = group4_sum(res);
-    // second pass: the unit-norm row for the cosine screen, its BF16 copy and residual
-    double nbh = 0.0, nres = 0.0;
+    // second pass: the unit-norm row for the cosine screen, its BF16 and FP8
+    // (E4M3 of 256 x/|x|) copies and their residuals
+    double nbh = 0.0, nres = 0.0, nbh8 = 0.0, nres8 = 0.0;
     if (active) {
         const double ixn = sq > 0.0 ? 1.0 / sqrt(sq) : 0.0;
         for (size_t j = 2 * s; j < ld; j += 8) {
@@ -92,12 +97,24 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
             nres = fma(ux - fx, ux - fx, nres);
             nres = fma(uy - fy, uy - fy, nres);
             *reinterpret_cast<__nv_bfloat162*>(xbn + bf16_tile_index(slot, j, ldb)) = __halves2bfloat162(hx, hy);
+            const __nv_fp8_storage_t ex = __nv_cvt_double_to_fp8(kF8RowScale * ux, __NV_SATFINITE, __NV_E4M3);
+            const __nv_fp8_storage_t ey = __nv_cvt_double_to_fp8(kF8RowScale * uy, __NV_SATFINITE, __NV_E4M3);
+            const double gx = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(ex, __NV_E4M3))) / kF8RowScale;
+            const double gy = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(ey, __NV_E4M3))) / kF8RowScale;
+            nbh8 = fma(gx, gx, nbh8);
+            nbh8 = fma(gy, gy, nbh8);
+            nres8 = fma(ux - gx, ux - gx, nres8);
+            nres8 = fma(uy - gy, uy - gy, nres8);
+            *reinterpret_cast<uint16_t*>(xbn8 + f8_tile_index(slot, j, ldb8)) = (uint16_t)(ex | ((uint16_t)ey << 8));
         }
         for (size_t j = ld + 2 * s; j < ldb; j += 8)
             *reinterpret_cast<__nv_bfloat162*>(xbn + bf16_tile_index(slot, j, ldb)) = __floats2bfloat162_rn(0.f, 0.f);
+        for (size_t j = ld + 2 * s; j < ldb8; j += 8) *reinterpret_cast<uint16_t*>(xbn8 + f8_tile_index(slot, j, ldb8)) = 0;
     }
     nbh = group4_sum(nbh);
     nres = group4_sum(nres);
+    nbh8 = group4_sum(nbh8);
+    nres8 = group4_sum(nres8);
     if (active && s == 0) {
         // x/|x| is itself rounded (relative 2^-52 per element): the 2^-30 margin covers it
         const double up = 1.0 + 9.313225746154785e-10;
@@ -109,6 +126,7 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
                                     lo > 0.0 ? __double2float_ru(0.5 / lo) : __int_as_float(0x7f800000));
         }
         rowpn[slot] = make_float2(__double2float_ru(sqrt(nbh) * up), __double2float_ru(sqrt(nres) * up + 1e-300));
+        rowpn8[slot] = make_float2(__double2float_ru(sqrt(nbh8) * up), __double2float_ru(sqrt(nres8) * up + 1e-300));
         sq64[slot] = sq;
         float4 p;
         p.x = __double2float_ru(sqrt(sq));
@@ -228,22 +246,29 @@ __global__ void __launch_bounds__(1024) k_map_write(const uint8_t* __restrict__ 
 // ... and the store-wide maxima of the unit-norm shadow's residual and norm
 // (count[1], count[2], float bits; non-negative floats order as ints)
 __global__ void k_count_unscreenable(const float4* __restrict__ rowp, const float2* __restrict__ rowpn,
-                                     const uint8_t* __restrict__ live, int64_t n, int* __restrict__ count) {
-    int c = 0, ra = 0, rb = 0;
+                                     const float2* __restrict__ rowpn8, const uint8_t* __restrict__ live, int64_t n,
+                                     int* __restrict__ count) {
+    int c = 0, ra = 0, rb = 0, ra8 = 0, rb8 = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (live[i] != 1) continue;
         c += !(rowp[i].z < 3.0e38f) ? 1 : 0;
-        const float2 pn = rowpn[i];
+        const float2 pn = rowpn[i], pn8 = rowpn8[i];
         ra = max(ra, __float_as_int(pn.y));
         rb = max(rb, __float_as_int(pn.x));
+        ra8 = max(ra8, __float_as_int(pn8.y));
+        rb8 = max(rb8, __float_as_int(pn8.x));
     }
     c = __reduce_add_sync(0xffffffffu, c);
     ra = __reduce_max_sync(0xffffffffu, ra);
     rb = __reduce_max_sync(0xffffffffu, rb);
+    ra8 = __reduce_max_sync(0xffffffffu, ra8);
+    rb8 = __reduce_max_sync(0xffffffffu, rb8);
     if ((threadIdx.x & 31) == 0) {
         if (c) atomicAdd(count, c);
         atomicMax(count + 1, ra);
         atomicMax(count + 2, rb);
+        atomicMax(count + 3, ra8);
+        atomicMax(count + 4, rb8);
     }
 }
 
@@ -365,7 +390,7 @@ int Store::ensure() {
     }
     cudaStream_t st = nullptr;
     SVDB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, 4 * sizeof(int)) != cudaSuccess ||
+    if (cudaMalloc(&d_nlive, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&d_count, 8 * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&d_err, sizeof(int)) != cudaSuccess || cudaMemset(d_err, 0, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         cudaStreamDestroy(st);
@@ -393,6 +418,8 @@ int Store::grow(size_t need) {
     float* nf = nullptr;
     __nv_bfloat16* nbn = nullptr;
     float2* npn = nullptr;
+    uint8_t* nb8 = nullptr;
+    float2* npn8 = nullptr;
     float4* nsf = nullptr;
     double* nsq = nullptr;
     float4* np = nullptr;
@@ -405,6 +432,8 @@ int Store::grow(size_t need) {
     if (e == cudaSuccess) e = cudaMalloc(&nf, nc * ld * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&nbn, nc * ldb * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc(&npn, nc * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&nb8, nc * ldb8);
+    if (e == cudaSuccess) e = cudaMalloc(&npn8, nc * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&nsf, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
@@ -418,6 +447,8 @@ int Store::grow(size_t need) {
         cudaFree(nf);
         cudaFree(nbn);
         cudaFree(npn);
+        cudaFree(nb8);
+        cudaFree(npn8);
         cudaFree(nsf);
         cudaFree(nsq);
         cudaFree(np);
@@ -430,6 +461,7 @@ int Store::grow(size_t need) {
     // BF16 shadows: whole 256-row tiles; rows never written stay zero
     SVDB_CUDA(cudaMemsetAsync(nb, 0, nc * ldb * sizeof(__nv_bfloat16), stream));
     SVDB_CUDA(cudaMemsetAsync(nbn, 0, nc * ldb * sizeof(__nv_bfloat16), stream));
+    SVDB_CUDA(cudaMemsetAsync(nb8, 0, nc * ldb8, stream));
     if (slots) {
         const size_t tile_rows = round_up(slots, 256);
         SVDB_CUDA(cudaMemcpyAsync(nx, x64, slots * ld * sizeof(double), cudaMemcpyDeviceToDevice, stream));
@@ -437,6 +469,8 @@ int Store::grow(size_t need) {
         SVDB_CUDA(cudaMemcpyAsync(nf, x32, slots * ld * sizeof(float), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nbn, xbn, tile_rows * ldb * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(npn, rowpn, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nb8, xbn8, tile_rows * ldb8, cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(npn8, rowpn8, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsf, sqf, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
@@ -449,6 +483,8 @@ int Store::grow(size_t need) {
     cudaFree(x32);
     cudaFree(xbn);
     cudaFree(rowpn);
+    cudaFree(xbn8);
+    cudaFree(rowpn8);
     cudaFree(sqf);
     cudaFree(sq64);
     cudaFree(rowp);
@@ -460,6 +496,8 @@ int Store::grow(size_t need) {
     x32 = nf;
     xbn = nbn;
     rowpn = npn;
+    xbn8 = nb8;
+    rowpn8 = npn8;
     sqf = nsf;
     sq64 = nsq;
     rowp = np;
@@ -573,7 +611,8 @@ int Store::sync() {
         const int64_t n = derive_hi - derive_lo;
         const int threads = 256;
         const int64_t blocks = (n * 4 + threads - 1) / threads;
-        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp, live, derive_lo,
+        k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp, xbn8,
+                                                              ldb8, rowpn8, live, derive_lo,
                                                               derive_hi, nullptr);
         SVDB_LAUNCH_CHECK();
     }
@@ -585,7 +624,8 @@ int Store::sync() {
         if (rc) return rc;
         d = (int64_t*)scratch;
         SVDB_CUDA(cudaMemcpyAsync(d, dirty_list.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
-        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp, live, 0,
+        k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp,
+                                                                         xbn8, ldb8, rowpn8, live, 0,
                                                                          n, d);
         SVDB_LAUNCH_CHECK();
         SVDB_CUDA(cudaStreamSynchronize(stream));
@@ -599,9 +639,9 @@ int Store::sync() {
         SVDB_LAUNCH_CHECK();
         k_map_write<<<(unsigned)nb, 1024, 0, stream>>>(live, (int64_t)slots, mapblk, logical);
         SVDB_LAUNCH_CHECK();
-        SVDB_CUDA(cudaMemsetAsync(d_count, 0, 3 * sizeof(int), stream));
+        SVDB_CUDA(cudaMemsetAsync(d_count, 0, 5 * sizeof(int), stream));
         k_count_unscreenable<<<(unsigned)std::min<size_t>((slots + 255) / 256, 1024), 256, 0, stream>>>(
-            rowp, rowpn, live, (int64_t)slots, d_count);
+            rowp, rowpn, rowpn8, live, (int64_t)slots, d_count);
         SVDB_LAUNCH_CHECK();
         int hc = 0;
         SVDB_CUDA(cudaMemcpyAsync(&h_nlive, d_nlive, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
@@ -634,6 +674,7 @@ svdbd_store* svdbd_store_create(size_t dim) {
     s->dim = dim;
     s->ld = svdb::round_up(dim, svdb::kRowAlign);
     s->ldb = svdb::round_up(dim, svdb::kBf16Align);
+    s->ldb8 = svdb::round_up(dim, 128);
     return reinterpret_cast<svdbd_store*>(s);
 }
 
@@ -652,6 +693,8 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->x32);
     cudaFree(s->xbn);
     cudaFree(s->rowpn);
+    cudaFree(s->xbn8);
+    cudaFree(s->rowpn8);
     cudaFree(s->sqf);
     cudaFree(s->sq64);
     cudaFree(s->rowp);

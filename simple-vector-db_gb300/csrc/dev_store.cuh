@@ -28,9 +28,12 @@ struct Store {
     float* x32 = nullptr;  // FP32 shadow (cap x ld), read by the refinement stage
     __nv_bfloat16* xbn = nullptr;  // BF16 shadow of x / |x| (cap x ldb): the cosine screen
     float2* rowpn = nullptr;       // {|bxn| up, |x/|x| - bxn| up} per row
+    size_t ldb8 = 0;               // FP8 shadow row length (bytes), D rounded up to 128
+    uint8_t* xbn8 = nullptr;       // E4M3 shadow of 256 x/|x| (cap x ldb8), FP8 cosine screen
+    float2* rowpn8 = nullptr;      // {|bxn8|/256 up, |x/|x| - bxn8/256| up} per row
     float4* sqf = nullptr;         // FP32 intervals for the refinement: {|x|^2 down, |x|^2 up,
                                    //  1/(2|x|) down, 1/(2|x|) up}
-    int* d_nmax = nullptr;         // {max |x/|x| - bxn|, max |bxn|} over searchable rows (float bits)
+    int* d_nmax = nullptr;         // (unused; the maxima live in d_count[1..4])
     double* sq64 = nullptr;
     float4* rowp = nullptr;  // {|x| up (-1: dead slot), |bf16 x| up, |x - bf16 x| up (inf: unscreenable), |x|^2/2}
     uint8_t* live = nullptr;

@@ -396,7 +396,7 @@ static void ragged_lock(svdb_ragged* r, int lock) {
 SVDB_API svdb_ragged* svdb_ragged_create(const svdb_ragged_part* parts, size_t nparts, int metric, int precision,
                                          unsigned flags) {
     if (!parts || nparts == 0 || metric < 0 || metric > 2 ||
-        (precision != SVDB_PREC_FP64 && precision != SVDB_PREC_BF16)) {
+        (precision != SVDB_PREC_FP64 && precision != SVDB_PREC_BF16 && precision != SVDB_PREC_FP8)) {
         svdb_set_error("svdb_ragged_create: bad argument (parts, metric or precision)");
         return NULL;
     }

@@ -20,7 +20,7 @@ _PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.environ.get("SVDB_LIB", os.path.join(_PKG, "_build", "libsvdb_gb300.so"))
 
 COSINE, EUCLIDEAN, DOT = 0, 1, 2
-PREC_FP64, PREC_BF16 = 0, 1
+PREC_FP64, PREC_BF16, PREC_FP8 = 0, 1, 2
 # status codes (include/svdb_gb300.h)
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENODEV = 0, -1, -2, -3, -4, -5
 METRIC_URLS = {"/compare/cosine_similarity": COSINE, "/compare/euclidean_distance": EUCLIDEAN,
