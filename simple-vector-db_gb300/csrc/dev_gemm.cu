@@ -1493,7 +1493,7 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 // ---------------------------------------------------------------------------
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    bool attr_set[9] = {false, false, false, false, false, false, false, false, false};
+    bool attr_set[12] = {};
     bool select_attr = false;
     bool sort_attr = false;
     bool rerank_attr = false;
@@ -1780,7 +1780,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                     : k <= 16 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
                     : k <= 32 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
                               : (norm ? k_screen_bf16<0, true> : k_screen_bf16<0, false>);
-        const int v = f8 ? 6 + (k <= 16 ? 0 : (k <= 32 ? 1 : 2)) : (k <= 16 ? 0 : (k <= 32 ? 2 : 4)) + (norm ? 1 : 0);
+        const int kc = k <= 16 ? 0 : k <= 32 ? 1 : 2;  // running top-k variant
+        const int v = f8 ? 8 + kc : 2 * kc + (norm ? 1 : 0);
         if (!gc->attr_set[v]) {
             SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
             gc->attr_set[v] = true;

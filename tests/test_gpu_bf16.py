@@ -135,7 +135,7 @@ def test_bf16_large_k_near_ties(S, oracle, metric):
     Q = C[rng.integers(0, 16, 30)] + 0.05 * rng.normal(size=(30, 128))
     db = S.VectorDatabase(0, 3)
     db.insert_batch(X)
-    for k in (33, 64, 100, 128):
+    for k in (33, 48, 64, 65, 100, 128):
         ids, vals, st = _search_both(S, db, Q, k, metric)
         wid, wval = oracle.topk(metric, X, Q, k)
         assert np.array_equal(ids, wid) and np.array_equal(vals, wval), k
