@@ -731,7 +731,8 @@ def run_decode(args, ws, rank, local):
     """POST /nearest request bodies decoded on the device: batches of 4,096
     bodies, each a JSON array of 768 numbers written with %.17g (N(0,1) x
     10^U[-8,8), seed 7; ~18 MB of text per batch), through svdb_decode_vectors
-    (host text in, host doubles out: copies inside the timed region).  CPU
+    (page-locked host text in, host doubles out: copies inside the timed
+    region).  CPU
     baseline: the oracle's restatement of cJSON_Parse + strtod, one thread."""
     import svdb_gb300 as S
     import torch
@@ -744,11 +745,14 @@ def run_decode(args, ws, rank, local):
     text = b"".join(bodies)
     off = np.zeros(nb + 1, np.uint64)
     off[1:] = np.cumsum([len(b) for b in bodies])
-    out = np.empty((nb, dim), np.float64)
-    st = np.empty(nb, np.int32)
+    # page-locked text and results, as a network front end's receive and send buffers would be
+    text_t = torch.frombuffer(bytearray(text), dtype=torch.uint8).pin_memory()
+    text_p = C.cast(C.c_void_p(text_t.data_ptr()), C.c_char_p)
+    out = torch.empty((nb, dim), dtype=torch.float64).pin_memory().numpy()
+    st = torch.empty(nb, dtype=torch.int32).pin_memory().numpy()
 
     def step():
-        S._check(S.lib.svdb_decode_vectors(text, off.ctypes.data_as(C.POINTER(C.c_uint64)), nb, dim,
+        S._check(S.lib.svdb_decode_vectors(text_p, off.ctypes.data_as(C.POINTER(C.c_uint64)), nb, dim,
                                            out.ctypes.data_as(S._dp), st.ctypes.data_as(C.POINTER(C.c_int32))),
                  "svdb_decode_vectors")
 

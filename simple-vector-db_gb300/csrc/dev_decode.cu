@@ -549,9 +549,21 @@ __global__ void k_decode_numbers(const uint8_t* __restrict__ text, const uint64_
     if (!ok) atomicExch(&status[r], SVDB_DEC_UNSUPPORTED);
 }
 
+bool host_pinned(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
 }  // namespace
 
 // Decode n bodies (host bytes text[off[i] .. off[i+1])) into n x dim doubles.
+// Page-locked text and outputs are read and written by DMA directly; pageable
+// ones go through the context's staging buffer.
 int decode_bodies(Store* s, const char* text, const uint64_t* off, size_t n, size_t dim, double* out,
                   int32_t* status) {
     if (n == 0) return SVDB_OK;
@@ -570,10 +582,13 @@ int decode_bodies(Store* s, const char* text, const uint64_t* off, size_t n, siz
     double* dval = (double*)(base + a_text + a_off + a_ch);
     int32_t* dst = (int32_t*)(base + a_text + a_off + a_ch + a_val);
     uint8_t* hp = (uint8_t*)s->pin;
-    std::memcpy(hp, text + off[0], tb);
+    const bool pin_in = host_pinned(text + off[0]);
+    const bool pin_out = host_pinned(out) && host_pinned(status);
+    if (!pin_in) std::memcpy(hp, text + off[0], tb);
     uint64_t* hoff = (uint64_t*)(hp + round_up(tb, 8));
     for (size_t i = 0; i <= n; ++i) hoff[i] = off[i] - off[0];
-    SVDB_CUDA(cudaMemcpyAsync(dtext, hp, tb, cudaMemcpyHostToDevice, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(dtext, pin_in ? (const void*)(text + off[0]) : (const void*)hp, tb,
+                              cudaMemcpyHostToDevice, s->stream));
     SVDB_CUDA(cudaMemcpyAsync(doff, hoff, ob, cudaMemcpyHostToDevice, s->stream));
     k_decode_parse<<<(unsigned)((n + 63) / 64), 64, 0, s->stream>>>(dtext, doff, (int)n, (int64_t)dim, dch, dst);
     SVDB_LAUNCH_CHECK();
@@ -582,6 +597,12 @@ int decode_bodies(Store* s, const char* text, const uint64_t* off, size_t n, siz
         k_decode_numbers<<<(unsigned)((total + 255) / 256), 256, 0, s->stream>>>(dtext, doff, (int)n, (int64_t)dim, dch,
                                                                              dst, dval);
     SVDB_LAUNCH_CHECK();
+    if (pin_out) {
+        SVDB_CUDA(cudaMemcpyAsync(out, dval, vb, cudaMemcpyDeviceToHost, s->stream));
+        SVDB_CUDA(cudaMemcpyAsync(status, dst, sb, cudaMemcpyDeviceToHost, s->stream));
+        SVDB_CUDA(cudaStreamSynchronize(s->stream));
+        return SVDB_OK;
+    }
     SVDB_CUDA(cudaStreamSynchronize(s->stream));  // the pinned buffer is reused for the results
     SVDB_CUDA(cudaMemcpyAsync(hp, dval, vb, cudaMemcpyDeviceToHost, s->stream));
     SVDB_CUDA(cudaMemcpyAsync(hp + vb, dst, sb, cudaMemcpyDeviceToHost, s->stream));
