@@ -182,9 +182,10 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     st = S.SearchStats()
 
-    def step(b, stats=None):
+    def step(b, stats=None, p=None):
         q = Qd[b % nbatch]
-        db.search_device(q.data_ptr(), nq, DIM, k, metric, prec, ids.data_ptr(), dists.data_ptr(), 0, stats)
+        db.search_device(q.data_ptr(), nq, DIM, k, metric, prec if p is None else p, ids.data_ptr(), dists.data_ptr(),
+                         0, stats)
 
     # correctness guard on a slice of the first batch: ids equal the device FP64 scan
     ids_ref, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP64)
@@ -228,6 +229,38 @@ def run_ours(args, ws, rank, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * nq * args.steps / (ms / 1e3)
+
+    # the FP8 screen (BF16-seeded thresholds, E4M3 tensor-core screen, same
+    # refinement and re-rank) on the same batches, for comparison
+    fp8 = None
+    if prec == S.PREC_BF16 and metric == S.COSINE and rank == 0:
+        ids_ref8, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP64)
+        ids_chk8, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP8)
+        if not np.array_equal(ids_ref8, ids_chk8):
+            raise SystemExit("bench: FP8 top-k ids differ from the FP64 scan")
+        for w in range(args.warmup):
+            step(w, p=S.PREC_FP8)
+        st8 = S.SearchStats()
+        step(0, st8, p=S.PREC_FP8)
+        db.profile(True)
+        db.profile_read(reset=True)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s_ in range(args.steps):
+            step(s_, p=S.PREC_FP8)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        n8, stage8 = db.profile_read(reset=True)
+        db.profile(False)
+        ms8 = e0.elapsed_time(e1)
+        fp8 = {"value": nq * args.steps / (ms8 / 1e3), "unit": "queries/s", "ms_per_step": ms8 / args.steps,
+               "stage_ms_per_step": {n: float(stage8[i] / max(n8, 1)) for i, n in
+                                     enumerate(("prep", "screen", "select", "refine", "rerank"))},
+               "funnel_per_query": {"screen_candidates": st8.candidates / nq, "survivors": st8.survivors / nq,
+                                    "fp64_reranked": st8.reranked / nq, "widened_queries": st8.widened,
+                                    "bound_failures": st8.bound_failures}}
 
     # e2e: host buffers through svdb_search_topk (query upload + result read
     # inside), queries and results in page-locked host memory
@@ -314,6 +347,8 @@ def run_ours(args, ws, rank, local):
                 "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": nq * DIM * 8,
                         "d2h_bytes_per_step": nq * k * 16},
                 "gpu_launches": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": cl}
+        if fp8:
+            line["fp8_screen"] = fp8
         print(json.dumps(line), flush=True)
     db.close()
     if dist:

@@ -923,11 +923,13 @@ __global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ r
     }
 }
 
+// seed (optional): a valid lower bound of each query's k-th best key, the
+// running threshold's starting value
 __global__ void k_init_search(int* tau, int* bins, int* cnt, int nsub, uint8_t* flags, int nq, int k, int* alpha,
-                              int* redo_n, unsigned long long* stats) {
+                              int* redo_n, unsigned long long* stats, const float* seed = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nq) {
-        tau[i] = f2ord(-INFINITY);
+        tau[i] = f2ord(seed ? seed[i] : -INFINITY);
         for (int t = 0; t < k; ++t) bins[(size_t)i * k + t] = f2ord(-INFINITY);
         for (int t = 0; t < nsub; ++t) cnt[(size_t)i * nsub + t] = 0;
         flags[i] = scr::kOk;
@@ -997,7 +999,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
                                                  int nsub, int subcap, const float4* __restrict__ rpar,
                                                  const float4* __restrict__ qpar, int k, int2* __restrict__ surv,
                                                  int* __restrict__ nsurv, int* __restrict__ sig,
-                                                 uint8_t* __restrict__ flags) {
+                                                 uint8_t* __restrict__ flags, float* __restrict__ kth_out = nullptr) {
     extern __shared__ uint32_t vals[];  // blockDim.x * k ordered lower bounds
     __shared__ int hist[256];
     __shared__ uint32_t s_sh[3];
@@ -1031,6 +1033,10 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     __syncthreads();
     const int n = s_pre[nsub];
     if (qp.w == 0.f || s_over) {
+        if (kth_out) {  // seed mode: no usable lower bound
+            if (threadIdx.x == 0) kth_out[q] = -INFINITY;
+            return;
+        }
         if (threadIdx.x == 0) {
             flags[q] = qp.w == 0.f ? scr::kInvalidQuery : scr::kOverflow;
             nsurv[q] = 0;
@@ -1076,6 +1082,13 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     } else {
         __syncthreads();
         if (n >= k) thr_ord = block_kth_largest(lower, n, k, hist, s_sh);
+    }
+    if (kth_out) {  // seed mode: the exact k-th largest lower bound over these candidates, nothing else
+        if (threadIdx.x == 0) {
+            const uint32_t u = thr_ord;
+            kth_out[q] = n >= k ? __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u) : -INFINITY;
+        }
+        return;
     }
     int2* sq = surv + (size_t)q * scr::kSurvCap;
     for (int i = threadIdx.x; i < n; i += bd) {
@@ -1564,7 +1577,7 @@ static int make_map8(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t 
 }
 
 struct Bf16Layout {
-    size_t qb, qscale, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
+    size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     int ntr, cap;
     int nctas, nsub, subcap;
     size_t npad;
@@ -1649,6 +1662,10 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.npad = (size_t)L.ntr * scr::kBN;
     L.qb = take(std::max(nq * s->ldb * 2, nq * s->ldb8));  // BF16 queries, or the E4M3 ones
     L.qscale = take(nq * sizeof(float));
+    // FP8 threshold seeding (BF16 screen of a sample of the rows)
+    L.qb16 = take(nq * s->ldb * 2);
+    L.qpar16 = take(nq * sizeof(float4));
+    L.seed = take(nq * sizeof(float));
     L.q32 = take(nq * s->ld * sizeof(float));
     L.qpar = take(nq * sizeof(float4));
     L.rpar = take(L.npad * sizeof(float4));
@@ -1729,6 +1746,111 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     float* qscale = reinterpret_cast<float*>(base + L.qscale);
     f8 = f8 && a.metric == SVDB_COSINE;  // the E4M3 shadow is the unit-norm (cosine) one
+    const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
+    const int kc = k <= 16 ? 0 : k <= 32 ? 1 : 2;  // running top-k variant of the screen and select
+    auto screen_kernel = [&](bool e4m3) {
+        return e4m3   ? (kc == 0 ? k_screen_bf16<16, true, true>
+                         : kc == 1 ? k_screen_bf16<32, true, true>
+                                   : k_screen_bf16<0, true, true>)
+               : kc == 0 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
+               : kc == 1 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
+                         : (norm ? k_screen_bf16<0, true> : k_screen_bf16<0, false>);
+    };
+    auto screen_attr = [&](bool e4m3) -> int {
+        const int v = e4m3 ? 8 + kc : 2 * kc + (norm ? 1 : 0);
+        if (!gc->attr_set[v]) {
+            SVDB_CUDA(cudaFuncSetAttribute(screen_kernel(e4m3), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)gc->screen_smem));
+            gc->attr_set[v] = true;
+        }
+        return SVDB_OK;
+    };
+    // small batches carry many candidates per query: wider blocks
+    const int sel_threads = nq >= 256 ? 256 : 1024;
+    const size_t sel_smem = k <= 32 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;
+    auto launch_select = [&](int nsub_, int subcap_, const float4* qp_, float* kth) -> int {
+        if (!gc->select_attr) {
+            SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+            gc->select_attr = true;
+        }
+        if (kc == 0)
+            k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_,
+                                                                             k, surv, nsurv, sig, flags, kth);
+        else if (kc == 1)
+            k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_,
+                                                                             k, surv, nsurv, sig, flags, kth);
+        else
+            k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_,
+                                                                            k, surv, nsurv, sig, flags, kth);
+        SVDB_LAUNCH_CHECK();
+        return SVDB_OK;
+    };
+
+    // FP8: seed the running thresholds with the exact k-th largest BF16 lower
+    // bound over a sample of the store (its first 1/16 of the rows, which are
+    // in no particular order).  The E4M3 bound is ~16x the BF16 one, so a
+    // screen whose thresholds start from random rows emits every row within
+    // that bound of them until it meets rows of the query's cluster; a sample
+    // holding enough of them puts the threshold at the cluster's level from
+    // the first tile.  A lower bound over a subset of the rows is a lower
+    // bound over all of them, so the seed is a valid starting threshold.
+    float* seed = nullptr;
+    if (f8 && L.ntr >= 32 && nq >= 32) {  // (a lone query's tile is split over every SM: its bins fill at once)
+        __nv_bfloat16* qb16 = reinterpret_cast<__nv_bfloat16*>(base + L.qb16);
+        float4* qpar16 = reinterpret_cast<float4*>(base + L.qpar16);
+        seed = reinterpret_cast<float*>(base + L.seed);
+        const int ntq = (nq + scr::kBM - 1) / scr::kBM;
+        const int ntr_seed = L.ntr / 16;
+        const int64_t npad_seed = (int64_t)ntr_seed * scr::kBN;
+        ScreenSched SS;
+        int maxsub_s = 1;
+        const int nctas_s = screen_schedule(ntq, ntr_seed, SS, &maxsub_s);
+        const int nsub_s = 2 * maxsub_s;
+        const int subcap_s = L.cap / nsub_s;
+        k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
+                                                                              qb16, q32, qpar16);
+        SVDB_LAUNCH_CHECK();
+        k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, nsub_s, flags, nq, k, alpha,
+                                                                             redo_n, dstats);
+        SVDB_LAUNCH_CHECK();
+        k_row_params<<<(unsigned)((npad_seed + 255) / 256), 256, 0, s->stream>>>(
+            s->rowp, s->sq64, s->live, std::min<int64_t>((int64_t)s->slots, npad_seed), npad_seed, a.metric, s->rowpn,
+            rpar, spar, alpha, vbits);
+        SVDB_LAUNCH_CHECK();
+        CUtensorMap tmq16;
+        rc = make_map(gc, &tmq16, qb16, a.nq, s->ldb, scr::kBM);
+        if (rc) return rc;
+        ScreenParams PS;
+        PS.xblk = reinterpret_cast<const uint8_t*>(s->xbn);
+        PS.qscale = qscale;
+        PS.rpar = rpar;
+        PS.spar = spar;
+        PS.alpha = alpha;
+        PS.vbits = vbits;
+        PS.nmax = s->d_count + 1;
+        PS.qpar = qpar16;
+        PS.tau = tau;
+        PS.bins = bins;
+        PS.cnt = cnt;
+        PS.cand = cand;
+        PS.err = s->d_err;
+        PS.nq = nq;
+        PS.k = k;
+        PS.cap = L.cap;
+        PS.nsub = nsub_s;
+        PS.subcap = subcap_s;
+        PS.kblocks = (int)(s->ldb / scr::kBK);
+        PS.sched = SS;
+        rc = screen_attr(false);
+        if (rc) return rc;
+        screen_kernel(false)<<<(unsigned)nctas_s, scr::kThreads, gc->screen_smem, s->stream>>>(tmq16, PS);
+        SVDB_LAUNCH_CHECK();
+        rc = launch_select(nsub_s, subcap_s, qpar16, seed);
+        if (rc) return rc;
+        kernels += 5;
+    }
+
     if (f8)
         k_prep_f8<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(
             a.q, a.qsq, nq, s->ld, s->ldb8, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
@@ -1737,7 +1859,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                                               a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
     k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, L.nsub, flags, nq, k, alpha, redo_n,
-                                                                         dstats);
+                                                                         dstats, seed);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
@@ -1748,7 +1870,6 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     CUtensorMap tmq;
     rc = f8 ? make_map8(gc, &tmq, qb, a.nq, s->ldb8, scr::kBM) : make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
-    const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
     if (rc) return rc;
 
     ScreenParams P;
@@ -1773,45 +1894,15 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
     P.sched = L.sched;
     const unsigned grid = (unsigned)L.nctas;
-    {
-        auto kern = f8        ? (k <= 16 ? k_screen_bf16<16, true, true>
-                                 : k <= 32 ? k_screen_bf16<32, true, true>
-                                           : k_screen_bf16<0, true, true>)
-                    : k <= 16 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
-                    : k <= 32 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
-                              : (norm ? k_screen_bf16<0, true> : k_screen_bf16<0, false>);
-        const int kc = k <= 16 ? 0 : k <= 32 ? 1 : 2;  // running top-k variant
-        const int v = f8 ? 8 + kc : 2 * kc + (norm ? 1 : 0);
-        if (!gc->attr_set[v]) {
-            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
-            gc->attr_set[v] = true;
-        }
-        kern<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, P);
-    }
+    rc = screen_attr(f8);
+    if (rc) return rc;
+    screen_kernel(f8)<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, P);
     SVDB_LAUNCH_CHECK();
     ++kernels;
     s->prof_mark(2);
 
-    {
-        // small batches carry many candidates per query: wider blocks
-        const int sel_threads = nq >= 256 ? 256 : 1024;
-        const size_t sel_smem = k <= 32 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;
-        if (!gc->select_attr) {
-            SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-            SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-            gc->select_attr = true;
-        }
-        if (k <= 16)
-            k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, L.nsub, L.subcap, rpar, qpar, k, surv,
-                                                                             nsurv, sig, flags);
-        else if (k <= 32)
-            k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, L.nsub, L.subcap, rpar, qpar, k, surv,
-                                                                             nsurv, sig, flags);
-        else
-            k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, L.nsub, L.subcap, rpar, qpar, k, surv,
-                                                                            nsurv, sig, flags);
-    }
-    SVDB_LAUNCH_CHECK();
+    rc = launch_select(L.nsub, L.subcap, qpar, nullptr);
+    if (rc) return rc;
     s->prof_mark(3);
     const size_t ref_smem = s->ld * sizeof(float);
     if (!gc->refine_attr) {
