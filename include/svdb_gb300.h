@@ -33,8 +33,9 @@ extern "C" {
 #define SVDB_PREC_FP64 0 /* plain FP64 streaming scan of the master copy */
 #define SVDB_PREC_BF16 1 /* BF16 tensor-core screen + certified FP64 re-rank */
 #define SVDB_PREC_FP8 2  /* cosine: FP8-E4M3 tensor-core screen on the unit-norm shadow (256 x/|x|, an exact
-                            power-of-two scale per query), same certified refinement and FP64 re-rank;
-                            dot / Euclidean searches run the BF16 screen */
+                            power-of-two scale per query), its thresholds seeded (batches of 32+ queries) by
+                            the BF16 screen of a 1/16 row sample, then the same certified refinement and
+                            FP64 re-rank; dot / Euclidean searches run the BF16 screen */
 
 /* return codes */
 #define SVDB_OK 0
