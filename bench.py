@@ -473,9 +473,11 @@ def run_ragged(args, ws, rank, local):
                        "precision": args.precision, "l2": "stores (5.4 GB FP64) larger than L2; no flush needed"},
             "plan": {"grouping": info["grouping"], "concurrent": info["concurrent"], "graph": info["graph"],
                      "searches_per_run": info["searches"], "graph_launches_per_step": 1,
+                     "fp8_screen_stores": [i for i in range(5) if info["fp8_stores"] >> i & 1],
                      "autotune_ms_per_run": {"(grouping 0, concurrent 1)": info["tuned_ms"][0],
                                              "(1, 1)": info["tuned_ms"][1], "(0, 0)": info["tuned_ms"][2],
                                              "(1, 0)": info["tuned_ms"][3]},
+                     "autotune_ms_with_store_screen_swapped": info["swap_ms"][:5],
                      "autotune_s": tune_s, "captures": info["captures"]},
             "clocks": clocks}
     print(json.dumps(line), flush=True)

@@ -200,7 +200,8 @@ typedef struct svdb_ragged_part {
     size_t stride;
 } svdb_ragged_part;
 
-#define SVDB_RAGGED_AUTOTUNE 1u /* time every execution choice on these inputs, keep the fastest */
+#define SVDB_RAGGED_AUTOTUNE 1u /* time the execution choices on these inputs, keep the fastest (cosine plans:
+                                   also each store's BF16 versus FP8 screen; the results are the same) */
 #define SVDB_RAGGED_NO_GRAPH 2u /* enqueue the kernels directly at each run (no graph) */
 
 typedef struct svdb_ragged_info {
@@ -208,9 +209,11 @@ typedef struct svdb_ragged_info {
     int32_t concurrent; /* 1: different stores' searches run at the same time; 0: one after another */
     int32_t graph;      /* 1: runs replay a captured CUDA graph */
     int32_t searches;   /* searches per run */
-    float tuned_ms[4];  /* autotuner's ms per run of (grouping, concurrent) = (0,1) (1,1) (0,0) (1,0); 0: not tried */
-    uint32_t captures;  /* graph captures so far */
-    uint32_t reserved;
+    float tuned_ms[4];   /* autotuner's ms per run of (grouping, concurrent) = (0,1) (1,1) (0,0) (1,0); 0: not tried */
+    uint32_t captures;   /* graph captures so far */
+    uint32_t fp8_stores; /* bit i: the plan's i-th distinct store (first-use order) runs the FP8 screen */
+    float swap_ms[8];    /* cosine plans with a tensor-core precision: autotuner's ms per run with store i's
+                            screen swapped BF16 <-> FP8 (kept when faster); 0: not tried */
 } svdb_ragged_info;
 
 typedef struct svdb_ragged svdb_ragged;

@@ -10,7 +10,7 @@
 // graph and replayed with one launch; it is captured again when a store
 // changes in a way the graph bakes in (the store's epoch).
 //
-// Two choices change the speed but not the results, and the autotuner times
+// Three choices change the speed but not the results, and the autotuner times
 // every combination on the plan's own inputs at creation:
 //   grouping   0: one search per part, k = the part's largest k;
 //              1: one search per k class (k <= 16, <= 32, <= 128: the screen's
@@ -18,7 +18,9 @@
 //                 so small-k queries do not pay for the part's largest k;
 //   concurrent 1: the parts of different stores run on their stores' streams
 //                 at the same time (a screen fills the SMs another part's
-//                 screen leaves idle at its tail); 0: one part after another.
+//                 screen leaves idle at its tail); 0: one part after another;
+//   screen     (cosine with a tensor-core precision) per store, the BF16 or
+//              the FP8 screen.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -80,6 +82,7 @@ struct Plan {
     std::vector<Part> parts;
     std::vector<Store*> stores;  // distinct, in first-use order
     int metric = 0, precision = 0;
+    std::vector<int> sprec;  // per store: the precision its searches run with (the autotuner may swap BF16 / FP8)
     bool graph_on = true;
     int grouping = 0, concurrent = 1;
     std::vector<Group> groups;
@@ -90,6 +93,7 @@ struct Plan {
     cudaGraphExec_t exec = nullptr;
     std::vector<uint64_t> epochs;
     float tuned_ms[4] = {0, 0, 0, 0};
+    float swap_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint32_t captures = 0;
 };
 
@@ -149,8 +153,9 @@ int make_groups(Plan* p) {
     return SVDB_OK;
 }
 
-// the searches of one part's store, on that store's stream
-int enqueue_store(Plan* p, Store* s) {
+// the searches of one part's store (the plan's i-th), on that store's stream
+int enqueue_store(Plan* p, size_t si) {
+    Store* s = p->stores[si];
     for (const Group& g : p->groups) {
         const Part& P = p->parts[g.part];
         if (P.s != s) continue;
@@ -163,7 +168,7 @@ int enqueue_store(Plan* p, Store* s) {
             q = g.d_q;
         }
         int rc = svdbd_search(reinterpret_cast<svdbd_store*>(s), q, (size_t)g.n, (size_t)g.kg, p->metric,
-                              p->precision, g.d_ids, g.d_dists, nullptr, 1, nullptr);
+                              p->sprec[si], g.d_ids, g.d_dists, nullptr, 1, nullptr);
         if (rc) return rc;
         const size_t total = (size_t)g.n * P.stride;
         k_ragged_scatter<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s->stream>>>(
@@ -180,7 +185,7 @@ int enqueue(Plan* p) {
     for (size_t i = 0; i < p->stores.size(); ++i) {
         Store* s = p->stores[i];
         SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->concurrent ? p->ev_fork : prev, 0));
-        int rc = enqueue_store(p, s);
+        int rc = enqueue_store(p, i);
         if (rc) return rc;
         SVDB_CUDA(cudaEventRecord(p->ev_store[i], s->stream));
         prev = p->ev_store[i];
@@ -275,10 +280,23 @@ int configure(Plan* p, int grouping, int concurrent) {
     return regroup ? make_groups(p) : SVDB_OK;
 }
 
-// ms per run of the current configuration: one untimed run (capture
-// included), then the best of `reps` timed runs
-int time_config(Plan* p, int reps, float* ms) {
-    int rc = run(p);
+// ms per run of the current configuration: one direct run (it sizes the
+// stores' scratch; a configuration slower than `cutoff` ms stops there), then
+// the capture, then the best of `reps` timed runs
+int time_config(Plan* p, int reps, float cutoff, float* ms) {
+    SVDB_CUDA(cudaEventRecord(p->ev_t0, p->origin));
+    int rc = enqueue(p);
+    if (rc) return rc;
+    SVDB_CUDA(cudaEventRecord(p->ev_t1, p->origin));
+    SVDB_CUDA(cudaEventSynchronize(p->ev_t1));
+    float t = 0;
+    SVDB_CUDA(cudaEventElapsedTime(&t, p->ev_t0, p->ev_t1));
+    rc = check_stores(p);
+    if (rc || t > cutoff) {
+        *ms = t;
+        return rc;
+    }
+    rc = run(p);
     if (rc) return rc;
     SVDB_CUDA(cudaStreamSynchronize(p->origin));
     float best = 1e30f;
@@ -288,7 +306,6 @@ int time_config(Plan* p, int reps, float* ms) {
         if (rc) return rc;
         SVDB_CUDA(cudaEventRecord(p->ev_t1, p->origin));
         SVDB_CUDA(cudaEventSynchronize(p->ev_t1));
-        float t = 0;
         SVDB_CUDA(cudaEventElapsedTime(&t, p->ev_t0, p->ev_t1));
         best = std::min(best, t);
     }
@@ -296,6 +313,13 @@ int time_config(Plan* p, int reps, float* ms) {
     return check_stores(p);
 }
 
+// First the layout: every (grouping, concurrency) pair with the plan's
+// precision.  Then, for a cosine plan with a tensor-core precision, each
+// store's screen in turn is swapped (BF16 <-> FP8: the same exact answers, at
+// a speed that depends on the store's data and its queries) and the swap is
+// kept when the run gets faster.  A trial already slower than 1.5x the best
+// after its first run is not repeated (an FP8 screen over near-orthogonal
+// rows passes most of them on to the refinement).
 int autotune(Plan* p) {
     bool mixed = false;  // does any part hold queries of more than one k class?
     for (const Part& P : p->parts)
@@ -306,11 +330,26 @@ int autotune(Plan* p) {
         if (cfg[c][0] && !mixed) continue;
         if (!cfg[c][1] && p->stores.size() < 2) continue;
         int rc = configure(p, cfg[c][0], cfg[c][1]);
-        if (!rc) rc = time_config(p, 3, &p->tuned_ms[c]);
+        if (!rc) rc = time_config(p, 3, best < 0 ? 1e30f : 1.5f * p->tuned_ms[best], &p->tuned_ms[c]);
         if (rc) return rc;
         if (best < 0 || p->tuned_ms[c] < p->tuned_ms[best]) best = c;
     }
-    return configure(p, cfg[best][0], cfg[best][1]);
+    int rc = configure(p, cfg[best][0], cfg[best][1]);
+    if (rc || p->metric != SVDB_COSINE || p->precision == SVDB_PREC_FP64) return rc;
+    float best_ms = p->tuned_ms[best];
+    for (size_t i = 0; i < p->stores.size() && i < 8; ++i) {
+        const int keep = p->sprec[i];
+        p->sprec[i] = keep == SVDB_PREC_BF16 ? SVDB_PREC_FP8 : SVDB_PREC_BF16;
+        drop_graph(p);
+        rc = time_config(p, 3, 1.5f * best_ms, &p->swap_ms[i]);
+        if (rc) return rc;
+        if (p->swap_ms[i] < best_ms)
+            best_ms = p->swap_ms[i];
+        else
+            p->sprec[i] = keep;
+    }
+    drop_graph(p);
+    return SVDB_OK;
 }
 
 void destroy(Plan* p) {
@@ -407,6 +446,7 @@ svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts,
         rc = s->sync();
         if (rc) return fail(rc);
     }
+    p->sprec.assign(p->stores.size(), precision);
     rc = (flags & SVDB_RAGGED_AUTOTUNE) ? svdb::autotune(p) : svdb::configure(p, 0, 1);
     if (rc) return fail(rc);
     return reinterpret_cast<svdbd_ragged*>(p);
@@ -431,6 +471,9 @@ int svdbd_ragged_info(svdbd_ragged* hp, svdb_ragged_info* out) {
     out->searches = (int32_t)p->groups.size();
     for (int i = 0; i < 4; ++i) out->tuned_ms[i] = p->tuned_ms[i];
     out->captures = p->captures;
+    for (size_t i = 0; i < p->stores.size() && i < 32; ++i)
+        if (p->sprec[i] == SVDB_PREC_FP8) out->fp8_stores |= 1u << i;
+    for (int i = 0; i < 8; ++i) out->swap_ms[i] = p->swap_ms[i];
     return SVDB_OK;
 }
 

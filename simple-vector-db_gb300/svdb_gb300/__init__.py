@@ -63,7 +63,8 @@ class RaggedPart(C.Structure):
 class RaggedInfo(C.Structure):
     """svdb_ragged_info (include/svdb_gb300.h)."""
     _fields_ = [("grouping", C.c_int32), ("concurrent", C.c_int32), ("graph", C.c_int32), ("searches", C.c_int32),
-                ("tuned_ms", C.c_float * 4), ("captures", C.c_uint32), ("reserved", C.c_uint32)]
+                ("tuned_ms", C.c_float * 4), ("captures", C.c_uint32), ("fp8_stores", C.c_uint32),
+                ("swap_ms", C.c_float * 8)]
 
 
 RAGGED_AUTOTUNE, RAGGED_NO_GRAPH = 1, 2
@@ -456,7 +457,8 @@ class RaggedPlan:
         inf = RaggedInfo()
         _check(lib.svdb_ragged_get_info(self.ptr, C.byref(inf)), "svdb_ragged_get_info")
         return {"grouping": inf.grouping, "concurrent": inf.concurrent, "graph": inf.graph,
-                "searches": inf.searches, "tuned_ms": [float(x) for x in inf.tuned_ms], "captures": inf.captures}
+                "searches": inf.searches, "tuned_ms": [float(x) for x in inf.tuned_ms], "captures": inf.captures,
+                "fp8_stores": inf.fp8_stores, "swap_ms": [float(x) for x in inf.swap_ms]}
 
     def close(self) -> None:
         if getattr(self, "ptr", None):

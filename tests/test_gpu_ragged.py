@@ -75,7 +75,9 @@ def test_ragged_plan_matches_oracle(S, oracle, metric, precision):
     plan = S.RaggedPlan(parts, metric, precision, S.RAGGED_AUTOTUNE)
     info = plan.info()
     assert info["graph"] == 1 and info["captures"] >= 1
-    assert sum(t > 0 for t in info["tuned_ms"]) == 4  # mixed k classes, 3 stores: every choice was timed
+    assert sum(t > 0 for t in info["tuned_ms"]) == 4  # mixed k classes, 3 stores: every layout was timed
+    # cosine: each store's screen was also tried the other way (BF16 <-> FP8)
+    assert sum(t > 0 for t in info["swap_ms"]) == (3 if metric == 0 else 0)
     for b in bufs:  # the plan's results are rewritten by the runs below
         b[1].fill_(7)
     plan.run()
