@@ -102,8 +102,6 @@ int svdb_nearest_batch(VectorDatabase* db, const double* queries, size_t nq, siz
 #define SVDB_DEC_INVALID_JSON 1   /* 400 {"error": "Invalid JSON"} (:300-313) */
 #define SVDB_DEC_SIZE_MISMATCH 2  /* 400 {"error": "Vector size mismatch"} (:318-341) */
 #define SVDB_DEC_INVALID_DATA 3   /* 400 {"error": "Invalid vector data"} (:366-384): a child is not a number */
-#define SVDB_DEC_UNSUPPORTED 4    /* a number of more than 19 significant digits whose first 19 leave its
-                                     rounding open (not decoded; never produced by printf-style %.17g text) */
 int svdb_decode_vectors(const char* text, const uint64_t* offsets, size_t n, size_t dim, double* out,
                         int32_t* status);
 

@@ -205,7 +205,7 @@ def decode_vectors(bodies, dim: int):
     return out, st
 
 
-DEC_OK, DEC_INVALID_JSON, DEC_SIZE_MISMATCH, DEC_INVALID_DATA, DEC_UNSUPPORTED = range(5)
+DEC_OK, DEC_INVALID_JSON, DEC_SIZE_MISMATCH, DEC_INVALID_DATA = range(4)
 
 
 def cosine_similarity(a, b) -> np.float32:
