@@ -262,6 +262,42 @@ def run_ours(args, ws, rank, local):
                                     "fp64_reranked": st8.reranked / nq, "widened_queries": st8.widened,
                                     "bound_failures": st8.bound_failures}}
 
+    # the same searches replayed from captured CUDA graphs: one one-part plan
+    # (svdb_ragged_*) per batch buffer, one graph launch per step (the kernels
+    # of a search are launched back to back by the GPU instead of the host)
+    graph = None
+    if rank == 0 and nq <= 1024:
+        ks = np.full(nq, k, np.int64)
+        plans = [S.RaggedPlan([(db, Qd[b].data_ptr(), nq, DIM, ks, ids.data_ptr(), dists.data_ptr(), k)], metric,
+                              prec, 0) for b in range(nbatch)]
+        for w in range(max(args.warmup, 1)):
+            plans[w % nbatch].run()
+        for pl in plans:
+            pl.wait()
+        t = time.perf_counter()
+        for s in range(args.steps):
+            plans[s % nbatch].run()
+            plans[s % nbatch].wait()
+        gs = time.perf_counter() - t
+        t = time.perf_counter()
+        for s in range(args.steps):  # the direct search, timed the same way
+            step(s)
+            stream.synchronize()
+        ds = time.perf_counter() - t
+        graph = {"value": nq * args.steps / gs, "unit": "queries/s", "ms_per_step": 1e3 * gs / args.steps,
+                 "direct_ms_per_step": 1e3 * ds / args.steps,
+                 "how": "one graph launch per step (a one-part plan per batch buffer) against the direct search "
+                        "(its kernels launched by the host), both timed by the host clock around the call and "
+                        "the wait for it"}
+        ids_g = ids.cpu().numpy()
+        db.search_device(Qd[(args.steps - 1) % nbatch].data_ptr(), nq, DIM, k, metric, prec, ids.data_ptr(),
+                         dists.data_ptr(), 0)
+        torch.cuda.synchronize()
+        if not np.array_equal(ids_g, ids.cpu().numpy()):
+            raise SystemExit("bench: graph replay results differ from the direct search")
+        for pl in plans:
+            pl.close()
+
     # e2e: host buffers through svdb_search_topk (query upload + result read
     # inside), queries and results in page-locked host memory
     Qp = [torch.from_numpy(q).pin_memory().numpy() for q in Qh]
@@ -349,6 +385,8 @@ def run_ours(args, ws, rank, local):
                 "gpu_launches": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": cl}
         if fp8:
             line["fp8_screen"] = fp8
+        if graph:
+            line["graph_replay"] = graph
         print(json.dumps(line), flush=True)
     db.close()
     if dist:
