@@ -987,6 +987,212 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
     return sh[0];
 }
 
+// ---------------------------------------------------------------------------
+// stage 1 for a single cosine query: CUDA cores stream the unit-norm BF16
+// shadow (a 128-query tensor tile would be 1/128 used).  Measured on 1M x 768:
+// one query 0.537 ms per search against 0.579 ms through the tensor-core
+// screen; at four queries the FMAs make it slower (screen stage 0.53 ms
+// against ~0.42 ms), so batches of two or more take the tensor cores.
+// ---------------------------------------------------------------------------
+// The key is the same BF16 dot product bq . bxn as the tensor-core screen's,
+// summed in FP32 by FMAs: the products of BF16 values are exact, and each
+// lane adds KB x 8 of them before a 3-step shuffle tree, so its rounding is
+// below (8 KB + 3) 2^-24 |bq| |bxn| -- far inside the tensor-core
+// accumulation term of the screen bound (cacc |bq| |bxn|, cacc = 20 (ldb/16
+// + 1) 2^-23), so that bound, and everything after the screen, hold as they
+// are.  Three kernels: keys and per-tile maxima; per query the k-th largest
+// tile maximum (tiles are disjoint, so k tile maxima are keys of k distinct
+// rows: a valid lower bound of the k-th best key); then every row whose upper
+// bound reaches the k-th lower bound is a candidate.
+constexpr int kStreamQ = 1;             // queries per streamed search
+constexpr int kStreamStages = 6;        // 32 KB store blocks in flight per SM
+constexpr int kStreamWarps = 8;         // consumer warps (rows 32w .. 32w+31 of each tile)
+constexpr int kStreamQBytes = 32 * 1024;  // query values (FP32) that fit beside the ring
+
+size_t stream_smem(size_t nq, size_t ldb) {
+    return 1024 + (size_t)kStreamStages * 32768 + nq * ldb * sizeof(float) + 2 * kStreamStages * sizeof(uint64_t);
+}
+
+// One CTA per SM over a contiguous range of store tiles: a producer thread
+// keeps the ring of contiguous 32 KB shadow blocks (256 rows x one 128-byte
+// k block, as the tensor-core screen reads them) full with bulk copies; each
+// consumer warp takes 32 rows of the tile, four at a time (8 lanes per row,
+// one 16-byte chunk each), moves its stage into registers and releases it.
+// Keys go to keys[q][slot]; each warp's maximum over its 32 rows of a tile to
+// wmax[q][tile * 8 + warp] (disjoint rows: k of them bound the k-th best key).
+__global__ void __launch_bounds__(32 * (kStreamWarps + 1), 1)
+    k_stream_keys(const uint8_t* __restrict__ xbn, int KB, const __nv_bfloat16* __restrict__ qb, size_t ldb, int nq,
+                  const uint32_t* __restrict__ vbits, size_t npad, int ntr, float* __restrict__ keys,
+                  float* __restrict__ wmax, int* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int K = KB * 64;
+    float* s_q = reinterpret_cast<float*>(ring + (size_t)kStreamStages * 32768);
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_q + (size_t)nq * K);  // K is a multiple of 64: 8-byte aligned
+    uint64_t* empty = full + kStreamStages;
+    __shared__ int s_abort;
+    volatile int* abort = &s_abort;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStreamStages; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], kStreamWarps);
+        }
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    for (int i = threadIdx.x; i < nq * K; i += blockDim.x) {
+        const int qi = i / K;
+        s_q[i] = __bfloat162float(qb[(size_t)qi * ldb + (i - qi * K)]);
+    }
+    __syncthreads();
+    const int t0 = (int)((int64_t)blockIdx.x * ntr / gridDim.x), t1 = (int)((int64_t)(blockIdx.x + 1) * ntr / gridDim.x);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == kStreamWarps) {
+        if (lane == 0) {  // producer
+            uint32_t g = 0;
+            bool ok = true;
+            for (int t = t0; t < t1 && ok; ++t)
+                for (int kb = 0; kb < KB; ++kb) {
+                    const uint32_t st = g % kStreamStages;
+                    if (!mbar_wait(&empty[st], ((g / kStreamStages) & 1u) ^ 1u, abort, scr::kWaitLimitNs)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(&full[st], 32768);
+                    bulk_load(ring + (size_t)st * 32768, xbn + ((size_t)t * KB + kb) * 32768, 32768, &full[st]);
+                    ++g;
+                }
+            // every issued copy lands before the CTA may exit
+            volatile int no_abort = 0;
+            for (uint32_t i = 0; i < (g < (uint32_t)kStreamStages ? g : (uint32_t)kStreamStages); ++i) {
+                const uint32_t n = g - 1 - i;
+                mbar_wait(&full[n % kStreamStages], (n / kStreamStages) & 1u, &no_abort, scr::kWaitLimitNs / 4);
+            }
+        }
+    } else {
+        const int g8 = lane & 7, rsub = lane >> 3;
+        // the 128-byte swizzle: granule g8 of a row r holds chunk g8 ^ (r & 7); the
+        // rows of step s are 32 warp + 4 s + rsub, so r & 7 = rsub (even s) or rsub + 4
+        const int ce = g8 ^ rsub, co = g8 ^ (rsub + 4);
+        uint32_t g = 0;
+        bool alive = true;
+        for (int t = t0; t < t1 && alive; ++t) {
+            float acc[8][kStreamQ];
+#pragma unroll
+            for (int s = 0; s < 8; ++s)
+#pragma unroll
+                for (int qi = 0; qi < kStreamQ; ++qi) acc[s][qi] = 0.f;
+            for (int kb = 0; kb < KB; ++kb, ++g) {
+                const uint32_t st = g % kStreamStages;
+                const bool got = mbar_wait(&full[st], (g / kStreamStages) & 1u, abort, scr::kWaitLimitNs);
+                if (!__all_sync(0xffffffffu, got)) {
+                    alive = false;
+                    break;
+                }
+                const uint8_t* blk = ring + (size_t)st * 32768 + (size_t)(warp * 32 + rsub) * 128 + g8 * 16;
+                uint4 v[8];
+#pragma unroll
+                for (int s = 0; s < 8; ++s) v[s] = *reinterpret_cast<const uint4*>(blk + s * 512);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&empty[st]);  // the stage is in registers
+#pragma unroll
+                for (int qi = 0; qi < kStreamQ; ++qi) {
+                    if (qi < nq) {
+                        const float* qq = s_q + (size_t)qi * K + kb * 64;
+                        const float4 e0 = *reinterpret_cast<const float4*>(qq + ce * 8);
+                        const float4 e1 = *reinterpret_cast<const float4*>(qq + ce * 8 + 4);
+                        const float4 o0 = *reinterpret_cast<const float4*>(qq + co * 8);
+                        const float4 o1 = *reinterpret_cast<const float4*>(qq + co * 8 + 4);
+#pragma unroll
+                        for (int s = 0; s < 8; ++s) {
+                            const float4 a = (s & 1) ? o0 : e0, b = (s & 1) ? o1 : e1;
+                            float r = acc[s][qi];
+                            r = __fmaf_rn(__uint_as_float(v[s].x << 16), a.x, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].x & 0xffff0000u), a.y, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].y << 16), a.z, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].y & 0xffff0000u), a.w, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].z << 16), b.x, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].z & 0xffff0000u), b.y, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].w << 16), b.z, r);
+                            r = __fmaf_rn(__uint_as_float(v[s].w & 0xffff0000u), b.w, r);
+                            acc[s][qi] = r;
+                        }
+                    }
+                }
+            }
+            if (!alive) break;
+            const uint32_t vw = __ldg(vbits + (((size_t)t * 256 + warp * 32) >> 5));  // this warp's 32 rows
+            float m[kStreamQ];
+#pragma unroll
+            for (int qi = 0; qi < kStreamQ; ++qi) m[qi] = -INFINITY;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                const int rw = s * 4 + rsub;  // row within the warp's 32
+                const bool valid = (vw >> rw) & 1u;
+                const size_t slot = (size_t)t * 256 + warp * 32 + rw;
+#pragma unroll
+                for (int qi = 0; qi < kStreamQ; ++qi) {
+                    float a = acc[s][qi];
+                    a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 1));
+                    a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 2));
+                    a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 4));
+                    if (qi < nq) {
+                        if (g8 == 0) keys[(size_t)qi * npad + slot] = valid ? a : __int_as_float(0x7fc00000);
+                        if (valid) m[qi] = fmaxf(m[qi], a);
+                    }
+                }
+            }
+#pragma unroll
+            for (int qi = 0; qi < kStreamQ; ++qi) {
+                float x = m[qi];
+                for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+                if (lane == 0 && qi < nq) wmax[(size_t)qi * ntr * kStreamWarps + (size_t)t * kStreamWarps + warp] = x;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_abort) atomicExch(err, 1);
+}
+
+// per query: the candidate cut = (k-th largest warp maximum - E) - E, E the
+// query's bound over every row (the screen's cosine eq0), rounded down
+__global__ void __launch_bounds__(1024) k_stream_cut(const float* __restrict__ tmax, int ntr, int k,
+                                                    const float4* __restrict__ qpar, const int* __restrict__ nmax,
+                                                    float* __restrict__ cut) {
+    __shared__ int hist[256];
+    __shared__ uint32_t sh[3];
+    const int q = blockIdx.x;
+    const float* t = tmax + (size_t)q * ntr;
+    const uint32_t u = ntr >= k ? block_kth_largest([&](int i) { return f2u_ord(t[i]); }, ntr, k, hist, sh)
+                                : f2u_ord(-INFINITY);
+    if (threadIdx.x == 0) {
+        const float4 qp = qpar[q];
+        const float kth = __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+        const float e = __fmaf_ru(qp.x, __int_as_float(__ldg(nmax)), __fmaf_ru(qp.y, __int_as_float(__ldg(nmax + 1)), qp.z));
+        cut[q] = qp.w != 0.f ? __fsub_rd(__fsub_rd(kth, e), e) : INFINITY;  // invalid queries: no candidates
+    }
+}
+
+// every row whose key reaches the cut, into the query's single candidate list
+__global__ void __launch_bounds__(256) k_stream_emit(const float* __restrict__ keys, size_t npad, int nq,
+                                                     const float* __restrict__ cut, int cap, int* __restrict__ cnt,
+                                                     int2* __restrict__ cand) {
+    const size_t row = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    for (int qi = 0; qi < nq; ++qi) {
+        const float key = row < npad ? keys[(size_t)qi * npad + row] : __int_as_float(0x7fc00000);
+        const bool want = key >= __ldg(cut + qi);  // NaN rows never
+        const uint32_t m = __ballot_sync(0xffffffffu, want);
+        if (!m) continue;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(cnt + qi, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int slot = base + __popc(m & ((1u << lane) - 1u));
+        if (want && slot < cap) cand[(size_t)qi * cap + slot] = make_int2((int)row, __float_as_int(key));
+    }
+}
+
 // Pass 1: every thread keeps the k best lower bounds of its candidates
 // (registers); their union holds the k best overall, so a radix select over
 // it in shared memory gives the exact k-th largest.  Pass 2: survivors.
@@ -1511,6 +1717,7 @@ struct GemmPlanCache {
     bool sort_attr = false;
     bool rerank_attr = false;
     bool refine_attr = false;
+    bool stream_attr = false;
     size_t screen_smem = 0;
 };
 
@@ -1578,6 +1785,7 @@ static int make_map8(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t 
 
 struct Bf16Layout {
     size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
+    size_t tmax = 0, cut = 0;  // the streamed screen of a single query (its keys reuse spar: npad floats)
     int ntr, cap;
     int nctas, nsub, subcap;
     size_t npad;
@@ -1673,6 +1881,10 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.vbits = take(L.npad / 8);
     L.tau = take(nq * sizeof(int));
     L.bins = take(nq * k_max_bf16 * sizeof(int));
+    if (nq <= (size_t)kStreamQ) {
+        L.tmax = take(nq * (size_t)L.ntr * kStreamWarps * sizeof(float));
+        L.cut = take(nq * sizeof(float));
+    }
     int maxsub = 1;
     L.nctas = screen_schedule((int)((nq + scr::kBM - 1) / scr::kBM), L.ntr, L.sched, &maxsub);
     L.nsub = 2 * maxsub;
@@ -1858,8 +2070,11 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
                                                                               a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
-    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, L.nsub, flags, nq, k, alpha, redo_n,
-                                                                         dstats, seed);
+    // a single cosine query: the streamed screen, one candidate list
+    const bool stream = norm && !f8 && nq <= kStreamQ && (size_t)nq * s->ldb * sizeof(float) <= (size_t)kStreamQBytes;
+    const int nsub_use = stream ? 1 : L.nsub, subcap_use = stream ? L.cap : L.subcap;
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, nsub_use, flags, nq, k, alpha,
+                                                                         redo_n, dstats, seed);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
                                                                           (int64_t)s->slots, (int64_t)L.npad,
@@ -1868,6 +2083,27 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
+    if (stream) {
+        float* keys = reinterpret_cast<float*>(spar);  // nq x npad floats: the cosine screen does not use spar
+        float* tmax = reinterpret_cast<float*>(base + L.tmax);
+        float* cut = reinterpret_cast<float*>(base + L.cut);
+        const int KB = (int)(s->ldb / scr::kBK);
+        const size_t smem = stream_smem((size_t)nq, s->ldb);
+        if (!gc->stream_attr) {
+            SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)stream_smem(kStreamQ, kStreamQBytes / (kStreamQ * sizeof(float)))));
+            gc->stream_attr = true;
+        }
+        const int grid = std::min(L.ntr, num_sms());
+        k_stream_keys<<<(unsigned)grid, 32 * (kStreamWarps + 1), smem, s->stream>>>(
+            reinterpret_cast<const uint8_t*>(s->xbn), KB, qb, s->ldb, nq, vbits, L.npad, L.ntr, keys, tmax, s->d_err);
+        SVDB_LAUNCH_CHECK();
+        k_stream_cut<<<(unsigned)nq, 1024, 0, s->stream>>>(tmax, L.ntr * kStreamWarps, k, qpar, s->d_count + 1, cut);
+        SVDB_LAUNCH_CHECK();
+        k_stream_emit<<<(unsigned)(L.npad / 256), 256, 0, s->stream>>>(keys, L.npad, nq, cut, L.cap, cnt, cand);
+        SVDB_LAUNCH_CHECK();
+        kernels += 3;
+    } else {
     CUtensorMap tmq;
     rc = f8 ? make_map8(gc, &tmq, qb, a.nq, s->ldb8, scr::kBM) : make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
     if (rc) return rc;
@@ -1899,9 +2135,10 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     screen_kernel(f8)<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, P);
     SVDB_LAUNCH_CHECK();
     ++kernels;
+    }
     s->prof_mark(2);
 
-    rc = launch_select(L.nsub, L.subcap, qpar, nullptr);
+    rc = launch_select(nsub_use, subcap_use, qpar, nullptr);
     if (rc) return rc;
     s->prof_mark(3);
     const size_t ref_smem = s->ld * sizeof(float);
@@ -1964,7 +2201,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     // queries the screen could not certify: exact FP64 scan, entirely on the
     // device (no host round trip; with nothing to redo the kernels exit at once)
-    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, L.nsub, nsurv, nref, nq, redo, redo_n,
+    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, nsub_use, nsurv, nref, nq, redo, redo_n,
                                                                           dstats);
     SVDB_LAUNCH_CHECK();
     {

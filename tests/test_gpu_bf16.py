@@ -281,3 +281,41 @@ def test_bf16_grouped_refinement_wide_rows(S, oracle, d):
             assert np.array_equal(vals, wval), (metric, k)
             assert st.bound_failures == 0 and st.widened == 0, (metric, k)
     db.close()
+
+
+@pytest.mark.parametrize("d", [64, 200, 768, 1536])
+def test_bf16_streamed_few_queries(S, oracle, d):
+    """A single cosine query takes the CUDA-core streamed screen (2 to 5 take
+    the tensor-core one): near-tie mixtures, every k class, exact
+    duplicates, zero and deleted rows, a partial last tile, and a query that
+    is zero (its cosines are NaN: no candidates, answered by the FP64 scan).
+    Every single-query cosine search of the other tests takes it too."""
+    rng = np.random.default_rng(900 + d)
+    C, X = _mixture(rng, 20_000 + 77, d, 16)
+    X[[5, 9000]] = 0.0
+    X[12000] = X[11999]  # an exact duplicate: ties to the lower index
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    host = list(X)
+    for i in (0, 100, 15000):
+        db.delete(i)
+        host.pop(i)
+    H = np.stack(host)
+    for nq in (1, 2, 3, 4, 5):
+        Q = C[rng.integers(0, 16, nq)] + 0.05 * rng.normal(size=(nq, d))
+        if nq == 3:
+            Q[1] = H[11998] * 2.0  # the duplicated row's direction: two exact ties at the top
+        if nq == 4:
+            Q[2] = 0.0
+        for k in (1, 10, 33, 100, 128):
+            ids, vals, st = _search_both(S, db, Q, k, 0)
+            wid, wval = oracle.topk(0, H, Q, k)
+            assert np.array_equal(ids, wid), (nq, k, st.widened)
+            assert ((vals == wval) | (np.isnan(vals) & np.isnan(wval))).all(), (nq, k)
+            assert st.bound_failures == 0
+            zero = 1 if nq == 4 else 0
+            if k <= 33:  # answered by the screen (not the FP64 scan), but for the zero query
+                assert st.widened == zero, (nq, k, st.widened)
+            else:
+                assert st.widened <= zero + (nq - zero) // 2, (nq, k, st.widened)
+    db.close()
