@@ -990,8 +990,8 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
 // ---------------------------------------------------------------------------
 // stage 1 for a single cosine query: CUDA cores stream the unit-norm BF16
 // shadow (a 128-query tensor tile would be 1/128 used).  Measured on 1M x 768:
-// one query 0.537 ms per search against 0.579 ms through the tensor-core
-// screen; at four queries the FMAs make it slower (screen stage 0.53 ms
+// one query 0.51 ms per search against 0.579 ms through the tensor-core
+// screen; at four queries the FMAs made it slower (screen stage 0.53 ms
 // against ~0.42 ms), so batches of two or more take the tensor cores.
 // ---------------------------------------------------------------------------
 // The key is the same BF16 dot product bq . bxn as the tensor-core screen's,
@@ -1004,155 +1004,113 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
 // tile maximum (tiles are disjoint, so k tile maxima are keys of k distinct
 // rows: a valid lower bound of the k-th best key); then every row whose upper
 // bound reaches the k-th lower bound is a candidate.
-constexpr int kStreamQ = 1;             // queries per streamed search
-constexpr int kStreamStages = 6;        // 32 KB store blocks in flight per SM
-constexpr int kStreamWarps = 8;         // consumer warps (rows 32w .. 32w+31 of each tile)
-constexpr int kStreamQBytes = 32 * 1024;  // query values (FP32) that fit beside the ring
+constexpr int kStreamQ = 1;               // queries per streamed search
+constexpr int kStreamWarps = 8;           // warps per store tile (rows 32w .. 32w+31)
+constexpr int kStreamQBytes = 32 * 1024;  // query values (FP32) in shared memory
 
-size_t stream_smem(size_t nq, size_t ldb) {
-    return 1024 + (size_t)kStreamStages * 32768 + nq * ldb * sizeof(float) + 2 * kStreamStages * sizeof(uint64_t);
-}
+size_t stream_smem(size_t nq, size_t ldb) { return nq * ldb * sizeof(float); }
 
-// One CTA per SM over a contiguous range of store tiles: a producer thread
-// keeps the ring of contiguous 32 KB shadow blocks (256 rows x one 128-byte
-// k block, as the tensor-core screen reads them) full with bulk copies; each
-// consumer warp takes 32 rows of the tile, four at a time (8 lanes per row,
-// one 16-byte chunk each), moves its stage into registers and releases it.
-// Keys go to keys[q][slot]; each warp's maximum over its 32 rows of a tile to
+// One block per 256-row store tile, reading the tile's 32 KB blocks (256
+// rows x one 128-byte k block, as stored for the tensor-core screen) whole
+// and in order: warp w takes rows 32w .. 32w+31, four at a time (8 lanes per
+// row, one 16-byte chunk each), 16 loads in flight per lane.  Plain vector
+// loads from many resident blocks stream HBM faster here than a bulk-copy
+// ring: on 1M x 768 the screen stage takes 0.345 ms, against 0.371 ms with
+// one CTA per SM keeping six 32 KB bulk copies in flight.  Keys go
+// to keys[q][slot]; each warp's maximum over its 32 rows of a tile to
 // wmax[q][tile * 8 + warp] (disjoint rows: k of them bound the k-th best key).
-__global__ void __launch_bounds__(32 * (kStreamWarps + 1), 1)
+__global__ void __launch_bounds__(32 * kStreamWarps)
     k_stream_keys(const uint8_t* __restrict__ xbn, int KB, const __nv_bfloat16* __restrict__ qb, size_t ldb, int nq,
                   const uint32_t* __restrict__ vbits, size_t npad, int ntr, float* __restrict__ keys,
-                  float* __restrict__ wmax, int* __restrict__ err) {
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t* ring = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+                  float* __restrict__ wmax) {
+    extern __shared__ float s_q[];  // nq x K query values (BF16 -> FP32 is exact)
     const int K = KB * 64;
-    float* s_q = reinterpret_cast<float*>(ring + (size_t)kStreamStages * 32768);
-    uint64_t* full = reinterpret_cast<uint64_t*>(s_q + (size_t)nq * K);  // K is a multiple of 64: 8-byte aligned
-    uint64_t* empty = full + kStreamStages;
-    __shared__ int s_abort;
-    volatile int* abort = &s_abort;
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < kStreamStages; ++i) {
-            mbar_init(&full[i], 1);
-            mbar_init(&empty[i], kStreamWarps);
-        }
-        s_abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
     for (int i = threadIdx.x; i < nq * K; i += blockDim.x) {
         const int qi = i / K;
         s_q[i] = __bfloat162float(qb[(size_t)qi * ldb + (i - qi * K)]);
     }
     __syncthreads();
-    const int t0 = (int)((int64_t)blockIdx.x * ntr / gridDim.x), t1 = (int)((int64_t)(blockIdx.x + 1) * ntr / gridDim.x);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp == kStreamWarps) {
-        if (lane == 0) {  // producer
-            uint32_t g = 0;
-            bool ok = true;
-            for (int t = t0; t < t1 && ok; ++t)
-                for (int kb = 0; kb < KB; ++kb) {
-                    const uint32_t st = g % kStreamStages;
-                    if (!mbar_wait(&empty[st], ((g / kStreamStages) & 1u) ^ 1u, abort, scr::kWaitLimitNs)) {
-                        ok = false;
-                        break;
-                    }
-                    mbar_expect_tx(&full[st], 32768);
-                    bulk_load(ring + (size_t)st * 32768, xbn + ((size_t)t * KB + kb) * 32768, 32768, &full[st]);
-                    ++g;
+    const int t = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g8 = lane & 7, rsub = lane >> 3;
+    // the 128-byte swizzle: granule g8 of a row r holds chunk g8 ^ (r & 7); the
+    // rows of step s are 32 warp + 4 s + rsub, so r & 7 = rsub (even s) or rsub + 4
+    const int ce = g8 ^ rsub, co = g8 ^ (rsub + 4);
+    const uint8_t* src = xbn + ((size_t)t * KB * 256 + warp * 32 + rsub) * 128 + g8 * 16;
+    float acc[8][kStreamQ];
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+#pragma unroll
+        for (int qi = 0; qi < kStreamQ; ++qi) acc[s][qi] = 0.f;
+    auto fold = [&](const uint4 (&v)[8], int kb) {
+#pragma unroll
+        for (int qi = 0; qi < kStreamQ; ++qi) {
+            if (qi < nq) {
+                const float* qq = s_q + (size_t)qi * K + kb * 64;
+                const float4 e0 = *reinterpret_cast<const float4*>(qq + ce * 8);
+                const float4 e1 = *reinterpret_cast<const float4*>(qq + ce * 8 + 4);
+                const float4 o0 = *reinterpret_cast<const float4*>(qq + co * 8);
+                const float4 o1 = *reinterpret_cast<const float4*>(qq + co * 8 + 4);
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    const float4 a = (s & 1) ? o0 : e0, b = (s & 1) ? o1 : e1;
+                    float r = acc[s][qi];
+                    r = __fmaf_rn(__uint_as_float(v[s].x << 16), a.x, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].x & 0xffff0000u), a.y, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].y << 16), a.z, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].y & 0xffff0000u), a.w, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].z << 16), b.x, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].z & 0xffff0000u), b.y, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].w << 16), b.z, r);
+                    r = __fmaf_rn(__uint_as_float(v[s].w & 0xffff0000u), b.w, r);
+                    acc[s][qi] = r;
                 }
-            // every issued copy lands before the CTA may exit
-            volatile int no_abort = 0;
-            for (uint32_t i = 0; i < (g < (uint32_t)kStreamStages ? g : (uint32_t)kStreamStages); ++i) {
-                const uint32_t n = g - 1 - i;
-                mbar_wait(&full[n % kStreamStages], (n / kStreamStages) & 1u, &no_abort, scr::kWaitLimitNs / 4);
             }
         }
-    } else {
-        const int g8 = lane & 7, rsub = lane >> 3;
-        // the 128-byte swizzle: granule g8 of a row r holds chunk g8 ^ (r & 7); the
-        // rows of step s are 32 warp + 4 s + rsub, so r & 7 = rsub (even s) or rsub + 4
-        const int ce = g8 ^ rsub, co = g8 ^ (rsub + 4);
-        uint32_t g = 0;
-        bool alive = true;
-        for (int t = t0; t < t1 && alive; ++t) {
-            float acc[8][kStreamQ];
+    };
+    int kb = 0;
+    for (; kb + 1 < KB; kb += 2) {  // two k blocks (16 loads) in flight
+        uint4 v0[8], v1[8];
 #pragma unroll
-            for (int s = 0; s < 8; ++s)
+        for (int s = 0; s < 8; ++s) {
+            v0[s] = __ldcs(reinterpret_cast<const uint4*>(src + (size_t)kb * 32768 + s * 512));
+            v1[s] = __ldcs(reinterpret_cast<const uint4*>(src + (size_t)(kb + 1) * 32768 + s * 512));
+        }
+        fold(v0, kb);
+        fold(v1, kb + 1);
+    }
+    if (kb < KB) {
+        uint4 v0[8];
 #pragma unroll
-                for (int qi = 0; qi < kStreamQ; ++qi) acc[s][qi] = 0.f;
-            for (int kb = 0; kb < KB; ++kb, ++g) {
-                const uint32_t st = g % kStreamStages;
-                const bool got = mbar_wait(&full[st], (g / kStreamStages) & 1u, abort, scr::kWaitLimitNs);
-                if (!__all_sync(0xffffffffu, got)) {
-                    alive = false;
-                    break;
-                }
-                const uint8_t* blk = ring + (size_t)st * 32768 + (size_t)(warp * 32 + rsub) * 128 + g8 * 16;
-                uint4 v[8];
+        for (int s = 0; s < 8; ++s) v0[s] = __ldcs(reinterpret_cast<const uint4*>(src + (size_t)kb * 32768 + s * 512));
+        fold(v0, kb);
+    }
+    const uint32_t vw = __ldg(vbits + (((size_t)t * 256 + warp * 32) >> 5));  // this warp's 32 rows
+    float m[kStreamQ];
 #pragma unroll
-                for (int s = 0; s < 8; ++s) v[s] = *reinterpret_cast<const uint4*>(blk + s * 512);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&empty[st]);  // the stage is in registers
+    for (int qi = 0; qi < kStreamQ; ++qi) m[qi] = -INFINITY;
 #pragma unroll
-                for (int qi = 0; qi < kStreamQ; ++qi) {
-                    if (qi < nq) {
-                        const float* qq = s_q + (size_t)qi * K + kb * 64;
-                        const float4 e0 = *reinterpret_cast<const float4*>(qq + ce * 8);
-                        const float4 e1 = *reinterpret_cast<const float4*>(qq + ce * 8 + 4);
-                        const float4 o0 = *reinterpret_cast<const float4*>(qq + co * 8);
-                        const float4 o1 = *reinterpret_cast<const float4*>(qq + co * 8 + 4);
+    for (int s = 0; s < 8; ++s) {
+        const int rw = s * 4 + rsub;  // row within the warp's 32
+        const bool valid = (vw >> rw) & 1u;
+        const size_t slot = (size_t)t * 256 + warp * 32 + rw;
 #pragma unroll
-                        for (int s = 0; s < 8; ++s) {
-                            const float4 a = (s & 1) ? o0 : e0, b = (s & 1) ? o1 : e1;
-                            float r = acc[s][qi];
-                            r = __fmaf_rn(__uint_as_float(v[s].x << 16), a.x, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].x & 0xffff0000u), a.y, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].y << 16), a.z, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].y & 0xffff0000u), a.w, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].z << 16), b.x, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].z & 0xffff0000u), b.y, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].w << 16), b.z, r);
-                            r = __fmaf_rn(__uint_as_float(v[s].w & 0xffff0000u), b.w, r);
-                            acc[s][qi] = r;
-                        }
-                    }
-                }
-            }
-            if (!alive) break;
-            const uint32_t vw = __ldg(vbits + (((size_t)t * 256 + warp * 32) >> 5));  // this warp's 32 rows
-            float m[kStreamQ];
-#pragma unroll
-            for (int qi = 0; qi < kStreamQ; ++qi) m[qi] = -INFINITY;
-#pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                const int rw = s * 4 + rsub;  // row within the warp's 32
-                const bool valid = (vw >> rw) & 1u;
-                const size_t slot = (size_t)t * 256 + warp * 32 + rw;
-#pragma unroll
-                for (int qi = 0; qi < kStreamQ; ++qi) {
-                    float a = acc[s][qi];
-                    a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 1));
-                    a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 2));
-                    a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 4));
-                    if (qi < nq) {
-                        if (g8 == 0) keys[(size_t)qi * npad + slot] = valid ? a : __int_as_float(0x7fc00000);
-                        if (valid) m[qi] = fmaxf(m[qi], a);
-                    }
-                }
-            }
-#pragma unroll
-            for (int qi = 0; qi < kStreamQ; ++qi) {
-                float x = m[qi];
-                for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
-                if (lane == 0 && qi < nq) wmax[(size_t)qi * ntr * kStreamWarps + (size_t)t * kStreamWarps + warp] = x;
+        for (int qi = 0; qi < kStreamQ; ++qi) {
+            float a = acc[s][qi];
+            a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 1));
+            a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 2));
+            a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 4));
+            if (qi < nq) {
+                if (g8 == 0) keys[(size_t)qi * npad + slot] = valid ? a : __int_as_float(0x7fc00000);
+                if (valid) m[qi] = fmaxf(m[qi], a);
             }
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && s_abort) atomicExch(err, 1);
+#pragma unroll
+    for (int qi = 0; qi < kStreamQ; ++qi) {
+        float x = m[qi];
+        for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if (lane == 0 && qi < nq) wmax[(size_t)qi * ntr * kStreamWarps + (size_t)t * kStreamWarps + warp] = x;
+    }
 }
 
 // per query: the candidate cut = (k-th largest warp maximum - E) - E, E the
@@ -2090,13 +2048,11 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         const int KB = (int)(s->ldb / scr::kBK);
         const size_t smem = stream_smem((size_t)nq, s->ldb);
         if (!gc->stream_attr) {
-            SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)stream_smem(kStreamQ, kStreamQBytes / (kStreamQ * sizeof(float)))));
+            SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamQBytes));
             gc->stream_attr = true;
         }
-        const int grid = std::min(L.ntr, num_sms());
-        k_stream_keys<<<(unsigned)grid, 32 * (kStreamWarps + 1), smem, s->stream>>>(
-            reinterpret_cast<const uint8_t*>(s->xbn), KB, qb, s->ldb, nq, vbits, L.npad, L.ntr, keys, tmax, s->d_err);
+        k_stream_keys<<<(unsigned)L.ntr, 32 * kStreamWarps, smem, s->stream>>>(
+            reinterpret_cast<const uint8_t*>(s->xbn), KB, qb, s->ldb, nq, vbits, L.npad, L.ntr, keys, tmax);
         SVDB_LAUNCH_CHECK();
         k_stream_cut<<<(unsigned)nq, 1024, 0, s->stream>>>(tmax, L.ntr * kStreamWarps, k, qpar, s->d_count + 1, cut);
         SVDB_LAUNCH_CHECK();
