@@ -125,6 +125,18 @@ def _el_numbers(seed):
     return [t.encode() for t in texts]
 
 
+def test_oracle_numbers_at_every_exponent(oracle):
+    """The oracle (cJSON's run + the C library's strtod) on the exponent and
+    tie corpus equals Python's correctly rounded float() bit for bit."""
+    texts = _el_numbers(5)
+    for i in range(0, len(texts), 64):
+        chunk = texts[i:i + 64]
+        st, v = oracle.decode_body(b"[" + b",".join(chunk) + b"]", len(chunk))
+        assert st == 0
+        want = np.array([float(t) for t in chunk], np.float64)
+        assert v.tobytes() == want.tobytes(), i
+
+
 @pytest.mark.gpu
 def test_device_numbers_at_every_exponent(svdb, oracle):
     """The fast conversion (128-bit powers of five) and the exact fallback it
