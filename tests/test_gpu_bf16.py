@@ -318,4 +318,10 @@ def test_bf16_streamed_few_queries(S, oracle, d):
                 assert st.widened == zero, (nq, k, st.widened)
             else:
                 assert st.widened <= zero + (nq - zero) // 2, (nq, k, st.widened)
+    Z = np.zeros((1, d))  # a lone zero query on the streamed path: no candidates, the FP64 scan answers
+    ids, vals, st = _search_both(S, db, Z, 10, 0)
+    wid, wval = oracle.topk(0, H, Z, 10)
+    assert np.array_equal(ids, wid)
+    assert ((vals == wval) | (np.isnan(vals) & np.isnan(wval))).all()
+    assert st.widened == 1 and st.bound_failures == 0
     db.close()
