@@ -1877,7 +1877,9 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     return L;
 }
 
-size_t search_bf16_scratch(const Store* s, size_t nq, size_t k) { return bf16_layout(s, nq).total; }
+size_t search_bf16_scratch(const Store* s, size_t nq, size_t /*k: the layout holds k up to k_max_bf16*/) {
+    return bf16_layout(s, nq).total;
+}
 
 bool bf16_supported(const Store* s, size_t k) { return k <= k_max_bf16 && s->n_unscreen == 0 && s->nlive > 0; }
 
