@@ -143,3 +143,47 @@ def test_library_fails_loudly_without_gpu(svdb):
     with pytest.raises(svdb.SvdbError):
         db.find_uuid(["a"])
     db.close()
+
+
+def test_binding_structs_match_the_header(svdb, tmp_path):
+    """The Python mirrors of the header's structs (ctypes classes and the
+    serving NumPy dtypes) have the C compiler's sizes and field offsets."""
+    import shutil
+
+    from svdb_gb300 import serve
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    here = os.path.dirname(os.path.abspath(__file__))
+    inc = os.path.join(here, os.pardir, "include")
+    mirrors = {
+        "svdb_search_stats": svdb.SearchStats,
+        "svdb_ragged_part": svdb.RaggedPart,
+        "svdb_ragged_info": svdb.RaggedInfo,
+    }
+    dtypes = {"svdb_request": serve.REQ_DTYPE, "svdb_response": serve.RESP_DTYPE}
+    lines = []
+    for name, cls in mirrors.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f in cls._fields_:
+            lines.append(f'printf("{name}.{f[0]} %zu\\n", offsetof({name}, {f[0]}));')
+    for name, dt in dtypes.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f in dt.names:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"svdb_gb300.h\"\nint main(void) {\n" +
+                   "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                  text=True).stdout.splitlines())
+    for name, cls in mirrors.items():
+        assert int(got[name]) == C.sizeof(cls), name
+        for f in cls._fields_:
+            assert int(got[f"{name}.{f[0]}"]) == getattr(cls, f[0]).offset, (name, f[0])
+    for name, dt in dtypes.items():
+        assert int(got[name]) == dt.itemsize, name
+        for f in dt.names:
+            assert int(got[f"{name}.{f}"]) == dt.fields[f][1], (name, f)
