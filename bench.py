@@ -44,10 +44,11 @@ METRICS = {"cosine": 0, "euclidean": 1, "dot": 2}
 N_ROWS, DIM, K_TOP, SEED = 1_000_000, 768, 10, 3
 N_ROWS_DEFAULT = N_ROWS
 METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GPU; p50/p99 ms"
-# DRAM bytes (read + write) of one k_screen_bf16 launch per store row, from the
-# ncu capture summarised in profiles/k_screen_bf16_200kx768_q4096.md (a 200,000-row
-# store, 4096 cosine queries; the bytes grow with the rows, so a full launch is
-# this times N).  None when no capture of the current kernel exists.
+# DRAM bytes (read + write) of one k_screen_bf16 launch per store row, from an
+# ncu capture of the screen on a 200,000-row store of the same mixture with the
+# same 4096 cosine queries (the shadow is read once per launch, so the bytes
+# grow with the rows and a full launch is this times N).  None when no capture
+# of the current kernel exists.
 SCREEN_DRAM_BYTES_PER_ROW = (420.257536e6 + 19.836416e6) / 200_000
 
 
@@ -109,6 +110,41 @@ def dist_env():
     return ws, rank, local
 
 
+def workloads():
+    """The seeded workload generators (svdb_gb300/workloads.py, numpy only),
+    loaded from their file so that the CPU reference arm never imports the
+    package, whose import loads the CUDA library."""
+    import importlib.util
+    name = "svdb_workloads_standalone"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, os.path.join(PKG, "svdb_gb300", "workloads.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        sys.modules[name] = mod
+    return sys.modules[name]
+
+
+def headline_config(args, ws):
+    """The workload both arms measure (identical dicts: the reference arm
+    times a bounded sample of it, described in its cpu_baseline)."""
+    return {"workload": f"1M x 768 FP64 Gaussian mixture (1024 centres, sigma 0.05, seed 3), exact top-{K_TOP} "
+                        f"{args.metric}", "rows": N_ROWS, "dim": DIM, "k": K_TOP, "metric": args.metric,
+            "query_batch": args.q, "parallelism": f"replicas{ws}",
+            "l2": "store (6.1 GB FP64) larger than L2; no flush needed"}
+
+
+def guard_sample(nq):
+    """Queries checked against the oracle: one in every 128-query tile (its
+    middle), plus the batch's first and last."""
+    return np.union1d(np.arange(64, nq, 128), [0, nq - 1]) if nq > 1 else np.array([0])
+
+
+def oracle_topk(X, Q, metric, k):
+    import oracle as O
+    O.build(ref=False)
+    return O.Oracle().topk(metric, X, Q, k, threads=os.cpu_count() or 1)
+
+
 def cpu_baseline(X, Q, metric, k, sample, threads):
     """Oracle FP64 brute force on `sample` queries, all given threads."""
     import oracle as O
@@ -122,14 +158,18 @@ def cpu_baseline(X, Q, metric, k, sample, threads):
 
 
 def run_reference(args, ws, rank):
+    """The CPU path: the oracle's multi-threaded FP64 brute force (the
+    reference's metric formulas over every stored row, heap top-k) on all
+    host cores, each step a bounded sample of the headline batch.  Touches
+    neither the GPU nor the CUDA library."""
     if rank != 0:
         return
-    from svdb_gb300 import workloads as W
+    W = workloads()
     mix, X = W.config3(N_ROWS, DIM, SEED)
     metric = METRICS[args.metric]
     threads = os.cpu_count() or 1
     times = []
-    sample = args.cpu_sample
+    sample = min(args.cpu_sample, args.q)
     Qs = mix.sample(sample * (args.steps + args.warmup), 1)
     for s in range(args.warmup + args.steps):
         _, dt = cpu_baseline(X, Qs[s * sample:], metric, K_TOP, sample, threads)
@@ -140,11 +180,10 @@ def run_reference(args, ws, rank):
     line = {"impl": "reference", "metric": METRIC_NAME, "value": v, "unit": "queries/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "1M x 768 FP64 Gaussian mixture (1024 centres, sigma 0.05, "
-                                                         "seed 3), exact top-10 " + args.metric,
-                                            "query_batch": sample, "l2": "store (6.1 GB) larger than L2"},
+            "data": "synthetic", "config": headline_config(args, ws),
             "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} queries per step over the full 1M x 768 store"},
+                             "sample": f"{sample} queries of the {args.q}-query batch per step over the full "
+                                       f"1M x 768 store (FP64 brute force, {threads} threads)"},
             "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -152,7 +191,7 @@ def run_reference(args, ws, rank):
 def run_ours(args, ws, rank, local):
     import torch
     import svdb_gb300 as S
-    from svdb_gb300 import workloads as W
+    W = workloads()
 
     torch.cuda.set_device(local)
     dist = None
@@ -187,11 +226,18 @@ def run_ours(args, ws, rank, local):
         db.search_device(q.data_ptr(), nq, DIM, k, metric, prec if p is None else p, ids.data_ptr(), dists.data_ptr(),
                          0, stats)
 
-    # correctness guard on a slice of the first batch: ids equal the device FP64 scan
-    ids_ref, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP64)
-    ids_chk, _ = db.search(Qh[0][:8], k, metric, prec)
-    if not np.array_equal(ids_ref, ids_chk):
-        raise SystemExit("bench: top-k ids of the measured precision differ from the FP64 scan")
+    # correctness guard (outside the timed region): the whole first batch is
+    # searched as measured, and a sample of its queries spread over every
+    # 128-query tile must equal the oracle's FP64 brute force (ids and values)
+    guard = guard_sample(nq)
+    want_guard = oracle_topk(X, Qh[0][guard], metric, k)
+
+    def check_guard(p, what):
+        gi, gv = db.search(Qh[0], k, metric, p)
+        if not (np.array_equal(gi[guard], want_guard[0]) and np.array_equal(gv[guard], want_guard[1])):
+            raise SystemExit(f"bench: {what} top-k differs from the oracle on the guard sample")
+
+    check_guard(prec, args.precision)
 
     for w in range(args.warmup):
         step(w)
@@ -234,10 +280,7 @@ def run_ours(args, ws, rank, local):
     # refinement and re-rank) on the same batches, for comparison
     fp8 = None
     if prec == S.PREC_BF16 and metric == S.COSINE and rank == 0:
-        ids_ref8, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP64)
-        ids_chk8, _ = db.search(Qh[0][:8], k, metric, S.PREC_FP8)
-        if not np.array_equal(ids_ref8, ids_chk8):
-            raise SystemExit("bench: FP8 top-k ids differ from the FP64 scan")
+        check_guard(S.PREC_FP8, "fp8")
         for w in range(args.warmup):
             step(w, p=S.PREC_FP8)
         st8 = S.SearchStats()
@@ -368,11 +411,7 @@ def run_ours(args, ws, rank, local):
         line = {"metric": METRIC_NAME, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": {S.PREC_BF16: "bf16+f64", S.PREC_FP8: "e4m3+f32+f64"}.get(prec, "f64"),
-                "data": "synthetic",
-                "config": {"workload": f"1M x 768 FP64 Gaussian mixture (1024 centres, sigma 0.05, seed 3), "
-                                       f"exact top-{k} {args.metric}, {args.precision}",
-                           "query_batch": nq, "precision": args.precision, "parallelism": f"replicas{ws}",
-                           "l2": "store (6.1 GB FP64) larger than L2; no flush needed"},
+                "data": "synthetic", "precision": args.precision, "config": headline_config(args, ws),
                 "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
                 "stage_ms_per_step": {n: float(stage_ms[i] / max(ncalls, 1)) for i, n in
                                       enumerate(["prep", "screen", "select", "refine", "rerank"])},
@@ -400,7 +439,7 @@ def run_scan128(args, ws, rank, local):
     HBM bytes per second."""
     import torch
     import svdb_gb300 as S
-    from svdb_gb300 import workloads as W
+    W = workloads()
 
     torch.cuda.set_device(local)
     n, d = args.rows if args.rows != N_ROWS_DEFAULT else 1_000_000, 128
@@ -454,7 +493,7 @@ def run_ragged(args, ws, rank, local):
     each query answered with its own k."""
     import torch
     import svdb_gb300 as S
-    from svdb_gb300 import workloads as W
+    W = workloads()
 
     torch.cuda.set_device(local)
     prec = S.PREC_BF16 if args.precision == "bf16" else S.PREC_FP64
@@ -477,15 +516,16 @@ def run_ragged(args, ws, rank, local):
     tune_s = time.perf_counter() - t0
     info = plan.info()
 
-    # correctness guard: a few queries of every collection against the device FP64 scan
+    # correctness guard: a few queries of every collection against the oracle
     plan.run()
     plan.wait()
     for (X, Q, ks), db, (_, ids, dd) in zip(cols, dbs, bufs):
+        gi, gd = ids.cpu().numpy(), dd.cpu().numpy()
         for i in (0, Q.shape[0] // 2, Q.shape[0] - 1):
             k = int(ks[i])
-            ref_ids, _ = db.search(Q[i:i + 1], k, S.COSINE, S.PREC_FP64)
-            if not np.array_equal(ids[i, :k].cpu().numpy(), ref_ids[0]):
-                raise SystemExit("bench: ragged plan ids differ from the FP64 scan")
+            wi, wv = oracle_topk(X, Q[i:i + 1], S.COSINE, k)
+            if not (np.array_equal(gi[i, :k], wi[0]) and np.array_equal(gd[i, :k], wv[0])):
+                raise SystemExit("bench: ragged plan results differ from the oracle")
 
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stream = torch.cuda.ExternalStream(plan.stream())
@@ -537,7 +577,8 @@ def run_serve(args, ws, rank, local):
     back to it."""
     import torch
     import svdb_gb300 as S
-    from svdb_gb300 import serve, workloads as W
+    from svdb_gb300 import serve
+    W = workloads()
 
     torch.cuda.set_device(local)
     m = W.Mixture(DIM, 5)
@@ -712,7 +753,7 @@ def run_nearest(args, ws, rank, local):
     thread, on part 1."""
     import torch
     import svdb_gb300 as S
-    from svdb_gb300 import workloads as W
+    W = workloads()
 
     torch.cuda.set_device(local)
     X, Q, kd = W.config1()

@@ -158,9 +158,15 @@ int svdb_search_topk_device(VectorDatabase* db, const double* d_queries, size_t 
  * bytes per (query, result, row slice), at most 592 slices (64 queries of
  * D = 768, top-32: about 3 MB); one that needs more is rejected with
  * SVDB_EINVAL and a message saying how much it needed.  The store must have no pending
- * mutations (call svdb_sync before; syncing can allocate).  The first call on
- * a device looks up the array's device address for that device; make that
- * first call before any stream capture.  Every call shares the array: calls
+ * mutations (call svdb_sync before; syncing can allocate).  The array's
+ * device address is looked up when a database first sets up its device
+ * store (its first sync), with that device current, which also loads the
+ * array; a call looks it up again only if the device's context was created
+ * anew since (after cudaDeviceReset).  The scan kernels' code is loaded by
+ * the first search of any kind in the process (CUDA's lazy module loading),
+ * which may allocate for that code: make one search call, of any kind, before
+ * the phase that must not allocate and before any stream capture; every later
+ * call allocates nothing.  Every call shares the array: calls
  * whose work overlaps on the GPU (other streams, other databases) race, so
  * order them.
  */

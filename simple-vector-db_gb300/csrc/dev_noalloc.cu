@@ -17,6 +17,20 @@
 // byte a call reads was written earlier in the same call).  Two calls whose
 // work overlaps on the GPU -- on different streams, or from two stores --
 // race on the array; callers must order them.
+//
+// Loading.  With CUDA's lazy module loading, the code module holding the
+// array (and so the array itself) is loaded, and its memory allocated, by the
+// first use of anything in this file.  The store's own device set-up (its
+// first device allocation, Store::ensure) calls noalloc_setup(), so by the
+// time a store can be searched the array exists and its device address is
+// known: the entry point then only reads that address.  The kernels it
+// launches live in other modules (the FP64 scan's); their code is loaded by
+// their first launch in the process, which the regular search's first call
+// also does.  So the first search of any kind on a device may still allocate
+// for module code; every later no-allocation call allocates nothing.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstring>
 #include <mutex>
 
@@ -30,12 +44,49 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};  // device address of the array, per device
+struct ScratchSlot {
+    unsigned long long ctx_id;  // the context the address belongs to (0: none yet)
+    void* addr;
+};
+ScratchSlot g_slot[kMaxDevices] = {};
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+PFN_cuCtxGetId_v12000 g_ctx_id = nullptr;
+
+// Unique id of the calling thread's current context (never reused within the
+// process), so an address cached for a context that was torn down and created
+// again (cudaDeviceReset, a reset primary context) is looked up afresh.
+int current_context_id(unsigned long long* id) {
+    if (!g_ctx_current || !g_ctx_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || !f1 ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f2) {
+            cudaGetLastError();
+            svdb_set_error("search_noalloc: cuCtxGetCurrent / cuCtxGetId are not available from the driver");
+            return SVDB_ECUDA;
+        }
+        g_ctx_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f1);
+        g_ctx_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_id(ctx, id) != CUDA_SUCCESS) {
+        svdb_set_error("search_noalloc: no current CUDA context");
+        return SVDB_ECUDA;
+    }
+    return SVDB_OK;
+}
+
+}  // namespace
 
 // Host code cannot use g_noalloc_scratch directly: its name stands for a host
-// shadow, not a device address.  Look the device address up once per device,
-// with that device current.
-int scratch_address(void** out) {
+// shadow, not a device address.  Look the device address up once per device
+// (and context), with that device current.  Called by the store's device
+// set-up, and by the entry point (which finds the address already known
+// unless the context changed since).
+int noalloc_setup(void** out) {
     int dev = 0;
     SVDB_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) {
@@ -43,7 +94,10 @@ int scratch_address(void** out) {
         return SVDB_EINVAL;
     }
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc) return rc;
+    if (g_slot[dev].ctx_id != id || !g_slot[dev].addr) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -51,11 +105,14 @@ int scratch_address(void** out) {
             svdb_set_error("search_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return SVDB_ECUDA;
         }
-        g_scratch_addr[dev] = p;
+        g_slot[dev].addr = p;
+        g_slot[dev].ctx_id = id;
     }
-    *out = g_scratch_addr[dev];
+    if (out) *out = g_slot[dev].addr;
     return SVDB_OK;
 }
+
+namespace {
 
 __global__ void k_noalloc_fill_empty(int64_t* ids, double* dists, size_t n) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -86,6 +143,14 @@ extern "C" int svdbd_search_noalloc(svdbd_store* hs, const double* d_queries, si
         svdb_set_error("search_noalloc: the store has changes not yet on the device; call svdb_sync first");
         return SVDB_EINVAL;
     }
+    // bound nq before any size arithmetic, so no product below can wrap
+    if (s->ld == 0 || nq > kNoAllocScratchBytes / (s->ld * sizeof(double))) {
+        svdb_set_error(
+            "search_noalloc: %zu queries at dimension %zu do not fit the fixed %zu-byte scratch array (use fewer "
+            "queries per call)",
+            nq, s->dim, kNoAllocScratchBytes);
+        return SVDB_EINVAL;
+    }
     const size_t qbytes = round_up(nq * s->ld * sizeof(double), 256);
     const size_t sqbytes = round_up(nq * sizeof(double), 256);
     const size_t kbytes = s->nlive ? search_fp64_scratch(s, nq, k) : 0;
@@ -98,7 +163,7 @@ extern "C" int svdbd_search_noalloc(svdbd_store* hs, const double* d_queries, si
         return SVDB_EINVAL;
     }
     void* base = nullptr;
-    int rc = scratch_address(&base);
+    int rc = noalloc_setup(&base);
     if (rc) return rc;
     unsigned char* b = reinterpret_cast<unsigned char*>(base);
     double* qbuf = reinterpret_cast<double*>(b);

@@ -398,6 +398,10 @@ int Store::ensure() {
         return SVDB_ENOMEM;
     }
     stream = st;
+    // the no-allocation search's array: loaded now, with the store's own
+    // allocations, so that search never loads it (a failure here is reported
+    // by that search itself, which tries again)
+    if (noalloc_setup(nullptr) != SVDB_OK) cudaGetLastError();
     return SVDB_OK;
 }
 

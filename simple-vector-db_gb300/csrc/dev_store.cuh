@@ -119,4 +119,9 @@ struct Store {
     void release_extra();
 };
 
+// Device address of the no-allocation search's fixed scratch array for the
+// current device and context (dev_noalloc.cu); the store's device set-up calls
+// it so that the array's module is loaded with the store's own allocations.
+int noalloc_setup(void** out);
+
 }  // namespace svdb

@@ -11,8 +11,25 @@ for p in (os.path.join(ROOT, "oracle"), PKG, os.path.join(ROOT, "tests", "golden
         sys.path.insert(0, p)
 
 
+_PARITY_LINES = []
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def parity_report():
+    """Lines describing what a parity test checked (sample sizes, the
+    screen's certification statistics), printed at the end of the run."""
+    return _PARITY_LINES
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    if _PARITY_LINES:
+        terminalreporter.write_sep("-", "parity at the measured sizes")
+        for line in _PARITY_LINES:
+            terminalreporter.write_line(line)
 
 
 @pytest.fixture(scope="session")
