@@ -361,6 +361,62 @@ def run_ours(args, ws, rank, local):
         e2e_s = float(tt.item())
     e2e = ws * nq * args.steps / e2e_s
 
+    # other batch sizes and metrics on the same store, device-resident queries,
+    # CUDA events on the library's stream (reported beside the headline)
+    batches = None
+    if rank == 0 and args.extra:
+        batches = {}
+
+        def timed(qn, m, p, steps):
+            for w in range(3):
+                db.search_device(Qd[w % nbatch].data_ptr(), qn, DIM, k, m, p, ids.data_ptr(), dists.data_ptr(), 0)
+            a_ = torch.cuda.Event(enable_timing=True)
+            b_ = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a_.record(stream)
+            for s_ in range(steps):
+                db.search_device(Qd[s_ % nbatch].data_ptr(), qn, DIM, k, m, p, ids.data_ptr(), dists.data_ptr(), 0)
+            b_.record(stream)
+            torch.cuda.synchronize()
+            ms_ = a_.elapsed_time(b_) / steps
+            return {"queries_per_s": qn / (ms_ / 1e3), "ms_per_batch": ms_}
+
+        for mname in ("cosine", "euclidean"):
+            m = METRICS[mname]
+            for qn in (1, 64, 1024):
+                batches[f"{mname}_bf16_q{qn}"] = timed(qn, m, S.PREC_BF16, 20)
+            batches[f"{mname}_bf16_q{nq}"] = timed(nq, m, S.PREC_BF16, 10)
+            batches[f"{mname}_fp8_q{nq}"] = timed(nq, m, S.PREC_FP8, 10)
+        gi, gv = db.search(Qh[0], k, S.EUCLIDEAN, S.PREC_FP8)  # the FP8 Euclidean path, guarded too
+        want_e = oracle_topk(X, Qh[0][guard], S.EUCLIDEAN, k)
+        if not (np.array_equal(gi[guard], want_e[0]) and np.array_equal(gv[guard], want_e[1])):
+            raise SystemExit("bench: fp8 euclidean top-k differs from the oracle on the guard sample")
+
+    # a short serving trace on a second, server-side store of the same size:
+    # Poisson arrivals at --rate (70 % /nearest top-10, 10 % /compare, 15 %
+    # insert, 3 % update, 2 % delete), batched as they arrive
+    served = None
+    if rank == 0 and args.extra and args.serve_seconds_headline > 0:
+        from svdb_gb300 import serve
+        m5 = W.Mixture(DIM, 5)
+        nreq = int(args.rate * args.serve_seconds_headline)
+        srv = serve.Server(DIM, N_ROWS + 2 * nreq + 4096)
+        st_ = 1000
+        while srv.size < N_ROWS:
+            srv.insert_block(m5.sample(min(1 << 18, N_ROWS - srv.size), st_))
+            st_ += 1
+        serve.replay(srv, serve.make_trace(m5.sample, srv.size, max(1000, nreq // 4), args.rate, seed=50),
+                     S.PREC_BF16)
+        tr = serve.make_trace(m5.sample, srv.size, nreq, args.rate, seed=5)
+        r_ = serve.replay(srv, tr, S.PREC_BF16)
+        served = {"store_rows": N_ROWS, "offered_per_s": args.rate, "trace_s": args.serve_seconds_headline,
+                  "requests": r_["requests"], "served_per_s": r_["served_per_s"], "p50_ms": r_["p50_ms"],
+                  "p99_ms": r_["p99_ms"], "max_ms": r_["max_ms"], "mean_batch": r_["mean_batch"],
+                  "widened": r_["widened"], "bound_failures": r_["bound_failures"], "mix": tr.counts(),
+                  "how": "svdb_server_execute batches formed as requests arrive (host clock: completion - "
+                         "arrival, queueing included); rows from pageable host memory"}
+        srv.close()
+
     # plain FP64 GPU path on the same batches (the comparison the metric names)
     plain = None
     if prec != S.PREC_FP64 and args.plain_q:
@@ -424,6 +480,10 @@ def run_ours(args, ws, rank, local):
                 "gpu_launches": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": cl}
         if fp8:
             line["fp8_screen"] = fp8
+        if batches:
+            line["batches"] = batches
+        if served:
+            line["serve_20k"] = served
         if graph:
             line["graph_replay"] = graph
         print(json.dumps(line), flush=True)
@@ -931,6 +991,10 @@ def main():
     ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
     ap.add_argument("--fp64-seconds", type=float, default=2.0, help="serve: cut-off of the plain FP64 trace")
+    ap.add_argument("--extra", type=int, default=1, help="mixture: also time other batch sizes, metrics and a serve "
+                                                         "trace (outside the timed region)")
+    ap.add_argument("--serve-seconds-headline", type=float, default=1.0,
+                    help="mixture: length of the serving trace reported beside the headline")
     args = ap.parse_args()
     N_ROWS = args.rows
     if args.q is None:

@@ -326,6 +326,39 @@ int svdb_server_execute(svdb_server* s, const svdb_request* req, size_t n, svdb_
 int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, uint32_t* gave_up);
 
 /*
+ * vector_db_save with options (replaces reference src/vector_database.c:203-223
+ * when flags ask for a change).  The reference writes db->size as the row
+ * count and then skips rows without data (dimension 0 or NULL data), so a
+ * store holding such rows produces a file that promises more rows than it
+ * holds; loading it reads past the last row.  vector_db_save keeps that
+ * behaviour byte for byte.  SVDB_SAVE_EXACT_COUNT writes the number of rows
+ * actually written instead (opt-in: the rows and their bytes are unchanged).
+ * Returns SVDB_OK or SVDB_EINVAL (bad argument, file not writable).
+ */
+#define SVDB_SAVE_EXACT_COUNT 1u
+int svdb_save(VectorDatabase* db, const char* filename, unsigned flags);
+
+/*
+ * Diagnostics of the screen's certification (no reference counterpart; not a
+ * search).  The exact top-k rests on a bound of the tensor core's FP32
+ * accumulation error, |acc - sum(bq_i bx_i)| <= c_acc |bq| |bx|, whose
+ * internal order the hardware does not document.  This runs the screen
+ * kernel itself, in a form whose epilogue stores instead of screens, for nq
+ * (1..256; more than 128 run the paired two-SM form) host queries against
+ * the store's first `rows` slots (synced
+ * first) and returns every raw FP32 accumulator (acc: nq x rows), the query
+ * operands the MMAs read (query_ops: nq x *op_bytes; may be NULL) and the
+ * rows' shadow operands (row_ops: rows x *op_bytes, un-swizzled; may be
+ * NULL).  precision SVDB_PREC_BF16: BF16 operands (cosine: the unit-norm
+ * shadow; dot / Euclidean: the plain shadow); SVDB_PREC_FP8: E4M3 operands
+ * (the query scaled by its power of two).  *op_bytes = 2 ldb (BF16) or ldb8
+ * bytes.  Synchronous; uses the store's scratch.
+ */
+int svdb_debug_screen_accumulators(VectorDatabase* db, const double* queries, size_t nq, size_t dim, int metric,
+                                   int precision, size_t rows, float* acc, void* query_ops, void* row_ops,
+                                   size_t* op_bytes);
+
+/*
  * Merge of per-shard top-k lists (host only, no GPU; no reference
  * counterpart).  A store split by row ranges over several GPUs or processes
  * answers a query with one exact top-k per shard; this combines nshards such

@@ -44,6 +44,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "dev_search.cuh"
@@ -74,21 +75,29 @@ constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key
 // flags
 constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4;
 
-struct Smem {
+// Shared memory of one CTA.  PAIR (a CTA pair on two SMs, cta_group::2):
+// each CTA holds its own 128 queries and half of the 256-row store tile, so
+// a stage is 32 KB instead of 48 KB and the ring is 6 deep.
+template <bool PAIR>
+struct SmemT {
+    static constexpr int ST = PAIR ? 6 : kStages;
+    static constexpr uint32_t SA = kStageA;
+    static constexpr uint32_t SB = PAIR ? kStageB / 2 : kStageB;
     // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
-    uint8_t a[kStages][kStageA];
-    uint8_t b[kStages][kStageB];
+    uint8_t a[ST][SA];
+    uint8_t b[ST][SB];
     float4 rp[2][kBN];  // screen parameters of the store tile in the accumulator of the same index
     uint64_t rp_full[2];
     uint64_t rp_empty[2];
-    uint64_t full[kStages];
-    uint64_t empty[kStages];
+    uint64_t full[ST];
+    uint64_t empty[ST];
     uint64_t accfull[2];
     uint64_t accempty[2];
     uint64_t done;
     uint32_t tmem_base;
     int abort;
 };
+using Smem = SmemT<false>;
 }  // namespace scr
 
 // ---------------------------------------------------------------------------
@@ -192,6 +201,77 @@ __device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t
 // arrive on `bar` once every tcgen05 op issued so far by this thread has completed
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// ---- CTA pairs (cta_group::2): two CTAs of a cluster on two SMs share one
+// MMA of M = 256 (128 queries each) over the whole 256-row store tile, each
+// holding half of that tile; one thread of the even CTA issues the MMAs.
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// the shared::cluster address of this CTA's shared variable at `a` in CTA `rank`
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t a, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// arrive on an mbarrier given by its shared::cluster address (this CTA's or the peer's)
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cbar) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cbar) : "memory");
+}
+// tiled TMA load into this CTA's shared memory, completing on an mbarrier of
+// either CTA of the pair (cbar: shared::cluster address)
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint32_t cbar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+        "%4}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(cbar), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// arrive on `bar` in both CTAs of the pair once the MMAs issued so far have completed
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"((uint16_t)3)
+        : "memory");
+}
+// ... on `bar` of the issuing CTA only
+__device__ __forceinline__ void mma_commit_pair_local(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
 }
 
@@ -323,9 +403,10 @@ struct ScreenSched {
     int ntr;
 };
 
-__device__ __forceinline__ ScreenSeg sched_seg(const ScreenSched& S, int sg) {
-    if (S.direct) return ScreenSeg{0, S.ntr, (uint16_t)blockIdx.x, 0};
-    return S.seg[blockIdx.x][sg];
+// `u`: the schedule unit, a CTA (or a CTA pair: both CTAs share the unit's segments)
+__device__ __forceinline__ ScreenSeg sched_seg(const ScreenSched& S, int u, int sg) {
+    if (S.direct) return ScreenSeg{0, S.ntr, (uint16_t)u, 0};
+    return S.seg[u][sg];
 }
 
 struct ScreenParams {
@@ -342,6 +423,8 @@ struct ScreenParams {
     int* cnt;            // per (query, sub-list) candidate count (may exceed subcap: overflow)
     int2* cand;          // per query: nsub sub-lists of subcap x {row slot, key bits}, stride cap
     int* err;            // set to 1 when a wait timed out
+    float* dump;         // DUMP (diagnostics) only: raw accumulators, nq x dump_ld
+    size_t dump_ld;
     int nq, k, cap;
     int nsub, subcap;    // sub-list = (row group, column half): one emitting thread each
     int kblocks;  // ldb / 64
@@ -353,30 +436,54 @@ struct ScreenParams {
 //   E = |q| max|x/|x| - bxn| + eqq max|bxn| + eq0;
 // the epilogue is a max, a compare and a mask per element, and a validity
 // bit per row keeps dead, zero and padding rows out of the lower bounds.
-// F8 (cosine only): E4M3 operands, kind::f8f6f4 with 128 elements per stage;
-// the accumulator is in units of 2^e times the key (query scale x 256), so
+// F8: E4M3 operands, kind::f8f6f4 with 128 elements per stage.  Cosine: the
+// accumulator is in units of 2^e times the key (query scale x 256), so
 // thresholds are scaled into accumulator units once per tile and emitted
-// keys back once per candidate, both exactly (powers of two).
-template <int KL, bool NORM, bool F8 = false>
+// keys back once per candidate, both exactly (powers of two).  Dot /
+// Euclidean: the rows carry their own power of two 2^f_i, so each
+// accumulator is scaled into key units (x 2^-e, exact) before the row's
+// multiplier 2^-f_i and offset apply, as in the BF16 form.
+// DUMP (diagnostics, never used by a search): the epilogue writes every raw
+// FP32 accumulator value to P.dump instead of screening, so a test can compare
+// the tensor core's accumulation with an exact sum of the same operands.
+// PAIR: a cluster of two CTAs (ranks 0, 1) on two SMs works as one unit on
+// query tiles of 256 (rank r: queries 128 r .. 128 r + 127).  Each CTA loads
+// its own queries and half of the 256-row store tile (rows 128 r ..; through
+// the tensor map tmx over the shadow's tiles); the even CTA's MMA thread
+// issues cta_group::2 MMAs of M = 256, N = 256 that read both CTAs' halves
+// and write each CTA's 128 x 256 accumulator into that CTA's TMEM.  Stage
+// completions land on the even CTA's full barriers (it expects both CTAs'
+// bytes), MMA completions on both CTAs' empty / accumulator barriers, and
+// both CTAs' epilogue warps free an accumulator on the even CTA's barrier.
+// Per SM a K step moves 8 KB of operands instead of 12 KB.
+template <int KL, bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false>
 __global__ void __launch_bounds__(scr::kThreads, 1)
-    k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const ScreenParams P) {
-    static_assert(!F8 || NORM, "the FP8 screen is the cosine screen");
+    k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
+                  const ScreenParams P) {
     using namespace scr;
+    using SM = SmemT<PAIR>;
+    constexpr int ST = SM::ST;
+    // cosine FP8 works in accumulator units (thresholds scaled in, keys out);
+    // dot / Euclidean FP8 scales each accumulator into key units at once
+    constexpr bool ACCU = F8 && NORM;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    SM& S = *reinterpret_cast<SM*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nseg = P.sched.direct ? 1 : P.sched.nseg[blockIdx.x];
+    const uint32_t rank = PAIR ? cluster_rank() : 0u;
+    const bool leader = rank == 0;
+    const int unit = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int nseg = P.sched.direct ? 1 : P.sched.nseg[unit];
     const int KB = P.kblocks;
     volatile int* abort = &S.abort;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < kStages; ++i) {
+        for (int i = 0; i < ST; ++i) {
             mbar_init(&S.full[i], 1);
             mbar_init(&S.empty[i], 1);
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(&S.accfull[i], 1);
-            mbar_init(&S.accempty[i], kEpiWarps);
+            mbar_init(&S.accempty[i], PAIR ? 2 * kEpiWarps : kEpiWarps);
         }
         mbar_init(&S.done, 1);
         for (int i = 0; i < 2; ++i) {
@@ -389,8 +496,16 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
     }
     if (warp == 0 && lane == 0) {
         tma_prefetch_desc(&tmq);
+        if (PAIR) tma_prefetch_desc(&tmx);
     }
-    if (warp == 1) tmem_alloc(&S.tmem_base, kTmemCols);
+    // the peer's barriers exist before anything is signalled across the pair
+    if constexpr (PAIR) cluster_sync_all();
+    if (warp == 1) {
+        if constexpr (PAIR)
+            tmem_alloc_pair(&S.tmem_base, kTmemCols);  // one warp of each CTA, collectively
+        else
+            tmem_alloc(&S.tmem_base, kTmemCols);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -406,7 +521,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             bool ok = true;
             uint32_t jt = 0;  // tiles so far (all segments)
             for (int sg = 0; sg < nseg && ok; ++sg) {
-            const ScreenSeg seg = sched_seg(P.sched, sg);
+            const ScreenSeg seg = sched_seg(P.sched, unit, sg);
             const int qt = seg.qt;
             for (int r = seg.lo; r < seg.hi && ok; ++r, ++jt) {
                 if (!NORM) {  // the tile's screen parameters into the 2-slot ring (freed by the epilogue)
@@ -424,12 +539,21 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(&S.full[stage], kStageA + kStageB);
-                    tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * (F8 ? 2 * kBK : kBK), qt * kBM);
-                    // the store tile: one contiguous 32 KB block, already swizzled
-                    bulk_load(S.b[stage], P.xblk + ((size_t)r * KB + kb) * kStageB, kStageB, &S.full[stage]);
+                    if constexpr (PAIR) {
+                        // both CTAs' halves complete on the even CTA's barrier, which expects them all
+                        if (leader) mbar_expect_tx(&S.full[stage], 2 * (SM::SA + SM::SB));
+                        const uint32_t fb = cluster_addr(smem_u32(&S.full[stage]), 0);
+                        tma_load_2d_pair(S.a[stage], &tmq, fb, kb * (F8 ? 2 * kBK : kBK),
+                                         qt * 2 * kBM + (int)rank * kBM);
+                        tma_load_2d_pair(S.b[stage], &tmx, fb, 0, (r * KB + kb) * kBN + (int)rank * (kBN / 2));
+                    } else {
+                        mbar_expect_tx(&S.full[stage], kStageA + kStageB);
+                        tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * (F8 ? 2 * kBK : kBK), qt * kBM);
+                        // the store tile: one contiguous 32 KB block, already swizzled
+                        bulk_load(S.b[stage], P.xblk + ((size_t)r * KB + kb) * kStageB, kStageB, &S.full[stage]);
+                    }
                     ++issued;
-                    if (++stage == kStages) {
+                    if (++stage == ST) {
                         stage = 0;
                         phase ^= 1;
                     }
@@ -437,12 +561,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             }
             // every issued load must have landed before the CTA may exit:
-            // wait (bounded) for the completion of the last kStages loads
-            const uint32_t last = issued < (uint32_t)kStages ? issued : (uint32_t)kStages;
+            // wait (bounded) for the completion of the last ST loads (a pair's
+            // loads all complete on the even CTA's barriers, so it waits for both)
+            const uint32_t last = issued < (uint32_t)ST ? issued : (uint32_t)ST;
             volatile int no_abort = 0;
-            for (uint32_t i = 0; i < last; ++i) {
+            for (uint32_t i = 0; i < last && (!PAIR || leader); ++i) {
                 const uint32_t n = issued - 1 - i;  // load number n went to stage n % S, phase (n / S) & 1
-                mbar_wait(&S.full[n % kStages], (n / kStages) & 1u, &no_abort, kWaitLimitNs / 4);
+                mbar_wait(&S.full[n % ST], (n / ST) & 1u, &no_abort, kWaitLimitNs / 4);
             }
             const uint32_t rlast = rp_issued < 2u ? rp_issued : 2u;
             for (uint32_t i = 0; i < rlast; ++i) {
@@ -452,14 +577,15 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         }
     } else if (warp == 1) {
         // ------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            constexpr uint32_t idesc = F8 ? idesc_e4m3(kBM, kBN) : idesc_bf16(kBM, kBN);
+        if (lane == 0 && (!PAIR || leader)) {
+            constexpr int M = PAIR ? 2 * kBM : kBM;
+            constexpr uint32_t idesc = F8 ? idesc_e4m3(M, kBN) : idesc_bf16(M, kBN);
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
             int j = 0;
             for (int sg = 0; sg < nseg && ok; ++sg)
-            for (int r = sched_seg(P.sched, sg).lo, rh = sched_seg(P.sched, sg).hi; r < rh && ok; ++r, ++j) {
+            for (int r = sched_seg(P.sched, unit, sg).lo, rh = sched_seg(P.sched, unit, sg).hi; r < rh && ok; ++r, ++j) {
                 const int b = j & 1;
                 const uint32_t use = (uint32_t)j >> 1;
                 if (!mbar_wait(&S.accempty[b], (use & 1u) ^ 1u, abort, kWaitLimitNs)) break;
@@ -475,21 +601,36 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     const uint64_t bd = sdesc_sw128(smem_u32(S.b[stage]));
 #pragma unroll
                     for (int kk = 0; kk < kBK / 16; ++kk) {  // +32 bytes per K step (16 BF16 or 32 E4M3)
-                        if constexpr (F8)
+                        if constexpr (PAIR && F8)
+                            mma_f8_pair(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
+                        else if constexpr (PAIR)
+                            mma_bf16_pair(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
+                        else if constexpr (F8)
                             mma_f8(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
                         else
                             mma_bf16(d, ad + 2u * kk, bd + 2u * kk, idesc, (kb | kk) != 0);
                     }
-                    mma_commit(&S.empty[stage]);
-                    if (++stage == kStages) {
+                    if constexpr (PAIR)
+                        mma_commit_pair(&S.empty[stage]);  // frees the stage in both CTAs
+                    else
+                        mma_commit(&S.empty[stage]);
+                    if (++stage == ST) {
                         stage = 0;
                         phase ^= 1;
                     }
                 }
-                if (ok) mma_commit(&S.accfull[b]);
+                if (ok) {
+                    if constexpr (PAIR)
+                        mma_commit_pair(&S.accfull[b]);
+                    else
+                        mma_commit(&S.accfull[b]);
+                }
             }
             // all MMAs issued by this thread complete before TMEM is released
-            mma_commit(&S.done);
+            if constexpr (PAIR)
+                mma_commit_pair_local(&S.done);
+            else
+                mma_commit(&S.done);
             volatile int no_abort = 0;
             mbar_wait(&S.done, 0, &no_abort, kWaitLimitNs / 4);
         }
@@ -503,10 +644,12 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         const int col0 = half * (kBN / 2);
         int j = 0;  // tiles so far (all segments): accumulator buffer and phase
         bool alive = true;
+        // the even CTA's accumulator-free barrier, which both CTAs' epilogues arrive on
+        const uint32_t accempty_c0 = PAIR ? cluster_addr(smem_u32(&S.accempty[0]), 0) : 0u;
         for (int sg = 0; sg < nseg && alive; ++sg) {
         // every segment starts afresh: its query tile, running top-k, warm-up
-        const ScreenSeg seg = sched_seg(P.sched, sg);
-        const int q = seg.qt * kBM + qi;
+        const ScreenSeg seg = sched_seg(P.sched, unit, sg);
+        const int q = PAIR ? seg.qt * 2 * kBM + (int)rank * kBM + qi : seg.qt * kBM + qi;
         float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0 (NORM: eq0 = E)
         bool valid = false;
         // F8: key = accumulator x cs, cs a power of two (so both directions are exact)
@@ -542,7 +685,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // cosine: validity words of this warp's 128 rows (lane c holds the word
             // of chunk c), loaded before the wait so their latency is hidden
             uint32_t vbl = 0;
-            if (NORM && lane < kBN / 2 / 32) vbl = __ldg(P.vbits + ((r * kBN + col0) >> 5) + lane);
+            if (NORM && !DUMP && lane < kBN / 2 / 32) vbl = __ldg(P.vbits + ((r * kBN + col0) >> 5) + lane);
             // tcgen05.ld is warp-collective (.sync.aligned): every branch that
             // leads to one must be taken by the whole warp, including this wait
             bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
@@ -554,6 +697,30 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             tc_fence_after();
             const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * kBN + col0);
             const int row0 = r * kBN + col0;
+            if constexpr (DUMP) {
+#pragma unroll 1
+                for (int c = 0; c < kBN / 2 / 32; ++c) {
+                    uint32_t v[32];
+                    __syncwarp();  // converged warp for the collective load
+                    tmem_ld32(tbase + (uint32_t)(c * 32), v);
+                    tmem_ld_wait();
+                    if (q < P.nq) {
+                        float* o = P.dump + (size_t)q * P.dump_ld + row0 + c * 32;
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) o[i] = __uint_as_float(v[i]);
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    if constexpr (PAIR)
+                        mbar_arrive_cluster(accempty_c0 + (uint32_t)(b * sizeof(uint64_t)));
+                    else
+                        mbar_arrive(&S.accempty[b]);
+                    if (!NORM) mbar_arrive(&S.rp_empty[b]);
+                }
+                continue;
+            }
             if (js == 0) {  // warp-uniform: lanes of invalid queries load and discard
                 // Warm-up on the segment's first tile, before anything is emitted: fold the
                 // lower bound of every row into the running k best (rows, not chunk
@@ -584,7 +751,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
 #pragma unroll
                         for (int i = 0; i < kChunk; ++i) {
                             const float4 p = rc[i];
-                            const float key = __fmaf_rn(__uint_as_float(v[i]), p.x, -p.z);
+                            const float key = __fmaf_rn(F8 ? __uint_as_float(v[i]) * cs : __uint_as_float(v[i]), p.x, -p.z);
                             const float l = __fsub_rd(__fsub_rd(key, __fmaf_ru(eq, p.y, p.w)), eq0);
                             maxl = fmaxf(maxl, l);
                             if (valid && l > top.mn) top.push(l);
@@ -606,8 +773,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
             // the query's eq0 is folded into the threshold and the maxima
-            // in accumulator units (F8: exact rescale by a power of two)
-            const float thr2 = F8 ? __fsub_rd(thr, eq0) * ics : __fsub_rd(thr, eq0);
+            // in accumulator units (cosine F8: exact rescale by a power of two)
+            const float thr2 = ACCU ? __fsub_rd(thr, eq0) * ics : __fsub_rd(thr, eq0);
             constexpr int C = NORM ? 32 : 16;  // accumulator columns per collective load
             float tmax = -INFINITY;            // best lower bound (less eq0) of this warp's 128 rows
 #pragma unroll 1
@@ -649,7 +816,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
                             const float4 p = rc[8 * g + i];
-                            const float key = __fmaf_rn(__uint_as_float(v[8 * g + i]), p.x, -p.z);
+                            const float acc = __uint_as_float(v[8 * g + i]);
+                            const float key = __fmaf_rn(F8 ? acc * cs : acc, p.x, -p.z);
                             const float e = __fmaf_ru(eq, p.y, p.w);
                             tmax = fmaxf(tmax, __fsub_rd(key, e));
                             m = fmaxf(m, __fadd_ru(key, e));
@@ -686,8 +854,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                                 const int slot = base + __popc(mask & ((1u << i) - 1u));
                                 if (((mask >> i) & 1u) && slot < P.subcap)
                                     cq[slot] = make_int2(rw + 8 * g + i,
-                                                         F8 ? __float_as_int(__uint_as_float(v[8 * g + i]) * cs)
-                                                            : (int)v[8 * g + i]);
+                                                         ACCU ? __float_as_int(__uint_as_float(v[8 * g + i]) * cs)
+                                                              : (int)v[8 * g + i]);
                             }
                         }
                     }
@@ -702,7 +870,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // offsets; the warm-up tile's rows are already in the bins as chunks
             // and are not published a second time (a row in two bins would make
             // their minimum exceed the k-th best lower bound).
-            const float maxl = __fsub_rd(F8 ? tmax * cs : tmax, eq0);
+            const float maxl = __fsub_rd(ACCU ? tmax * cs : tmax, eq0);
             if (valid && js > 0 && maxl > thr) {
                 const int unit = 2 * kWarmUnits * nsq + (js - 1) * 2 * nsq + 2 * seg.sub + half;
                 atomicMax(&P.bins[(size_t)q * P.k + unit % P.k], f2ord(maxl));
@@ -711,7 +879,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
-                mbar_arrive(&S.accempty[b]);
+                if constexpr (PAIR)
+                    mbar_arrive_cluster(accempty_c0 + (uint32_t)(b * sizeof(uint64_t)));
+                else
+                    mbar_arrive(&S.accempty[b]);
                 if (!NORM) mbar_arrive(&S.rp_empty[b]);
             }
             if (valid && top.mn > published) {
@@ -719,15 +890,21 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 published = top.mn;
             }
         }
-        if (q < P.nq) P.cnt[(size_t)q * P.nsub + sub] = nemit;
+        if (!DUMP && q < P.nq) P.cnt[(size_t)q * P.nsub + sub] = nemit;
         }
     }
 
     __syncthreads();
     if (threadIdx.x == 0 && S.abort) atomicExch(P.err, 1);
+    // neither CTA of a pair leaves (or frees TMEM) while the other may still
+    // signal its barriers or the MMAs may still read its shared memory
+    if constexpr (PAIR) cluster_sync_all();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, kTmemCols);
+        if constexpr (PAIR)
+            tmem_dealloc_pair(tmem, kTmemCols);
+        else
+            tmem_dealloc(tmem, kTmemCols);
     }
 }
 
@@ -794,17 +971,19 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
     }
 }
 
-// The FP8 (cosine) form of k_prep_bf16: the query scaled by a power of two
-// 2^e (the largest with max |q_i| 2^e <= 448, E4M3's largest finite value),
-// its E4M3 copy (nq x ldb8 bytes, zero padded), the FP32 copy for the
-// refinement, the bound terms and qscale = 2^-(e+8): key = accumulator x
-// qscale exactly (the store's shadow carries 256 x/|x|).  The tensor core's
+// The FP8 form of k_prep_bf16: the query scaled by a power of two 2^e (the
+// largest with max |q_i| 2^e <= 448, E4M3's largest finite value), its E4M3
+// copy (nq x ldb8 bytes, zero padded), the FP32 copy for the refinement, the
+// bound terms and qscale: cosine 2^-(e+8), key = accumulator x qscale exactly
+// (the unit-norm shadow carries 256 x/|x|); dot / Euclidean 2^-e, key =
+// accumulator x qscale x 2^-f_i - m_i with the row's own power of two (the
+// plain E4M3 shadow carries x 2^f_i).  The tensor core's
 // accumulation of E4M3 products is modelled pessimistically, as if each K=32
 // step kept only 13 bits: c_acc = (ldb8/32 + 1) x 40 x 2^-13 of |bq| |bx|
 // (for D = 768 about 0.12; the E4M3 rounding itself is ~0.04 per vector).
 __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
-                          size_t ldb8, uint8_t* __restrict__ q8, float* __restrict__ q32, float4* __restrict__ qpar,
-                          float* __restrict__ qscale) {
+                          size_t ldb8, int metric, uint8_t* __restrict__ q8, float* __restrict__ q32,
+                          float4* __restrict__ qpar, float* __restrict__ qscale) {
     const int lane = threadIdx.x & 31, s = lane & 3;
     const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
     const bool active = qi < nq;
@@ -860,21 +1039,26 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
         const double cacc = (double)(ldb8 / 32 + 1) * 40.0 * 1.220703125e-04;
         const double eqq = (eq + cacc * bqn) * (1.0 + 9.5367431640625e-07) + 3.637978807091713e-12 * qn +
                            9.5367431640625e-07 * (1.0 + cacc) * 1.02 * bqn;
-        const double eq0 = 9.094947017729282e-13 * qn + 1e-30;
-        // the key's rescale 2^-(e+8) stays a normal FP32 power of two
-        const bool ok = all_finite && isfinite(sq) && sq < 1e30 && sq > 0.0 && e > -100 && e < 100;
+        const double eq0 = 9.094947017729282e-13 * (metric == SVDB_EUCLIDEAN ? sq : qn) + 1e-30;
+        // the key's rescale 2^-(e+8) (cosine: the rows carry 256 x/|x|) or 2^-e
+        // (dot / Euclidean: the rows' own scale is applied per row) stays a
+        // normal FP32 power of two
+        const bool ok = all_finite && isfinite(sq) && sq < 1e30 && (metric != SVDB_COSINE || sq > 0.0) && e > -100 &&
+                        e < 100;
         float4 p;
         p.x = __double2float_ru(qn);
         p.y = __double2float_ru(eqq);
         p.z = __double2float_ru(eq0);
         p.w = ok && isfinite(p.x) && isfinite(p.y) ? 1.0f : 0.0f;
         qpar[qi] = p;
-        qscale[qi] = (float)ldexp(1.0, -(e + 8));
+        qscale[qi] = (float)ldexp(1.0, -(e + (metric == SVDB_COSINE ? 8 : 0)));
     }
 }
 
 // Per-row screen parameters for one metric; rows >= nslots (tile padding),
-// dead slots and placeholder rows get NaN (never candidates).
+// dead slots and placeholder rows get NaN (never candidates).  rowp8 (dot /
+// Euclidean on the E4M3 shadow): the rows' own power-of-two multiplier and
+// the E4M3 residual and norm replace the BF16 ones.
 //   rpar = {mult, a, b, m}: the tight bound E = |q| a + eqq b + 2^-19 m + eq0
 //   spar = {mult, b, m, 2^-19 m}: the screen's one-FMA form, with a <= alpha b
 //   vbits: 1 bit per row whose parameters are finite (the cosine screen's mask)
@@ -885,8 +1069,9 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
 __global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ rowp, const double* __restrict__ sq64,
                                                     const uint8_t* __restrict__ live, int64_t nslots, int64_t npad,
                                                     int metric, const float2* __restrict__ rowpn,
-                                                    float4* __restrict__ rpar, float4* __restrict__ spar,
-                                                    int* __restrict__ alpha, uint32_t* __restrict__ vbits) {
+                                                    const float4* __restrict__ rowp8, float4* __restrict__ rpar,
+                                                    float4* __restrict__ spar, int* __restrict__ alpha,
+                                                    uint32_t* __restrict__ vbits) {
     __shared__ int wmax[8];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const float nan = __int_as_float(0x7fc00000);
@@ -899,6 +1084,9 @@ __global__ void __launch_bounds__(256) k_row_params(const float4* __restrict__ r
                 const float2 pn = rowpn[i];
                 out = make_float4(1.0f, pn.y, pn.x, 0.0f);
             }
+        } else if (rowp8) {  // the E4M3 shadow x 2^f: mult = 2^-f, a and b of its residual and norm
+            const float4 p8 = rowp8[i];
+            out = make_float4(p8.z, p8.y, p8.x, metric == SVDB_DOT ? 0.0f : __double2float_rn(0.5 * sq));
         } else if (metric == SVDB_DOT) {
             out = make_float4(1.0f, rp.z, rp.y, 0.0f);
         } else {
@@ -1670,13 +1858,15 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 // ---------------------------------------------------------------------------
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    bool attr_set[12] = {};
+    bool attr_set[16] = {};
     bool select_attr = false;
     bool sort_attr = false;
     bool rerank_attr = false;
     bool refine_attr = false;
     bool stream_attr = false;
     size_t screen_smem = 0;
+    size_t screen_smem_pair = 0;
+    bool attr_pair[16] = {};
 };
 
 static int gemm_cache(Store* s, GemmPlanCache** out) {
@@ -1698,6 +1888,7 @@ static int gemm_cache(Store* s, GemmPlanCache** out) {
         }
         c->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
         c->screen_smem = sizeof(scr::Smem) + 1024;
+        c->screen_smem_pair = sizeof(scr::SmemT<true>) + 1024;
         s->gemm = c;
     }
     *out = s->gemm;
@@ -1741,7 +1932,93 @@ static int make_map8(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t 
     return SVDB_OK;
 }
 
+// The paired screen (cta_group::2) for batches of more than one 128-query
+// tile; SVDB_SCREEN_PAIR=0 in the environment keeps the single-CTA form
+// (for comparisons).  Pairs that can run at once: every two SMs, as far as
+// the cluster scheduler places them (asked once per process).
+static bool pair_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("SVDB_SCREEN_PAIR");
+        on = (e && e[0] == '0') ? 0 : 1;
+    }
+    return on == 1;
+}
+
+static bool screen_pair(size_t nq) { return nq > (size_t)scr::kBM && pair_enabled(); }
+
+static int pair_units() {
+    static int n = 0;
+    if (!n) {
+        n = std::max(1, num_sms() / 2);
+        auto kern = k_screen_bf16<16, true, false, false, true>;
+        const int smem = (int)(sizeof(scr::SmemT<true>) + 1024);
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = 2;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3((unsigned)(2 * n));
+            cfg.blockDim = dim3(scr::kThreads);
+            cfg.dynamicSmemBytes = (size_t)smem;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int m = 0;
+            if (cudaOccupancyMaxActiveClusters(&m, (void*)kern, &cfg) == cudaSuccess && m > 0) n = std::min(n, m);
+        }
+        cudaGetLastError();
+    }
+    return n;
+}
+
+static int screen_units(bool pair) { return pair ? pair_units() : std::min(num_sms(), kMaxCtas); }
+
+// tensor map over a shadow's swizzled tiles as rows of 128 bytes (256 rows per
+// tile and k block), copied as they are (the paired screen loads half a tile)
+static int make_map_tiles(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t rows) {
+    const cuuint64_t dims[2] = {128, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {128, (cuuint32_t)(scr::kBN / 2)};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = c->encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        svdb_set_error("search_bf16: cuTensorMapEncodeTiled (store tiles) failed (%d)", (int)r);
+        return SVDB_ECUDA;
+    }
+    return SVDB_OK;
+}
+
+// one screen launch: `units` CTAs, or `units` clusters of a CTA pair
+template <class K>
+static int launch_screen(K kern, bool pair, int units, size_t smem, cudaStream_t st, const CUtensorMap& tmq,
+                         const CUtensorMap& tmx, const ScreenParams& P) {
+    if (!pair) {
+        kern<<<(unsigned)units, scr::kThreads, smem, st>>>(tmq, tmx, P);
+        SVDB_LAUNCH_CHECK();
+        return SVDB_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(2 * units));
+    cfg.blockDim = dim3(scr::kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SVDB_CUDA(cudaLaunchKernelEx(&cfg, kern, tmq, tmx, P));
+    return SVDB_OK;
+}
+
 struct Bf16Layout {
+    bool pair = false;  // the paired screen (query tiles of 256)
     size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     size_t tmax = 0, cut = 0;  // the streamed screen of a single query (its keys reuse spar: npad floats)
     int ntr, cap;
@@ -1750,7 +2027,8 @@ struct Bf16Layout {
     ScreenSched sched;
 };
 
-// The screen's work, query tiles x store tiles, over G = one CTA per SM.  With
+// The screen's work, query tiles x store tiles, over G units: one CTA per SM,
+// or one CTA pair per two SMs (then a query tile is 256 queries).  With
 // G = base * ntq + ea, query tiles [0, ea) get base + 1 CTAs that split the
 // store tiles evenly, the others base CTAs of T = ceil(ntq * ntr / G) tiles
 // each; what those leave at the end of the store (ntr - base * T tiles per
@@ -1758,10 +2036,10 @@ struct Bf16Layout {
 // shorter.  Every CTA then has ~T tiles; CTAs that cover the same store rows
 // do so at the same time (a row is read from HBM about once per family).
 // Returns the number of CTAs; *maxsub = most segments of one query tile.
-static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub) {
+static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub, int units) {
     std::memset(&S, 0, sizeof(S));
     S.ntr = ntr;
-    const int G = std::min(num_sms(), kMaxCtas);
+    const int G = std::min(units, kMaxCtas);
     if (ntq >= G) {
         S.direct = 1;
         *maxsub = 1;
@@ -1844,7 +2122,9 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
         L.cut = take(nq * sizeof(float));
     }
     int maxsub = 1;
-    L.nctas = screen_schedule((int)((nq + scr::kBM - 1) / scr::kBM), L.ntr, L.sched, &maxsub);
+    L.pair = screen_pair(nq);
+    const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
+    L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair));
     L.nsub = 2 * maxsub;
     L.cnt = take(nq * (size_t)L.nsub * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
@@ -1917,25 +2197,41 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     uint32_t kernels = 0;
 
     float* qscale = reinterpret_cast<float*>(base + L.qscale);
-    f8 = f8 && a.metric == SVDB_COSINE;  // the E4M3 shadow is the unit-norm (cosine) one
+    // f8: cosine screens the E4M3 unit-norm shadow, dot / Euclidean the E4M3
+    // shadow with per-row power-of-two scales
     const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
     const int kc = k <= 16 ? 0 : k <= 32 ? 1 : 2;  // running top-k variant of the screen and select
-    auto screen_kernel = [&](bool e4m3) {
-        return e4m3   ? (kc == 0 ? k_screen_bf16<16, true, true>
-                         : kc == 1 ? k_screen_bf16<32, true, true>
-                                   : k_screen_bf16<0, true, true>)
-               : kc == 0 ? (norm ? k_screen_bf16<16, true> : k_screen_bf16<16, false>)
-               : kc == 1 ? (norm ? k_screen_bf16<32, true> : k_screen_bf16<32, false>)
-                         : (norm ? k_screen_bf16<0, true> : k_screen_bf16<0, false>);
+    auto screen_kernel_of = [&](bool e4m3, auto pair_tag) {
+        constexpr bool PR = decltype(pair_tag)::value;
+        return e4m3   ? (kc == 0 ? (norm ? k_screen_bf16<16, true, true, false, PR> : k_screen_bf16<16, false, true, false, PR>)
+                         : kc == 1 ? (norm ? k_screen_bf16<32, true, true, false, PR> : k_screen_bf16<32, false, true, false, PR>)
+                                   : (norm ? k_screen_bf16<0, true, true, false, PR> : k_screen_bf16<0, false, true, false, PR>))
+               : kc == 0 ? (norm ? k_screen_bf16<16, true, false, false, PR> : k_screen_bf16<16, false, false, false, PR>)
+               : kc == 1 ? (norm ? k_screen_bf16<32, true, false, false, PR> : k_screen_bf16<32, false, false, false, PR>)
+                         : (norm ? k_screen_bf16<0, true, false, false, PR> : k_screen_bf16<0, false, false, false, PR>);
     };
-    auto screen_attr = [&](bool e4m3) -> int {
-        const int v = e4m3 ? 8 + kc : 2 * kc + (norm ? 1 : 0);
-        if (!gc->attr_set[v]) {
-            SVDB_CUDA(cudaFuncSetAttribute(screen_kernel(e4m3), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)gc->screen_smem));
-            gc->attr_set[v] = true;
+    // one screen over nunits units (CTAs or pairs) with the query tensor map tmq_;
+    // the paired form also gets the tensor map of the shadow's tiles
+    auto run_screen = [&](bool e4m3, bool pair, int nunits, const CUtensorMap& tmq_, const ScreenParams& P_) -> int {
+        const int v = e4m3 ? 6 + 2 * kc + (norm ? 1 : 0) : 2 * kc + (norm ? 1 : 0);
+        if (!pair) {
+            auto kern = screen_kernel_of(e4m3, std::false_type());
+            if (!gc->attr_set[v]) {
+                SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
+                gc->attr_set[v] = true;
+            }
+            return launch_screen(kern, false, nunits, gc->screen_smem, s->stream, tmq_, tmq_, P_);
         }
-        return SVDB_OK;
+        auto kern = screen_kernel_of(e4m3, std::true_type());
+        if (!gc->attr_pair[v]) {
+            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_pair));
+            gc->attr_pair[v] = true;
+        }
+        CUtensorMap tmx;
+        const size_t kbl = e4m3 ? s->ldb8 / (2 * scr::kBK) : s->ldb / scr::kBK;
+        const int rc_ = make_map_tiles(gc, &tmx, P_.xblk, (size_t)L.ntr * kbl * scr::kBN);
+        if (rc_) return rc_;
+        return launch_screen(kern, true, nunits, gc->screen_smem_pair, s->stream, tmq_, tmx, P_);
     };
     // small batches carry many candidates per query: wider blocks
     const int sel_threads = nq >= 256 ? 256 : 1024;
@@ -1972,12 +2268,13 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         __nv_bfloat16* qb16 = reinterpret_cast<__nv_bfloat16*>(base + L.qb16);
         float4* qpar16 = reinterpret_cast<float4*>(base + L.qpar16);
         seed = reinterpret_cast<float*>(base + L.seed);
-        const int ntq = (nq + scr::kBM - 1) / scr::kBM;
+        const int tq = L.pair ? 2 * scr::kBM : scr::kBM;
+        const int ntq = (nq + tq - 1) / tq;
         const int ntr_seed = L.ntr / 16;
         const int64_t npad_seed = (int64_t)ntr_seed * scr::kBN;
         ScreenSched SS;
         int maxsub_s = 1;
-        const int nctas_s = screen_schedule(ntq, ntr_seed, SS, &maxsub_s);
+        const int nctas_s = screen_schedule(ntq, ntr_seed, SS, &maxsub_s, screen_units(L.pair));
         const int nsub_s = 2 * maxsub_s;
         const int subcap_s = L.cap / nsub_s;
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
@@ -1988,13 +2285,13 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         SVDB_LAUNCH_CHECK();
         k_row_params<<<(unsigned)((npad_seed + 255) / 256), 256, 0, s->stream>>>(
             s->rowp, s->sq64, s->live, std::min<int64_t>((int64_t)s->slots, npad_seed), npad_seed, a.metric, s->rowpn,
-            rpar, spar, alpha, vbits);
+            nullptr, rpar, spar, alpha, vbits);
         SVDB_LAUNCH_CHECK();
         CUtensorMap tmq16;
         rc = make_map(gc, &tmq16, qb16, a.nq, s->ldb, scr::kBM);
         if (rc) return rc;
         ScreenParams PS;
-        PS.xblk = reinterpret_cast<const uint8_t*>(s->xbn);
+        PS.xblk = reinterpret_cast<const uint8_t*>(norm ? (const void*)s->xbn : (const void*)s->xb);
         PS.qscale = qscale;
         PS.rpar = rpar;
         PS.spar = spar;
@@ -2014,10 +2311,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         PS.subcap = subcap_s;
         PS.kblocks = (int)(s->ldb / scr::kBK);
         PS.sched = SS;
-        rc = screen_attr(false);
+        rc = run_screen(false, L.pair, nctas_s, tmq16, PS);
         if (rc) return rc;
-        screen_kernel(false)<<<(unsigned)nctas_s, scr::kThreads, gc->screen_smem, s->stream>>>(tmq16, PS);
-        SVDB_LAUNCH_CHECK();
         rc = launch_select(nsub_s, subcap_s, qpar16, seed);
         if (rc) return rc;
         kernels += 5;
@@ -2025,7 +2320,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 
     if (f8)
         k_prep_f8<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(
-            a.q, a.qsq, nq, s->ld, s->ldb8, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
+            a.q, a.qsq, nq, s->ld, s->ldb8, a.metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
     else
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
                                                                               a.metric, qb, q32, qpar);
@@ -2036,10 +2331,9 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, nsub_use, flags, nq, k, alpha,
                                                                          redo_n, dstats, seed);
     SVDB_LAUNCH_CHECK();
-    k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(s->rowp, s->sq64, s->live,
-                                                                          (int64_t)s->slots, (int64_t)L.npad,
-                                                                          a.metric, f8 ? s->rowpn8 : s->rowpn, rpar, spar,
-                                                                          alpha, vbits);
+    k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(
+        s->rowp, s->sq64, s->live, (int64_t)s->slots, (int64_t)L.npad, a.metric, f8 ? s->rowpn8 : s->rowpn,
+        f8 && !norm ? s->rowp8 : nullptr, rpar, spar, alpha, vbits);
     SVDB_LAUNCH_CHECK();
     kernels += 3;
 
@@ -2067,7 +2361,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     if (rc) return rc;
 
     ScreenParams P;
-    P.xblk = reinterpret_cast<const uint8_t*>(f8 ? (const void*)s->xbn8 : norm ? (const void*)s->xbn : (const void*)s->xb);
+    P.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
+                                                 : norm ? (const void*)s->xbn : (const void*)s->xb);
     P.qscale = qscale;
     P.rpar = rpar;
     P.spar = spar;
@@ -2087,11 +2382,8 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     P.subcap = L.subcap;
     P.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
     P.sched = L.sched;
-    const unsigned grid = (unsigned)L.nctas;
-    rc = screen_attr(f8);
+    rc = run_screen(f8, L.pair, L.nctas, tmq, P);
     if (rc) return rc;
-    screen_kernel(f8)<<<grid, scr::kThreads, gc->screen_smem, s->stream>>>(tmq, P);
-    SVDB_LAUNCH_CHECK();
     ++kernels;
     }
     s->prof_mark(2);
@@ -2253,8 +2545,138 @@ int selftest_wait(Store* s, uint32_t limit_us, uint32_t* gave_up) {
     return s->check_error();
 }
 
+// ---------------------------------------------------------------------------
+// diagnostics: the screen's raw accumulators and the operands behind them
+// ---------------------------------------------------------------------------
+// Runs the screen kernel (DUMP form: same producer, same MMA issue sequence,
+// same tiles and descriptors; the paired form for more than 128 queries) for
+// up to 256 host queries against the store's
+// first `rows` slots and returns every raw FP32 accumulator value, the query
+// operand the MMAs read (BF16, or E4M3 scaled by the query's power of two) and
+// the rows' shadow operand (un-swizzled), so the accumulation can be compared
+// with an exact sum of the same products.  Not a search: nothing screened.
+int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8, size_t rows, float* acc,
+                     void* qops, void* rops, size_t* opbytes) {
+    if (nq == 0 || nq > 2 * (size_t)scr::kBM || metric < 0 || metric > 2 || !hq || !acc) {
+        svdb_set_error("debug_screen_acc: bad argument (1..256 queries)");
+        return SVDB_EINVAL;
+    }
+    int rc = s->sync();
+    if (rc) return rc;
+    if (rows == 0 || rows > s->slots) {
+        svdb_set_error("debug_screen_acc: rows must be 1..%zu", s->slots);
+        return SVDB_EINVAL;
+    }
+    GemmPlanCache* gc = nullptr;
+    rc = gemm_cache(s, &gc);
+    if (rc) return rc;
+    const bool norm = metric == SVDB_COSINE;
+    const size_t ob = f8 ? s->ldb8 : s->ldb * 2;  // operand bytes per row
+    if (opbytes) *opbytes = ob;
+    const size_t ntiles = (rows + scr::kBN - 1) / scr::kBN, dld = ntiles * scr::kBN;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += round_up(bytes, 1024);
+        return o;
+    };
+    const size_t o_raw = take(nq * s->dim * sizeof(double)), o_qbuf = take(nq * s->ld * sizeof(double)),
+                 o_qsq = take(nq * sizeof(double)), o_qb = take(nq * std::max(s->ldb * 2, s->ldb8)),
+                 o_q32 = take(nq * s->ld * sizeof(float)), o_qpar = take(nq * sizeof(float4)),
+                 o_qscale = take(nq * sizeof(float)), o_spar = take(dld * sizeof(float4)), o_alpha = take(sizeof(int)),
+                 o_dump = take(nq * dld * sizeof(float));
+    rc = s->scratch_reserve(off);
+    if (rc) return rc;
+    uint8_t* base = reinterpret_cast<uint8_t*>(s->scratch);
+    double* qraw = reinterpret_cast<double*>(base + o_raw);
+    double* qbuf = reinterpret_cast<double*>(base + o_qbuf);
+    double* qsq = reinterpret_cast<double*>(base + o_qsq);
+    void* qb = base + o_qb;
+    float* q32 = reinterpret_cast<float*>(base + o_q32);
+    float4* qpar = reinterpret_cast<float4*>(base + o_qpar);
+    float* qscale = reinterpret_cast<float*>(base + o_qscale);
+    float* dump = reinterpret_cast<float*>(base + o_dump);
+    SVDB_CUDA(cudaMemcpyAsync(qraw, hq, nq * s->dim * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    rc = prep_queries_fp64(s, qraw, s->dim, nq, qbuf, qsq);
+    if (rc) return rc;
+    if (f8)
+        k_prep_f8<<<(unsigned)((nq * 4 + 255) / 256), 256, 0, s->stream>>>(
+            qbuf, qsq, (int)nq, s->ld, s->ldb8, metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
+    else
+        k_prep_bf16<<<(unsigned)((nq * 4 + 255) / 256), 256, 0, s->stream>>>(
+            qbuf, qsq, (int)nq, s->ld, s->ldb, metric, reinterpret_cast<__nv_bfloat16*>(qb), q32, qpar);
+    SVDB_LAUNCH_CHECK();
+    CUtensorMap tmq;
+    rc = f8 ? make_map8(gc, &tmq, qb, nq, s->ldb8, scr::kBM) : make_map(gc, &tmq, qb, nq, s->ldb, scr::kBM);
+    if (rc) return rc;
+    ScreenParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
+                                                 : norm ? (const void*)s->xbn : (const void*)s->xb);
+    P.qscale = qscale;
+    P.spar = reinterpret_cast<const float4*>(base + o_spar);
+    P.alpha = reinterpret_cast<const int*>(base + o_alpha);
+    P.nmax = s->d_count + (f8 ? 3 : 1);
+    P.qpar = qpar;
+    P.err = s->d_err;
+    P.dump = dump;
+    P.dump_ld = dld;
+    P.nq = (int)nq;
+    P.k = 1;
+    P.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
+    P.sched.direct = 1;
+    P.sched.ntr = (int)ntiles;
+    // more than 128 queries: the paired form (one cluster of two CTAs, M = 256)
+    const bool pair = nq > (size_t)scr::kBM;
+    if (!pair) {
+        auto kern = f8 ? (norm ? k_screen_bf16<0, true, true, true> : k_screen_bf16<0, false, true, true>)
+                       : norm ? k_screen_bf16<0, true, false, true> : k_screen_bf16<0, false, false, true>;
+        SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
+        rc = launch_screen(kern, false, 1, gc->screen_smem, s->stream, tmq, tmq, P);
+    } else {
+        auto kern = f8 ? (norm ? k_screen_bf16<0, true, true, true, true> : k_screen_bf16<0, false, true, true, true>)
+                       : norm ? k_screen_bf16<0, true, false, true, true> : k_screen_bf16<0, false, false, true, true>;
+        SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_pair));
+        CUtensorMap tmx;
+        const size_t kbl = f8 ? s->ldb8 / (2 * scr::kBK) : s->ldb / scr::kBK;
+        const size_t ntr_all = (std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN;
+        rc = make_map_tiles(gc, &tmx, P.xblk, ntr_all * kbl * scr::kBN);
+        if (!rc) rc = launch_screen(kern, true, 1, gc->screen_smem_pair, s->stream, tmq, tmx, P);
+    }
+    if (rc) return rc;
+    std::vector<float> hacc(nq * dld);
+    SVDB_CUDA(cudaMemcpyAsync(hacc.data(), dump, hacc.size() * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    std::vector<uint8_t> hx;
+    if (rops) {
+        hx.resize(dld * ob);
+        SVDB_CUDA(cudaMemcpyAsync(hx.data(), P.xblk, hx.size(), cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (qops) SVDB_CUDA(cudaMemcpyAsync(qops, qb, nq * ob, cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    rc = s->check_error();
+    if (rc) return rc;
+    for (size_t q = 0; q < nq; ++q) std::memcpy(acc + q * rows, hacc.data() + q * dld, rows * sizeof(float));
+    if (rops) {
+        uint8_t* out = reinterpret_cast<uint8_t*>(rops);
+        for (size_t r = 0; r < rows; ++r) {
+            if (f8)
+                for (size_t e = 0; e < ob; ++e) out[r * ob + e] = hx[f8_tile_index((int64_t)r, e, s->ldb8)];
+            else
+                for (size_t e = 0; e < ob / 2; ++e)
+                    std::memcpy(out + r * ob + 2 * e, hx.data() + 2 * bf16_tile_index((int64_t)r, e, s->ldb), 2);
+        }
+    }
+    return SVDB_OK;
+}
+
 }  // namespace svdb
 
 extern "C" int svdbd_selftest_wait(svdbd_store* hs, uint32_t limit_us, uint32_t* gave_up) {
     return svdb::selftest_wait(reinterpret_cast<svdb::Store*>(hs), limit_us, gave_up);
+}
+
+extern "C" int svdbd_debug_screen_acc(svdbd_store* hs, const double* q, size_t nq, int metric, int f8, size_t rows,
+                                      float* acc, void* qops, void* rops, size_t* opbytes) {
+    return svdb::debug_screen_acc(reinterpret_cast<svdb::Store*>(hs), q, nq, metric, f8 != 0, rows, acc, qops, rops,
+                                  opbytes);
 }

@@ -9,6 +9,9 @@
 //   rowpn   C        float2   {|bxn| up, |x/|x| - bxn| up}
 //   xbn8    C x ldb8 e4m3     FP8 shadow of 256 x / |x| (FP8 cosine screen), ldb8 = D rounded up to 128
 //   rowpn8  C        float2   {|bxn8|/256 up, |x/|x| - bxn8/256| up}
+//   xb8     C x ldb8 e4m3     FP8 shadow of x 2^f per row (FP8 dot / Euclidean screen): 2^f the largest
+//                              power of two with max_j |x_j| 2^f <= 448 (E4M3's largest finite value)
+//   rowp8   C        float4   {|bx8| up, |x - bx8| up, 2^-f, 0}, bx8 = e4m3(x 2^f) 2^-f
 //   sqf     C        float4   {|x|^2 down, |x|^2 up, 1/(2|x|) down, 1/(2|x|) up} in FP32
 //   sq64    C        double   canonical sum of squares of the master row
 //   rowp    C        float4   {|x| up, |bf16(x)| up, |x - bf16(x)| up, |x|^2/2}
@@ -52,7 +55,8 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
                               size_t ldb, float* __restrict__ x32, __nv_bfloat16* __restrict__ xbn,
                               float2* __restrict__ rowpn, float4* __restrict__ sqf, double* __restrict__ sq64,
                               float4* __restrict__ rowp, uint8_t* __restrict__ xbn8, size_t ldb8,
-                              float2* __restrict__ rowpn8, const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
+                              float2* __restrict__ rowpn8, uint8_t* __restrict__ xb8, float4* __restrict__ rowp8,
+                              const uint8_t* __restrict__ live, int64_t lo, int64_t hi,
                               const int64_t* __restrict__ list) {
     const int lane = threadIdx.x & 31, s = lane & 3;
     const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
@@ -61,10 +65,11 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     const int64_t slot = active ? (list ? list[gid] : lo + gid) : 0;
     const double* x = x64 + slot * ld;
     float* xf = x32 + slot * ld;
-    double sq = 0.0, bh = 0.0, res = 0.0;
+    double sq = 0.0, bh = 0.0, res = 0.0, mx = 0.0;
     if (active) {
         for (size_t j = 2 * s; j < ld; j += 8) {
             const double2 v = *reinterpret_cast<const double2*>(x + j);
+            mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
             sq = fma(v.x, v.x, sq);
             sq = fma(v.y, v.y, sq);
             const __nv_bfloat16 hx = __double2bfloat16(v.x), hy = __double2bfloat16(v.y);
@@ -82,13 +87,37 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     sq = group4_sum(sq);
     bh = group4_sum(bh);
     res = group4_sum(res);
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+    // the row's E4M3 scale: the largest power of two 2^f with mx 2^f <= 448,
+    // kept within 2^+-120 so 2^-f is a normal FP32 number (a row outside that
+    // range only loses E4M3 precision, which its residual term accounts for)
+    int f = 0;
+    if (mx > 0.0 && isfinite(mx)) {
+        f = (int)floor(log2(448.0 / mx));
+        while (mx * ldexp(1.0, f) > 448.0) --f;
+        f = max(-120, min(120, f));
+    }
+    const double sc8 = ldexp(1.0, f);
     // second pass: the unit-norm row for the cosine screen, its BF16 and FP8
-    // (E4M3 of 256 x/|x|) copies and their residuals
-    double nbh = 0.0, nres = 0.0, nbh8 = 0.0, nres8 = 0.0;
+    // (E4M3 of 256 x/|x|) copies and their residuals, and the E4M3 copy of
+    // x 2^f for the dot / Euclidean screen and its residual
+    double nbh = 0.0, nres = 0.0, nbh8 = 0.0, nres8 = 0.0, pb8 = 0.0, pres8 = 0.0;
     if (active) {
         const double ixn = sq > 0.0 ? 1.0 / sqrt(sq) : 0.0;
         for (size_t j = 2 * s; j < ld; j += 8) {
             const double2 v = *reinterpret_cast<const double2*>(x + j);
+            {
+                const __nv_fp8_storage_t px = __nv_cvt_double_to_fp8(v.x * sc8, __NV_SATFINITE, __NV_E4M3);
+                const __nv_fp8_storage_t py = __nv_cvt_double_to_fp8(v.y * sc8, __NV_SATFINITE, __NV_E4M3);
+                const double gx = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(px, __NV_E4M3))) / sc8;
+                const double gy = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(py, __NV_E4M3))) / sc8;
+                pb8 = fma(gx, gx, pb8);
+                pb8 = fma(gy, gy, pb8);
+                pres8 = fma(v.x - gx, v.x - gx, pres8);
+                pres8 = fma(v.y - gy, v.y - gy, pres8);
+                *reinterpret_cast<uint16_t*>(xb8 + f8_tile_index(slot, j, ldb8)) = (uint16_t)(px | ((uint16_t)py << 8));
+            }
             const double ux = v.x * ixn, uy = v.y * ixn;
             const __nv_bfloat16 hx = __double2bfloat16(ux), hy = __double2bfloat16(uy);
             const double fx = (double)__bfloat162float(hx), fy = (double)__bfloat162float(hy);
@@ -109,12 +138,17 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
         }
         for (size_t j = ld + 2 * s; j < ldb; j += 8)
             *reinterpret_cast<__nv_bfloat162*>(xbn + bf16_tile_index(slot, j, ldb)) = __floats2bfloat162_rn(0.f, 0.f);
-        for (size_t j = ld + 2 * s; j < ldb8; j += 8) *reinterpret_cast<uint16_t*>(xbn8 + f8_tile_index(slot, j, ldb8)) = 0;
+        for (size_t j = ld + 2 * s; j < ldb8; j += 8) {
+            *reinterpret_cast<uint16_t*>(xbn8 + f8_tile_index(slot, j, ldb8)) = 0;
+            *reinterpret_cast<uint16_t*>(xb8 + f8_tile_index(slot, j, ldb8)) = 0;
+        }
     }
     nbh = group4_sum(nbh);
     nres = group4_sum(nres);
     nbh8 = group4_sum(nbh8);
     nres8 = group4_sum(nres8);
+    pb8 = group4_sum(pb8);
+    pres8 = group4_sum(pres8);
     if (active && s == 0) {
         // x/|x| is itself rounded (relative 2^-52 per element): the 2^-30 margin covers it
         const double up = 1.0 + 9.313225746154785e-10;
@@ -127,15 +161,21 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
         }
         rowpn[slot] = make_float2(__double2float_ru(sqrt(nbh) * up), __double2float_ru(sqrt(nres) * up + 1e-300));
         rowpn8[slot] = make_float2(__double2float_ru(sqrt(nbh8) * up), __double2float_ru(sqrt(nres8) * up + 1e-300));
+        rowp8[slot] = make_float4(__double2float_ru(sqrt(pb8) * up), __double2float_ru(sqrt(pres8) * up + 1e-300),
+                                  (float)(1.0 / sc8), 0.0f);
         sq64[slot] = sq;
         float4 p;
         p.x = __double2float_ru(sqrt(sq));
         p.y = __double2float_ru(sqrt(bh));
         p.z = __double2float_ru(sqrt(res));
         p.w = __double2float_rn(0.5 * sq);
-        // rows the BF16 screen cannot bound (overflow, non-finite): mark them
-        // always-candidate with an infinite error term; dead slots: |x| = -1
-        if (!(sq < 1e30) || !isfinite(p.y) || (bh == 0.0 && res > 0.0)) p.z = __int_as_float(0x7f800000);
+        // rows the screens cannot bound (overflow, non-finite, a nonzero row
+        // whose BF16 copy or E4M3 copy of x 2^f is all zero -- the screens'
+        // one-FMA bound needs |x - bx| <= alpha |bx|): mark them with an
+        // infinite error term (the store then answers searches by the exact
+        // scan); dead slots: |x| = -1
+        if (!(sq < 1e30) || !isfinite(p.y) || (bh == 0.0 && res > 0.0) || (pb8 == 0.0 && pres8 > 0.0))
+            p.z = __int_as_float(0x7f800000);
         if (live[slot] != 1) p.x = -1.0f;
         rowp[slot] = p;
     }
@@ -302,17 +342,23 @@ __device__ float ref_metric(int metric, const double* __restrict__ a, const doub
     return __double2float_rn(__ddiv_rn((double)dot, __dmul_rn(__dsqrt_rn((double)na), __dsqrt_rn((double)nb))));
 }
 
+// metrics: per pair (the drop-in calls combined into one launch), or NULL for `metric`
 __global__ void k_compare_slots(const double* __restrict__ x64, size_t ld, int d, int metric,
-                                const int64_t* __restrict__ s1, const int64_t* __restrict__ s2, int n,
-                                float* __restrict__ out) {
+                                const int* __restrict__ metrics, const int64_t* __restrict__ s1,
+                                const int64_t* __restrict__ s2, int n, float* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    out[i] = ref_metric(metric, x64 + s1[i] * ld, x64 + s2[i] * ld, d);
+    out[i] = ref_metric(metrics ? metrics[i] : metric, x64 + s1[i] * ld, x64 + s2[i] * ld, d);
 }
 
-__global__ void k_compare_vec(const double* __restrict__ a, const double* __restrict__ b, int d, int metric,
-                              float* __restrict__ out) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *out = ref_metric(metric, a, b, d);
+// pairs of free-standing vectors packed into one buffer: pair i is
+// {a offset, b offset, dimension, metric} (in doubles)
+__global__ void k_compare_vecs(const double* __restrict__ buf, const int64_t* __restrict__ desc, int n,
+                               float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t* p = desc + 4 * (size_t)i;
+    out[i] = ref_metric((int)p[3], buf + p[0], buf + p[1], (int)p[2]);
 }
 
 // ---------------------------------------------------------------------------
@@ -424,6 +470,8 @@ int Store::grow(size_t need) {
     float2* npn = nullptr;
     uint8_t* nb8 = nullptr;
     float2* npn8 = nullptr;
+    uint8_t* nx8 = nullptr;
+    float4* np8 = nullptr;
     float4* nsf = nullptr;
     double* nsq = nullptr;
     float4* np = nullptr;
@@ -438,6 +486,8 @@ int Store::grow(size_t need) {
     if (e == cudaSuccess) e = cudaMalloc(&npn, nc * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&nb8, nc * ldb8);
     if (e == cudaSuccess) e = cudaMalloc(&npn8, nc * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&nx8, nc * ldb8);
+    if (e == cudaSuccess) e = cudaMalloc(&np8, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nsf, nc * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&nsq, nc * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&np, nc * sizeof(float4));
@@ -453,6 +503,8 @@ int Store::grow(size_t need) {
         cudaFree(npn);
         cudaFree(nb8);
         cudaFree(npn8);
+        cudaFree(nx8);
+        cudaFree(np8);
         cudaFree(nsf);
         cudaFree(nsq);
         cudaFree(np);
@@ -466,6 +518,7 @@ int Store::grow(size_t need) {
     SVDB_CUDA(cudaMemsetAsync(nb, 0, nc * ldb * sizeof(__nv_bfloat16), stream));
     SVDB_CUDA(cudaMemsetAsync(nbn, 0, nc * ldb * sizeof(__nv_bfloat16), stream));
     SVDB_CUDA(cudaMemsetAsync(nb8, 0, nc * ldb8, stream));
+    SVDB_CUDA(cudaMemsetAsync(nx8, 0, nc * ldb8, stream));
     if (slots) {
         const size_t tile_rows = round_up(slots, 256);
         SVDB_CUDA(cudaMemcpyAsync(nx, x64, slots * ld * sizeof(double), cudaMemcpyDeviceToDevice, stream));
@@ -475,6 +528,8 @@ int Store::grow(size_t need) {
         SVDB_CUDA(cudaMemcpyAsync(npn, rowpn, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nb8, xbn8, tile_rows * ldb8, cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(npn8, rowpn8, slots * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(nx8, xb8, tile_rows * ldb8, cudaMemcpyDeviceToDevice, stream));
+        SVDB_CUDA(cudaMemcpyAsync(np8, rowp8, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsf, sqf, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(nsq, sq64, slots * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         SVDB_CUDA(cudaMemcpyAsync(np, rowp, slots * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
@@ -489,6 +544,8 @@ int Store::grow(size_t need) {
     cudaFree(rowpn);
     cudaFree(xbn8);
     cudaFree(rowpn8);
+    cudaFree(xb8);
+    cudaFree(rowp8);
     cudaFree(sqf);
     cudaFree(sq64);
     cudaFree(rowp);
@@ -502,6 +559,8 @@ int Store::grow(size_t need) {
     rowpn = npn;
     xbn8 = nb8;
     rowpn8 = npn8;
+    xb8 = nx8;
+    rowp8 = np8;
     sqf = nsf;
     sq64 = nsq;
     rowp = np;
@@ -616,7 +675,7 @@ int Store::sync() {
         const int threads = 256;
         const int64_t blocks = (n * 4 + threads - 1) / threads;
         k_derive_rows<<<(unsigned)blocks, threads, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp, xbn8,
-                                                              ldb8, rowpn8, live, derive_lo,
+                                                              ldb8, rowpn8, xb8, rowp8, live, derive_lo,
                                                               derive_hi, nullptr);
         SVDB_LAUNCH_CHECK();
     }
@@ -629,7 +688,7 @@ int Store::sync() {
         d = (int64_t*)scratch;
         SVDB_CUDA(cudaMemcpyAsync(d, dirty_list.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
         k_derive_rows<<<(unsigned)((n * 4 + 255) / 256), 256, 0, stream>>>(x64, ld, xb, ldb, x32, xbn, rowpn, sqf, sq64, rowp,
-                                                                         xbn8, ldb8, rowpn8, live, 0,
+                                                                         xbn8, ldb8, rowpn8, xb8, rowp8, live, 0,
                                                                          n, d);
         SVDB_LAUNCH_CHECK();
         SVDB_CUDA(cudaStreamSynchronize(stream));
@@ -699,6 +758,8 @@ void svdbd_store_destroy(svdbd_store* hs) {
     cudaFree(s->rowpn);
     cudaFree(s->xbn8);
     cudaFree(s->rowpn8);
+    cudaFree(s->xb8);
+    cudaFree(s->rowp8);
     cudaFree(s->sqf);
     cudaFree(s->sq64);
     cudaFree(s->rowp);
@@ -892,7 +953,7 @@ int svdbd_compare_slots(svdbd_store* hs, int metric, const int64_t* slot1, const
     std::memcpy((int64_t*)s->pin + n, slot2, n * sizeof(int64_t));
     SVDB_CUDA(cudaMemcpyAsync(d1, s->pin, 2 * n * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
     svdb::k_compare_slots<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(s->x64, s->ld, (int)s->dim, metric,
-                                                                             d1, d2, (int)n, dout);
+                                                                             nullptr, d1, d2, (int)n, dout);
     SVDB_LAUNCH_CHECK();
     float* hout = (float*)((int64_t*)s->pin + 2 * n);
     SVDB_CUDA(cudaMemcpyAsync(hout, dout, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
@@ -901,39 +962,101 @@ int svdbd_compare_slots(svdbd_store* hs, int metric, const int64_t* slot1, const
     return SVDB_OK;
 }
 
-// The drop-in metric functions take two free-standing host vectors; they
-// share one small device buffer and stream guarded by a mutex.
+// the same with a metric per pair (the drop-in metric calls, combined)
+int svdbd_compare_slots_mixed(svdbd_store* hs, const int32_t* metric, const int64_t* slot1, const int64_t* slot2,
+                              size_t n, float* out) {
+    Store* s = reinterpret_cast<Store*>(hs);
+    if (n == 0) return SVDB_OK;
+    int rc = s->sync();
+    if (rc) return rc;
+    const size_t bytes = n * (2 * sizeof(int64_t) + sizeof(int32_t) + sizeof(float));
+    rc = s->scratch_reserve(bytes);
+    if (!rc) rc = s->pinned_reserve(bytes);
+    if (rc) return rc;
+    int64_t* d1 = (int64_t*)s->scratch;
+    int64_t* d2 = d1 + n;
+    int32_t* dm = (int32_t*)(d2 + n);
+    float* dout = (float*)(dm + n);
+    int64_t* h1 = (int64_t*)s->pin;
+    std::memcpy(h1, slot1, n * sizeof(int64_t));
+    std::memcpy(h1 + n, slot2, n * sizeof(int64_t));
+    std::memcpy((int32_t*)(h1 + 2 * n), metric, n * sizeof(int32_t));
+    SVDB_CUDA(cudaMemcpyAsync(d1, h1, n * (2 * sizeof(int64_t) + sizeof(int32_t)), cudaMemcpyHostToDevice,
+                              s->stream));
+    svdb::k_compare_slots<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(s->x64, s->ld, (int)s->dim, 0, dm, d1,
+                                                                             d2, (int)n, dout);
+    SVDB_LAUNCH_CHECK();
+    float* hout = (float*)((int32_t*)(h1 + 2 * n) + n);
+    SVDB_CUDA(cudaMemcpyAsync(hout, dout, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    std::memcpy(out, hout, n * sizeof(float));
+    return SVDB_OK;
+}
+
+// Free-standing host vectors (rows of no store, or of another dimension):
+// packed into one page-locked block, one copy to the device, one launch.
+// The buffers and stream are shared, guarded by a mutex.
 namespace {
 std::mutex g_vec_mu;
-double* g_vec_buf = nullptr;
-size_t g_vec_cap = 0;
-float* g_vec_out = nullptr;
+double* g_vec_buf = nullptr;  // device: vectors, then descriptors, then results
+size_t g_vec_cap = 0;         // bytes
+void* g_vec_pin = nullptr;
+size_t g_vec_pin_cap = 0;
 cudaStream_t g_vec_stream = nullptr;
 }  // namespace
 
-int svdbd_compare_vectors(int metric, const double* a, const double* b, size_t d, float* out) {
+int svdbd_compare_vectors_batch(const int32_t* metric, const double* const* a, const double* const* b,
+                                const size_t* d, size_t n, float* out) {
+    if (n == 0) return SVDB_OK;
     std::lock_guard<std::mutex> lk(g_vec_mu);
-    if (!g_vec_stream) {
-        SVDB_CUDA(cudaStreamCreateWithFlags(&g_vec_stream, cudaStreamNonBlocking));
-        SVDB_CUDA(cudaMalloc(&g_vec_out, sizeof(float)));
-    }
-    if (d * 2 > g_vec_cap) {
+    if (!g_vec_stream) SVDB_CUDA(cudaStreamCreateWithFlags(&g_vec_stream, cudaStreamNonBlocking));
+    size_t nd = 0;
+    for (size_t i = 0; i < n; ++i) nd += 2 * d[i];
+    const size_t vbytes = svdb::round_up(nd * sizeof(double), 256), dbytes = svdb::round_up(n * 4 * sizeof(int64_t), 256);
+    const size_t bytes = vbytes + dbytes + n * sizeof(float);
+    if (bytes > g_vec_cap) {
         cudaFree(g_vec_buf);
         g_vec_buf = nullptr;
         g_vec_cap = 0;
-        size_t nc = svdb::round_up(d * 2, 4096);
-        SVDB_CUDA(cudaMalloc(&g_vec_buf, nc * sizeof(double)));
+        const size_t nc = svdb::round_up(bytes, 1 << 16);
+        SVDB_CUDA(cudaMalloc(&g_vec_buf, nc));
         g_vec_cap = nc;
     }
-    if (d) {
-        SVDB_CUDA(cudaMemcpyAsync(g_vec_buf, a, d * sizeof(double), cudaMemcpyHostToDevice, g_vec_stream));
-        SVDB_CUDA(cudaMemcpyAsync(g_vec_buf + d, b, d * sizeof(double), cudaMemcpyHostToDevice, g_vec_stream));
+    if (bytes > g_vec_pin_cap) {
+        cudaFreeHost(g_vec_pin);
+        g_vec_pin = nullptr;
+        g_vec_pin_cap = 0;
+        const size_t nc = svdb::round_up(bytes, 1 << 16);
+        SVDB_CUDA(cudaMallocHost(&g_vec_pin, nc));
+        g_vec_pin_cap = nc;
     }
-    svdb::k_compare_vec<<<1, 32, 0, g_vec_stream>>>(g_vec_buf, g_vec_buf + d, (int)d, metric, g_vec_out);
+    double* hv = (double*)g_vec_pin;
+    int64_t* hd = (int64_t*)((char*)g_vec_pin + vbytes);
+    size_t o = 0;
+    for (size_t i = 0; i < n; ++i) {
+        std::memcpy(hv + o, a[i], d[i] * sizeof(double));
+        std::memcpy(hv + o + d[i], b[i], d[i] * sizeof(double));
+        hd[4 * i] = (int64_t)o;
+        hd[4 * i + 1] = (int64_t)(o + d[i]);
+        hd[4 * i + 2] = (int64_t)d[i];
+        hd[4 * i + 3] = metric[i];
+        o += 2 * d[i];
+    }
+    SVDB_CUDA(cudaMemcpyAsync(g_vec_buf, g_vec_pin, vbytes + dbytes, cudaMemcpyHostToDevice, g_vec_stream));
+    float* dout = (float*)((char*)g_vec_buf + vbytes + dbytes);
+    svdb::k_compare_vecs<<<(unsigned)((n + 127) / 128), 128, 0, g_vec_stream>>>(
+        g_vec_buf, (const int64_t*)((char*)g_vec_buf + vbytes), (int)n, dout);
     SVDB_LAUNCH_CHECK();
-    SVDB_CUDA(cudaMemcpyAsync(out, g_vec_out, sizeof(float), cudaMemcpyDeviceToHost, g_vec_stream));
+    float* hout = (float*)((char*)g_vec_pin + vbytes + dbytes);
+    SVDB_CUDA(cudaMemcpyAsync(hout, dout, n * sizeof(float), cudaMemcpyDeviceToHost, g_vec_stream));
     SVDB_CUDA(cudaStreamSynchronize(g_vec_stream));
+    std::memcpy(out, hout, n * sizeof(float));
     return SVDB_OK;
+}
+
+int svdbd_compare_vectors(int metric, const double* a, const double* b, size_t d, float* out) {
+    const int32_t m = metric;
+    return svdbd_compare_vectors_batch(&m, &a, &b, &d, 1, out);
 }
 
 }  // extern "C"

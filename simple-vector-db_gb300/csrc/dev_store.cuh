@@ -31,6 +31,8 @@ struct Store {
     size_t ldb8 = 0;               // FP8 shadow row length (bytes), D rounded up to 128
     uint8_t* xbn8 = nullptr;       // E4M3 shadow of 256 x/|x| (cap x ldb8), FP8 cosine screen
     float2* rowpn8 = nullptr;      // {|bxn8|/256 up, |x/|x| - bxn8/256| up} per row
+    uint8_t* xb8 = nullptr;        // E4M3 shadow of x 2^f_i (cap x ldb8), f_i per row: FP8 dot / Euclidean screen
+    float4* rowp8 = nullptr;       // {|bx8| up, |x - bx8| up, 2^-f_i, 0} per row, bx8 = e4m3(x 2^f_i) 2^-f_i
     float4* sqf = nullptr;         // FP32 intervals for the refinement: {|x|^2 down, |x|^2 up,
                                    //  1/(2|x|) down, 1/(2|x|) up}
     int* d_nmax = nullptr;         // (unused; the maxima live in d_count[1..4])

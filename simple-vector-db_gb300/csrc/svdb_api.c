@@ -13,17 +13,132 @@
 
 int svdb_kd_nearest_batch(KDTree* tree, const double* q, size_t nq, size_t stride, int64_t* out);
 
+/* One drop-in metric call (cosine_similarity & co.), combined with the
+ * calls of other threads into one launch (svdb_combine.c). */
+typedef struct {
+    svdb_call h;
+    int metric;
+    const double* a;
+    const double* b;
+    size_t d;
+    float out;
+    int rc;
+    char err[160];
+} metric_call;
+
+static svdb_combiner g_metric_comb = SVDB_COMBINER_INIT;
+
+/* Answers a batch of metric calls: pairs of rows of one store (found by their
+ * host buffers) are compared where they are in HBM, one launch per store;
+ * every other pair is copied to the device, all of them in one block. */
+static void run_metric_batch(void* ctx, svdb_call** calls, size_t n) {
+    (void)ctx;
+    metric_call** c = (metric_call**)calls;
+    svdb_db** st = (svdb_db**)calloc(n, sizeof(svdb_db*));
+    int64_t* s1 = (int64_t*)malloc(n * 2 * sizeof(int64_t));
+    int32_t* mt = (int32_t*)malloc(n * sizeof(int32_t));
+    size_t* pos = (size_t*)malloc(n * sizeof(size_t));
+    float* res = (float*)malloc(n * sizeof(float));
+    const double** va = (const double**)malloc(n * 2 * sizeof(double*));
+    size_t* vd = (size_t*)malloc(n * sizeof(size_t));
+    if (!st || !s1 || !mt || !pos || !res || !va || !vd) {
+        for (size_t i = 0; i < n; ++i) {
+            c[i]->rc = SVDB_ENOMEM;
+            snprintf(c[i]->err, sizeof(c[i]->err), "metric: out of host memory");
+        }
+        goto done;
+    }
+    int64_t* s2 = s1 + n;
+    for (size_t i = 0; i < n; ++i) {
+        svdb_db *da = NULL, *db = NULL;
+        int64_t sa = -1, sb = -1;
+        if (c[i]->d && svdb_rows_find(c[i]->a, &da, &sa) && svdb_rows_find(c[i]->b, &db, &sb) && da == db &&
+            da->dim == c[i]->d) {
+            st[i] = da;
+            s1[i] = sa;
+            s2[i] = sb;
+        }
+    }
+    /* stored pairs, store by store (a store whose lock is held elsewhere has
+     * its pairs copied instead, so no caller can wait on itself) */
+    for (size_t i = 0; i < n; ++i) {
+        svdb_db* d = st[i];
+        if (!d) continue;
+        int64_t* t1 = (int64_t*)malloc(n * 2 * sizeof(int64_t));
+        if (!t1 || pthread_mutex_trylock(&d->pub.mutex) != 0) {
+            free(t1);
+            for (size_t j = i; j < n; ++j)
+                if (st[j] == d) st[j] = NULL;
+            continue;
+        }
+        size_t m = 0;
+        for (size_t j = i; j < n; ++j)
+            if (st[j] == d) {
+                t1[m] = s1[j];
+                t1[n + m] = s2[j];
+                mt[m] = c[j]->metric;
+                pos[m++] = j;
+            }
+        const int rc = d->dev ? svdbd_compare_slots_mixed(d->dev, mt, t1, t1 + n, m, res) : SVDB_ENODEV;
+        pthread_mutex_unlock(&d->pub.mutex);
+        for (size_t j = 0; j < m; ++j) {
+            metric_call* r = c[pos[j]];
+            r->rc = rc;
+            r->out = rc ? NAN : res[j];
+            if (rc) snprintf(r->err, sizeof(r->err), "%s", svdb_last_error());
+            st[pos[j]] = (svdb_db*)(uintptr_t)1; /* answered */
+        }
+        free(t1);
+    }
+    /* everything else: the vectors themselves, in one copy */
+    {
+        size_t m = 0;
+        for (size_t i = 0; i < n; ++i)
+            if (st[i] != (svdb_db*)(uintptr_t)1) {
+                va[m] = c[i]->a;
+                va[n + m] = c[i]->b;
+                vd[m] = c[i]->d;
+                mt[m] = c[i]->metric;
+                pos[m++] = i;
+            }
+        if (m) {
+            const int rc = svdbd_compare_vectors_batch(mt, va, va + n, vd, m, res);
+            for (size_t j = 0; j < m; ++j) {
+                metric_call* r = c[pos[j]];
+                r->rc = rc;
+                r->out = rc ? NAN : res[j];
+                if (rc) snprintf(r->err, sizeof(r->err), "%s", svdb_last_error());
+            }
+        }
+    }
+done:
+    free(st);
+    free(s1);
+    free(mt);
+    free(pos);
+    free(res);
+    free(va);
+    free(vd);
+}
+
 static float metric_vectors(int metric, Vector a, Vector b) {
     if (a.dimension != b.dimension) {
         fprintf(stderr, "Vectors have different dimensions\n"); /* src/vector_database.c:302-305 */
         return -1.0f;
     }
-    float out = NAN;
-    if (svdbd_compare_vectors(metric, a.data, b.data, a.dimension, &out) != SVDB_OK) {
-        fprintf(stderr, "metric: %s\n", svdb_last_error());
+    metric_call call;
+    memset(&call, 0, sizeof(call));
+    call.metric = metric;
+    call.a = a.data;
+    call.b = b.data;
+    call.d = a.dimension;
+    svdb_combine(&g_metric_comb, &call.h, run_metric_batch, NULL);
+    if (call.rc != SVDB_OK) {
+        svdb_set_error("%s", call.err);
+        fprintf(stderr, "metric: %s\n", call.err);
         return NAN;
     }
-    return out;
+    return call.out;
 }
 
 SVDB_API float cosine_similarity(Vector vec1, Vector vec2) { return metric_vectors(SVDB_COSINE, vec1, vec2); }
@@ -236,6 +351,8 @@ SVDB_API int svdb_insert_batch(VectorDatabase* db, const double* rows, size_t n,
             return r;
         }
         for (size_t i = 0; i < n; ++i) d->slot_of[db->size + i] = (int64_t)(slot0 + i);
+        if (dim == d->dim)
+            for (size_t i = 0; i < n; ++i) svdb_rows_put(db->vectors[db->size + i].data, d, (int64_t)(slot0 + i));
     } else {
         for (size_t i = 0; i < n; ++i) d->slot_of[db->size + i] = -1;
     }
@@ -522,6 +639,31 @@ SVDB_API int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, u
         rc = SVDB_EINVAL;
     } else {
         rc = svdbd_selftest_wait(d->dev, limit_us, gave_up);
+    }
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
+/* See include/svdb_gb300.h: the screen's raw accumulators (diagnostics). */
+SVDB_API int svdb_debug_screen_accumulators(VectorDatabase* db, const double* queries, size_t nq, size_t dim,
+                                            int metric, int precision, size_t rows, float* acc, void* query_ops,
+                                            void* row_ops, size_t* op_bytes) {
+    if (!db || (precision != SVDB_PREC_BF16 && precision != SVDB_PREC_FP8)) {
+        svdb_set_error("svdb_debug_screen_accumulators: NULL database or precision not BF16/FP8");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc;
+    if (!d->dev) {
+        svdb_set_error("svdb_debug_screen_accumulators: the store holds no rows (no device store yet)");
+        rc = SVDB_EINVAL;
+    } else if (dim != d->dim) {
+        svdb_set_error("svdb_debug_screen_accumulators: query dimension %zu != store dimension %zu", dim, d->dim);
+        rc = SVDB_EINVAL;
+    } else {
+        rc = svdbd_debug_screen_acc(d->dev, queries, nq, metric, precision == SVDB_PREC_FP8, rows, acc, query_ops,
+                                    row_ops, op_bytes);
     }
     pthread_mutex_unlock(&db->mutex);
     return rc;

@@ -64,9 +64,15 @@ int svdbd_store_profile_read(svdbd_store* s, double* ms, int reset);
 /* reference-exact /compare for n slot pairs (host arrays in/out) */
 int svdbd_compare_slots(svdbd_store* s, int metric, const int64_t* slot1, const int64_t* slot2, size_t n,
                         float* out);
+/* the same with a metric per pair (combined drop-in metric calls) */
+int svdbd_compare_slots_mixed(svdbd_store* s, const int32_t* metric, const int64_t* slot1, const int64_t* slot2,
+                              size_t n, float* out);
 /* reference-exact metric of two host vectors (the drop-in cosine_similarity
- * etc. take Vectors that need not be stored rows) */
+ * etc. take Vectors that need not be stored rows); the batch form packs n
+ * pairs of any dimensions into one copy and one launch */
 int svdbd_compare_vectors(int metric, const double* a, const double* b, size_t d, float* out);
+int svdbd_compare_vectors_batch(const int32_t* metric, const double* const* a, const double* const* b,
+                                const size_t* d, size_t n, float* out);
 
 /* exact top-k; q/ids/dists/err in host memory unless on_device */
 int svdbd_search(svdbd_store* s, const double* q, size_t nq, size_t k, int metric, int precision,
@@ -77,6 +83,13 @@ int svdbd_search(svdbd_store* s, const double* q, size_t nq, size_t k, int metri
 int svdbd_selftest_wait(svdbd_store* s, uint32_t limit_us, uint32_t* gave_up);
 int svdbd_search_noalloc(svdbd_store* s, const double* d_queries, size_t nq, size_t k, int metric, int64_t* d_ids,
                          double* d_dists);
+
+/* diagnostics: the screen's raw FP32 accumulators for nq <= 128 host queries
+ * against the first `rows` slots, with the query and row operands the MMAs
+ * read (opbytes per row; row operands un-swizzled); f8: the E4M3 cosine
+ * operands (dev_gemm.cu) */
+int svdbd_debug_screen_acc(svdbd_store* s, const double* q, size_t nq, int metric, int f8, size_t rows, float* acc,
+                           void* qops, void* rops, size_t* opbytes);
 
 /* uuid of a slot (char[37] as the reference stores it; staged, applied at
  * sync), batched lookup of positions by uuid (-1: none), rows of the

@@ -20,6 +20,8 @@ SVDB_API KDTree* kdtree_create(size_t dimension) {
     t->pub.root = NULL;
     t->pub.dimension = dimension;
     pthread_mutex_init(&t->lock, NULL);
+    pthread_mutex_init(&t->comb.mu, NULL);
+    pthread_cond_init(&t->comb.cv, NULL);
     return &t->pub;
 }
 
@@ -32,6 +34,9 @@ SVDB_API void kdtree_free(KDTree* tree) {
     free(t->left);
     free(t->right);
     free(t->patch);
+    free(t->comb.q);
+    pthread_cond_destroy(&t->comb.cv);
+    pthread_mutex_destroy(&t->comb.mu);
     pthread_mutex_destroy(&t->lock);
     free(t);
 }
@@ -151,13 +156,46 @@ int svdb_kd_nearest_batch(KDTree* tree, const double* q, size_t nq, size_t strid
     return rc;
 }
 
+/* One kdtree_nearest call, combined with other threads' calls on the same
+ * tree into one descent launch (svdb_combine.c). */
+typedef struct {
+    svdb_call h;
+    const double* q;
+    int64_t out;
+    int rc;
+    char err[160];
+} nearest_call;
+
+static void run_nearest_batch(void* ctx, svdb_call** calls, size_t n) {
+    svdb_kd* t = (svdb_kd*)ctx;
+    nearest_call** c = (nearest_call**)calls;
+    const size_t kd = t->pub.dimension;
+    double* q = (double*)malloc((n * kd ? n * kd : 1) * sizeof(double));
+    int64_t* out = (int64_t*)malloc(n * sizeof(int64_t));
+    int rc = (q && out) ? SVDB_OK : SVDB_ENOMEM;
+    if (!rc) {
+        for (size_t i = 0; i < n; ++i) memcpy(q + i * kd, c[i]->q, kd * sizeof(double));
+        rc = svdb_kd_nearest_batch(&t->pub, q, n, kd, out);
+    }
+    for (size_t i = 0; i < n; ++i) {
+        c[i]->rc = rc;
+        c[i]->out = rc ? -1 : out[i];
+        if (rc) snprintf(c[i]->err, sizeof(c[i]->err), "%s", rc == SVDB_ENOMEM ? "out of host memory" : svdb_last_error());
+    }
+    free(q);
+    free(out);
+}
+
 SVDB_API size_t kdtree_nearest(KDTree* tree, const double* point) {
-    int64_t out = -1;
     if (!tree || !point) return (size_t)-1;
-    int rc = svdb_kd_nearest_batch(tree, point, 1, tree->dimension, &out);
-    if (rc) {
-        fprintf(stderr, "kdtree_nearest: %s\n", svdb_last_error());
+    nearest_call call;
+    memset(&call, 0, sizeof(call));
+    call.q = point;
+    svdb_combine(&svdb_kd_of(tree)->comb, &call.h, run_nearest_batch, svdb_kd_of(tree));
+    if (call.rc) {
+        svdb_set_error("%s", call.err);
+        fprintf(stderr, "kdtree_nearest: %s\n", call.err);
         return (size_t)-1;
     }
-    return out < 0 ? (size_t)-1 : (size_t)out;
+    return call.out < 0 ? (size_t)-1 : (size_t)call.out;
 }

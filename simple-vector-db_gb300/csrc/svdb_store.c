@@ -63,7 +63,10 @@ SVDB_API VectorDatabase* vector_db_init(size_t initial_capacity, size_t dimensio
 SVDB_API void vector_db_free(VectorDatabase* db) {
     if (!db) return;
     svdb_db* d = svdb_of(db);
-    for (size_t i = 0; i < db->size; ++i) free(db->vectors[i].data);
+    for (size_t i = 0; i < db->size; ++i) {
+        svdb_rows_drop(db->vectors[i].data);
+        free(db->vectors[i].data);
+    }
     kdtree_free(db->kdtree);
     free(db->vectors);
     free(d->slot_of);
@@ -149,6 +152,7 @@ static size_t insert_locked(svdb_db* d, Vector vec) {
     }
     db->vectors[db->size] = vec; /* uuid included, as src/vector_database.c:113 */
     d->slot_of[db->size] = slot;
+    if (d->dev && row_flag(d, &vec) == 1) svdb_rows_put(vec.data, d, slot);
     svdb_kd_insert_prefix(db->kdtree, vec.data, vec.data ? vec.dimension : 0, db->size);
     return db->size++;
 }
@@ -210,8 +214,10 @@ SVDB_API void vector_db_update(VectorDatabase* db, size_t index, Vector vec) {
                  (svdbd_store_overwrite(d->dev, d->slot_of[index], vec.data, row_flag(d, &vec)) != SVDB_OK ||
                   svdbd_store_set_uuid(d->dev, d->slot_of[index], vec.uuid) != SVDB_OK))
             fprintf(stderr, "vector_db_update: %s\n", svdb_last_error());
+        svdb_rows_drop(db->vectors[index].data);
         free(db->vectors[index].data);
         db->vectors[index] = vec;
+        if (d->dev && row_flag(d, &vec) == 1) svdb_rows_put(vec.data, d, d->slot_of[index]);
         svdb_kd_insert_prefix(db->kdtree, vec.data, vec.data ? vec.dimension : 0, index);
     }
     pthread_mutex_unlock(&db->mutex);
@@ -224,6 +230,7 @@ SVDB_API void vector_db_delete(VectorDatabase* db, size_t index) {
     if (index < db->size) {
         if (d->dev && d->slot_of[index] >= 0 && svdbd_store_kill(d->dev, d->slot_of[index]) != SVDB_OK)
             fprintf(stderr, "vector_db_delete: %s\n", svdb_last_error());
+        svdb_rows_drop(db->vectors[index].data);
         free(db->vectors[index].data);
         memmove(db->vectors + index, db->vectors + index + 1, (db->size - index - 1) * sizeof(Vector));
         memmove(d->slot_of + index, d->slot_of + index + 1, (db->size - index - 1) * sizeof(int64_t));
@@ -235,28 +242,58 @@ SVDB_API void vector_db_delete(VectorDatabase* db, size_t index) {
 /* file format of src/vector_database.c:203-228: size_t n, then per row
  * uuid[37], size_t dim, double[dim]; rows with no data are skipped but still
  * counted in n, exactly as the reference writes them. */
-SVDB_API void vector_db_save(VectorDatabase* db, const char* filename) {
-    if (!db || !filename) return;
-    pthread_mutex_lock(&db->mutex);
+/* The file format of src/vector_database.c:203-223: the row count, then per
+ * row uuid[37], size_t dimension, double[dimension].  Rows without data are
+ * skipped; the reference still writes db->size as the count (so such a file
+ * promises more rows than it holds).  exact_count writes the number of rows
+ * actually written instead (svdb_save with SVDB_SAVE_EXACT_COUNT). */
+static int save_locked(VectorDatabase* db, const char* filename, int exact_count) {
     FILE* f = fopen(filename, "wb");
     if (!f) {
         perror("Failed to open file for writing");
-        pthread_mutex_unlock(&db->mutex);
-        return;
+        svdb_set_error("save: cannot open %s for writing", filename);
+        return SVDB_EINVAL;
     }
-    fwrite(&db->size, sizeof(size_t), 1, f);
+    size_t n = db->size;
+    if (exact_count) {
+        n = 0;
+        for (size_t i = 0; i < db->size; ++i) n += db->vectors[i].dimension != 0 && db->vectors[i].data != NULL;
+    }
+    int ok = fwrite(&n, sizeof(size_t), 1, f) == 1;
     for (size_t i = 0; i < db->size; ++i) {
         const Vector* v = &db->vectors[i];
         if (v->dimension == 0 || v->data == NULL) {
             fprintf(stderr, "Invalid vector at index %zu, skipping\n", i);
             continue;
         }
-        fwrite(v->uuid, sizeof(char), UUID_SIZE, f);
-        fwrite(&v->dimension, sizeof(size_t), 1, f);
-        fwrite(v->data, sizeof(double), v->dimension, f);
+        ok = ok && fwrite(v->uuid, sizeof(char), UUID_SIZE, f) == UUID_SIZE;
+        ok = ok && fwrite(&v->dimension, sizeof(size_t), 1, f) == 1;
+        ok = ok && fwrite(v->data, sizeof(double), v->dimension, f) == v->dimension;
     }
-    fclose(f);
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) {
+        svdb_set_error("save: write to %s failed", filename);
+        return SVDB_EINVAL;
+    }
+    return SVDB_OK;
+}
+
+SVDB_API void vector_db_save(VectorDatabase* db, const char* filename) {
+    if (!db || !filename) return;
+    pthread_mutex_lock(&db->mutex);
+    save_locked(db, filename, 0);
     pthread_mutex_unlock(&db->mutex);
+}
+
+SVDB_API int svdb_save(VectorDatabase* db, const char* filename, unsigned flags) {
+    if (!db || !filename || (flags & ~(unsigned)SVDB_SAVE_EXACT_COUNT)) {
+        svdb_set_error("svdb_save: NULL argument or unknown flag");
+        return SVDB_EINVAL;
+    }
+    pthread_mutex_lock(&db->mutex);
+    const int rc = save_locked(db, filename, (flags & SVDB_SAVE_EXACT_COUNT) != 0);
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
 }
 
 SVDB_API VectorDatabase* vector_db_load(const char* filename, size_t dimension) {

@@ -68,6 +68,7 @@ class RaggedInfo(C.Structure):
 
 
 RAGGED_AUTOTUNE, RAGGED_NO_GRAPH = 1, 2
+SAVE_EXACT_COUNT = 1
 
 
 class SvdbError(RuntimeError):
@@ -111,6 +112,9 @@ def _load():
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
         "svdb_selftest_bounded_wait": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_uint32)]),
+        "svdb_save": (C.c_int, [vp, C.c_char_p, C.c_uint]),
+        "svdb_debug_screen_accumulators": (C.c_int, [vp, _dp, sz, sz, C.c_int, C.c_int, sz,
+                                                     C.POINTER(C.c_float), vp, vp, C.POINTER(C.c_size_t)]),
         "svdb_server_create": (vp, [sz, sz]),
         "svdb_server_destroy": (None, [vp]),
         "svdb_server_size": (sz, [vp]),
@@ -305,8 +309,13 @@ class VectorDatabase:
     def delete(self, index: int) -> None:
         lib.vector_db_delete(self.ptr, index)
 
-    def save(self, filename: str) -> None:
-        lib.vector_db_save(self.ptr, filename.encode())
+    def save(self, filename: str, exact_count: bool = False) -> None:
+        """vector_db_save (the reference's bytes), or svdb_save with
+        SVDB_SAVE_EXACT_COUNT: the row count written is the rows written."""
+        if exact_count:
+            _check(lib.svdb_save(self.ptr, filename.encode(), SAVE_EXACT_COUNT), "svdb_save")
+        else:
+            lib.vector_db_save(self.ptr, filename.encode())
 
     def sync(self) -> None:
         _check(lib.svdb_sync(self.ptr), "svdb_sync")
@@ -413,6 +422,24 @@ class VectorDatabase:
         g = C.c_uint32(0)
         rc = lib.svdb_selftest_bounded_wait(self.ptr, limit_us, C.byref(g))
         return rc, g.value, last_error()
+
+    def screen_accumulators(self, queries, metric: int, precision: int, rows: int):
+        """svdb_debug_screen_accumulators (1..256 queries; more than 128 run
+        the paired screen) -> (acc [nq, rows] float32, query operands
+        [nq, op_bytes] uint8, row operands [rows, op_bytes] uint8)."""
+        q = _f64(queries)
+        q = q.reshape(-1, q.shape[-1])
+        nq, d = q.shape
+        ob = (d + 63) // 64 * 128 if precision == PREC_BF16 else (d + 127) // 128 * 128
+        acc = np.empty((nq, rows), np.float32)
+        qo = np.empty((nq, ob), np.uint8)
+        ro = np.empty((rows, ob), np.uint8)
+        got = C.c_size_t(0)
+        _check(lib.svdb_debug_screen_accumulators(self.ptr, q.ctypes.data_as(_dp), nq, d, metric, precision, rows,
+                                                  acc.ctypes.data_as(C.POINTER(C.c_float)), qo.ctypes.data,
+                                                  ro.ctypes.data, C.byref(got)), "svdb_debug_screen_accumulators")
+        assert got.value == ob, (got.value, ob)
+        return acc, qo, ro
 
     def search_device(self, q_ptr: int, nq: int, dim: int, k: int, metric: int, precision: int, ids_ptr: int,
                       dists_ptr: int, err_ptr: int = 0, stats: SearchStats | None = None) -> None:

@@ -107,6 +107,39 @@ def test_save_load_roundtrip_and_format(svdb, tmp_path):
     db2.close()
 
 
+def test_save_exact_count_option(svdb, tmp_path):
+    """A row without data is skipped by the reference's save but still
+    counted (src/vector_database.c:213-218): vector_db_save keeps that count,
+    svdb_save(SVDB_SAVE_EXACT_COUNT) writes the rows actually written, with
+    the same row bytes; both files load back to the complete rows."""
+    db = svdb.VectorDatabase(0, 3)
+    r = np.random.default_rng(8)
+    X = r.uniform(-1, 1, (5, 4))
+    for i, x in enumerate(X):
+        db.insert(x, f"{i:036d}")
+    db.insert(np.zeros(0), "no-data")  # dimension 0: skipped by the save
+    db.insert(X[0] + 1.0, "last")
+    assert db.size == 7
+    f1, f2 = str(tmp_path / "counted.db"), str(tmp_path / "exact.db")
+    db.save(f1)
+    db.save(f2, exact_count=True)
+    raw1, raw2 = open(f1, "rb").read(), open(f2, "rb").read()
+    row = 37 + 8 + 4 * 8
+    assert len(raw1) == len(raw2) == 8 + 6 * row
+    assert int.from_bytes(raw1[:8], "little") == 7  # the reference's count: one row more than the file holds
+    assert int.from_bytes(raw2[:8], "little") == 6
+    assert raw1[8:] == raw2[8:]
+    for f in (f1, f2):  # the drop-in load keeps every complete row of either file
+        d2 = svdb.VectorDatabase.load(f, 3)
+        assert d2.size == 6
+        for i in range(5):
+            assert np.array_equal(d2.read(i), X[i])
+        assert np.array_equal(d2.read(5), X[0] + 1.0) and d2.uuid(5) == b"last"
+        d2.close()
+    assert svdb.lib.svdb_save(db.ptr, str(tmp_path / "x.db").encode(), 2) == svdb.EINVAL  # unknown flag
+    db.close()
+
+
 def test_save_file_identical_to_reference(svdb, refstore, tmp_path):
     import oracle as O
     r = np.random.default_rng(5)

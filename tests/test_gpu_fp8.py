@@ -1,13 +1,14 @@
-"""GPU parity of the FP8-E4M3 cosine screen (SVDB_PREC_FP8).
+"""GPU parity of the FP8-E4M3 screens (SVDB_PREC_FP8).
 
-The unit-norm shadow is stored as E4M3 of 256 x/|x|; queries are scaled by a
-power of two, so keys are the accumulator times an exact power of two.  Bar:
-the same as the BF16 screen -- ids identical to the FP64 oracle (ties to the
-lowest index), FP64 values bit-identical to the oracle's canonical order, the
-certified bound never failing against the exact value -- on near-tie
-mixtures, after mutations, with k up to 128; dot and Euclidean searches with
-this precision run the BF16 screen and are exact too; data the FP8 bound
-cannot separate (uniform rows) falls back to the exact FP64 scan.
+Cosine screens an E4M3 copy of 256 x/|x|; dot and Euclidean screen an E4M3
+copy of x 2^f_i, 2^f_i a per-row power of two (the largest with max |x_j|
+2^f_i <= 448).  Queries are scaled by a power of two, so every key is the
+accumulator times exact powers of two.  Bar: the same as the BF16 screen --
+ids identical to the FP64 oracle (ties to the lowest index), FP64 values
+bit-identical to the oracle's canonical order, the certified bound never
+failing against the exact value -- on near-tie mixtures, rows of widely
+different magnitudes, after mutations, with k up to 128; data the FP8
+bound cannot separate (uniform rows) falls back to the exact FP64 scan.
 """
 import numpy as np
 import pytest
@@ -36,17 +37,18 @@ def _search(S, db, Q, k, metric=0):
     return ids, vals, st
 
 
+@pytest.mark.parametrize("metric", [0, 1, 2])
 @pytest.mark.parametrize("d", [64, 128, 200, 768])
-def test_fp8_cosine_mixture_near_ties(S, oracle, d):
-    rng = np.random.default_rng(80 + d)
+def test_fp8_mixture_near_ties(S, oracle, d, metric):
+    rng = np.random.default_rng(80 + d + 7 * metric)
     n = 30000 if d <= 200 else 12000
     C, X = _mixture(rng, n, d, 32)
     Q = C[rng.integers(0, 32, 300)] + 0.05 * rng.normal(size=(300, d))
     db = S.VectorDatabase(0, 3)
     db.insert_batch(X)
     for k in (1, 10, 100):
-        ids, vals, st = _search(S, db, Q, k)
-        wid, wval = oracle.topk(0, X, Q, k)
+        ids, vals, st = _search(S, db, Q, k, metric)
+        wid, wval = oracle.topk(metric, X, Q, k)
         assert np.array_equal(ids, wid), (k, st.widened)
         assert np.array_equal(vals, wval), k
         assert st.bound_failures == 0
@@ -54,8 +56,9 @@ def test_fp8_cosine_mixture_near_ties(S, oracle, d):
     db.close()
 
 
-def test_fp8_query_tiles_mutations_and_k128(S, oracle):
-    rng = np.random.default_rng(81)
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_fp8_query_tiles_mutations_and_k128(S, oracle, metric):
+    rng = np.random.default_rng(81 + metric)
     C, X = _mixture(rng, 9000 + 77, 96, 20)
     db = S.VectorDatabase(0, 3)
     db.insert_batch(X)
@@ -71,32 +74,47 @@ def test_fp8_query_tiles_mutations_and_k128(S, oracle):
     for nq in (1, 127, 129, 520):
         Q = C[rng.integers(0, 20, nq)] + 0.05 * rng.normal(size=(nq, 96))
         for k in (16, 33, 128):
-            ids, vals, st = _search(S, db, Q, k)
-            wid, wval = oracle.topk(0, Xc, Q, k)
+            ids, vals, st = _search(S, db, Q, k, metric)
+            wid, wval = oracle.topk(metric, Xc, Q, k)
             assert np.array_equal(ids, wid), (nq, k)
             assert np.array_equal(vals, wval), (nq, k)
             assert st.bound_failures == 0
     db.close()
 
 
-def test_fp8_other_metrics_and_unseparable_data(S, oracle):
-    rng = np.random.default_rng(82)
-    C, X = _mixture(rng, 8000, 128, 16)
-    Q = C[rng.integers(0, 16, 100)] + 0.05 * rng.normal(size=(100, 128))
+@pytest.mark.parametrize("metric", [1, 2])
+def test_fp8_per_row_scales_on_rows_of_every_magnitude(S, oracle, metric):
+    """Rows scaled by 10^U[-12, 12] (their E4M3 scales 2^f span a range of
+    2^80), a zero row, and rows of norm 1e-35 (scales clamped at 2^120, so
+    their E4M3 copies lose most digits): the per-row scale and residual keep
+    every bound valid, and the screen still answers the batch."""
+    rng = np.random.default_rng(83 + metric)
+    C, X = _mixture(rng, 12000, 96, 24)
+    X *= 10.0 ** rng.uniform(-12, 12, (X.shape[0], 1))
+    X[7] = 0.0
+    X[100:110] *= 1e-35 / np.linalg.norm(X[100:110], axis=1, keepdims=True)
+    Q = C[rng.integers(0, 24, 200)] + 0.05 * rng.normal(size=(200, 96))
     db = S.VectorDatabase(0, 3)
     db.insert_batch(X)
-    for metric in (1, 2):  # the BF16 screen answers these
-        ids, vals, st = _search(S, db, Q, 10, metric)
-        wid, wval = oracle.topk(metric, X, Q, 10)
-        assert np.array_equal(ids, wid) and np.array_equal(vals, wval), metric
+    for k in (1, 10, 64):
+        ids, vals, st = _search(S, db, Q, k, metric)
+        wid, wval = oracle.topk(metric, X, Q, k)
+        assert np.array_equal(ids, wid), (k, st.widened)
+        assert np.array_equal(vals, wval), k
         assert st.bound_failures == 0
+        assert st.widened < Q.shape[0], k
     db.close()
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_fp8_unseparable_data_falls_back_exact(S, oracle, metric):
+    rng = np.random.default_rng(82 + metric)
     U = rng.uniform(-1, 1, (20000, 64))  # no clusters: the FP8 bound admits too much, the exact scan answers
     Qu = rng.uniform(-1, 1, (50, 64))
     db = S.VectorDatabase(0, 3)
     db.insert_batch(U)
-    ids, vals, st = _search(S, db, Qu, 10)
-    wid, wval = oracle.topk(0, U, Qu, 10)
+    ids, vals, st = _search(S, db, Qu, 10, metric)
+    wid, wval = oracle.topk(metric, U, Qu, 10)
     assert np.array_equal(ids, wid) and np.array_equal(vals, wval)
     assert st.bound_failures == 0
     db.close()
