@@ -903,6 +903,119 @@ def run_nearest(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_percall(args, ws, rank, local):
+    """The drop-in per-call path as the unmodified server drives it: one
+    thread per connection, one call per request (src/main.c:381,
+    src/compare_handler.c:153-159,403).  Store: the CPU-runnable case,
+    N=10,000 x 128 U[-1,1] (seed 0), KD dimension 3; queries U[-1,1] (seed 1).
+    T threads (1 and --percall-threads) each call cosine_similarity on two
+    stored rows (the Vectors vector_db_read returns) or kdtree_nearest, one
+    call at a time, timed per call in C (libsvdb_percall.so, no interpreter in
+    the loop).  The CPU baseline is the oracle's restatement of the same two
+    functions (the reference's float loop and insertion-order tree) driven
+    the same way."""
+    import torch
+    import svdb_gb300 as S
+    W = workloads()
+
+    torch.cuda.set_device(local)
+    X, Q, kd = W.config1()
+    db = S.VectorDatabase(X.shape[0], kd)
+    db.insert_batch(X)
+    db.sync()
+    drv = C.CDLL(os.path.join(PKG, "_build", "libsvdb_percall.so"))
+    drv.svdb_percall_metric.restype = C.c_int
+    drv.svdb_percall_metric.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int,
+                                        C.c_size_t, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    drv.svdb_percall_nearest.restype = C.c_int
+    drv.svdb_percall_nearest.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_int,
+                                         C.c_size_t, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    r = np.random.default_rng(1)
+    npairs = 1000
+    i1, i2 = r.integers(0, X.shape[0], npairs), r.integers(0, X.shape[0], npairs)
+    VA, VB = (S.Vector * npairs)(), (S.Vector * npairs)()
+    for j in range(npairs):  # the store's own rows, as vector_db_read returns them
+        VA[j] = S.lib.vector_db_read(db.ptr, int(i1[j])).contents
+        VB[j] = S.lib.vector_db_read(db.ptr, int(i2[j])).contents
+    Qc = np.ascontiguousarray(Q)
+
+    def metric_run(fn, abi, threads, calls):
+        lat = np.empty(threads * calls)
+        out = np.empty(threads * calls, np.float32)
+        wall = C.c_double(0)
+        rc = drv.svdb_percall_metric(fn, abi, 0, C.addressof(VA), C.addressof(VB), npairs, threads, calls,
+                                     lat.ctypes.data, out.ctypes.data, C.byref(wall))
+        if rc:
+            raise SystemExit("bench: percall metric harness failed")
+        return lat, out, wall.value
+
+    def nearest_run(fn, tree, threads, calls):
+        lat = np.empty(threads * calls)
+        out = np.empty(threads * calls, np.int64)
+        wall = C.c_double(0)
+        rc = drv.svdb_percall_nearest(fn, tree, Qc.ctypes.data, Qc.shape[0], Qc.shape[1], threads, calls,
+                                      lat.ctypes.data, out.ctypes.data, C.byref(wall))
+        if rc:
+            raise SystemExit("bench: percall nearest harness failed")
+        return lat, out, wall.value
+
+    def summary(lat, wall, n):
+        return {"p50_us": float(np.percentile(lat, 50)) / 1e3, "p99_us": float(np.percentile(lat, 99)) / 1e3,
+                "calls_per_s": n / (wall / 1e9)}
+
+    import oracle as O
+    O.build(ref=False)
+    o = O.Oracle()
+    okd = O.OracleKD(o, kd)
+    for i in range(X.shape[0]):
+        okd.insert(X[i], i)
+    want_m = np.array([o.ref_metric(0, X[a], X[b]) for a, b in zip(i1, i2)], np.float32)
+    want_n = np.array([okd.nearest(q) for q in Qc])
+    f_cos = C.cast(S.lib.cosine_similarity, C.c_void_p).value
+    f_near = C.cast(S.lib.kdtree_nearest, C.c_void_p).value
+    o_cos = C.cast(o.L.orc_ref_metric, C.c_void_p).value
+    o_near = C.cast(o.L.orc_kd_nearest, C.c_void_p).value
+    res = {}
+    clk = Clocks(local)
+    for T in sorted({1, args.percall_threads}):
+        calls = max(50, args.percall_calls // T)
+        metric_run(f_cos, 0, T, 20)  # warm-up
+        lat, out, wall = metric_run(f_cos, 0, T, calls)
+        idx = np.arange(T * calls) % npairs
+        if out.tobytes() != want_m[idx].tobytes():
+            raise SystemExit("bench: per-call cosine_similarity differs from the oracle")
+        res[f"cosine_similarity_threads{T}"] = summary(lat, wall, T * calls)
+        nearest_run(f_near, db.kdtree, T, 20)
+        lat, outn, wall = nearest_run(f_near, db.kdtree, T, calls)
+        if not np.array_equal(outn, want_n[np.arange(T * calls) % Qc.shape[0]]):
+            raise SystemExit("bench: per-call kdtree_nearest differs from the oracle")
+        res[f"kdtree_nearest_threads{T}"] = summary(lat, wall, T * calls)
+    clocks = clk.stop()
+    cpu = {}
+    for T in sorted({1, args.percall_threads}):
+        calls = max(2000, 20 * args.percall_calls // T)
+        lat, out, wall = metric_run(o_cos, 1, T, calls)
+        cpu[f"cosine_similarity_threads{T}"] = summary(lat, wall, T * calls)
+        lat, outn, wall = nearest_run(o_near, okd.h, T, calls)
+        cpu[f"kdtree_nearest_threads{T}"] = summary(lat, wall, T * calls)
+    T = args.percall_threads
+    head = res[f"cosine_similarity_threads{T}"]
+    line = {"metric": f"drop-in /compare calls/s, {T} threads one call at a time (N=10k x 128)",
+            "value": head["calls_per_s"], "unit": "calls/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (float accumulation, as the reference)", "data": "synthetic",
+            "config": {"workload": "N=10,000 x 128 U[-1,1] seed 0, kd 3; cosine_similarity on stored rows and "
+                                   "kdtree_nearest, one call per thread at a time", "threads": T,
+                       "l2": "store (10 MB) fits in L2: latency-bound"},
+            "per_call": res,
+            "cpu_baseline": {"kind": "port", "cores": T, "per_call": cpu,
+                             "sample": "the oracle's restatement of cosine_similarity and kdtree_nearest, driven by "
+                                       "the same C harness"},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    db.close()
+
+
 def run_decode(args, ws, rank, local):
     """POST /nearest request bodies decoded on the device: batches of 4,096
     bodies, each a JSON array of 768 numbers written with %.17g (N(0,1) x
@@ -982,7 +1095,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest", "decode"],
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest", "decode", "percall"],
                     help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
                          "ragged: one batch over 5 collections of different dimensions; serve: the serving loop; "
                          "uuid: GET /vector?uuid= lookups and persistence; nearest: the CPU-runnable config-1 "
@@ -991,6 +1104,8 @@ def main():
     ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
     ap.add_argument("--fp64-seconds", type=float, default=2.0, help="serve: cut-off of the plain FP64 trace")
+    ap.add_argument("--percall-threads", type=int, default=16, help="percall: concurrent caller threads")
+    ap.add_argument("--percall-calls", type=int, default=32000, help="percall: calls across all threads")
     ap.add_argument("--extra", type=int, default=1, help="mixture: also time other batch sizes, metrics and a serve "
                                                          "trace (outside the timed region)")
     ap.add_argument("--serve-seconds-headline", type=float, default=1.0,
@@ -1014,6 +1129,8 @@ def main():
         run_nearest(args, ws, rank, local)
     elif args.workload == "decode":
         run_decode(args, ws, rank, local)
+    elif args.workload == "percall":
+        run_percall(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 

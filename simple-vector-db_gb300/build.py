@@ -17,6 +17,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libsvdb_gb300.so")
+PERCALL_LIB = os.path.join(OUT, "libsvdb_percall.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 C_SOURCES = ["svdb_store.c", "svdb_kdtree.c", "svdb_api.c", "svdb_server.c", "svdb_combine.c"]
@@ -82,6 +83,11 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
     if jobs or not os.path.exists(LIB):
         _run([nvcc, ARCH, "-shared", "-o", LIB, *objs, "-Xlinker", "-Bsymbolic", "-lpthread", "-ldl", "-lrt"],
              verbose)
+    # the per-call timing harness (bench.py --workload percall): its own small library
+    drv_src = os.path.join(CSRC, "percall_driver.c")
+    if force or _stale(PERCALL_LIB, drv_src, deps):
+        _run(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fvisibility=hidden", "-Wall", "-Wextra", "-D_GNU_SOURCE",
+              *inc, "-o", PERCALL_LIB, drv_src, "-lpthread"], verbose)
     return LIB
 
 

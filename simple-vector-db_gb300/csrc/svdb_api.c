@@ -27,6 +27,7 @@ typedef struct {
 } metric_call;
 
 static svdb_combiner g_metric_comb = SVDB_COMBINER_INIT;
+#define ANSWERED ((svdb_db*)(uintptr_t)1) /* a call of the batch already answered */
 
 /* Answers a batch of metric calls: pairs of rows of one store (found by their
  * host buffers) are compared where they are in HBM, one launch per store;
@@ -60,10 +61,11 @@ static void run_metric_batch(void* ctx, svdb_call** calls, size_t n) {
         }
     }
     /* stored pairs, store by store (a store whose lock is held elsewhere has
-     * its pairs copied instead, so no caller can wait on itself) */
+     * its pairs copied instead, so no caller can wait on itself); answered
+     * calls are marked ANSWERED */
     for (size_t i = 0; i < n; ++i) {
         svdb_db* d = st[i];
-        if (!d) continue;
+        if (!d || d == ANSWERED) continue;
         int64_t* t1 = (int64_t*)malloc(n * 2 * sizeof(int64_t));
         if (!t1 || pthread_mutex_trylock(&d->pub.mutex) != 0) {
             free(t1);
@@ -86,7 +88,7 @@ static void run_metric_batch(void* ctx, svdb_call** calls, size_t n) {
             r->rc = rc;
             r->out = rc ? NAN : res[j];
             if (rc) snprintf(r->err, sizeof(r->err), "%s", svdb_last_error());
-            st[pos[j]] = (svdb_db*)(uintptr_t)1; /* answered */
+            st[pos[j]] = ANSWERED;
         }
         free(t1);
     }
@@ -94,7 +96,7 @@ static void run_metric_batch(void* ctx, svdb_call** calls, size_t n) {
     {
         size_t m = 0;
         for (size_t i = 0; i < n; ++i)
-            if (st[i] != (svdb_db*)(uintptr_t)1) {
+            if (st[i] != ANSWERED) {
                 va[m] = c[i]->a;
                 va[n + m] = c[i]->b;
                 vd[m] = c[i]->d;

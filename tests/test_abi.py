@@ -161,6 +161,57 @@ def test_save_file_identical_to_reference(svdb, refstore, tmp_path):
     db.close()
 
 
+def test_dropin_calls_from_many_threads_host_logic(svdb):
+    """The drop-in per-call path's host side (row registry, call combiner,
+    grouping by store) driven from 16 threads on stored rows, free vectors
+    and rows of two stores at once.  With no GPU every call must come back
+    as the failure the reference's callers can see (NaN, or -1.0f for a
+    dimension mismatch) -- and nothing may crash or hang."""
+    import threading
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (the GPU test checks the values)")
+    r = np.random.default_rng(3)
+    dbs = [svdb.VectorDatabase(0, 3), svdb.VectorDatabase(0, 3)]
+    for d in dbs:
+        for x in r.uniform(-1, 1, (300, 16)):
+            d.insert(x)  # staged on the host (no GPU here)
+    rows = [[svdb.lib.vector_db_read(d.ptr, i).contents for i in range(300)] for d in dbs]
+    free = [svdb.make_vector(r.uniform(-1, 1, 16), owned=False) for _ in range(8)]
+    short = svdb.make_vector(np.ones(5), owned=False)
+    fns = (svdb.lib.cosine_similarity, svdb.lib.euclidean_distance, svdb.lib.dot_product)
+    bad = []
+
+    def work(t):
+        g = np.random.default_rng(t)
+        for j in range(60):
+            m, a, b = int(g.integers(0, 3)), int(g.integers(0, 300)), int(g.integers(0, 300))
+            kind = j % 4
+            if kind == 0:
+                v = fns[m](rows[t % 2][a], rows[t % 2][b])
+            elif kind == 1:
+                v = fns[m](rows[0][a], rows[1][b])  # rows of two stores
+            elif kind == 2:
+                v = fns[m](free[a % 8], rows[0][b])
+            else:
+                v = fns[m](short, rows[0][b])
+                if v != np.float32(-1.0):
+                    bad.append((t, j, v))
+                continue
+            if not np.isnan(v):
+                bad.append((t, j, v))
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(16)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join(timeout=120)
+        assert not th.is_alive()
+    assert not bad, bad[:5]
+    for d in dbs:
+        d.close()
+
+
 def test_library_fails_loudly_without_gpu(svdb):
     """No CPU fallback: without a usable GPU every compute call errors."""
     import torch

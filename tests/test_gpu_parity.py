@@ -54,6 +54,76 @@ def test_dropin_metrics_adversarial(S, golden):
         assert fns[m](np.ones(4), np.ones(5)) == np.float32(-1.0)
 
 
+def test_dropin_calls_from_many_threads(S, golden, oracle):
+    """The unmodified server's call pattern (src/compare_handler.c:153-159,
+    403): one thread per connection, each calling cosine_similarity /
+    euclidean_distance / dot_product on the store's own rows (the Vectors
+    vector_db_read returns, so the rows are found where they are in HBM),
+    on free-standing vectors, and kdtree_nearest, one call at a time and all
+    at once.  Concurrent calls are combined into shared launches; every result
+    is the reference's, bit for bit."""
+    import ctypes as C
+    import threading
+    X, pairs = compare_inputs()
+    db = _db(S, X)
+    db.sync()
+    fns = (S.lib.cosine_similarity, S.lib.euclidean_distance, S.lib.dot_product)
+    rows = [S.lib.vector_db_read(db.ptr, i).contents for i in range(X.shape[0])]
+    r = np.random.default_rng(31)
+    free_a = r.uniform(-1, 1, (64, 128))
+    free_b = r.uniform(-1, 1, (64, 128))
+    fa = [S.make_vector(v, owned=False) for v in free_a]
+    fb = [S.make_vector(v, owned=False) for v in free_b]
+    Q = r.uniform(-1, 1, (400, 128))
+    want_near = np.array([db.kdtree_nearest(q) for q in Q[:8]])  # single calls first
+    O_kd = oracle.kd(3)
+    for i in range(X.shape[0]):
+        O_kd.insert(X[i], i)
+    want_q = np.array([O_kd.nearest(q) for q in Q])
+    assert np.array_equal(want_near, want_q[:8])
+    nthreads, per = 16, 120
+    got = np.zeros((nthreads, per), np.float32)
+    want = np.zeros((nthreads, per), np.float32)
+    near = np.full((nthreads, 25), -2, np.int64)
+    errs = []
+
+    def work(t_):
+        try:
+            g = np.random.default_rng(100 + t_)
+            for j in range(per):
+                m = int(g.integers(0, 3))
+                if g.random() < 0.75:  # two stored rows
+                    p = pairs[int(g.integers(0, len(pairs)))]
+                    got[t_, j] = fns[m](rows[p[0]], rows[p[1]])
+                    want[t_, j] = golden["compare_vals"][np.flatnonzero((pairs == p).all(1))[0], m]
+                else:  # vectors of no store
+                    k = int(g.integers(0, 64))
+                    got[t_, j] = fns[m](fa[k], fb[k])
+                    want[t_, j] = oracle.ref_metric(m, free_a[k], free_b[k])
+                if j % 5 == 0:
+                    qi = (t_ * 25 + j // 5) % len(Q)
+                    near[t_, j // 5] = S.lib.kdtree_nearest(db.kdtree, Q[qi].ctypes.data_as(S._dp))
+        except Exception as e:  # pragma: no cover - reported below
+            errs.append(e)
+
+    ths = [threading.Thread(target=work, args=(t_,)) for t_ in range(nthreads)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    assert not errs, errs
+    assert got.tobytes() == want.tobytes()
+    for t_ in range(nthreads):
+        for j in range(0, per, 5):
+            assert near[t_, j // 5] == want_q[(t_ * 25 + j // 5) % len(Q)]
+    # a stored row changed through the store API is seen by the next call
+    new = r.uniform(-1, 1, 128)
+    db.update(3, new)
+    v3 = S.lib.vector_db_read(db.ptr, 3).contents
+    assert np.float32(S.lib.cosine_similarity(v3, rows[7])) == oracle.ref_metric(0, new, X[7])
+    db.close()
+
+
 def test_compare_rows_of_mixed_dimension(S, oracle):
     db = S.VectorDatabase(0, 3)
     r = np.random.default_rng(21)
