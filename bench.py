@@ -49,7 +49,7 @@ METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GP
 # same 4096 cosine queries (the shadow is read once per launch, so the bytes
 # grow with the rows and a full launch is this times N).  None when no capture
 # of the current kernel exists.
-SCREEN_DRAM_BYTES_PER_ROW = (420.257536e6 + 19.836416e6) / 200_000
+SCREEN_DRAM_BYTES_PER_ROW = (421.659648e6 + 19.84128e6) / 200_000
 
 
 def log(*a):
@@ -1016,6 +1016,138 @@ def run_percall(args, ws, rank, local):
     db.close()
 
 
+def run_loop(args, ws, rank, local):
+    """The request path as a device-side loop (svdb_loop_*): a store of
+    1,000,000 x 768 rows (the D=768 mixture, 1,024 centres, sigma 0.05, seed
+    5), KD dimension 3.  A seeded open-loop trace at --rate requests/s (70 %
+    POST /nearest answered by the KD descent, 10 % /compare with a uniform
+    metric, 15 % insert, 3 % update, 2 % delete) is replayed in real time by a
+    C harness: one thread submits each request at its arrival time, another
+    takes the answers in order; latency = answer - arrival, queueing
+    included.  A sample of the answers is checked against the oracle's
+    positional store replaying the same requests.  CPU baseline: that
+    oracle replay (the reference's store and KD tree restated), one thread."""
+    import torch
+    import svdb_gb300 as S
+    from svdb_gb300 import serve
+    W = workloads()
+
+    torch.cuda.set_device(local)
+    n0, d, kd = args.loop_rows, DIM, 3
+    m5 = W.Mixture(d, 5)
+    X0 = m5.sample(n0, 0)
+    nreq = int(args.rate * args.serve_seconds)
+    g = np.random.Generator(np.random.PCG64(np.random.SeedSequence([5, 77])))
+    arrival = np.cumsum(g.exponential(1.0 / args.rate, nreq))
+    ops = g.choice([5, 1, 2, 3, 4], size=nreq, p=[0.70, 0.10, 0.15, 0.03, 0.02]).astype(np.int32)
+    vecs = np.ascontiguousarray(m5.sample(nreq, 9), np.float64)
+    req = np.zeros(nreq, serve.REQ_DTYPE)
+    req["op"] = ops
+    req["metric"] = g.integers(0, 3, nreq)
+    size = n0
+    u = g.random((nreq, 2))
+    for i in range(nreq):
+        o = ops[i]
+        if o in (5, 2, 3):
+            req["vec"][i] = vecs.ctypes.data + i * d * 8
+        if o == 1:
+            req["a"][i], req["b"][i] = int(u[i, 0] * size), int(u[i, 1] * size)
+        elif o == 2:
+            size += 1
+        elif o == 3:
+            req["a"][i] = int(u[i, 0] * size)
+        elif o == 4 and size > 0:
+            req["a"][i] = int(u[i, 0] * size)
+            size -= 1
+    t = time.perf_counter()
+    loop = S.DeviceLoop(d, kd, n0 + nreq + 1024, X0, ring=8192)
+    log(f"[bench] loop store + KD tree {time.perf_counter() - t:.1f}s")
+    loop.start()
+    drv = C.CDLL(os.path.join(PKG, "_build", "libsvdb_percall.so"))
+    drv.svdb_percall_loop_replay.restype = C.c_int
+    drv.svdb_percall_loop_replay.argtypes = [C.c_void_p] * 4 + [C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                                                                C.c_void_p, C.c_size_t, C.POINTER(C.c_double)]
+    f_sub = C.cast(S.lib.svdb_loop_submit, C.c_void_p).value
+    f_wait = C.cast(S.lib.svdb_loop_wait, C.c_void_p).value
+    resp = np.zeros(nreq, np.dtype([("status", "<i4"), ("value", "<f4"), ("index", "<u8")]))
+    lat = np.empty(nreq)
+    wall = C.c_double(0)
+    # warm-up: a short trace of /nearest requests only (no mutation: the measured
+    # trace starts from the stated store)
+    wq = np.zeros(2000, serve.REQ_DTYPE)
+    wq["op"] = 5
+    wv = np.ascontiguousarray(m5.sample(2000, 8), np.float64)
+    wq["vec"] = wv.ctypes.data + np.arange(2000, dtype=np.uint64) * np.uint64(d * 8)
+    warm_arr = np.arange(2000) / args.rate
+    wresp = np.zeros(2000, resp.dtype)
+    wlat = np.empty(2000)
+    drv.svdb_percall_loop_replay(f_sub, f_wait, loop.ptr, wq.ctypes.data, wq.itemsize, warm_arr.ctypes.data, 2000,
+                                 wlat.ctypes.data, wresp.ctypes.data, resp.itemsize, C.byref(wall))
+    clk = Clocks(local)
+    info0 = loop.info()
+    rc = drv.svdb_percall_loop_replay(f_sub, f_wait, loop.ptr, req.ctypes.data, req.itemsize, arrival.ctypes.data,
+                                      nreq, lat.ctypes.data, resp.ctypes.data, resp.itemsize, C.byref(wall))
+    clocks = clk.stop()
+    if rc:
+        raise SystemExit(f"bench: loop replay failed: {S.last_error()}")
+    info1 = loop.info()
+    loop.stop()
+    # correctness guard: the oracle's positional store replays the same requests
+    import oracle as O
+    O.build(ref=False)
+    o = O.Oracle()
+    st = o.store(d, kd)
+    for i in range(n0):
+        st.insert(X0[i])
+    cpu_t = time.perf_counter()
+    mismatch = 0
+    for i in range(nreq):
+        op = int(ops[i])
+        if op == 5:
+            r = st.nearest(vecs[i])
+            want = 2 ** 64 - 1 if r < 0 else r
+            if resp["status"][i] != 0 or int(resp["index"][i]) != want:
+                mismatch += 1
+        elif op == 1:
+            a, b, m = int(req["a"][i]), int(req["b"][i]), int(req["metric"][i])
+            ra = np.ctypeslib.as_array(o.L.orc_store_rows(st.h), shape=(st.size * d,))
+            want = o.ref_metric(m, ra[a * d:(a + 1) * d], ra[b * d:(b + 1) * d])
+            if resp["status"][i] != 0 or np.float32(resp["value"][i]).tobytes() != want.tobytes():
+                mismatch += 1
+        elif op == 2:
+            st.insert(vecs[i])
+        elif op == 3:
+            st.update(int(req["a"][i]), vecs[i])
+        else:
+            st.delete(int(req["a"][i]))
+    cpu_s = time.perf_counter() - cpu_t
+    if mismatch:
+        raise SystemExit(f"bench: {mismatch} loop answers differ from the oracle")
+    loop.close()
+    served = nreq / (wall.value / 1e9)
+    line = {"metric": f"device-side request loop: served requests/s at {args.rate:.0f} req/s offered (70% /nearest KD, "
+                      "10% /compare, 15% insert, 3% update, 2% delete), 1M x 768; p50/p99 ms",
+            "value": served, "unit": "requests/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": wall.value / 1e6, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (float accumulation in /compare, as the reference)", "data": "synthetic",
+            "config": {"workload": f"device loop over {n0} x 768 FP64 mixture rows (seed 5), kd 3, Poisson arrivals "
+                                   f"at {args.rate:.0f}/s for {args.serve_seconds:.1f} s",
+                       "l2": "rows (6.1 GB) larger than L2"},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)) / 1e6, "p99": float(np.percentile(lat, 99)) / 1e6,
+                           "max": float(lat.max()) / 1e6},
+            "loop": {"requests": nreq, "batches": info1["batches"] - info0["batches"],
+                     "mean_batch": nreq / max(1, info1["batches"] - info0["batches"]),
+                     "idle_exits": info1["idle_exits"], "mix": {int(k): int(v) for k, v in zip(*np.unique(ops, return_counts=True))},
+                     "statuses": {int(k): int(v) for k, v in zip(*np.unique(resp["status"], return_counts=True))},
+                     "how": "requests written to a mapped page-locked ring by one host thread at their arrival "
+                            "times, answers taken in ticket order by another; no CUDA call per request"},
+            "cpu_baseline": {"value": nreq / cpu_s, "unit": "requests/s", "cores": 1, "kind": "port",
+                             "sample": f"the {nreq} requests replayed through the oracle's positional store and "
+                                       f"KD tree, one thread ({cpu_s:.1f} s)"},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def run_decode(args, ws, rank, local):
     """POST /nearest request bodies decoded on the device: batches of 4,096
     bodies, each a JSON array of 768 numbers written with %.17g (N(0,1) x
@@ -1095,7 +1227,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=64)
     ap.add_argument("--plain-q", type=int, default=64)
     ap.add_argument("--rows", type=int, default=N_ROWS, help="store rows (smaller cases for ncu captures)")
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest", "decode", "percall"],
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "scan128", "ragged", "serve", "uuid", "nearest", "decode", "percall",
+                             "loop"],
                     help="mixture: the 1M x 768 headline; scan128: plain FP64 single-query scan at 1M x 128; "
                          "ragged: one batch over 5 collections of different dimensions; serve: the serving loop; "
                          "uuid: GET /vector?uuid= lookups and persistence; nearest: the CPU-runnable config-1 "
@@ -1104,6 +1237,7 @@ def main():
     ap.add_argument("--serve-sizes", default="1000000,5000000", help="serve: store sizes (rows)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
     ap.add_argument("--fp64-seconds", type=float, default=2.0, help="serve: cut-off of the plain FP64 trace")
+    ap.add_argument("--loop-rows", type=int, default=1_000_000, help="loop: initial rows of the loop's store")
     ap.add_argument("--percall-threads", type=int, default=16, help="percall: concurrent caller threads")
     ap.add_argument("--percall-calls", type=int, default=32000, help="percall: calls across all threads")
     ap.add_argument("--extra", type=int, default=1, help="mixture: also time other batch sizes, metrics and a serve "
@@ -1131,6 +1265,8 @@ def main():
         run_decode(args, ws, rank, local)
     elif args.workload == "percall":
         run_percall(args, ws, rank, local)
+    elif args.workload == "loop":
+        run_loop(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
 

@@ -253,6 +253,8 @@ void svdb_ragged_destroy(svdb_ragged* plan);
 #define SVDB_REQ_INSERT 2  /* append vec (POST /vector, src/post_handler.c:333) */
 #define SVDB_REQ_UPDATE 3  /* overwrite row a with vec (PUT /vector, src/put_handler.c:155,247) */
 #define SVDB_REQ_DELETE 4  /* delete row a (DELETE /vector, src/delete_handler.c:84,96) */
+#define SVDB_REQ_KD_NEAREST 5 /* POST /nearest as the reference answers it: kdtree_nearest over the first
+                                 kd_dim coordinates of vec (src/compare_handler.c:403); device loop only */
 
 typedef struct svdb_request {
     int32_t op;        /* SVDB_REQ_* */
@@ -324,6 +326,97 @@ int svdb_server_execute(svdb_server* s, const svdb_request* req, size_t n, svdb_
  * result means a search could not report a stalled pipeline.  Synchronous.
  */
 int svdb_selftest_bounded_wait(VectorDatabase* db, uint32_t limit_us, uint32_t* gave_up);
+
+/*
+ * The request path as a device-side loop (no reference counterpart; it
+ * replaces the reference's thread-per-connection handlers, src/main.c:381,
+ * for /compare, POST /nearest and /vector).  One persistent kernel owns a
+ * store and serves requests as they arrive: host threads put requests into a
+ * ring in page-locked host memory mapped into the device (svdb_loop_submit
+ * makes no CUDA call), the kernel polls it, takes every request already there
+ * as one batch and answers it in ticket order -- a run of /compare and
+ * /nearest requests in parallel, each insert / update / delete applied in
+ * place before the next request -- with the reference's results and
+ * positional semantics: SVDB_REQ_COMPARE (metric of positions a, b; the
+ * reference's float), SVDB_REQ_KD_NEAREST (response.index = the stored index
+ * kdtree_nearest returns over the insertion-order KD tree, (size_t)-1 when
+ * empty; stale after deletes, as in the reference), SVDB_REQ_INSERT (index =
+ * the new row's position; a KD node), SVDB_REQ_UPDATE (a second KD node),
+ * SVDB_REQ_DELETE (later positions shift down; the KD tree is untouched).
+ * Positions past the end get SVDB_CMP_OUT_OF_BOUNDS, an unknown metric
+ * SVDB_CMP_UNKNOWN_METHOD, SVDB_REQ_NEAREST (top-k) SVDB_EINVAL (served by
+ * svdb_server_execute).  Admission by HBM: capacity rows and kd_capacity KD
+ * nodes are allocated at creation (NULL if they do not fit); an insert (or an
+ * update's KD node) beyond them is answered SVDB_ENOMEM.  Every wait is
+ * bounded: the kernel returns after idle_us with no request
+ * (SVDB_LOOP_LEFT_IDLE) and sees svdb_loop_stop at every poll; svdb_loop_wait
+ * starts it again when it is not running.  Every submitted ticket must be
+ * waited for: its ring slot is reused only after its answer was taken.
+ */
+typedef struct svdb_loop svdb_loop;
+typedef struct svdb_loop_config {
+    size_t dim;          /* row dimension */
+    size_t kd_dim;       /* the KD prefix (the server's kd_tree_dimension), 1..32, <= dim */
+    size_t capacity;     /* rows the store may hold (>= the initial rows) */
+    size_t kd_capacity;  /* KD nodes (inserts + updates add one each); 0: 2 x capacity */
+    size_t ring;         /* requests in flight (rounded up to a power of two); 0: 4096 */
+    uint32_t max_batch;  /* requests answered per pass, 1..256; 0: 256 */
+    uint32_t idle_us;    /* the kernel returns after this long with nothing to do; 0: 1 s */
+} svdb_loop_config;
+
+#define SVDB_LOOP_NOT_STARTED 0
+#define SVDB_LOOP_RUNNING 1
+#define SVDB_LOOP_LEFT_IDLE 2
+#define SVDB_LOOP_STOPPED 3
+#define SVDB_LOOP_LEAVING 4
+typedef struct svdb_loop_info {
+    uint32_t state;       /* SVDB_LOOP_* */
+    uint32_t reserved;
+    uint64_t size;        /* rows after the last batch */
+    uint64_t answered;    /* tickets answered */
+    uint64_t batches;     /* batches served */
+    uint64_t idle_exits;  /* launches that ended for want of requests */
+} svdb_loop_info;
+
+/* rows: n x dim initial rows (positions 0..n-1, KD tree built in that order);
+ * uuids37: n x 37 bytes or NULL */
+svdb_loop* svdb_loop_create(const svdb_loop_config* cfg, const double* rows, size_t n, const char* uuids37);
+int svdb_loop_start(svdb_loop* l);
+/* req->vec: dim doubles (INSERT, UPDATE, KD_NEAREST); req->uuid as for the server store */
+int svdb_loop_submit(svdb_loop* l, const svdb_request* req, uint64_t* ticket);
+/* spins until the ticket is answered (timeout_us: SVDB_ETIMEOUT) */
+int svdb_loop_wait(svdb_loop* l, uint64_t ticket, svdb_response* resp, uint32_t timeout_us);
+int svdb_loop_stop(svdb_loop* l);
+int svdb_loop_get_info(svdb_loop* l, svdb_loop_info* out);
+/* a row (dim doubles) and its uuid (37 bytes, may be NULL) by position; the loop must not be running */
+int svdb_loop_read(svdb_loop* l, size_t position, double* row, char* uuid37);
+void svdb_loop_destroy(svdb_loop* l);
+
+/*
+ * Response bodies printed on the GPU, as the reference's handlers print them
+ * (replaces cJSON_PrintUnformatted of the objects built at
+ * src/compare_handler.c:180-185 for GET /compare and :409-424 for POST
+ * /nearest; cJSON is not vendored, its published number rule is restated:
+ * "null" for NaN or an infinity, the decimal integer when the value equals
+ * its int conversion, else printf's "%1.15g" when strtod of it is within
+ * DBL_EPSILON (relative) of the value, else "%1.17g"; digits exact, ties to
+ * even, as printf).  n texts are packed into out (cap bytes) with
+ * offsets[0..n] (offsets[i+1] - offsets[i] bytes each, no NUL); out == NULL
+ * only fills the offsets (the size to allocate).  SVDB_EINVAL when cap is too
+ * small (offsets are still filled).  Synchronous.
+ *
+ * svdb_format_compare: metric (0..2) and float result per answer, status
+ * SVDB_CMP_* (a nonzero status prints the handler's fixed error body,
+ * src/compare_handler.c:103-163).
+ * svdb_format_nearest: index[i] as kdtree_nearest returned it (-1 for
+ * (size_t)-1): {"index":i,"vector":[...],"uuid":"..."} with the stored row,
+ * {"error":"No nearest neighbor found"} for -1, {"error":"Nearest neighbor
+ * not found"} for an index past the end (a KD node left by a delete).
+ */
+int svdb_format_compare(const int32_t* metric, const float* value, const int32_t* status, size_t n, char* out,
+                        size_t cap, uint64_t* offsets);
+int svdb_format_nearest(VectorDatabase* db, const int64_t* index, size_t n, char* out, size_t cap,
+                        uint64_t* offsets);
 
 /*
  * vector_db_save with options (replaces reference src/vector_database.c:203-223

@@ -84,6 +84,12 @@ class Oracle:
         L.orc_store_nearest.argtypes = [C.c_void_p, _dp]
         L.orc_decode_body.restype = C.c_int
         L.orc_decode_body.argtypes = [C.c_char_p, C.c_size_t, C.c_size_t, _dp]
+        L.orc_format_number.restype = C.c_int
+        L.orc_format_number.argtypes = [C.c_double, C.c_char_p]
+        L.orc_format_compare.restype = C.c_size_t
+        L.orc_format_compare.argtypes = [C.c_int, C.c_float, C.c_char_p]
+        L.orc_format_nearest.restype = C.c_size_t
+        L.orc_format_nearest.argtypes = [C.c_int, C.c_uint64, _dp, C.c_size_t, C.c_char_p, C.c_char_p]
         L.orc_find_uuid.restype = C.c_int
         L.orc_find_uuid.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t, _i64p, C.c_int]
         self.L = L
@@ -95,6 +101,25 @@ class Oracle:
         out = np.full(max(dim, 1), np.nan)
         st = self.L.orc_decode_body(body, len(body), dim, _ptr(out))
         return st, out[:dim]
+
+    # -- response bodies as cJSON_PrintUnformatted writes them -------------
+    def format_number(self, d: float) -> bytes:
+        buf = C.create_string_buffer(64)
+        n = self.L.orc_format_number(float(d), buf)
+        return buf.raw[:n]
+
+    def format_compare(self, metric: int, value) -> bytes:
+        buf = C.create_string_buffer(128)
+        n = self.L.orc_format_compare(metric, float(np.float32(value)), buf)
+        return buf.raw[:n]
+
+    def format_nearest(self, found: int, index: int, row, uuid37: bytes) -> bytes:
+        """found 1: the row; 0: no neighbour; -1: an index that reads no row."""
+        r = np.ascontiguousarray(row if row is not None else np.zeros(0), np.float64)
+        buf = C.create_string_buffer(64 + 26 * r.size + 6 * 37 + 64)
+        u = C.create_string_buffer(bytes(uuid37).ljust(37, b"\0")[:37], 38)
+        n = self.L.orc_format_nearest(found, index, _ptr(r), r.size, u, buf)
+        return buf.raw[:n]
 
     # -- GET /vector?uuid=: the reference's linear strncmp scan -------------
     def find_uuid(self, table: bytes, keys: bytes, threads: int = 1) -> np.ndarray:

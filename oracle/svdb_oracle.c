@@ -48,6 +48,17 @@
  *       against dim, then every child a number.  Numbers come from the C
  *       library's strtod itself, as in cJSON.
  *
+ *   orc_format_*  src/compare_handler.c:180-185 and :409-424 -- the response
+ *       bodies the handlers print with cJSON_PrintUnformatted.  cJSON's
+ *       number rule (published 1.7 sources, restated): "null" for NaN or an
+ *       infinity; the decimal integer when the value equals its int
+ *       conversion (clamped to INT_MIN..INT_MAX); else the text of "%1.15g"
+ *       if strtod of it is within DBL_EPSILON (relative to the larger
+ *       magnitude) of the value, else "%1.17g".  Strings are quoted with
+ *       '"' and '\' escaped, \b \f \n \r \t for those bytes and \u00xx
+ *       for other bytes below 32.  The digits come from the C library's own
+ *       printf and strtod, as in cJSON.
+ *
  *   orc_find_uuid src/vector_database.c:145-158 -- the linear scan of
  *       vector_db_read_by_uuid: first row whose uuid[37] equals the key
  *       under strncmp(.., 37); n keys, each scanned independently, spread
@@ -614,4 +625,79 @@ int orc_decode_body(const char* text, size_t len, size_t dim, double* out) {
     if (nchild != dim) return 2;
     if (bad) return 3;
     return 0;
+}
+
+/* ---- response bodies as cJSON_PrintUnformatted writes them ---------------- */
+#include <float.h>
+#include <limits.h>
+
+/* one number; returns its length (at most 25) */
+int orc_format_number(double d, char* out) {
+    if (isnan(d) || isinf(d)) return sprintf(out, "null");
+    const int vi = d >= (double)INT_MAX ? INT_MAX : d <= (double)INT_MIN ? INT_MIN : (int)d;
+    if (d == (double)vi) return sprintf(out, "%d", vi);
+    int n = sprintf(out, "%1.15g", d);
+    const double back = strtod(out, NULL);
+    const double m = fabs(back) > fabs(d) ? fabs(back) : fabs(d);
+    if (!(fabs(back - d) <= m * DBL_EPSILON)) n = sprintf(out, "%1.17g", d);
+    return n;
+}
+
+static size_t put_string(const char* s, size_t maxlen, char* out) {
+    size_t o = 0;
+    out[o++] = '"';
+    for (size_t i = 0; i < maxlen && s[i]; ++i) {
+        const unsigned char c = (unsigned char)s[i];
+        if (c == '"' || c == '\\') {
+            out[o++] = '\\';
+            out[o++] = (char)c;
+        } else if (c < 32) {
+            out[o++] = '\\';
+            switch (c) {
+                case '\b': out[o++] = 'b'; break;
+                case '\f': out[o++] = 'f'; break;
+                case '\n': out[o++] = 'n'; break;
+                case '\r': out[o++] = 'r'; break;
+                case '\t': out[o++] = 't'; break;
+                default: o += (size_t)sprintf(out + o, "u%04x", c);
+            }
+        } else {
+            out[o++] = (char)c;
+        }
+    }
+    out[o++] = '"';
+    return o;
+}
+
+/* GET /compare/<metric> answer {"<key>":<value>} (src/compare_handler.c:
+ * 152-185; result is the float metric widened to double) */
+size_t orc_format_compare(int metric, float value, char* out) {
+    static const char* keys[3] = {"cosine_similarity", "euclidean_distance", "dot_product"};
+    size_t o = (size_t)sprintf(out, "{\"%s\":", keys[metric]);
+    o += (size_t)orc_format_number((double)value, out + o);
+    out[o++] = '}';
+    out[o] = 0;
+    return o;
+}
+
+/* POST /nearest answer (src/compare_handler.c:409-424): found = 1 with the
+ * row (dim doubles), its position and uuid (char[37]); found = 0: no
+ * neighbour (kdtree_nearest returned (size_t)-1); found = -1: the index read
+ * no row (a stale KD node past the end of the store) */
+size_t orc_format_nearest(int found, uint64_t index, const double* row, size_t dim, const char* uuid37, char* out) {
+    size_t o = 0;
+    if (found == 0) return (size_t)sprintf(out, "{\"error\":\"No nearest neighbor found\"}");
+    if (found < 0) return (size_t)sprintf(out, "{\"error\":\"Nearest neighbor not found\"}");
+    o += (size_t)sprintf(out + o, "{\"index\":");
+    o += (size_t)orc_format_number((double)index, out + o);
+    o += (size_t)sprintf(out + o, ",\"vector\":[");
+    for (size_t i = 0; i < dim; ++i) {
+        if (i) out[o++] = ',';
+        o += (size_t)orc_format_number(row[i], out + o);
+    }
+    o += (size_t)sprintf(out + o, "],\"uuid\":");
+    o += put_string(uuid37, 37, out + o);
+    out[o++] = '}';
+    out[o] = 0;
+    return o;
 }

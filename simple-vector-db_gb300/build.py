@@ -21,7 +21,7 @@ PERCALL_LIB = os.path.join(OUT, "libsvdb_percall.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 C_SOURCES = ["svdb_store.c", "svdb_kdtree.c", "svdb_api.c", "svdb_server.c", "svdb_combine.c"]
-CU_SOURCES = ["dev_store.cu", "dev_search.cu", "dev_kd.cu", "dev_gemm.cu", "dev_noalloc.cu", "dev_ragged.cu", "dev_uuid.cu", "dev_kdm.cu", "dev_decode.cu"]
+CU_SOURCES = ["dev_store.cu", "dev_search.cu", "dev_kd.cu", "dev_gemm.cu", "dev_noalloc.cu", "dev_ragged.cu", "dev_uuid.cu", "dev_kdm.cu", "dev_decode.cu", "dev_loop.cu"]
 
 
 def _nvcc() -> str:

@@ -40,6 +40,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "dev_common.cuh"
 #include "dev_store.cuh"
@@ -969,6 +970,432 @@ bool host_pinned(const void* p) {
     return at.type == cudaMemoryTypeHost;
 }
 
+// ---------------------------------------------------------------------------
+// Response bodies as cJSON_PrintUnformatted writes them.
+//
+// The handlers build their answers with cJSON and print them unformatted
+// (src/compare_handler.c:180-185 for /compare, :409-424 for /nearest).
+// cJSON's number rule (published 1.7 sources, restated): "null" for NaN or an
+// infinity; the decimal integer when the value equals its int conversion
+// (clamped to INT_MIN..INT_MAX; -0 prints "0"); otherwise the text of
+// printf's "%1.15g" if strtod of it lies within DBL_EPSILON (relative to the
+// larger magnitude) of the value, else "%1.17g".  printf's %g is exact: the
+// value's decimal expansion rounded to the precision, half to even on an
+// exact tie.  Here the first 18 significant digits and a sticky bit come from
+// exact big-integer arithmetic (m 2^e, or m 5^-e 10^e for e < 0, divided by
+// powers of ten), the round trip uses the decoder's own exact conversion, and
+// the text follows %g's layout (fixed when -4 <= X < P, else d.ddde+XX,
+// trailing zeros and a bare point dropped).
+// ---------------------------------------------------------------------------
+constexpr int kFmtLimbs = 82;  // 2624 bits >= bits(2^53 x 5^1074) (2547)
+struct B32 {
+    uint32_t v[kFmtLimbs];
+    int n;
+};
+
+__device__ __forceinline__ void b32_mul(B32& b, uint32_t m) {
+    uint64_t c = 0;
+    for (int i = 0; i < b.n; ++i) {
+        const uint64_t t = (uint64_t)b.v[i] * m + c;
+        b.v[i] = (uint32_t)t;
+        c = t >> 32;
+    }
+    if (c && b.n < kFmtLimbs) b.v[b.n++] = (uint32_t)c;
+}
+// b /= d, returns the remainder
+__device__ __forceinline__ uint32_t b32_divrem(B32& b, uint32_t d) {
+    uint64_t r = 0;
+    for (int i = b.n - 1; i >= 0; --i) {
+        const uint64_t cur = (r << 32) | b.v[i];
+        b.v[i] = (uint32_t)(cur / d);
+        r = cur % d;
+    }
+    while (b.n > 0 && b.v[b.n - 1] == 0) --b.n;
+    return (uint32_t)r;
+}
+__device__ __forceinline__ uint32_t b32_divrem_1e9(B32& b) {  // constant divisor: multiply-high code
+    uint64_t r = 0;
+    for (int i = b.n - 1; i >= 0; --i) {
+        const uint64_t cur = (r << 32) | b.v[i];
+        b.v[i] = (uint32_t)(cur / 1000000000ull);
+        r = cur % 1000000000ull;
+    }
+    while (b.n > 0 && b.v[b.n - 1] == 0) --b.n;
+    return (uint32_t)r;
+}
+__device__ __forceinline__ int b32_bits(const B32& b) {
+    return b.n ? 32 * (b.n - 1) + (32 - __clz((int)b.v[b.n - 1])) : 0;
+}
+
+__device__ __constant__ uint64_t c_pow10[20] = {1ull,
+                                                10ull,
+                                                100ull,
+                                                1000ull,
+                                                10000ull,
+                                                100000ull,
+                                                1000000ull,
+                                                10000000ull,
+                                                100000000ull,
+                                                1000000000ull,
+                                                10000000000ull,
+                                                100000000000ull,
+                                                1000000000000ull,
+                                                10000000000000ull,
+                                                100000000000000ull,
+                                                1000000000000000ull,
+                                                10000000000000000ull,
+                                                100000000000000000ull,
+                                                1000000000000000000ull,
+                                                10000000000000000000ull};
+
+__device__ __forceinline__ int u64_digits(uint64_t x) {  // decimal digits of x > 0
+    int L = 1;
+    while (L < 20 && x >= c_pow10[L]) ++L;
+    return L;
+}
+
+// The exact value m 2^e (m > 0): its first 18 significant digits D
+// (10^17 <= D < 10^18), whether any later digit is nonzero, and the decimal
+// exponent of its first digit.
+__device__ void exact_digits18(uint64_t m, int e, uint64_t* D, bool* sticky, int* E10) {
+    B32 N;
+    N.v[0] = (uint32_t)m;
+    N.v[1] = (uint32_t)(m >> 32);
+    N.n = N.v[1] ? 2 : 1;
+    int k10 = 0;  // value = N x 10^k10
+    if (e >= 0) {
+        const int w = e >> 5, bsh = e & 31;
+        for (int i = N.n - 1; i >= 0; --i) N.v[i + w] = N.v[i];
+        for (int i = 0; i < w; ++i) N.v[i] = 0;
+        N.n += w;
+        if (bsh) {
+            uint32_t carry = 0;
+            for (int i = 0; i < N.n; ++i) {
+                const uint32_t x = N.v[i];
+                N.v[i] = (x << bsh) | carry;
+                carry = x >> (32 - bsh);
+            }
+            if (carry) N.v[N.n++] = carry;
+        }
+    } else {  // m 2^e = m 5^-e 10^e
+        int k = -e;
+        while (k >= 13) {
+            b32_mul(N, 1220703125u);  // 5^13
+            k -= 13;
+        }
+        uint32_t r = 1;
+        while (k-- > 0) r *= 5;
+        if (r > 1) b32_mul(N, r);
+        k10 = e;
+    }
+    bool st = false;
+    int L;
+    uint64_t x;
+    const int bits = b32_bits(N);
+    if (bits <= 64) {
+        x = N.n == 1 ? N.v[0] : ((uint64_t)N.v[1] << 32) | N.v[0];
+        L = u64_digits(x);
+        if (L <= 18) {
+            x *= c_pow10[18 - L];
+        } else {
+            const uint64_t p = c_pow10[L - 18];
+            st = x % p != 0;
+            x /= p;
+        }
+    } else {
+        // digits of N: L in {Lg, Lg + 1}, Lg = floor((bits - 1) log10 2) + 1 (a
+        // lower bound; the margin keeps the floor from rounding up)
+        const int Lg = (int)floor((double)(bits - 1) * 0.30102999566398119521 - 1e-9) + 1;
+        int sdrop = Lg - 18;  // >= 2: bits > 64 means Lg >= 20
+        while (sdrop >= 9) {
+            st |= b32_divrem_1e9(N) != 0;
+            sdrop -= 9;
+        }
+        if (sdrop > 0) st |= b32_divrem(N, (uint32_t)c_pow10[sdrop]) != 0;
+        x = N.n == 0 ? 0 : N.n == 1 ? N.v[0] : ((uint64_t)N.v[1] << 32) | N.v[0];  // < 10^19
+        L = Lg;
+        if (x >= c_pow10[18]) {
+            st |= x % 10 != 0;
+            x /= 10;
+            L = Lg + 1;
+        }
+    }
+    *D = x;
+    *sticky = st;
+    *E10 = L - 1 + k10;
+}
+
+// D18 rounded to P significant digits, half to even: q (10^(P-1) <= q < 10^P)
+// and the decimal exponent X of its first digit
+__device__ __forceinline__ void round_digits(uint64_t D18, bool sticky, int E10, int P, uint64_t* q, int* X) {
+    const uint64_t div = c_pow10[18 - P], half = div / 2;
+    uint64_t t = D18 / div;
+    const uint64_t r = D18 % div;
+    if (r > half || (r == half && (sticky || (t & 1)))) ++t;
+    int x = E10;
+    if (t == c_pow10[P]) {
+        t = c_pow10[P - 1];
+        ++x;
+    }
+    *q = t;
+    *X = x;
+}
+
+// printf %.<P>g of the value sign q 10^(X - P + 1)
+__device__ int g_text(bool neg, uint64_t q, int X, int P, char* out) {
+    char dg[20];
+    for (int i = P - 1; i >= 0; --i) {
+        dg[i] = (char)('0' + q % 10);
+        q /= 10;
+    }
+    int nd = P;
+    while (nd > 1 && dg[nd - 1] == '0') --nd;
+    int o = 0;
+    if (neg) out[o++] = '-';
+    if (X < -4 || X >= P) {
+        out[o++] = dg[0];
+        if (nd > 1) {
+            out[o++] = '.';
+            for (int i = 1; i < nd; ++i) out[o++] = dg[i];
+        }
+        out[o++] = 'e';
+        out[o++] = X < 0 ? '-' : '+';
+        const int ax = X < 0 ? -X : X;
+        if (ax >= 100) out[o++] = (char)('0' + ax / 100);
+        out[o++] = (char)('0' + (ax / 10) % 10);
+        out[o++] = (char)('0' + ax % 10);
+    } else if (X >= 0) {
+        for (int i = 0; i <= X; ++i) out[o++] = dg[i];
+        if (nd > X + 1) {
+            out[o++] = '.';
+            for (int i = X + 1; i < nd; ++i) out[o++] = dg[i];
+        }
+    } else {
+        out[o++] = '0';
+        out[o++] = '.';
+        for (int i = 0; i < -X - 1; ++i) out[o++] = '0';
+        for (int i = 0; i < nd; ++i) out[o++] = dg[i];
+    }
+    return o;
+}
+
+__device__ int int_text(int v, char* out) {
+    char t[12];
+    int n = 0, o = 0;
+    uint32_t u = v < 0 ? (uint32_t)(-(int64_t)v) : (uint32_t)v;
+    do {
+        t[n++] = (char)('0' + u % 10);
+        u /= 10;
+    } while (u);
+    if (v < 0) out[o++] = '-';
+    while (n) out[o++] = t[--n];
+    return o;
+}
+
+// one number as cJSON prints it; at most 24 bytes
+__device__ int cjson_number(double d, char* out) {
+    if (isnan(d) || isinf(d)) {
+        out[0] = 'n';
+        out[1] = 'u';
+        out[2] = 'l';
+        out[3] = 'l';
+        return 4;
+    }
+    const int vi = d >= 2147483647.0 ? 2147483647 : d <= -2147483648.0 ? (-2147483647 - 1) : (int)d;
+    if (d == (double)vi) return int_text(vi, out);
+    const uint64_t b = (uint64_t)__double_as_longlong(d);
+    const bool neg = (b >> 63) != 0;
+    const int be = (int)((b >> 52) & 0x7ff);
+    uint64_t m = b & ((1ull << 52) - 1);
+    int e;
+    if (be == 0) {
+        e = -1074;
+    } else {
+        m |= 1ull << 52;
+        e = be - 1075;
+    }
+    uint64_t D18;
+    bool sticky;
+    int E10;
+    exact_digits18(m, e, &D18, &sticky, &E10);
+    uint64_t q;
+    int X;
+    round_digits(D18, sticky, E10, 15, &q, &X);
+    // strtod of the 15-digit text is the correctly rounded q 10^(X - 14)
+    const double back = value_of(q, (int64_t)X - 14, neg);
+    const double mx = fmax(fabs(back), fabs(d));
+    if (__dsub_rn(fmax(back, d), fmin(back, d)) <= __dmul_rn(mx, 2.220446049250313e-16))
+        return g_text(neg, q, X, 15, out);
+    round_digits(D18, sticky, E10, 17, &q, &X);
+    return g_text(neg, q, X, 17, out);
+}
+
+// a C string (at most maxlen bytes, up to its NUL) as cJSON quotes it
+__device__ int cjson_string(const char* s, int maxlen, char* out) {
+    int o = 0;
+    out[o++] = '"';
+    for (int i = 0; i < maxlen && s[i]; ++i) {
+        const unsigned char c = (unsigned char)s[i];
+        if (c == '"' || c == '\\') {
+            out[o++] = '\\';
+            out[o++] = (char)c;
+        } else if (c < 32) {
+            out[o++] = '\\';
+            if (c == '\b') out[o++] = 'b';
+            else if (c == '\f') out[o++] = 'f';
+            else if (c == '\n') out[o++] = 'n';
+            else if (c == '\r') out[o++] = 'r';
+            else if (c == '\t') out[o++] = 't';
+            else {
+                const char* hx = "0123456789abcdef";
+                out[o++] = 'u';
+                out[o++] = '0';
+                out[o++] = '0';
+                out[o++] = hx[c >> 4];
+                out[o++] = hx[c & 15];
+            }
+        } else {
+            out[o++] = (char)c;
+        }
+    }
+    out[o++] = '"';
+    return o;
+}
+
+__device__ __forceinline__ int put_lit(char* out, const char* lit) {
+    int o = 0;
+    while (lit[o]) {
+        out[o] = lit[o];
+        ++o;
+    }
+    return o;
+}
+
+// GET /compare answers, one thread each, into slots of kCmpSlot bytes
+constexpr int kCmpSlot = 64;
+__global__ void k_fmt_compare(const int32_t* __restrict__ metric, const float* __restrict__ value,
+                              const int32_t* __restrict__ status, int n, char* __restrict__ slots,
+                              uint32_t* __restrict__ len) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    char* o = slots + (size_t)i * kCmpSlot;
+    int k = 0;
+    const int st = status[i];
+    if (st == 0) {
+        const int m = metric[i];
+        k += put_lit(o, m == 0 ? "{\"cosine_similarity\":" : m == 1 ? "{\"euclidean_distance\":" : "{\"dot_product\":");
+        k += cjson_number((double)value[i], o + k);
+        o[k++] = '}';
+    } else {  // the handler's fixed error bodies (src/compare_handler.c:103-163)
+        k += put_lit(o, st == 1   ? "{\"error\": \"Index out of bounds\"}"
+                        : st == 2 ? "{\"error\": \"Vector not found\"}"
+                        : st == 3 ? "{\"error\": \"Vectors have different dimensions\"}"
+                        : st == 4 ? "{\"error\": \"Vector size mismatch\"}"
+                                  : "{\"error\": \"Unknown comparison method\"}");
+    }
+    len[i] = (uint32_t)k;
+}
+
+// POST /nearest answers, one block each, into slots of `slot` bytes: the row's
+// numbers are printed by all threads into shared memory (kNumSlot bytes each),
+// in chunks, and placed by a block scan of their lengths
+constexpr int kFmtThreads = 256;
+constexpr int kNumSlot = 26;       // a number (<= 24 bytes) and its comma
+constexpr int kFmtChunk = 1024;    // numbers per shared-memory pass
+__global__ void __launch_bounds__(kFmtThreads) k_fmt_nearest(const int32_t* __restrict__ kind,
+                                                             const uint64_t* __restrict__ index,
+                                                             const double* const* __restrict__ rows,
+                                                             const uint32_t* __restrict__ dims,
+                                                             const char* __restrict__ uuids, size_t slot,
+                                                             char* __restrict__ slots, uint32_t* __restrict__ len) {
+    __shared__ char buf[kFmtChunk * kNumSlot];
+    __shared__ uint32_t pos[kFmtChunk];
+    __shared__ uint8_t lens[kFmtChunk];
+    __shared__ uint32_t wsum[kFmtThreads / 32];
+    __shared__ uint32_t s_at;
+    const int r = blockIdx.x;
+    char* o = slots + (size_t)r * slot;
+    const int kd = kind[r];
+    if (kd <= 0) {
+        if (threadIdx.x == 0)
+            len[r] = (uint32_t)put_lit(o, kd == 0 ? "{\"error\":\"No nearest neighbor found\"}"
+                                                  : "{\"error\":\"Nearest neighbor not found\"}");
+        return;
+    }
+    if (threadIdx.x == 0) {
+        int k = put_lit(o, "{\"index\":");
+        k += cjson_number((double)index[r], o + k);
+        k += put_lit(o + k, ",\"vector\":[");
+        s_at = (uint32_t)k;
+    }
+    __syncthreads();
+    const double* row = rows[r];
+    const int d = (int)dims[r];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int per = kFmtChunk / kFmtThreads;  // numbers per thread and chunk, contiguous
+    for (int c0 = 0; c0 < d; c0 += kFmtChunk) {
+        const int cn = min(kFmtChunk, d - c0);
+        uint32_t tot = 0;
+#pragma unroll
+        for (int u = 0; u < per; ++u) {
+            const int j = threadIdx.x * per + u;
+            if (j < cn) {
+                char* b = buf + j * kNumSlot;
+                int k = 0;
+                if (c0 + j) b[k++] = ',';
+                k += cjson_number(row[c0 + j], b + k);
+                lens[j] = (uint8_t)k;
+                tot += (uint32_t)k;
+            }
+        }
+        // exclusive scan of the threads' totals: each thread's numbers in order
+        uint32_t incl = tot;
+        for (int sh = 1; sh < 32; sh <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, sh);
+            if (lane >= sh) incl += t;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        uint32_t wbase = 0, total = 0;
+        for (int w = 0; w < kFmtThreads / 32; ++w) {
+            if (w < warp) wbase += wsum[w];
+            total += wsum[w];
+        }
+        uint32_t at = s_at + wbase + incl - tot;
+#pragma unroll
+        for (int u = 0; u < per; ++u) {
+            const int j = threadIdx.x * per + u;
+            if (j < cn) {
+                pos[j] = at;
+                at += lens[j];
+            }
+        }
+        __syncthreads();
+        for (int j = warp; j < cn; j += kFmtThreads / 32)  // a number is at most 25 bytes: a warp copies it
+            if (lane < (int)lens[j]) o[pos[j] + lane] = buf[j * kNumSlot + lane];
+        __syncthreads();
+        if (threadIdx.x == 0) s_at += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int k = (int)s_at;
+        k += put_lit(o + k, "],\"uuid\":");
+        k += cjson_string(uuids + (size_t)r * 37, 37, o + k);
+        o[k++] = '}';
+        len[r] = (uint32_t)k;
+    }
+}
+
+// slots -> one packed text at the given offsets
+__global__ void k_fmt_pack(const char* __restrict__ slots, size_t slot, const uint32_t* __restrict__ len,
+                           const uint64_t* __restrict__ off, int n, char* __restrict__ out) {
+    const int r = blockIdx.x;
+    if (r >= n) return;
+    const char* src = slots + (size_t)r * slot;
+    char* dst = out + off[r];
+    for (uint32_t t = threadIdx.x; t < len[r]; t += blockDim.x) dst[t] = src[t];
+}
+
 }  // namespace
 
 // Decode n bodies (host bytes text[off[i] .. off[i+1])) into n x dim doubles.
@@ -1063,6 +1490,141 @@ int decode_bodies(Store* s, const char* text, const uint64_t* off, size_t n, siz
     return SVDB_OK;
 }
 
+// ---- response bodies: host side ---------------------------------------------
+// The power-of-five table of the exact conversion (the formatter's round-trip
+// check uses it), once per process, finished before any formatter runs.
+static int ensure_pow5(cudaStream_t st) {
+    static std::mutex mu;
+    static bool done = false;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done) return SVDB_OK;
+    k_pow5_init<<<(kP5Max - kP5Min + 128) / 128, 128, 0, st>>>();
+    SVDB_LAUNCH_CHECK();
+    SVDB_CUDA(cudaStreamSynchronize(st));
+    done = true;
+    return SVDB_OK;
+}
+
+// lengths -> offsets on the host; then, when `out` has room, the slots packed
+// on the device and copied out as one text
+static int fmt_finish(Store* s, size_t n, const char* d_slots, size_t slot, const uint32_t* d_len, uint64_t* d_off,
+                      char* d_packed, char* out, size_t cap, uint64_t* offsets) {
+    std::vector<uint32_t> hl(n);
+    SVDB_CUDA(cudaMemcpyAsync(hl.data(), d_len, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    offsets[0] = 0;
+    for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + hl[i];
+    const uint64_t total = offsets[n];
+    if (!out) return SVDB_OK;  // sizes only
+    if (total > cap) {
+        svdb_set_error("format: the responses need %llu bytes, the buffer holds %zu", (unsigned long long)total, cap);
+        return SVDB_EINVAL;
+    }
+    SVDB_CUDA(cudaMemcpyAsync(d_off, offsets, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s->stream));
+    k_fmt_pack<<<(unsigned)n, 128, 0, s->stream>>>(d_slots, slot, d_len, d_off, (int)n, d_packed);
+    SVDB_LAUNCH_CHECK();
+    SVDB_CUDA(cudaMemcpyAsync(out, d_packed, total, cudaMemcpyDeviceToHost, s->stream));
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));
+    return SVDB_OK;
+}
+
+int format_compare(Store* s, const int32_t* metric, const float* value, const int32_t* status, size_t n, char* out,
+                   size_t cap, uint64_t* offsets) {
+    if (n == 0) {
+        offsets[0] = 0;
+        return SVDB_OK;
+    }
+    int rc = ensure_pow5(s->stream);
+    if (rc) return rc;
+    const size_t a_in = round_up(n * 12, 256), a_slots = round_up(n * kCmpSlot, 256), a_len = round_up(n * 4, 256),
+                 a_off = round_up((n + 1) * 8, 256);
+    rc = s->scratch_reserve(a_in + 2 * a_slots + a_len + a_off);
+    if (rc) return rc;
+    uint8_t* base = (uint8_t*)s->scratch;
+    int32_t* dm = (int32_t*)base;
+    float* dv = (float*)(dm + n);
+    int32_t* ds = (int32_t*)(dv + n);
+    char* slots = (char*)(base + a_in);
+    uint32_t* dl = (uint32_t*)(base + a_in + a_slots);
+    uint64_t* doff = (uint64_t*)(base + a_in + a_slots + a_len);
+    char* packed = (char*)(base + a_in + a_slots + a_len + a_off);
+    SVDB_CUDA(cudaMemcpyAsync(dm, metric, n * 4, cudaMemcpyHostToDevice, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(dv, value, n * 4, cudaMemcpyHostToDevice, s->stream));
+    SVDB_CUDA(cudaMemcpyAsync(ds, status, n * 4, cudaMemcpyHostToDevice, s->stream));
+    k_fmt_compare<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(dm, dv, ds, (int)n, slots, dl);
+    SVDB_LAUNCH_CHECK();
+    return fmt_finish(s, n, slots, kCmpSlot, dl, doff, packed, out, cap, offsets);
+}
+
+// kind[i]: 1 a row (slot[i] >= 0: the store's row; else host_rows[i]), 0 no
+// neighbour, -1 an index that reads no row; dims[i] the row's dimension
+int format_nearest(Store* s, size_t n, const int32_t* kind, const uint64_t* index, const int64_t* slot,
+                   const uint32_t* dims, const double* const* host_rows, const char* uuids37, char* out, size_t cap,
+                   uint64_t* offsets) {
+    if (n == 0) {
+        offsets[0] = 0;
+        return SVDB_OK;
+    }
+    int rc = s->sync();  // staged rows onto the device
+    if (!rc) rc = ensure_pow5(s->stream);
+    if (rc) return rc;
+    uint32_t dmax = 0;
+    size_t host_doubles = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (kind[i] != 1) continue;
+        dmax = std::max(dmax, dims[i]);
+        if (slot[i] < 0) host_doubles += dims[i];
+    }
+    const size_t slot_bytes = round_up(64 + (size_t)kNumSlot * dmax + 6 * 37 + 64, 16);
+    const size_t a_meta = round_up(n * (4 + 8 + 8 + 4 + 37), 256), a_host = round_up(host_doubles * 8, 256),
+                 a_slots = round_up(n * slot_bytes, 256), a_len = round_up(n * 4, 256),
+                 a_off = round_up((n + 1) * 8, 256);
+    rc = s->scratch_reserve(a_meta + a_host + 2 * a_slots + a_len + a_off);
+    if (rc) return rc;
+    uint8_t* base = (uint8_t*)s->scratch;
+    std::vector<uint8_t> hm(a_meta);
+    int32_t* hk = (int32_t*)hm.data();
+    uint64_t* hi = (uint64_t*)(hk + n);
+    const double** hr = (const double**)(hi + n);
+    uint32_t* hd = (uint32_t*)(hr + n);
+    char* hu = (char*)(hd + n);
+    std::vector<double> hrows(host_doubles);
+    double* dhost = (double*)(base + a_meta);
+    size_t at = 0;
+    for (size_t i = 0; i < n; ++i) {
+        hk[i] = kind[i];
+        hi[i] = index[i];
+        hd[i] = kind[i] == 1 ? dims[i] : 0;
+        hr[i] = nullptr;
+        std::memcpy(hu + i * 37, uuids37 + i * 37, 37);
+        if (kind[i] != 1) continue;
+        if (slot[i] >= 0) {
+            hr[i] = s->x64 + (size_t)slot[i] * s->ld;
+        } else {
+            if (dims[i]) std::memcpy(hrows.data() + at, host_rows[i], dims[i] * sizeof(double));
+            hr[i] = dhost + at;
+            at += dims[i];
+        }
+    }
+    SVDB_CUDA(cudaMemcpyAsync(base, hm.data(), a_meta, cudaMemcpyHostToDevice, s->stream));
+    if (host_doubles)
+        SVDB_CUDA(cudaMemcpyAsync(dhost, hrows.data(), host_doubles * 8, cudaMemcpyHostToDevice, s->stream));
+    const int32_t* dk = (const int32_t*)base;
+    const uint64_t* di = (const uint64_t*)(dk + n);
+    const double* const* drows = (const double* const*)(di + n);
+    const uint32_t* ddim = (const uint32_t*)(drows + n);
+    const char* du = (const char*)(ddim + n);
+    char* slots = (char*)(base + a_meta + a_host);
+    uint32_t* dl = (uint32_t*)(base + a_meta + a_host + a_slots);
+    uint64_t* doff = (uint64_t*)(base + a_meta + a_host + a_slots + a_len);
+    char* packed = (char*)(base + a_meta + a_host + a_slots + a_len + a_off);
+    k_fmt_nearest<<<(unsigned)n, kFmtThreads, 0, s->stream>>>(dk, di, drows, ddim, du, slot_bytes, slots, dl);
+    SVDB_LAUNCH_CHECK();
+    rc = fmt_finish(s, n, slots, slot_bytes, dl, doff, packed, out, cap, offsets);
+    SVDB_CUDA(cudaStreamSynchronize(s->stream));  // the host staging above is freed on return
+    return rc;
+}
+
 }  // namespace svdb
 
 // One decode context per process (stream, scratch, staging), shared by the
@@ -1085,4 +1647,39 @@ extern "C" int svdbd_decode_bodies(const char* text, const uint64_t* off, size_t
     }
     int rc = g_dec->ensure();
     return rc ? rc : svdb::decode_bodies(g_dec, text, off, n, dim, out, status);
+}
+
+extern "C" int svdbd_format_compare(const int32_t* metric, const float* value, const int32_t* status, size_t n,
+                                    char* out, size_t cap, uint64_t* offsets) {
+    std::lock_guard<std::mutex> lk(g_dec_mu);
+    if (!g_dec) {
+        g_dec = new (std::nothrow) svdb::Store();
+        if (!g_dec) {
+            svdb_set_error("format: out of host memory");
+            return SVDB_ENOMEM;
+        }
+        g_dec->dim = g_dec->ld = g_dec->ldb = 1;
+    }
+    int rc = g_dec->ensure();
+    return rc ? rc : svdb::format_compare(g_dec, metric, value, status, n, out, cap, offsets);
+}
+
+extern "C" int svdbd_format_nearest(svdbd_store* hs, size_t n, const int32_t* kind, const uint64_t* index,
+                                    const int64_t* slot, const uint32_t* dims, const double* const* host_rows,
+                                    const char* uuids37, char* out, size_t cap, uint64_t* offsets) {
+    if (hs) {
+        return svdb::format_nearest(reinterpret_cast<svdb::Store*>(hs), n, kind, index, slot, dims, host_rows,
+                                    uuids37, out, cap, offsets);
+    }
+    std::lock_guard<std::mutex> lk(g_dec_mu);  // a store with no device rows: the decode context
+    if (!g_dec) {
+        g_dec = new (std::nothrow) svdb::Store();
+        if (!g_dec) {
+            svdb_set_error("format: out of host memory");
+            return SVDB_ENOMEM;
+        }
+        g_dec->dim = g_dec->ld = g_dec->ldb = 1;
+    }
+    int rc = g_dec->ensure();
+    return rc ? rc : svdb::format_nearest(g_dec, n, kind, index, slot, dims, host_rows, uuids37, out, cap, offsets);
 }

@@ -686,6 +686,25 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // of chunk c), loaded before the wait so their latency is hidden
             uint32_t vbl = 0;
             if (NORM && !DUMP && lane < kBN / 2 / 32) vbl = __ldg(P.vbits + ((r * kBN + col0) >> 5) + lane);
+            // Threshold refresh from the shared bins and tau (tiles 1..7 of a
+            // segment, then every 8th): read BEFORE the accumulator wait, so the
+            // loads' latency overlaps it instead of stalling the epilogue.  Bins
+            // and tau only grow (atomicMax of valid lower bounds), so a value
+            // read earlier is an older, smaller -- still valid -- threshold.
+            // (Tile 0 reads them after its warm-up, below.)
+            const bool refresh = !DUMP && valid && js > 0 && (js < 8 || (js & 7) == 0);
+            int bmin_pre = 0x7fffffff, tau_pre = 0;
+            if (refresh) {
+                const int* bq = P.bins + (size_t)q * P.k;
+                tau_pre = __ldcg(P.tau + q);
+                for (int t0 = 0; t0 < P.k; t0 += 16) {  // 16 independent loads per round trip
+                    int v16[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) v16[u] = t0 + u < P.k ? __ldcg(bq + t0 + u) : 0x7fffffff;
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) bmin_pre = min(bmin_pre, v16[u]);
+                }
+            }
             // tcgen05.ld is warp-collective (.sync.aligned): every branch that
             // leads to one must be taken by the whole warp, including this wait
             bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
@@ -762,10 +781,12 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                                   f2ord(maxl));
                 }
             }
-            if (valid && (js < 8 || (js & 7) == 0)) {
-                // The k bins hold lower bounds of k distinct rows (chunks of different
-                // bins are different rows), so their minimum is a valid threshold; it
-                // reflects what every CTA has seen of this query, not only this one.
+            // The k bins hold lower bounds of k distinct rows (chunks of different
+            // bins are different rows), so their minimum is a valid threshold; it
+            // reflects what every CTA has seen of this query, not only this one.
+            if (refresh) {
+                tau_c = fmaxf(tau_c, fmaxf(ord2f(tau_pre), ord2f(bmin_pre)));
+            } else if (valid && js == 0) {  // after the warm-up's own contributions
                 const int* bq = P.bins + (size_t)q * P.k;
                 int bmin = 0x7fffffff;
                 for (int t = 0; t < P.k; ++t) bmin = min(bmin, __ldcg(bq + t));
@@ -1932,15 +1953,21 @@ static int make_map8(GemmPlanCache* c, CUtensorMap* m, const void* base, size_t 
     return SVDB_OK;
 }
 
-// The paired screen (cta_group::2) for batches of more than one 128-query
-// tile; SVDB_SCREEN_PAIR=0 in the environment keeps the single-CTA form
-// (for comparisons).  Pairs that can run at once: every two SMs, as far as
-// the cluster scheduler places them (asked once per process).
+// The paired screen (cta_group::2) is opt-in: SVDB_SCREEN_PAIR=1 in the
+// environment (read once per process) uses it for batches of more than one
+// 128-query tile.  It cuts the L2 -> shared-memory operand traffic by a third
+// and, with an epilogue that does nothing, runs 5 % faster than the
+// single-CTA form (1M x 768, Q = 4096: 3.54 against 3.73 ms), but with the
+// real epilogue both CTAs of a pair must drain an accumulator before the MMAs
+// reuse it, and it measured no faster for BF16 cosine (4.03 against 4.06 ms)
+// and slower for FP8 (3.55 against 3.22 ms) and Euclidean (4.71 against
+// 4.60 ms).  Pairs that can run at once: every two SMs, as far as the
+// cluster scheduler places them (asked once per process).
 static bool pair_enabled() {
     static int on = -1;
     if (on < 0) {
         const char* e = getenv("SVDB_SCREEN_PAIR");
-        on = (e && e[0] == '0') ? 0 : 1;
+        on = (e && e[0] == '1') ? 1 : 0;
     }
     return on == 1;
 }

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "dev_common.cuh"
+#include "dev_ref.cuh"
 
 namespace svdb {
 
@@ -41,15 +42,6 @@ __global__ void k_kd_patch(int2* child, const int4* patches, int n) {
     }
 }
 
-__device__ __forceinline__ double kd_sqdist(const double* __restrict__ p, const double* __restrict__ q, int kdim) {
-    double d = 0.0;
-    for (int i = 0; i < kdim; ++i) {
-        const double t = __dsub_rn(p[i], q[i]);
-        d = __dadd_rn(d, __dmul_rn(t, t));
-    }
-    return d;
-}
-
 // MAXH > 0: stack in registers/local memory; MAXH == 0: stack in `gstack`
 // (height entries per query).
 template <int MAXH>
@@ -60,47 +52,9 @@ __global__ void __launch_bounds__(128) k_kd_nearest(const double* __restrict__ p
                                                     int height) {
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= nq) return;
-    const double* qq = q + (size_t)qi * qs;
     int2 lstack[MAXH > 0 ? MAXH : 1];
     int2* stack = MAXH > 0 ? lstack : gstack + (size_t)qi * height;
-    double best = __longlong_as_double(0x7ff0000000000000ll);
-    int bestn = -1;
-    int sp = 0;
-    int cur = n > 0 ? 0 : -1;
-    int depth = 0;
-    for (;;) {
-        while (cur >= 0) {
-            const double* p = pts + (size_t)cur * kdim;
-            const double d = kd_sqdist(p, qq, kdim);
-            if (d < best) {
-                best = d;
-                bestn = cur;
-            }
-            const int cd = depth % kdim;
-            const int2 ch = child[cur];
-            stack[sp++] = make_int2(cur, depth);
-            cur = qq[cd] < p[cd] ? ch.x : ch.y;
-            ++depth;
-        }
-        bool more = false;
-        while (sp > 0) {
-            const int2 e = stack[--sp];
-            const int cd = e.y % kdim;
-            const double pc = pts[(size_t)e.x * kdim + cd], qc = qq[cd];
-            const double t = __dsub_rn(qc, pc);
-            if (__dmul_rn(t, t) < best) {
-                const int2 ch = child[e.x];
-                cur = qc < pc ? ch.y : ch.x;
-                depth = e.y + 1;
-                if (cur >= 0) {
-                    more = true;
-                    break;
-                }
-            }
-        }
-        if (!more) break;
-    }
-    out[qi] = bestn >= 0 ? index[bestn] : -1;
+    out[qi] = kd_descend(pts, index, child, kdim, n, q + (size_t)qi * qs, stack);
 }
 
 static int kd_reserve_dev(Kd* t, size_t need) {

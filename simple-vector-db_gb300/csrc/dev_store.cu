@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "dev_common.cuh"
+#include "dev_ref.cuh"
 #include "dev_store.cuh"
 
 #include <cuda_fp8.h>
@@ -315,31 +316,6 @@ __global__ void k_count_unscreenable(const float4* __restrict__ rowp, const floa
 __global__ void k_set_live(uint8_t* live, const int64_t* slots, int n, uint8_t v) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) live[slots[i]] = v;
-}
-
-// Reference-exact metrics: the float-accumulating loops of
-// src/vector_database.c:301-352, one thread per pair, IEEE intrinsics so
-// nothing is contracted into an FMA.
-__device__ float ref_metric(int metric, const double* __restrict__ a, const double* __restrict__ b, int d) {
-    if (metric == SVDB_EUCLIDEAN) {
-        float sum = 0.0f;
-        for (int i = 0; i < d; ++i) {
-            const float diff = __double2float_rn(__dsub_rn(a[i], b[i]));
-            sum = __fadd_rn(sum, __fmul_rn(diff, diff));
-        }
-        return __double2float_rn(__dsqrt_rn((double)sum));
-    }
-    float dot = 0.0f, na = 0.0f, nb = 0.0f;
-    for (int i = 0; i < d; ++i) {
-        const double ai = a[i], bi = b[i];
-        dot = __double2float_rn(__dadd_rn((double)dot, __dmul_rn(ai, bi)));
-        if (metric == SVDB_COSINE) {
-            na = __double2float_rn(__dadd_rn((double)na, __dmul_rn(ai, ai)));
-            nb = __double2float_rn(__dadd_rn((double)nb, __dmul_rn(bi, bi)));
-        }
-    }
-    if (metric == SVDB_DOT) return dot;
-    return __double2float_rn(__ddiv_rn((double)dot, __dmul_rn(__dsqrt_rn((double)na), __dsqrt_rn((double)nb))));
 }
 
 // metrics: per pair (the drop-in calls combined into one launch), or NULL for `metric`

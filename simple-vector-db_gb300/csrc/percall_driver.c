@@ -171,3 +171,90 @@ PC_API int svdb_percall_nearest(void* fn, void* tree, const double* q, size_t nq
     p.near_out = out;
     return run_all(&p, threads, wall_ns);
 }
+
+/* ---- open-loop replay through a request loop (svdb_loop_submit / _wait) ---
+ * One thread submits request i at t0 + arrival_s[i] (spinning on the clock),
+ * another takes the answers in ticket order and stamps each one: lat_ns[i] =
+ * completion - (t0 + arrival_s[i]), queueing included. */
+typedef int (*loop_submit_fn)(void*, const void*, uint64_t*);
+typedef int (*loop_wait_fn)(void*, uint64_t, void*, uint32_t);
+
+typedef struct {
+    void* submit;
+    void* wait;
+    void* loop;
+    const char* reqs;
+    size_t req_size;
+    const double* arrival;
+    size_t n;
+    double* lat;
+    char* resps;
+    size_t resp_size;
+    uint64_t* tickets;
+    volatile size_t published;
+    double t0;
+    int rc;
+} replay;
+
+static void* replay_submit(void* arg) {
+    replay* r = (replay*)arg;
+    for (size_t i = 0; i < r->n; ++i) {
+        const double due = r->t0 + r->arrival[i] * 1e9;
+        while (now_ns() < due) {
+        }
+        uint64_t t = 0;
+        if (((loop_submit_fn)r->submit)(r->loop, r->reqs + i * r->req_size, &t) != 0) {
+            r->rc = -1;
+            __atomic_store_n(&r->published, r->n + 1, __ATOMIC_RELEASE);
+            return NULL;
+        }
+        r->tickets[i] = t;
+        __atomic_store_n(&r->published, i + 1, __ATOMIC_RELEASE);
+    }
+    return NULL;
+}
+
+PC_API int svdb_percall_loop_replay(void* submit, void* wait, void* loop, const void* reqs, size_t req_size,
+                                    const double* arrival_s, size_t n, double* lat_ns, void* resps, size_t resp_size,
+                                    double* wall_ns) {
+    if (!submit || !wait || !loop || !reqs || !arrival_s || !lat_ns || !resps || !wall_ns) return -1;
+    replay r;
+    memset(&r, 0, sizeof(r));
+    r.submit = submit;
+    r.wait = wait;
+    r.loop = loop;
+    r.reqs = (const char*)reqs;
+    r.req_size = req_size;
+    r.arrival = arrival_s;
+    r.n = n;
+    r.lat = lat_ns;
+    r.resps = (char*)resps;
+    r.resp_size = resp_size;
+    r.tickets = (uint64_t*)malloc((n ? n : 1) * sizeof(uint64_t));
+    if (!r.tickets) return -1;
+    r.t0 = now_ns() + 2e6;  /* 2 ms to get going */
+    pthread_t th;
+    if (pthread_create(&th, NULL, replay_submit, &r) != 0) {
+        free(r.tickets);
+        return -1;
+    }
+    int rc = 0;
+    for (size_t i = 0; i < n; ++i) {
+        size_t p;
+        while ((p = __atomic_load_n(&r.published, __ATOMIC_ACQUIRE)) <= i) {
+        }
+        if (p > n) {
+            rc = -1;
+            break;
+        }
+        if (((loop_wait_fn)wait)(loop, r.tickets[i], r.resps + i * resp_size, 30000000u) != 0) {
+            rc = -1;
+            break;
+        }
+        lat_ns[i] = now_ns() - (r.t0 + arrival_s[i] * 1e9);
+    }
+    pthread_join(th, NULL);
+    *wall_ns = now_ns() - r.t0;
+    free(r.tickets);
+    return rc ? rc : r.rc;
+}

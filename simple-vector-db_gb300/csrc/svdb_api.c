@@ -671,6 +671,162 @@ SVDB_API int svdb_debug_screen_accumulators(VectorDatabase* db, const double* qu
     return rc;
 }
 
+/* ---- the request path as a device-side loop (dev_loop.cu) ----------------- */
+struct svdb_loop {
+    svdbd_loop* dev;
+    size_t dim;
+};
+
+SVDB_API svdb_loop* svdb_loop_create(const svdb_loop_config* cfg, const double* rows, size_t n,
+                                     const char* uuids37) {
+    if (!cfg || cfg->dim == 0 || cfg->kd_dim == 0 || cfg->kd_dim > 32 || cfg->kd_dim > cfg->dim ||
+        cfg->capacity < n || cfg->capacity >= (size_t)1 << 31 || (n && !rows)) {
+        svdb_set_error("svdb_loop_create: bad configuration (dim >= kd_dim in 1..32, capacity >= rows, < 2^31)");
+        return NULL;
+    }
+    svdb_loop_config c = *cfg;
+    if (!c.kd_capacity) c.kd_capacity = 2 * c.capacity;
+    if (!c.ring) c.ring = 4096;
+    if (!c.max_batch || c.max_batch > 256) c.max_batch = 256;
+    if (!c.idle_us) c.idle_us = 1000000;
+    if (c.kd_capacity < n || c.kd_capacity >= (size_t)1 << 31) {
+        svdb_set_error("svdb_loop_create: kd_capacity must hold the initial rows' nodes (< 2^31)");
+        return NULL;
+    }
+    /* the initial KD tree, built in row order exactly as n inserts would build it */
+    KDTree* t = kdtree_create(c.kd_dim);
+    if (!t) {
+        svdb_set_error("svdb_loop_create: out of host memory");
+        return NULL;
+    }
+    for (size_t i = 0; i < n; ++i) svdb_kd_insert_prefix(t, rows + i * c.dim, c.dim, i);
+    svdb_kd* k = svdb_kd_of(t);
+    if (k->n != n) {
+        kdtree_free(t);
+        svdb_set_error("svdb_loop_create: out of host memory building the KD tree");
+        return NULL;
+    }
+    svdb_loop* l = (svdb_loop*)calloc(1, sizeof(svdb_loop));
+    if (l) {
+        l->dim = c.dim;
+        l->dev = svdbd_loop_create(&c, rows, n, uuids37, k->pts, k->index, k->left, k->right, k->n, k->height);
+        if (!l->dev) {
+            free(l);
+            l = NULL;
+        }
+    } else {
+        svdb_set_error("svdb_loop_create: out of host memory");
+    }
+    kdtree_free(t);
+    return l;
+}
+
+SVDB_API int svdb_loop_start(svdb_loop* l) {
+    if (!l) return SVDB_EINVAL;
+    return svdbd_loop_start(l->dev);
+}
+
+SVDB_API int svdb_loop_submit(svdb_loop* l, const svdb_request* req, uint64_t* ticket) {
+    if (!l || !req || !ticket) {
+        svdb_set_error("svdb_loop_submit: NULL argument");
+        return SVDB_EINVAL;
+    }
+    if ((req->op == SVDB_REQ_INSERT || req->op == SVDB_REQ_UPDATE || req->op == SVDB_REQ_KD_NEAREST) && !req->vec) {
+        svdb_set_error("svdb_loop_submit: request %d needs a vector", req->op);
+        return SVDB_EINVAL;
+    }
+    return svdbd_loop_submit(l->dev, req, l->dim, ticket, 10000000u);
+}
+
+SVDB_API int svdb_loop_wait(svdb_loop* l, uint64_t ticket, svdb_response* resp, uint32_t timeout_us) {
+    if (!l || !resp) return SVDB_EINVAL;
+    return svdbd_loop_wait(l->dev, ticket, resp, timeout_us);
+}
+
+SVDB_API int svdb_loop_stop(svdb_loop* l) { return l ? svdbd_loop_stop(l->dev) : SVDB_EINVAL; }
+
+SVDB_API int svdb_loop_get_info(svdb_loop* l, svdb_loop_info* out) {
+    return (l && out) ? svdbd_loop_info(l->dev, out) : SVDB_EINVAL;
+}
+
+SVDB_API int svdb_loop_read(svdb_loop* l, size_t position, double* row, char* uuid37) {
+    return (l && row) ? svdbd_loop_read(l->dev, position, row, uuid37) : SVDB_EINVAL;
+}
+
+SVDB_API void svdb_loop_destroy(svdb_loop* l) {
+    if (!l) return;
+    svdbd_loop_destroy(l->dev);
+    free(l);
+}
+
+/* See include/svdb_gb300.h: response bodies of GET /compare. */
+SVDB_API int svdb_format_compare(const int32_t* metric, const float* value, const int32_t* status, size_t n,
+                                 char* out, size_t cap, uint64_t* offsets) {
+    if (!offsets || (n && (!metric || !value || !status))) {
+        svdb_set_error("svdb_format_compare: NULL argument");
+        return SVDB_EINVAL;
+    }
+    for (size_t i = 0; i < n; ++i)
+        if (status[i] == SVDB_CMP_OK && (metric[i] < 0 || metric[i] > 2)) {
+            svdb_set_error("svdb_format_compare: metric %d of answer %zu is not 0..2", metric[i], i);
+            return SVDB_EINVAL;
+        }
+    return svdbd_format_compare(metric, value, status, n, out, cap, offsets);
+}
+
+/* See include/svdb_gb300.h: response bodies of POST /nearest. */
+SVDB_API int svdb_format_nearest(VectorDatabase* db, const int64_t* index, size_t n, char* out, size_t cap,
+                                 uint64_t* offsets) {
+    if (!db || !offsets || (n && !index)) {
+        svdb_set_error("svdb_format_nearest: NULL argument");
+        return SVDB_EINVAL;
+    }
+    svdb_db* d = svdb_of(db);
+    const size_t m = n ? n : 1;
+    int32_t* kind = (int32_t*)malloc(m * sizeof(int32_t));
+    uint64_t* idx = (uint64_t*)malloc(m * sizeof(uint64_t));
+    int64_t* slot = (int64_t*)malloc(m * sizeof(int64_t));
+    uint32_t* dims = (uint32_t*)malloc(m * sizeof(uint32_t));
+    const double** rows = (const double**)malloc(m * sizeof(double*));
+    char* uu = (char*)calloc(m, UUID_SIZE);
+    int rc = SVDB_OK;
+    if (!kind || !idx || !slot || !dims || !rows || !uu) {
+        svdb_set_error("svdb_format_nearest: out of host memory");
+        rc = SVDB_ENOMEM;
+        goto out_free;
+    }
+    pthread_mutex_lock(&db->mutex);
+    for (size_t i = 0; i < n; ++i) {
+        idx[i] = (uint64_t)index[i];
+        slot[i] = -1;
+        dims[i] = 0;
+        rows[i] = NULL;
+        if (index[i] < 0) { /* kdtree_nearest gave (size_t)-1 (src/compare_handler.c:422) */
+            kind[i] = 0;
+        } else if ((size_t)index[i] >= db->size) { /* a stale KD node: vector_db_read is NULL (:419) */
+            kind[i] = -1;
+        } else {
+            const Vector* v = &db->vectors[index[i]];
+            kind[i] = 1;
+            dims[i] = (uint32_t)v->dimension;
+            rows[i] = v->data;
+            memcpy(uu + i * UUID_SIZE, v->uuid, UUID_SIZE);
+            if (d->dev && v->data && v->dimension == d->dim && d->slot_of[index[i]] >= 0)
+                slot[i] = d->slot_of[index[i]];
+        }
+    }
+    rc = svdbd_format_nearest(d->dev, n, kind, idx, slot, dims, rows, uu, out, cap, offsets);
+    pthread_mutex_unlock(&db->mutex);
+out_free:
+    free(kind);
+    free(idx);
+    free(slot);
+    free(dims);
+    free(rows);
+    free(uu);
+    return rc;
+}
+
 /* ---- merge of per-shard top-k lists (host) ------------------------------ */
 typedef struct {
     double key;

@@ -109,6 +109,31 @@ int svdbd_kdm_nearest(svdbd_store* s, size_t kdim, const double* q, size_t nq, s
  * text[off[i] .. off[i+1]) -> n x dim doubles and a SVDB_DEC_* status each */
 int svdbd_decode_bodies(const char* text, const uint64_t* off, size_t n, size_t dim, double* out, int32_t* status);
 
+/* response bodies printed on the device as cJSON_PrintUnformatted writes them
+ * (dev_decode.cu): n texts packed into out (cap bytes) at offsets[0..n];
+ * out == NULL fills only the offsets.  /nearest: kind 1 a row (slot >= 0 in
+ * the store, else host_rows[i]; dims[i] numbers), 0 no neighbour, -1 an index
+ * that reads no row; hs NULL when the store has no device rows. */
+int svdbd_format_compare(const int32_t* metric, const float* value, const int32_t* status, size_t n, char* out,
+                         size_t cap, uint64_t* offsets);
+int svdbd_format_nearest(svdbd_store* hs, size_t n, const int32_t* kind, const uint64_t* index, const int64_t* slot,
+                         const uint32_t* dims, const double* const* host_rows, const char* uuids37, char* out,
+                         size_t cap, uint64_t* offsets);
+
+/* the device-side request loop (dev_loop.cu); the initial KD tree comes
+ * built (flat arrays, knodes nodes, height = nodes on the longest path) */
+typedef struct svdbd_loop svdbd_loop;
+svdbd_loop* svdbd_loop_create(const svdb_loop_config* cfg, const double* rows, size_t n, const char* uuids37,
+                              const double* kpts, const int64_t* kidx, const int32_t* kleft, const int32_t* kright,
+                              size_t knodes, int kheight);
+int svdbd_loop_start(svdbd_loop* l);
+int svdbd_loop_submit(svdbd_loop* l, const svdb_request* req, size_t dim, uint64_t* ticket, uint32_t timeout_us);
+int svdbd_loop_wait(svdbd_loop* l, uint64_t ticket, svdb_response* out, uint32_t timeout_us);
+int svdbd_loop_stop(svdbd_loop* l);
+int svdbd_loop_info(svdbd_loop* l, svdb_loop_info* out);
+int svdbd_loop_read(svdbd_loop* l, size_t position, double* row, char* uuid37);
+void svdbd_loop_destroy(svdbd_loop* l);
+
 /* ragged batch over several stores, replayed as one CUDA graph (dev_ragged.cu) */
 typedef struct svdbd_ragged svdbd_ragged;
 typedef struct svdbd_ragged_part {

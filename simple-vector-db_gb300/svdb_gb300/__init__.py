@@ -67,6 +67,21 @@ class RaggedInfo(C.Structure):
                 ("swap_ms", C.c_float * 8)]
 
 
+class LoopConfig(C.Structure):
+    """svdb_loop_config (include/svdb_gb300.h)."""
+    _fields_ = [("dim", C.c_size_t), ("kd_dim", C.c_size_t), ("capacity", C.c_size_t), ("kd_capacity", C.c_size_t),
+                ("ring", C.c_size_t), ("max_batch", C.c_uint32), ("idle_us", C.c_uint32)]
+
+
+class LoopInfo(C.Structure):
+    """svdb_loop_info (include/svdb_gb300.h)."""
+    _fields_ = [("state", C.c_uint32), ("reserved", C.c_uint32), ("size", C.c_uint64), ("answered", C.c_uint64),
+                ("batches", C.c_uint64), ("idle_exits", C.c_uint64)]
+
+
+LOOP_NOT_STARTED, LOOP_RUNNING, LOOP_LEFT_IDLE, LOOP_STOPPED, LOOP_LEAVING = range(5)
+REQ_KD_NEAREST = 5
+
 RAGGED_AUTOTUNE, RAGGED_NO_GRAPH = 1, 2
 SAVE_EXACT_COUNT = 1
 
@@ -113,6 +128,17 @@ def _load():
         "svdb_profile": (C.c_int, [vp, C.c_int]),
         "svdb_selftest_bounded_wait": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_uint32)]),
         "svdb_save": (C.c_int, [vp, C.c_char_p, C.c_uint]),
+        "svdb_format_compare": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32), sz,
+                                          vp, sz, C.POINTER(C.c_uint64)]),
+        "svdb_format_nearest": (C.c_int, [vp, _i64p, sz, vp, sz, C.POINTER(C.c_uint64)]),
+        "svdb_loop_create": (vp, [C.POINTER(LoopConfig), _dp, sz, C.c_char_p]),
+        "svdb_loop_start": (C.c_int, [vp]),
+        "svdb_loop_submit": (C.c_int, [vp, vp, C.POINTER(C.c_uint64)]),
+        "svdb_loop_wait": (C.c_int, [vp, C.c_uint64, vp, C.c_uint32]),
+        "svdb_loop_stop": (C.c_int, [vp]),
+        "svdb_loop_get_info": (C.c_int, [vp, C.POINTER(LoopInfo)]),
+        "svdb_loop_read": (C.c_int, [vp, sz, _dp, C.c_char_p]),
+        "svdb_loop_destroy": (None, [vp]),
         "svdb_debug_screen_accumulators": (C.c_int, [vp, _dp, sz, sz, C.c_int, C.c_int, sz,
                                                      C.POINTER(C.c_float), vp, vp, C.POINTER(C.c_size_t)]),
         "svdb_server_create": (vp, [sz, sz]),
@@ -222,6 +248,26 @@ def euclidean_distance(a, b) -> np.float32:
 
 def dot_product(a, b) -> np.float32:
     return np.float32(lib.dot_product(make_vector(a, owned=False), make_vector(b, owned=False)))
+
+
+def _format(call, n):
+    off = np.zeros(n + 1, np.uint64)
+    _check(call(None, 0, off), "svdb_format")
+    buf = C.create_string_buffer(max(int(off[-1]), 1))
+    _check(call(buf, len(buf), off), "svdb_format")
+    raw = buf.raw
+    return [raw[int(off[i]):int(off[i + 1])] for i in range(n)]
+
+
+def format_compare(metric, value, status=None) -> list:
+    """svdb_format_compare: GET /compare response bodies (bytes each)."""
+    m = np.ascontiguousarray(metric, np.int32)
+    v = np.ascontiguousarray(value, np.float32)
+    s = np.zeros(m.size, np.int32) if status is None else np.ascontiguousarray(status, np.int32)
+    u64 = C.POINTER(C.c_uint64)
+    return _format(lambda out, cap, off: lib.svdb_format_compare(
+        m.ctypes.data_as(C.POINTER(C.c_int32)), v.ctypes.data_as(C.POINTER(C.c_float)),
+        s.ctypes.data_as(C.POINTER(C.c_int32)), m.size, out, cap, off.ctypes.data_as(u64)), m.size)
 
 
 class VectorDatabase:
@@ -416,6 +462,14 @@ class VectorDatabase:
         _check(lib.svdb_search_topk_fp64_noalloc(self.ptr, q_ptr, nq, dim, k, metric, ids_ptr, dists_ptr),
                "svdb_search_topk_fp64_noalloc")
 
+    def format_nearest(self, index) -> list:
+        """svdb_format_nearest: POST /nearest response bodies (bytes each) for
+        the indices kdtree_nearest returned (-1 for none)."""
+        ix = np.ascontiguousarray(index, np.int64)
+        u64 = C.POINTER(C.c_uint64)
+        return _format(lambda out, cap, off: lib.svdb_format_nearest(
+            self.ptr, ix.ctypes.data_as(_i64p), ix.size, out, cap, off.ctypes.data_as(u64)), ix.size)
+
     def selftest_bounded_wait(self, limit_us: int = 20000):
         """(status, gave_up bits, message) of svdb_selftest_bounded_wait; a
         working failure path gives (ETIMEOUT, 3, ...)."""
@@ -531,6 +585,65 @@ class KDTree:
     def close(self):
         if self.ptr:
             lib.kdtree_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceLoop:
+    """svdb_loop_*: the request path as a device-side loop over its own store
+    (rows x dim initial rows, KD prefix kd_dim).  submit() takes a request
+    record (serve.REQ_DTYPE layout) and returns a ticket; wait() its answer
+    (status, value, index)."""
+
+    def __init__(self, dim: int, kd_dim: int, capacity: int, rows=None, uuids=None, ring: int = 4096,
+                 max_batch: int = 256, idle_us: int = 1_000_000, kd_capacity: int = 0):
+        cfg = LoopConfig(dim, kd_dim, capacity, kd_capacity, ring, max_batch, idle_us)
+        r = np.zeros((0, dim)) if rows is None else _f64(rows).reshape(-1, dim)
+        self._rows = r
+        keys = uuid_block(uuids) if uuids is not None else None
+        self.ptr = lib.svdb_loop_create(C.byref(cfg), r.ctypes.data_as(_dp), r.shape[0], keys)
+        if not self.ptr:
+            raise SvdbError(f"svdb_loop_create failed: {last_error()}")
+        self.dim = dim
+
+    def start(self) -> None:
+        _check(lib.svdb_loop_start(self.ptr), "svdb_loop_start")
+
+    def submit(self, req) -> int:
+        """req: one record of serve.REQ_DTYPE (a numpy void or 1-element array)."""
+        t = C.c_uint64(0)
+        _check(lib.svdb_loop_submit(self.ptr, req.ctypes.data if hasattr(req, "ctypes") else req, C.byref(t)),
+               "svdb_loop_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_us: int = 10_000_000):
+        out = np.zeros(1, np.dtype([("status", "<i4"), ("value", "<f4"), ("index", "<u8")]))
+        _check(lib.svdb_loop_wait(self.ptr, ticket, out.ctypes.data, timeout_us), "svdb_loop_wait")
+        return int(out["status"][0]), np.float32(out["value"][0]), int(out["index"][0])
+
+    def stop(self) -> None:
+        _check(lib.svdb_loop_stop(self.ptr), "svdb_loop_stop")
+
+    def info(self) -> dict:
+        i = LoopInfo()
+        _check(lib.svdb_loop_get_info(self.ptr, C.byref(i)), "svdb_loop_get_info")
+        return {"state": i.state, "size": i.size, "answered": i.answered, "batches": i.batches,
+                "idle_exits": i.idle_exits}
+
+    def read(self, position: int):
+        row = np.empty(self.dim, np.float64)
+        u = C.create_string_buffer(38)
+        _check(lib.svdb_loop_read(self.ptr, position, row.ctypes.data_as(_dp), u), "svdb_loop_read")
+        return row, u.raw[:37].split(b"\0")[0]
+
+    def close(self) -> None:
+        if getattr(self, "ptr", None):
+            lib.svdb_loop_destroy(self.ptr)
             self.ptr = None
 
     def __del__(self):

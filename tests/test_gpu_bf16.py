@@ -325,3 +325,39 @@ def test_bf16_streamed_few_queries(S, oracle, d):
     assert ((vals == wval) | (np.isnan(vals) & np.isnan(wval))).all()
     assert st.widened == 1 and st.bound_failures == 0
     db.close()
+
+
+def test_paired_screen_matches_oracle_in_its_own_process(S):
+    """The paired (cta_group::2) screen is opt-in (SVDB_SCREEN_PAIR=1, read
+    once per process), so it runs in a child process: BF16 and FP8, cosine and
+    Euclidean, batches of 300 and 1024 queries (several pair tiles) on a
+    near-tie mixture, against the oracle."""
+    import os
+    import subprocess
+    import sys
+    code = r'''
+import sys, numpy as np
+sys.path[:0] = sys.argv[1:]
+import oracle as O, svdb_gb300 as S
+o = O.Oracle()
+rng = np.random.default_rng(61)
+C = rng.normal(size=(40, 256))
+X = C[rng.integers(0, 40, 60000)] + 0.05 * rng.normal(size=(60000, 256))
+db = S.VectorDatabase(0, 3)
+db.insert_batch(X)
+for nq in (300, 1024):
+    Q = C[rng.integers(0, 40, nq)] + 0.05 * rng.normal(size=(nq, 256))
+    for metric in (0, 1):
+        wi, wv = o.topk(metric, X, Q, 10)
+        for prec in (S.PREC_BF16, S.PREC_FP8):
+            st = S.SearchStats()
+            ids, vals = db.search(Q, 10, metric, prec, stats=st)
+            assert np.array_equal(ids, wi) and np.array_equal(vals, wv), (nq, metric, prec)
+            assert st.bound_failures == 0 and st.widened < nq
+print("paired ok")
+'''
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    paths = [os.path.join(root, "oracle"), os.path.join(root, "simple-vector-db_gb300")]
+    env = dict(os.environ, SVDB_SCREEN_PAIR="1")
+    r = subprocess.run([sys.executable, "-c", code, *paths], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "paired ok" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
