@@ -615,6 +615,12 @@ def run_ragged(args, ws, rank, local):
                      "autotune_ms_per_run": {"(grouping 0, concurrent 1)": info["tuned_ms"][0],
                                              "(1, 1)": info["tuned_ms"][1], "(0, 0)": info["tuned_ms"][2],
                                              "(1, 0)": info["tuned_ms"][3]},
+                     "autotune_ms_fused_screen": {"grouping 0": info["fused_ms"][0],
+                                                  "grouping 1": info["fused_ms"][1]},
+                     "fused_screen": info["fused"], "fused_launches_per_run": info["fused_launches"],
+                     "fused_epilogue_weight": info["epi_weight"],
+                     "autotune_ms_fused_epilogue_weight_1_4_8": info["weight_ms"],
+                     "seeded_thresholds": info["seeded"], "autotune_ms_seeded": info["seed_ms"],
                      "autotune_ms_with_store_screen_swapped": info["swap_ms"][:5],
                      "autotune_s": tune_s, "captures": info["captures"]},
             "clocks": clocks}

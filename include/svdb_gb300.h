@@ -207,6 +207,9 @@ typedef struct svdb_ragged_part {
 #define SVDB_RAGGED_AUTOTUNE 1u /* time the execution choices on these inputs, keep the fastest (cosine plans:
                                    also each store's BF16 versus FP8 screen; the results are the same) */
 #define SVDB_RAGGED_NO_GRAPH 2u /* enqueue the kernels directly at each run (no graph) */
+#define SVDB_RAGGED_FUSED 4u    /* without AUTOTUNE: screen the BF16 searches with one fused launch per k class */
+#define SVDB_RAGGED_BY_K_CLASS 8u /* without AUTOTUNE: one search per k class (else one per part) */
+#define SVDB_RAGGED_SEED 16u    /* start every tensor-core screen's thresholds from a 1/16 sample of the store */
 
 typedef struct svdb_ragged_info {
     int32_t grouping;   /* 0: one search per part with its largest k; 1: one per k class (<=16, <=32, <=128) */
@@ -218,6 +221,13 @@ typedef struct svdb_ragged_info {
     uint32_t fp8_stores; /* bit i: the plan's i-th distinct store (first-use order) runs the FP8 screen */
     float swap_ms[8];    /* cosine plans with a tensor-core precision: autotuner's ms per run with store i's
                             screen swapped BF16 <-> FP8 (kept when faster); 0: not tried */
+    int32_t fused;          /* 1: the BF16 searches' screens run as fused launches (one per k class) */
+    int32_t fused_launches; /* fused screen launches per run */
+    float fused_ms[2];      /* autotuner's ms per run with fused screens, grouping 0 / 1; 0: not tried */
+    float weight_ms[3];     /* autotuner's ms per run with the fused schedule's epilogue weight 1 / 4 / 8 */
+    float epi_weight;       /* the fused schedule's epilogue weight in use (k blocks per tile) */
+    int32_t seeded;         /* 1: screens start from thresholds seeded by a sample of the store */
+    float seed_ms;          /* autotuner's ms per run with seeded thresholds; 0: not tried */
 } svdb_ragged_info;
 
 typedef struct svdb_ragged svdb_ragged;
@@ -497,6 +507,16 @@ int svdb_sync(VectorDatabase* db);
 #define SVDB_NSTAGES 5
 int svdb_profile(VectorDatabase* db, int enable);
 int svdb_profile_read(VectorDatabase* db, double* ms, int reset);
+
+/* Threshold seeding of the tensor-core screens (SVDB_PREC_BF16 / FP8): the
+ * screen's running thresholds start from the exact k-th best lower bound
+ * over a 1/16 sample of the rows (one extra screen of the sample and its
+ * select).  Results are the same either way; the speed depends on the data:
+ * rows without clusters searched for a large k emit many times k candidates
+ * before unseeded thresholds settle.  mode -1: the default (FP8 screens
+ * only), 0: never, 1: always (on stores of at least 32 tiles of 256 rows,
+ * batches of at least 32 queries). */
+int svdb_set_screen_seeding(VectorDatabase* db, int mode);
 
 /* The CUDA stream (cudaStream_t) the database's kernels run on. */
 void* svdb_stream(VectorDatabase* db);

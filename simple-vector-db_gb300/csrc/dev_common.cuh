@@ -71,6 +71,16 @@ __device__ __forceinline__ double group4_sum(double p) {
     return p;
 }
 
+// The largest f with mx 2^f <= 448 (E4M3's largest finite value), for a
+// finite mx > 0, in closed form: mx = r 2^k with r in [0.5, 1) and
+// 448 = 0.875 x 2^9, so f = 9 - k when r <= 0.875, else 8 - k.  Exact for
+// subnormal mx too (f up to 1082: callers clamp it).
+__device__ __forceinline__ int e4m3_fit_exp(double mx) {
+    int k;
+    const double r = frexp(mx, &k);
+    return (r <= 0.875 ? 9 : 8) - k;
+}
+
 // ordering key of a metric value: ascending key = better; NaN last
 __device__ __forceinline__ double rank_key(int metric, double v) {
     double k = metric == SVDB_EUCLIDEAN ? v : -v;

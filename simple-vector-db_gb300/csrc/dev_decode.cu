@@ -1582,11 +1582,12 @@ int format_nearest(Store* s, size_t n, const int32_t* kind, const uint64_t* inde
     rc = s->scratch_reserve(a_meta + a_host + 2 * a_slots + a_len + a_off);
     if (rc) return rc;
     uint8_t* base = (uint8_t*)s->scratch;
+    // meta block: the 8-byte fields first, so every field is aligned for any n
     std::vector<uint8_t> hm(a_meta);
-    int32_t* hk = (int32_t*)hm.data();
-    uint64_t* hi = (uint64_t*)(hk + n);
+    uint64_t* hi = (uint64_t*)hm.data();
     const double** hr = (const double**)(hi + n);
-    uint32_t* hd = (uint32_t*)(hr + n);
+    int32_t* hk = (int32_t*)(hr + n);
+    uint32_t* hd = (uint32_t*)(hk + n);
     char* hu = (char*)(hd + n);
     std::vector<double> hrows(host_doubles);
     double* dhost = (double*)(base + a_meta);
@@ -1609,10 +1610,10 @@ int format_nearest(Store* s, size_t n, const int32_t* kind, const uint64_t* inde
     SVDB_CUDA(cudaMemcpyAsync(base, hm.data(), a_meta, cudaMemcpyHostToDevice, s->stream));
     if (host_doubles)
         SVDB_CUDA(cudaMemcpyAsync(dhost, hrows.data(), host_doubles * 8, cudaMemcpyHostToDevice, s->stream));
-    const int32_t* dk = (const int32_t*)base;
-    const uint64_t* di = (const uint64_t*)(dk + n);
+    const uint64_t* di = (const uint64_t*)base;
     const double* const* drows = (const double* const*)(di + n);
-    const uint32_t* ddim = (const uint32_t*)(drows + n);
+    const int32_t* dk = (const int32_t*)(drows + n);
+    const uint32_t* ddim = (const uint32_t*)(dk + n);
     const char* du = (const char*)(ddim + n);
     char* slots = (char*)(base + a_meta + a_host);
     uint32_t* dl = (uint32_t*)(base + a_meta + a_host + a_slots);

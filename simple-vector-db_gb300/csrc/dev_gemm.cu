@@ -391,25 +391,29 @@ struct TopL<0> {
 // its query tile (it selects the candidate sub-lists the segment writes).
 constexpr int kMaxCtas = 160;
 constexpr int kMaxSeg = 4;
+// grp: the search the segment belongs to (a fused launch screens several at
+// once; 0 otherwise); gq: the query tile's index among all the launch's query
+// tiles (its segment count is nsq[gq]); qt: the query tile within its search
 struct ScreenSeg {
     int32_t lo, hi;
-    uint16_t qt, sub;
+    uint16_t qt, sub, grp, gq;
 };
 struct ScreenSched {
     ScreenSeg seg[kMaxCtas][kMaxSeg];
     uint8_t nseg[kMaxCtas];
-    uint16_t nsq[kMaxCtas];  // segments of query tile qt (the `sub` values 0..nsq-1)
+    uint16_t nsq[kMaxCtas];  // segments of query tile gq (the `sub` values 0..nsq-1)
     int direct;  // 1: no table; CTA i takes query tile i against every store tile
     int ntr;
 };
 
 // `u`: the schedule unit, a CTA (or a CTA pair: both CTAs share the unit's segments)
 __device__ __forceinline__ ScreenSeg sched_seg(const ScreenSched& S, int u, int sg) {
-    if (S.direct) return ScreenSeg{0, S.ntr, (uint16_t)u, 0};
+    if (S.direct) return ScreenSeg{0, S.ntr, (uint16_t)u, 0, 0, (uint16_t)u};
     return S.seg[u][sg];
 }
 
-struct ScreenParams {
+// everything the screen needs about one search
+struct GroupParams {
     const uint8_t* xblk;  // the shadow being screened, in swizzled 256-row x 128-byte tiles (BF16 or E4M3)
     const float* qscale;  // FP8: per query, the exact power of two from accumulator units to key units
     const float4* rpar;  // per row {mult, a, b, m}; NaN rows are never candidates
@@ -419,7 +423,9 @@ struct ScreenParams {
     const int* nmax;        // cosine: {max |x/|x| - bxn|, max |bxn|} over the store (float bits)
     const float4* qpar;  // per query {qn, eqq, eq0, valid}
     int* tau;            // per query: shared lower bound of the k-th best key (ordered int)
-    int* bins;           // per query, k bins: best chunk maximum of the chunks whose index % k is the bin
+    int* bins;           // k bins per query, bin-major (bin t of query q at t * nq + q, so a warp's 32
+                         // queries read or raise one bin with one coalesced access): best chunk maximum
+                         // of the chunks whose index % k is the bin
     int* cnt;            // per (query, sub-list) candidate count (may exceed subcap: overflow)
     int2* cand;          // per query: nsub sub-lists of subcap x {row slot, key bits}, stride cap
     int* err;            // set to 1 when a wait timed out
@@ -428,8 +434,52 @@ struct ScreenParams {
     int nq, k, cap;
     int nsub, subcap;    // sub-list = (row group, column half): one emitting thread each
     int kblocks;  // ldb / 64
+};
+
+// one launch over a single search
+struct ScreenParams {
+    GroupParams g;
     ScreenSched sched;
 };
+
+// A fused launch over several searches (of several stores, dimensions and
+// query batches, one running top-k class): their query tensor maps and
+// parameters travel in the launch's own parameter space, and the schedule's
+// units are CTAs of any of the searches.
+constexpr int kMaxGroups = 16;     // searches in one fused launch
+constexpr int kMaxUnitsM = 320;    // CTAs of a fused launch
+constexpr int kMaxQTilesM = 640;   // query tiles over all its searches
+struct ScreenSchedMulti {
+    ScreenSeg seg[kMaxUnitsM][kMaxSeg];
+    uint8_t nseg[kMaxUnitsM];
+    uint16_t nsq[kMaxQTilesM];
+    int direct;  // always 0 (every unit has its table row)
+    int ntr;
+};
+struct ScreenParamsMulti {
+    CUtensorMap map[kMaxGroups];  // query tensor map of each search (64-byte aligned)
+    GroupParams grp[kMaxGroups];
+    ScreenSchedMulti sched;
+};
+
+// a launch's parameters are limited to 32,764 bytes
+static_assert(sizeof(ScreenParamsMulti) + 2 * sizeof(CUtensorMap) <= 32764, "fused launch parameters too large");
+static_assert(sizeof(ScreenParams) + 2 * sizeof(CUtensorMap) <= 32764, "screen launch parameters too large");
+
+__device__ __forceinline__ ScreenSeg sched_seg(const ScreenSchedMulti& S, int u, int sg) { return S.seg[u][sg]; }
+__device__ __forceinline__ const GroupParams& seg_params(const ScreenParams& P, const ScreenSeg&) { return P.g; }
+__device__ __forceinline__ const GroupParams& seg_params(const ScreenParamsMulti& P, const ScreenSeg& sg) {
+    return P.grp[sg.grp];
+}
+__device__ __forceinline__ const CUtensorMap* seg_qmap(const ScreenParams&, const ScreenSeg&, const CUtensorMap* tmq) {
+    return tmq;
+}
+__device__ __forceinline__ const CUtensorMap* seg_qmap(const ScreenParamsMulti& P, const ScreenSeg& sg,
+                                                       const CUtensorMap*) {
+    return &P.map[sg.grp];
+}
+template <bool MULTI>
+using ScreenParamsT = std::conditional_t<MULTI, ScreenParamsMulti, ScreenParams>;
 
 // NORM (cosine): the B operand is the unit-norm shadow, so the key is the
 // accumulator itself and the bound is one constant per query,
@@ -456,10 +506,15 @@ struct ScreenParams {
 // bytes), MMA completions on both CTAs' empty / accumulator barriers, and
 // both CTAs' epilogue warps free an accumulator on the even CTA's barrier.
 // Per SM a K step moves 8 KB of operands instead of 12 KB.
-template <int KL, bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false>
+// MULTI: a fused launch over several searches (of several stores, dimensions
+// and query batches): each segment carries its search (seg.grp), whose
+// parameters, shadow, K depth and query tensor map the three roles pick up at
+// the segment's start.
+template <int KL, bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false>
 __global__ void __launch_bounds__(scr::kThreads, 1)
     k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
-                  const ScreenParams P) {
+                  const __grid_constant__ ScreenParamsT<MULTI> P) {
+    static_assert(!(MULTI && (PAIR || DUMP)), "a fused launch is single-CTA and screens");
     using namespace scr;
     using SM = SmemT<PAIR>;
     constexpr int ST = SM::ST;
@@ -473,7 +528,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
     const bool leader = rank == 0;
     const int unit = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
     const int nseg = P.sched.direct ? 1 : P.sched.nseg[unit];
-    const int KB = P.kblocks;
     volatile int* abort = &S.abort;
 
     if (threadIdx.x == 0) {
@@ -523,6 +577,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             for (int sg = 0; sg < nseg && ok; ++sg) {
             const ScreenSeg seg = sched_seg(P.sched, unit, sg);
             const int qt = seg.qt;
+            const GroupParams& GP = seg_params(P, seg);
+            const CUtensorMap* tm = seg_qmap(P, seg, &tmq);
+            if (MULTI) tma_prefetch_desc(tm);
+            const int KB = GP.kblocks;
             for (int r = seg.lo; r < seg.hi && ok; ++r, ++jt) {
                 if (!NORM) {  // the tile's screen parameters into the 2-slot ring (freed by the epilogue)
                     const uint32_t slot = jt & 1u;
@@ -531,7 +589,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         break;
                     }
                     mbar_expect_tx(&S.rp_full[slot], kBN * sizeof(float4));
-                    bulk_load(S.rp[slot], P.spar + (size_t)r * kBN, kBN * sizeof(float4), &S.rp_full[slot]);
+                    bulk_load(S.rp[slot], GP.spar + (size_t)r * kBN, kBN * sizeof(float4), &S.rp_full[slot]);
                     ++rp_issued;
                 }
                 for (int kb = 0; kb < KB; ++kb) {
@@ -548,9 +606,9 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         tma_load_2d_pair(S.b[stage], &tmx, fb, 0, (r * KB + kb) * kBN + (int)rank * (kBN / 2));
                     } else {
                         mbar_expect_tx(&S.full[stage], kStageA + kStageB);
-                        tma_load_2d(S.a[stage], &tmq, &S.full[stage], kb * (F8 ? 2 * kBK : kBK), qt * kBM);
+                        tma_load_2d(S.a[stage], tm, &S.full[stage], kb * (F8 ? 2 * kBK : kBK), qt * kBM);
                         // the store tile: one contiguous 32 KB block, already swizzled
-                        bulk_load(S.b[stage], P.xblk + ((size_t)r * KB + kb) * kStageB, kStageB, &S.full[stage]);
+                        bulk_load(S.b[stage], GP.xblk + ((size_t)r * KB + kb) * kStageB, kStageB, &S.full[stage]);
                     }
                     ++issued;
                     if (++stage == ST) {
@@ -584,8 +642,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             uint32_t phase = 0;
             bool ok = true;
             int j = 0;
-            for (int sg = 0; sg < nseg && ok; ++sg)
-            for (int r = sched_seg(P.sched, unit, sg).lo, rh = sched_seg(P.sched, unit, sg).hi; r < rh && ok; ++r, ++j) {
+            for (int sg = 0; sg < nseg && ok; ++sg) {
+            const ScreenSeg sgm = sched_seg(P.sched, unit, sg);
+            const int KB = seg_params(P, sgm).kblocks;
+            for (int r = sgm.lo, rh = sgm.hi; r < rh && ok; ++r, ++j) {
                 const int b = j & 1;
                 const uint32_t use = (uint32_t)j >> 1;
                 if (!mbar_wait(&S.accempty[b], (use & 1u) ^ 1u, abort, kWaitLimitNs)) break;
@@ -626,6 +686,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         mma_commit(&S.accfull[b]);
                 }
             }
+            }
             // all MMAs issued by this thread complete before TMEM is released
             if constexpr (PAIR)
                 mma_commit_pair_local(&S.done);
@@ -649,34 +710,35 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         for (int sg = 0; sg < nseg && alive; ++sg) {
         // every segment starts afresh: its query tile, running top-k, warm-up
         const ScreenSeg seg = sched_seg(P.sched, unit, sg);
+        const GroupParams& GP = seg_params(P, seg);
         const int q = PAIR ? seg.qt * 2 * kBM + (int)rank * kBM + qi : seg.qt * kBM + qi;
         float eq = 0.f, eq0 = 0.f;  // screen bound: E = eq . b + 2^-19 m + eq0 (NORM: eq0 = E)
         bool valid = false;
         // F8: key = accumulator x cs, cs a power of two (so both directions are exact)
         float cs = 1.f, ics = 1.f;
-        if (F8 && q < P.nq) {
-            cs = P.qscale[q];
+        if (F8 && q < GP.nq) {
+            cs = GP.qscale[q];
             ics = __frcp_rn(cs);
         }
-        if (q < P.nq) {
-            const float4 qp = P.qpar[q];
+        if (q < GP.nq) {
+            const float4 qp = GP.qpar[q];
             if (NORM) {
-                eq0 = __fmaf_ru(qp.x, __int_as_float(__ldg(P.nmax)),
-                                __fmaf_ru(qp.y, __int_as_float(__ldg(P.nmax + 1)), qp.z));
+                eq0 = __fmaf_ru(qp.x, __int_as_float(__ldg(GP.nmax)),
+                                __fmaf_ru(qp.y, __int_as_float(__ldg(GP.nmax + 1)), qp.z));
             } else {
-                eq = __fmaf_ru(qp.x, __int_as_float(__ldg(P.alpha)), qp.y);
+                eq = __fmaf_ru(qp.x, __int_as_float(__ldg(GP.alpha)), qp.y);
                 eq0 = qp.z;
             }
             valid = qp.w != 0.f;
         }
         TopL<KL> top;
-        top.init(valid ? P.k : 0);  // invalid queries: threshold +inf, never emit, never push
-        const int nsq = P.sched.direct ? 1 : (int)P.sched.nsq[seg.qt];
+        top.init(valid ? GP.k : 0);  // invalid queries: threshold +inf, never emit, never push
+        const int nsq = P.sched.direct ? 1 : (int)P.sched.nsq[seg.gq];
         float tau_c = -INFINITY, published = -INFINITY;
         // this thread's own sub-list of the query's candidates: emission needs no
         // atomic, the count stays in a register and is stored once at the end
         const int sub = 2 * seg.sub + half;
-        int2* cq = P.cand + (size_t)(q < P.nq ? q : 0) * P.cap + (size_t)sub * P.subcap;
+        int2* cq = GP.cand + (size_t)(q < GP.nq ? q : 0) * GP.cap + (size_t)sub * GP.subcap;
         int nemit = 0;
         for (int r = seg.lo, js = 0; r < seg.hi; ++r, ++j, ++js) {
             const int b = j & 1;
@@ -685,7 +747,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // cosine: validity words of this warp's 128 rows (lane c holds the word
             // of chunk c), loaded before the wait so their latency is hidden
             uint32_t vbl = 0;
-            if (NORM && !DUMP && lane < kBN / 2 / 32) vbl = __ldg(P.vbits + ((r * kBN + col0) >> 5) + lane);
+            if (NORM && !DUMP && lane < kBN / 2 / 32) vbl = __ldg(GP.vbits + ((r * kBN + col0) >> 5) + lane);
             // Threshold refresh from the shared bins and tau (tiles 1..7 of a
             // segment, then every 8th): read BEFORE the accumulator wait, so the
             // loads' latency overlaps it instead of stalling the epilogue.  Bins
@@ -695,12 +757,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             const bool refresh = !DUMP && valid && js > 0 && (js < 8 || (js & 7) == 0);
             int bmin_pre = 0x7fffffff, tau_pre = 0;
             if (refresh) {
-                const int* bq = P.bins + (size_t)q * P.k;
-                tau_pre = __ldcg(P.tau + q);
-                for (int t0 = 0; t0 < P.k; t0 += 16) {  // 16 independent loads per round trip
+                const int* bq = GP.bins + q;
+                const size_t bs = (size_t)GP.nq;
+                tau_pre = __ldcg(GP.tau + q);
+                for (int t0 = 0; t0 < GP.k; t0 += 16) {  // 16 independent loads per round trip
                     int v16[16];
 #pragma unroll
-                    for (int u = 0; u < 16; ++u) v16[u] = t0 + u < P.k ? __ldcg(bq + t0 + u) : 0x7fffffff;
+                    for (int u = 0; u < 16; ++u) v16[u] = t0 + u < GP.k ? __ldcg(bq + (size_t)(t0 + u) * bs) : 0x7fffffff;
 #pragma unroll
                     for (int u = 0; u < 16; ++u) bmin_pre = min(bmin_pre, v16[u]);
                 }
@@ -723,8 +786,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     __syncwarp();  // converged warp for the collective load
                     tmem_ld32(tbase + (uint32_t)(c * 32), v);
                     tmem_ld_wait();
-                    if (q < P.nq) {
-                        float* o = P.dump + (size_t)q * P.dump_ld + row0 + c * 32;
+                    if (q < GP.nq) {
+                        float* o = GP.dump + (size_t)q * GP.dump_ld + row0 + c * 32;
 #pragma unroll
                         for (int i = 0; i < 32; ++i) o[i] = __uint_as_float(v[i]);
                     }
@@ -758,7 +821,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     float maxl = -INFINITY;
                     if (NORM) {
                         const int rw = row0 + c * kChunk;
-                        const uint32_t vb = __ldg(P.vbits + (rw >> 5)) >> (rw & 31);
+                        const uint32_t vb = __ldg(GP.vbits + (rw >> 5)) >> (rw & 31);
 #pragma unroll
                         for (int i = 0; i < kChunk; ++i) {
                             // masked rows are NaN: every comparison with them is false
@@ -777,7 +840,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         }
                     }
                     if (valid && maxl > -INFINITY)
-                        atomicMax(&P.bins[(size_t)q * P.k + ((2 * seg.sub + half) * kWarmUnits + c) % P.k],
+                        atomicMax(&GP.bins[(size_t)(((2 * seg.sub + half) * kWarmUnits + c) % GP.k) * GP.nq + q],
                                   f2ord(maxl));
                 }
             }
@@ -787,10 +850,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             if (refresh) {
                 tau_c = fmaxf(tau_c, fmaxf(ord2f(tau_pre), ord2f(bmin_pre)));
             } else if (valid && js == 0) {  // after the warm-up's own contributions
-                const int* bq = P.bins + (size_t)q * P.k;
+                const int* bq = GP.bins + q;
                 int bmin = 0x7fffffff;
-                for (int t = 0; t < P.k; ++t) bmin = min(bmin, __ldcg(bq + t));
-                tau_c = fmaxf(tau_c, fmaxf(ord2f(__ldcg(P.tau + q)), ord2f(bmin)));
+                for (int t = 0; t < GP.k; ++t) bmin = min(bmin, __ldcg(bq + (size_t)t * GP.nq));
+                tau_c = fmaxf(tau_c, fmaxf(ord2f(__ldcg(GP.tau + q)), ord2f(bmin)));
             }
             float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
             // the query's eq0 is folded into the threshold and the maxima
@@ -850,7 +913,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 float mu = gm[0];
 #pragma unroll
                 for (int g = 1; g < G; ++g) mu = fmaxf(mu, gm[g]);
-                const bool want = mu >= thr2 && q < P.nq;
+                const bool want = mu >= thr2 && q < GP.nq;
                 if (__any_sync(0xffffffffu, want)) {
 #pragma unroll
                     for (int g = 0; g < G; ++g) {
@@ -873,7 +936,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         for (int i = 0; i < 8; ++i) {
                             if ((any >> i) & 1u) {  // warp-uniform
                                 const int slot = base + __popc(mask & ((1u << i) - 1u));
-                                if (((mask >> i) & 1u) && slot < P.subcap)
+                                if (((mask >> i) & 1u) && slot < GP.subcap)
                                     cq[slot] = make_int2(rw + 8 * g + i,
                                                          ACCU ? __float_as_int(__uint_as_float(v[8 * g + i]) * cs)
                                                               : (int)v[8 * g + i]);
@@ -894,7 +957,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             const float maxl = __fsub_rd(ACCU ? tmax * cs : tmax, eq0);
             if (valid && js > 0 && maxl > thr) {
                 const int unit = 2 * kWarmUnits * nsq + (js - 1) * 2 * nsq + 2 * seg.sub + half;
-                atomicMax(&P.bins[(size_t)q * P.k + unit % P.k], f2ord(maxl));
+                atomicMax(&GP.bins[(size_t)(unit % GP.k) * GP.nq + q], f2ord(maxl));
             }
             if (valid && js > 0 && maxl > top.mn) top.push(maxl);
             tc_fence_before();
@@ -907,16 +970,17 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 if (!NORM) mbar_arrive(&S.rp_empty[b]);
             }
             if (valid && top.mn > published) {
-                atomicMax(&P.tau[q], f2ord(top.mn));
+                atomicMax(&GP.tau[q], f2ord(top.mn));
                 published = top.mn;
             }
         }
-        if (!DUMP && q < P.nq) P.cnt[(size_t)q * P.nsub + sub] = nemit;
+        if (!DUMP && q < GP.nq) GP.cnt[(size_t)q * GP.nsub + sub] = nemit;
         }
     }
 
     __syncthreads();
-    if (threadIdx.x == 0 && S.abort) atomicExch(P.err, 1);
+    if (threadIdx.x == 0 && S.abort)  // every search this CTA served
+        for (int sg = 0; sg < nseg; ++sg) atomicExch(seg_params(P, sched_seg(P.sched, unit, sg)).err, 1);
     // neither CTA of a pair leaves (or frees TMEM) while the other may still
     // signal its barriers or the MMAs may still read its shared memory
     if constexpr (PAIR) cluster_sync_all();
@@ -1021,8 +1085,7 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
     m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 1));
     int e = 0;
     if (m > 0.0 && isfinite(m)) {
-        e = (int)floor(log2(448.0 / m));
-        while (m * ldexp(1.0, e) > 448.0) --e;
+        e = max(-126, min(126, e4m3_fit_exp(m)));  // |e| >= 100 marks the query invalid below
     }
     const double sc = ldexp(1.0, e);
     double res = 0.0, bsq = 0.0;
@@ -1139,7 +1202,7 @@ __global__ void k_init_search(int* tau, int* bins, int* cnt, int nsub, uint8_t* 
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nq) {
         tau[i] = f2ord(seed ? seed[i] : -INFINITY);
-        for (int t = 0; t < k; ++t) bins[(size_t)i * k + t] = f2ord(-INFINITY);
+        for (int t = 0; t < k; ++t) bins[(size_t)t * nq + i] = f2ord(-INFINITY);  // bin-major
         for (int t = 0; t < nsub; ++t) cnt[(size_t)i * nsub + t] = 0;
         flags[i] = scr::kOk;
     }
@@ -2080,7 +2143,7 @@ static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub, int un
             fits = false;
             return;
         }
-        S.seg[c][S.nseg[c]++] = ScreenSeg{lo, hi, (uint16_t)qt, (uint16_t)ord[qt]++};
+        S.seg[c][S.nseg[c]++] = ScreenSeg{lo, hi, (uint16_t)qt, (uint16_t)ord[qt]++, 0, (uint16_t)qt};
     };
     const int base = G / ntq, ea = G % ntq;
     const int T = (int)(((int64_t)ntq * ntr + G - 1) / G);
@@ -2112,7 +2175,7 @@ static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub, int un
         for (int g = 0; g < base; ++g)
             for (int qt = 0; qt < ntq; ++qt, ++c)
                 S.seg[c][S.nseg[c]++] = ScreenSeg{(int)((int64_t)g * ntr / base), (int)((int64_t)(g + 1) * ntr / base),
-                                                  (uint16_t)qt, (uint16_t)ord[qt]++};
+                                                  (uint16_t)qt, (uint16_t)ord[qt]++, 0, (uint16_t)qt};
     }
     for (int qt = 0; qt < ntq; ++qt) S.nsq[qt] = (uint16_t)std::max(1, ord[qt]);
     *maxsub = std::max(1, *std::max_element(ord.begin(), ord.end()));
@@ -2121,7 +2184,9 @@ static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub, int un
 
 constexpr size_t k_max_bf16 = 128;  // largest k the screen certifies
 
-static Bf16Layout bf16_layout(const Store* s, size_t nq) {
+// maxsub_ext > 0: the search is screened by a fused launch whose schedule
+// gives each of its query tiles at most maxsub_ext segments (single-CTA form)
+static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
     Bf16Layout L;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -2144,14 +2209,21 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq) {
     L.vbits = take(L.npad / 8);
     L.tau = take(nq * sizeof(int));
     L.bins = take(nq * k_max_bf16 * sizeof(int));
-    if (nq <= (size_t)kStreamQ) {
+    if (nq <= (size_t)kStreamQ && maxsub_ext <= 0) {
         L.tmax = take(nq * (size_t)L.ntr * kStreamWarps * sizeof(float));
         L.cut = take(nq * sizeof(float));
     }
     int maxsub = 1;
-    L.pair = screen_pair(nq);
-    const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
-    L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair));
+    if (maxsub_ext > 0) {
+        std::memset(&L.sched, 0, sizeof(L.sched));
+        L.pair = false;
+        L.nctas = 0;
+        maxsub = maxsub_ext;
+    } else {
+        L.pair = screen_pair(nq);
+        const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
+        L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair));
+    }
     L.nsub = 2 * maxsub;
     L.cnt = take(nq * (size_t)L.nsub * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
@@ -2190,118 +2262,163 @@ size_t search_bf16_scratch(const Store* s, size_t nq, size_t /*k: the layout hol
 
 bool bf16_supported(const Store* s, size_t k) { return k <= k_max_bf16 && s->n_unscreen == 0 && s->nlive > 0; }
 
-int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st, bool f8) {
+// One BF16 / FP8 search between its phases: begin (queries, row terms, the
+// screen's parameters), the screen (a launch of its own, or its share of a
+// fused launch), end (select, refinement, re-rank, exact redo of what the
+// screen could not certify).  Every phase runs on the store's stream except a
+// fused screen.
+struct Bf16Run {
+    Store* s = nullptr;
+    SearchArgs a;
     GemmPlanCache* gc = nullptr;
-    int rc = gemm_cache(s, &gc);
+    Bf16Layout L;
+    uint8_t* base = nullptr;
+    bool f8 = false, norm = false, stream = false;
+    int kc = 0;  // running top-k variant of the screen and select: k <= 16, <= 32, <= 128
+    int nsub_use = 0, subcap_use = 0;
+    ScreenParams P;
+    CUtensorMap tmq;
+    uint32_t kernels = 0;
+    template <class T>
+    T* at(size_t off) const {
+        return reinterpret_cast<T*>(base + off);
+    }
+};
+
+static int k_class_of(size_t k) { return k <= 16 ? 0 : k <= 32 ? 1 : 2; }
+
+template <bool PR>
+static auto screen_kernel_of(bool e4m3, int kc, bool norm) {
+    return e4m3   ? (kc == 0 ? (norm ? k_screen_bf16<16, true, true, false, PR> : k_screen_bf16<16, false, true, false, PR>)
+                     : kc == 1 ? (norm ? k_screen_bf16<32, true, true, false, PR> : k_screen_bf16<32, false, true, false, PR>)
+                               : (norm ? k_screen_bf16<0, true, true, false, PR> : k_screen_bf16<0, false, true, false, PR>))
+           : kc == 0 ? (norm ? k_screen_bf16<16, true, false, false, PR> : k_screen_bf16<16, false, false, false, PR>)
+           : kc == 1 ? (norm ? k_screen_bf16<32, true, false, false, PR> : k_screen_bf16<32, false, false, false, PR>)
+                     : (norm ? k_screen_bf16<0, true, false, false, PR> : k_screen_bf16<0, false, false, false, PR>);
+}
+
+// one screen over nunits units (CTAs or pairs) with the query tensor map tmq_;
+// the paired form also gets the tensor map of the shadow's tiles
+static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtensorMap& tmq_, const ScreenParams& P_) {
+    GemmPlanCache* gc = R.gc;
+    Store* s = R.s;
+    const int v = e4m3 ? 6 + 2 * R.kc + (R.norm ? 1 : 0) : 2 * R.kc + (R.norm ? 1 : 0);
+    if (!pair) {
+        auto kern = screen_kernel_of<false>(e4m3, R.kc, R.norm);
+        if (!gc->attr_set[v]) {
+            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
+            gc->attr_set[v] = true;
+        }
+        return launch_screen(kern, false, nunits, gc->screen_smem, s->stream, tmq_, tmq_, P_);
+    }
+    auto kern = screen_kernel_of<true>(e4m3, R.kc, R.norm);
+    if (!gc->attr_pair[v]) {
+        SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_pair));
+        gc->attr_pair[v] = true;
+    }
+    CUtensorMap tmx;
+    const size_t kbl = e4m3 ? s->ldb8 / (2 * scr::kBK) : s->ldb / scr::kBK;
+    const int rc = make_map_tiles(gc, &tmx, P_.g.xblk, (size_t)R.L.ntr * kbl * scr::kBN);
     if (rc) return rc;
-    const Bf16Layout L = bf16_layout(s, a.nq);
+    return launch_screen(kern, true, nunits, gc->screen_smem_pair, s->stream, tmq_, tmx, P_);
+}
+
+static int launch_select(Bf16Run& R, int nsub_, int subcap_, const float4* qp_, float* kth) {
+    Store* s = R.s;
+    GemmPlanCache* gc = R.gc;
+    const Bf16Layout& L = R.L;
+    const int nq = (int)R.a.nq, k = (int)R.a.k;
+    // small batches carry many candidates per query: wider blocks
+    const int sel_threads = nq >= 256 ? 256 : 1024;
+    const size_t sel_smem = k <= 32 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;
+    if (!gc->select_attr) {
+        SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+        SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+        gc->select_attr = true;
+    }
+    int2* cand = R.at<int2>(L.cand);
+    int* cnt = R.at<int>(L.cnt);
+    const float4* rpar = R.at<float4>(L.rpar);
+    int2* surv = R.at<int2>(L.surv);
+    int* nsurv = R.at<int>(L.nsurv);
+    int* sig = R.at<int>(L.sig);
+    uint8_t* flags = R.at<uint8_t>(L.flags);
+    if (R.kc == 0)
+        k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k,
+                                                                         surv, nsurv, sig, flags, kth);
+    else if (R.kc == 1)
+        k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k,
+                                                                         surv, nsurv, sig, flags, kth);
+    else
+        k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k,
+                                                                        surv, nsurv, sig, flags, kth);
+    SVDB_LAUNCH_CHECK();
+    return SVDB_OK;
+}
+
+// queries, row terms and the screen's parameters (R.P, R.tmq); maxsub_ext > 0:
+// a fused screen (BF16 only) will take the place of bf16_screen
+static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, bool f8,
+                      int maxsub_ext) {
+    int rc = gemm_cache(s, &R.gc);
+    if (rc) return rc;
+    R.s = s;
+    R.a = a;
+    R.f8 = f8;
+    R.L = bf16_layout(s, a.nq, maxsub_ext);
+    const Bf16Layout& L = R.L;
     if (L.total > scratch_bytes) {
         svdb_set_error("search_bf16: scratch too small");
         return SVDB_EINVAL;
     }
-    uint8_t* base = reinterpret_cast<uint8_t*>(scratch);
-    __nv_bfloat16* qb = reinterpret_cast<__nv_bfloat16*>(base + L.qb);
-    float* q32 = reinterpret_cast<float*>(base + L.q32);
-    float4* qpar = reinterpret_cast<float4*>(base + L.qpar);
-    float4* rpar = reinterpret_cast<float4*>(base + L.rpar);
-    float4* spar = reinterpret_cast<float4*>(base + L.spar);
-    int* alpha = reinterpret_cast<int*>(base + L.alpha);
-    uint32_t* vbits = reinterpret_cast<uint32_t*>(base + L.vbits);
-    int* tau = reinterpret_cast<int*>(base + L.tau);
-    int* bins = reinterpret_cast<int*>(base + L.bins);
-    int* cnt = reinterpret_cast<int*>(base + L.cnt);
-    int2* cand = reinterpret_cast<int2*>(base + L.cand);
-    int2* surv = reinterpret_cast<int2*>(base + L.surv);
-    int* nsurv = reinterpret_cast<int*>(base + L.nsurv);
-    int* nref = reinterpret_cast<int*>(base + L.nref);
-    int* sig = reinterpret_cast<int*>(base + L.sig);
-    int* perm = reinterpret_cast<int*>(base + L.perm);
-    uint8_t* flags = base + L.flags;
-    int* redo = reinterpret_cast<int*>(base + L.redo);
-    int* redo_n = reinterpret_cast<int*>(base + L.redo_n);
-    unsigned long long* dstats = reinterpret_cast<unsigned long long*>(base + L.stats);
+    R.base = reinterpret_cast<uint8_t*>(scratch);
+    GemmPlanCache* gc = R.gc;
+    __nv_bfloat16* qb = R.at<__nv_bfloat16>(L.qb);
+    float* q32 = R.at<float>(L.q32);
+    float4* qpar = R.at<float4>(L.qpar);
+    float4* rpar = R.at<float4>(L.rpar);
+    float4* spar = R.at<float4>(L.spar);
+    int* alpha = R.at<int>(L.alpha);
+    uint32_t* vbits = R.at<uint32_t>(L.vbits);
+    int* tau = R.at<int>(L.tau);
+    int* bins = R.at<int>(L.bins);
+    int* cnt = R.at<int>(L.cnt);
+    int2* cand = R.at<int2>(L.cand);
+    uint8_t* flags = R.at<uint8_t>(L.flags);
+    int* redo_n = R.at<int>(L.redo_n);
+    unsigned long long* dstats = R.at<unsigned long long>(L.stats);
+    float* qscale = R.at<float>(L.qscale);
     const int nq = (int)a.nq, k = (int)a.k;
-    uint32_t kernels = 0;
-
-    float* qscale = reinterpret_cast<float*>(base + L.qscale);
     // f8: cosine screens the E4M3 unit-norm shadow, dot / Euclidean the E4M3
     // shadow with per-row power-of-two scales
-    const bool norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
-    const int kc = k <= 16 ? 0 : k <= 32 ? 1 : 2;  // running top-k variant of the screen and select
-    auto screen_kernel_of = [&](bool e4m3, auto pair_tag) {
-        constexpr bool PR = decltype(pair_tag)::value;
-        return e4m3   ? (kc == 0 ? (norm ? k_screen_bf16<16, true, true, false, PR> : k_screen_bf16<16, false, true, false, PR>)
-                         : kc == 1 ? (norm ? k_screen_bf16<32, true, true, false, PR> : k_screen_bf16<32, false, true, false, PR>)
-                                   : (norm ? k_screen_bf16<0, true, true, false, PR> : k_screen_bf16<0, false, true, false, PR>))
-               : kc == 0 ? (norm ? k_screen_bf16<16, true, false, false, PR> : k_screen_bf16<16, false, false, false, PR>)
-               : kc == 1 ? (norm ? k_screen_bf16<32, true, false, false, PR> : k_screen_bf16<32, false, false, false, PR>)
-                         : (norm ? k_screen_bf16<0, true, false, false, PR> : k_screen_bf16<0, false, false, false, PR>);
-    };
-    // one screen over nunits units (CTAs or pairs) with the query tensor map tmq_;
-    // the paired form also gets the tensor map of the shadow's tiles
-    auto run_screen = [&](bool e4m3, bool pair, int nunits, const CUtensorMap& tmq_, const ScreenParams& P_) -> int {
-        const int v = e4m3 ? 6 + 2 * kc + (norm ? 1 : 0) : 2 * kc + (norm ? 1 : 0);
-        if (!pair) {
-            auto kern = screen_kernel_of(e4m3, std::false_type());
-            if (!gc->attr_set[v]) {
-                SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
-                gc->attr_set[v] = true;
-            }
-            return launch_screen(kern, false, nunits, gc->screen_smem, s->stream, tmq_, tmq_, P_);
-        }
-        auto kern = screen_kernel_of(e4m3, std::true_type());
-        if (!gc->attr_pair[v]) {
-            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_pair));
-            gc->attr_pair[v] = true;
-        }
-        CUtensorMap tmx;
-        const size_t kbl = e4m3 ? s->ldb8 / (2 * scr::kBK) : s->ldb / scr::kBK;
-        const int rc_ = make_map_tiles(gc, &tmx, P_.xblk, (size_t)L.ntr * kbl * scr::kBN);
-        if (rc_) return rc_;
-        return launch_screen(kern, true, nunits, gc->screen_smem_pair, s->stream, tmq_, tmx, P_);
-    };
-    // small batches carry many candidates per query: wider blocks
-    const int sel_threads = nq >= 256 ? 256 : 1024;
-    const size_t sel_smem = k <= 32 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;
-    auto launch_select = [&](int nsub_, int subcap_, const float4* qp_, float* kth) -> int {
-        if (!gc->select_attr) {
-            SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-            SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-            gc->select_attr = true;
-        }
-        if (kc == 0)
-            k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_,
-                                                                             k, surv, nsurv, sig, flags, kth);
-        else if (kc == 1)
-            k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_,
-                                                                             k, surv, nsurv, sig, flags, kth);
-        else
-            k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_,
-                                                                            k, surv, nsurv, sig, flags, kth);
-        SVDB_LAUNCH_CHECK();
-        return SVDB_OK;
-    };
+    R.norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
+    R.kc = k_class_of(a.k);
+    const bool norm = R.norm;
 
-    // FP8: seed the running thresholds with the exact k-th largest BF16 lower
-    // bound over a sample of the store (its first 1/16 of the rows, which are
-    // in no particular order).  The E4M3 bound is ~16x the BF16 one, so a
-    // screen whose thresholds start from random rows emits every row within
-    // that bound of them until it meets rows of the query's cluster; a sample
-    // holding enough of them puts the threshold at the cluster's level from
-    // the first tile.  A lower bound over a subset of the rows is a lower
-    // bound over all of them, so the seed is a valid starting threshold.
+    // Seeding (the FP8 screen by default; BF16 when asked): start the running
+    // thresholds from the exact k-th largest BF16 lower bound over a sample of
+    // the store (its first 1/16 of the rows, which are in no particular
+    // order).  The E4M3 bound is ~16x the BF16 one, so an FP8 screen whose
+    // thresholds start from random rows emits every row within that bound of
+    // them until it meets rows of the query's cluster; a sample holding
+    // enough of them puts the threshold at the cluster's level from the first
+    // tile.  A BF16 screen of rows without clusters and a large k otherwise
+    // emits many times k rows before its shared thresholds settle.  A lower
+    // bound over a subset of the rows is a lower bound over all of them, so
+    // the seed is a valid starting threshold.
     float* seed = nullptr;
-    if (f8 && L.ntr >= 32 && nq >= 32) {  // (a lone query's tile is split over every SM: its bins fill at once)
-        __nv_bfloat16* qb16 = reinterpret_cast<__nv_bfloat16*>(base + L.qb16);
-        float4* qpar16 = reinterpret_cast<float4*>(base + L.qpar16);
-        seed = reinterpret_cast<float*>(base + L.seed);
+    const bool want_seed = a.seed > 0 || (a.seed < 0 && f8);
+    if (want_seed && L.ntr >= 32 && nq >= 32) {  // (a lone query's tile is split over every SM: its bins fill at once)
+        __nv_bfloat16* qb16 = R.at<__nv_bfloat16>(L.qb16);
+        float4* qpar16 = R.at<float4>(L.qpar16);
+        seed = R.at<float>(L.seed);
         const int tq = L.pair ? 2 * scr::kBM : scr::kBM;
         const int ntq = (nq + tq - 1) / tq;
         const int ntr_seed = L.ntr / 16;
         const int64_t npad_seed = (int64_t)ntr_seed * scr::kBN;
-        ScreenSched SS;
+        ScreenParams PS;
         int maxsub_s = 1;
-        const int nctas_s = screen_schedule(ntq, ntr_seed, SS, &maxsub_s, screen_units(L.pair));
+        const int nctas_s = screen_schedule(ntq, ntr_seed, PS.sched, &maxsub_s, screen_units(L.pair));
         const int nsub_s = 2 * maxsub_s;
         const int subcap_s = L.cap / nsub_s;
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
@@ -2317,32 +2434,33 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         CUtensorMap tmq16;
         rc = make_map(gc, &tmq16, qb16, a.nq, s->ldb, scr::kBM);
         if (rc) return rc;
-        ScreenParams PS;
-        PS.xblk = reinterpret_cast<const uint8_t*>(norm ? (const void*)s->xbn : (const void*)s->xb);
-        PS.qscale = qscale;
-        PS.rpar = rpar;
-        PS.spar = spar;
-        PS.alpha = alpha;
-        PS.vbits = vbits;
-        PS.nmax = s->d_count + 1;
-        PS.qpar = qpar16;
-        PS.tau = tau;
-        PS.bins = bins;
-        PS.cnt = cnt;
-        PS.cand = cand;
-        PS.err = s->d_err;
-        PS.nq = nq;
-        PS.k = k;
-        PS.cap = L.cap;
-        PS.nsub = nsub_s;
-        PS.subcap = subcap_s;
-        PS.kblocks = (int)(s->ldb / scr::kBK);
-        PS.sched = SS;
-        rc = run_screen(false, L.pair, nctas_s, tmq16, PS);
+        PS.g.xblk = reinterpret_cast<const uint8_t*>(norm ? (const void*)s->xbn : (const void*)s->xb);
+        PS.g.qscale = qscale;
+        PS.g.rpar = rpar;
+        PS.g.spar = spar;
+        PS.g.alpha = alpha;
+        PS.g.vbits = vbits;
+        PS.g.nmax = s->d_count + 1;
+        PS.g.qpar = qpar16;
+        PS.g.tau = tau;
+        PS.g.bins = bins;
+        PS.g.cnt = cnt;
+        PS.g.cand = cand;
+        PS.g.err = s->d_err;
+        PS.g.dump = nullptr;
+        PS.g.dump_ld = 0;
+        PS.g.nq = nq;
+        PS.g.k = k;
+        PS.g.cap = L.cap;
+        PS.g.nsub = nsub_s;
+        PS.g.subcap = subcap_s;
+        PS.g.kblocks = (int)(s->ldb / scr::kBK);
+        R.kc = k_class_of(a.k);
+        rc = run_screen(R, false, L.pair, nctas_s, tmq16, PS);
         if (rc) return rc;
-        rc = launch_select(nsub_s, subcap_s, qpar16, seed);
+        rc = launch_select(R, nsub_s, subcap_s, qpar16, seed);
         if (rc) return rc;
-        kernels += 5;
+        R.kernels += 5;
     }
 
     if (f8)
@@ -2353,69 +2471,106 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                                                                               a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
     // a single cosine query: the streamed screen, one candidate list
-    const bool stream = norm && !f8 && nq <= kStreamQ && (size_t)nq * s->ldb * sizeof(float) <= (size_t)kStreamQBytes;
-    const int nsub_use = stream ? 1 : L.nsub, subcap_use = stream ? L.cap : L.subcap;
-    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, nsub_use, flags, nq, k, alpha,
-                                                                         redo_n, dstats, seed);
+    R.stream = maxsub_ext <= 0 && norm && !f8 && nq <= kStreamQ &&
+               (size_t)nq * s->ldb * sizeof(float) <= (size_t)kStreamQBytes;
+    R.nsub_use = R.stream ? 1 : L.nsub;
+    R.subcap_use = R.stream ? L.cap : L.subcap;
+    k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, R.nsub_use, flags, nq, k,
+                                                                         alpha, redo_n, dstats, seed);
     SVDB_LAUNCH_CHECK();
     k_row_params<<<(unsigned)((L.npad + 255) / 256), 256, 0, s->stream>>>(
         s->rowp, s->sq64, s->live, (int64_t)s->slots, (int64_t)L.npad, a.metric, f8 ? s->rowpn8 : s->rowpn,
         f8 && !norm ? s->rowp8 : nullptr, rpar, spar, alpha, vbits);
     SVDB_LAUNCH_CHECK();
-    kernels += 3;
+    R.kernels += 3;
+    if (R.stream) return SVDB_OK;
 
-    if (stream) {
-        float* keys = reinterpret_cast<float*>(spar);  // nq x npad floats: the cosine screen does not use spar
-        float* tmax = reinterpret_cast<float*>(base + L.tmax);
-        float* cut = reinterpret_cast<float*>(base + L.cut);
-        const int KB = (int)(s->ldb / scr::kBK);
-        const size_t smem = stream_smem((size_t)nq, s->ldb);
-        if (!gc->stream_attr) {
-            SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamQBytes));
-            gc->stream_attr = true;
-        }
-        k_stream_keys<<<(unsigned)L.ntr, 32 * kStreamWarps, smem, s->stream>>>(
-            reinterpret_cast<const uint8_t*>(s->xbn), KB, qb, s->ldb, nq, vbits, L.npad, L.ntr, keys, tmax);
-        SVDB_LAUNCH_CHECK();
-        k_stream_cut<<<(unsigned)nq, 1024, 0, s->stream>>>(tmax, L.ntr * kStreamWarps, k, qpar, s->d_count + 1, cut);
-        SVDB_LAUNCH_CHECK();
-        k_stream_emit<<<(unsigned)(L.npad / 256), 256, 0, s->stream>>>(keys, L.npad, nq, cut, L.cap, cnt, cand);
-        SVDB_LAUNCH_CHECK();
-        kernels += 3;
-    } else {
-    CUtensorMap tmq;
-    rc = f8 ? make_map8(gc, &tmq, qb, a.nq, s->ldb8, scr::kBM) : make_map(gc, &tmq, qb, a.nq, s->ldb, scr::kBM);
+    rc = f8 ? make_map8(gc, &R.tmq, qb, a.nq, s->ldb8, scr::kBM) : make_map(gc, &R.tmq, qb, a.nq, s->ldb, scr::kBM);
     if (rc) return rc;
+    GroupParams& g = R.P.g;
+    g.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
+                                              : norm ? (const void*)s->xbn : (const void*)s->xb);
+    g.qscale = qscale;
+    g.rpar = rpar;
+    g.spar = spar;
+    g.alpha = alpha;
+    g.vbits = vbits;
+    g.nmax = s->d_count + (f8 ? 3 : 1);
+    g.qpar = qpar;
+    g.tau = tau;
+    g.bins = bins;
+    g.cnt = cnt;
+    g.cand = cand;
+    g.err = s->d_err;  // persistent: read at the next synchronous point
+    g.dump = nullptr;
+    g.dump_ld = 0;
+    g.nq = nq;
+    g.k = k;
+    g.cap = L.cap;
+    g.nsub = L.nsub;
+    g.subcap = L.subcap;
+    g.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
+    R.P.sched = L.sched;
+    return SVDB_OK;
+}
 
-    ScreenParams P;
-    P.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
-                                                 : norm ? (const void*)s->xbn : (const void*)s->xb);
-    P.qscale = qscale;
-    P.rpar = rpar;
-    P.spar = spar;
-    P.alpha = alpha;
-    P.vbits = vbits;
-    P.nmax = s->d_count + (f8 ? 3 : 1);
-    P.qpar = qpar;
-    P.tau = tau;
-    P.bins = bins;
-    P.cnt = cnt;
-    P.cand = cand;
-    P.err = s->d_err;  // persistent: read at the next synchronous point
-    P.nq = nq;
-    P.k = k;
-    P.cap = L.cap;
-    P.nsub = L.nsub;
-    P.subcap = L.subcap;
-    P.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
-    P.sched = L.sched;
-    rc = run_screen(f8, L.pair, L.nctas, tmq, P);
-    if (rc) return rc;
-    ++kernels;
+// the search's own screen: streamed (a single cosine query) or tensor-core
+static int bf16_screen(Bf16Run& R) {
+    Store* s = R.s;
+    const Bf16Layout& L = R.L;
+    if (!R.stream) {
+        const int rc = run_screen(R, R.f8, L.pair, L.nctas, R.tmq, R.P);
+        if (rc) return rc;
+        ++R.kernels;
+        return SVDB_OK;
     }
-    s->prof_mark(2);
+    const int nq = (int)R.a.nq, k = (int)R.a.k;
+    float* keys = R.at<float>(L.spar);  // nq x npad floats: the cosine screen does not use spar
+    float* tmax = R.at<float>(L.tmax);
+    float* cut = R.at<float>(L.cut);
+    const int KB = (int)(s->ldb / scr::kBK);
+    const size_t smem = stream_smem((size_t)nq, s->ldb);
+    if (!R.gc->stream_attr) {
+        SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamQBytes));
+        R.gc->stream_attr = true;
+    }
+    k_stream_keys<<<(unsigned)L.ntr, 32 * kStreamWarps, smem, s->stream>>>(
+        reinterpret_cast<const uint8_t*>(s->xbn), KB, R.at<__nv_bfloat16>(L.qb), s->ldb, nq, R.at<uint32_t>(L.vbits),
+        L.npad, L.ntr, keys, tmax);
+    SVDB_LAUNCH_CHECK();
+    k_stream_cut<<<(unsigned)nq, 1024, 0, s->stream>>>(tmax, L.ntr * kStreamWarps, k, R.at<float4>(L.qpar),
+                                                        s->d_count + 1, cut);
+    SVDB_LAUNCH_CHECK();
+    k_stream_emit<<<(unsigned)(L.npad / 256), 256, 0, s->stream>>>(keys, L.npad, nq, cut, L.cap, R.at<int>(L.cnt),
+                                                                   R.at<int2>(L.cand));
+    SVDB_LAUNCH_CHECK();
+    R.kernels += 3;
+    return SVDB_OK;
+}
 
-    rc = launch_select(nsub_use, subcap_use, qpar, nullptr);
+// select, refinement, re-rank and the exact redo, on the store's stream
+static int bf16_end(Bf16Run& R, svdb_search_stats* st) {
+    Store* s = R.s;
+    const SearchArgs& a = R.a;
+    const Bf16Layout& L = R.L;
+    GemmPlanCache* gc = R.gc;
+    const int nq = (int)a.nq, k = (int)a.k;
+    float4* qpar = R.at<float4>(L.qpar);
+    float4* rpar = R.at<float4>(L.rpar);
+    int* cnt = R.at<int>(L.cnt);
+    int2* cand = R.at<int2>(L.cand);
+    int2* surv = R.at<int2>(L.surv);
+    int* nsurv = R.at<int>(L.nsurv);
+    int* nref = R.at<int>(L.nref);
+    int* sig = R.at<int>(L.sig);
+    int* perm = R.at<int>(L.perm);
+    uint8_t* flags = R.at<uint8_t>(L.flags);
+    int* redo = R.at<int>(L.redo);
+    int* redo_n = R.at<int>(L.redo_n);
+    unsigned long long* dstats = R.at<unsigned long long>(L.stats);
+    float* q32 = R.at<float>(L.q32);
+
+    int rc = launch_select(R, R.nsub_use, R.subcap_use, qpar, nullptr);
     if (rc) return rc;
     s->prof_mark(3);
     const size_t ref_smem = s->ld * sizeof(float);
@@ -2435,7 +2590,7 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         }
         k_sort_queries<<<1, 1024, (size_t)n2 * sizeof(unsigned long long), s->stream>>>(sig, nq, n2, perm);
         SVDB_LAUNCH_CHECK();
-        ++kernels;
+        ++R.kernels;
         order = perm;
     }
     // the candidate list (cap >= 8192 entries per query) is dead after the select:
@@ -2450,9 +2605,9 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         k_refine_keep<<<(unsigned)nq, kRefThreads, 0, s->stream>>>(surv, nsurv, nref, reinterpret_cast<float2*>(cand),
                                                                     (size_t)L.cap, k, flags);
         SVDB_LAUNCH_CHECK();
-        ++kernels;
+        ++R.kernels;
     }
-    kernels += 2;
+    R.kernels += 2;
     s->prof_mark(4);
 
     {
@@ -2473,18 +2628,18 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
                 s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k, a.metric, (int)s->dim, rpar, qpar,
                 s->logical, a.ids, a.dists, a.err, flags);
         SVDB_LAUNCH_CHECK();
-        ++kernels;
+        ++R.kernels;
     }
 
     // queries the screen could not certify: exact FP64 scan, entirely on the
     // device (no host round trip; with nothing to redo the kernels exit at once)
-    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, nsub_use, nsurv, nref, nq, redo, redo_n,
-                                                                          dstats);
+    k_collect_redo<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(flags, cnt, R.nsub_use, nsurv, nref, nq, redo,
+                                                                          redo_n, dstats);
     SVDB_LAUNCH_CHECK();
     {
-        double* rq = reinterpret_cast<double*>(base + L.rq);
-        double* rsq = reinterpret_cast<double*>(base + L.rsq);
-        int64_t* rids = reinterpret_cast<int64_t*>(base + L.rres);
+        double* rq = R.at<double>(L.rq);
+        double* rsq = R.at<double>(L.rsq);
+        int64_t* rids = R.at<int64_t>(L.rres);
         double* rd = reinterpret_cast<double*>(rids + a.nq * a.k);
         double* re = rd + a.nq * a.k;
         k_gather_queries<<<(unsigned)nq, 256, 0, s->stream>>>(a.q, a.qsq, s->ld, redo, redo_n, rq, rsq);
@@ -2497,12 +2652,12 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         b.err = re;
         b.nq_dev = redo_n;
         uint32_t kk = 0;
-        rc = search_fp64(s, b, base + L.rscr, search_fp64_scratch(s, a.nq, a.k), &kk, false);
+        rc = search_fp64(s, b, R.base + L.rscr, search_fp64_scratch(s, a.nq, a.k), &kk, false);
         if (rc) return rc;
         k_scatter_results<<<(unsigned)((a.nq * a.k + 255) / 256), 256, 0, s->stream>>>(rids, rd, re, redo, redo_n,
                                                                                     (int)a.k, a.ids, a.dists, a.err);
         SVDB_LAUNCH_CHECK();
-        kernels += kk + 3;
+        R.kernels += kk + 3;
     }
     if (st) {  // statistics cost a host round trip: only when asked for
         unsigned long long h[5];
@@ -2515,9 +2670,236 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
         st->bound_failures += (uint32_t)h[4];
     }
     s->prof_mark(5);
-    if (st) st->kernels += kernels;
+    if (st) st->kernels += R.kernels;
     return SVDB_OK;
 }
+
+int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_bytes, svdb_search_stats* st, bool f8) {
+    Bf16Run* R = new (std::nothrow) Bf16Run();  // (the schedule table makes it ~9 KB)
+    if (!R) {
+        svdb_set_error("search_bf16: out of host memory");
+        return SVDB_ENOMEM;
+    }
+    int rc = bf16_begin(*R, s, a, scratch, scratch_bytes, f8, 0);
+    if (!rc) rc = bf16_screen(*R);
+    if (!rc) {
+        s->prof_mark(2);
+        rc = bf16_end(*R, st);
+    }
+    delete R;
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// fused screens: several BF16 searches, screened by one launch per running
+// top-k class
+// ---------------------------------------------------------------------------
+// A search's screen is one pass of tensor-core tiles over its store; a batch
+// spread over several stores (different dimensions, row counts and query
+// counts) screened one launch per search leaves SMs idle at the tail of each
+// launch and, for small searches, most of the launch.  A fused launch takes
+// the searches of one k class together: every search gets a share of the
+// launch's CTAs in proportion to its work (query tiles x store tiles x
+// (k blocks + epilogue weight)), given out greedily to the search with the
+// most work per CTA, and inside its share the single-search schedule
+// (screen_schedule).  Each CTA's segments then carry their search, whose
+// parameters and query tensor map travel in the launch's parameter space.
+struct FusedPlan {
+    struct Launch {
+        int kc = 0;
+        std::vector<int> items;  // search of each group slot
+        ScreenParamsMulti P;
+        int nctas = 0;
+    };
+    std::vector<FusedItem> items;
+    int metric = 0;
+    std::vector<int> maxsub;     // per item
+    std::vector<size_t> qoff;    // per item: offset of the screen's scratch after the padded queries
+    std::vector<size_t> bytes;   // per item
+    std::vector<int> launch_of, slot_of;
+    std::vector<Bf16Run*> runs;
+    std::vector<Launch*> launches;
+    ~FusedPlan() {
+        for (Bf16Run* r : runs) delete r;
+        for (Launch* l : launches) delete l;
+    }
+};
+
+// CTAs of the fused launch for each job, then the jobs' segments; false when
+// the launch's tables cannot hold the schedule
+static bool fused_schedule(const std::vector<int>& ntq, const std::vector<int>& ntr, const std::vector<int>& kb,
+                           int units, double epi_weight, ScreenSchedMulti& S, std::vector<int>& maxsub, int* nctas) {
+    const size_t n = ntq.size();
+    std::memset(&S, 0, sizeof(S));
+    if ((int)n > units) return false;
+    std::vector<double> w(n);
+    for (size_t i = 0; i < n; ++i) w[i] = (double)ntq[i] * ntr[i] * (kb[i] + epi_weight);
+    std::vector<int> u(n, 1);
+    for (int left = units - (int)n; left > 0; --left) {
+        size_t best = 0;
+        for (size_t i = 1; i < n; ++i)
+            if (w[i] / u[i] > w[best] / u[best]) best = i;
+        ++u[best];
+    }
+    int c = 0, gq = 0;
+    maxsub.assign(n, 1);
+    ScreenSched* one = new (std::nothrow) ScreenSched();
+    if (!one) return false;
+    bool ok = true;
+    for (size_t i = 0; i < n && ok; ++i) {
+        int ms = 1;
+        const int cg = screen_schedule(ntq[i], ntr[i], *one, &ms, u[i]);
+        if (c + cg > kMaxUnitsM || gq + ntq[i] > kMaxQTilesM) {
+            ok = false;
+            break;
+        }
+        for (int j = 0; j < cg; ++j) {
+            const int ns = one->direct ? 1 : one->nseg[j];
+            for (int sg = 0; sg < ns; ++sg) {
+                ScreenSeg e = one->direct ? ScreenSeg{0, ntr[i], (uint16_t)j, 0, 0, (uint16_t)j} : one->seg[j][sg];
+                e.grp = (uint16_t)i;
+                e.gq = (uint16_t)(gq + e.qt);
+                S.seg[c + j][sg] = e;
+            }
+            S.nseg[c + j] = (uint8_t)ns;
+        }
+        for (int q = 0; q < ntq[i]; ++q) S.nsq[gq + q] = one->direct ? 1 : one->nsq[q];
+        maxsub[i] = ms;
+        c += cg;
+        gq += ntq[i];
+    }
+    delete one;
+    S.direct = 0;
+    *nctas = c;
+    return ok;
+}
+
+int fused_create(const std::vector<FusedItem>& items, int metric, double epi_weight, FusedPlan** out,
+                 std::vector<size_t>* bytes) {
+    *out = nullptr;
+    FusedPlan* p = new (std::nothrow) FusedPlan();
+    if (!p) {
+        svdb_set_error("fused screen: out of host memory");
+        return SVDB_ENOMEM;
+    }
+    p->items = items;
+    p->metric = metric;
+    const size_t n = items.size();
+    p->maxsub.assign(n, 1);
+    p->launch_of.assign(n, -1);
+    p->slot_of.assign(n, -1);
+    // launches: one per k class, at most kMaxGroups searches each
+    for (int kc = 0; kc < 3; ++kc) {
+        FusedPlan::Launch* cur = nullptr;
+        for (size_t i = 0; i < n; ++i) {
+            if (k_class_of(items[i].k) != kc) continue;
+            if (!cur || cur->items.size() == (size_t)kMaxGroups) {
+                cur = new (std::nothrow) FusedPlan::Launch();
+                if (!cur) {
+                    delete p;
+                    svdb_set_error("fused screen: out of host memory");
+                    return SVDB_ENOMEM;
+                }
+                cur->kc = kc;
+                p->launches.push_back(cur);
+            }
+            p->launch_of[i] = (int)p->launches.size() - 1;
+            p->slot_of[i] = (int)cur->items.size();
+            cur->items.push_back((int)i);
+        }
+    }
+    const int units = num_sms();
+    for (FusedPlan::Launch* l : p->launches) {
+        std::vector<int> ntq, ntr, kb, ms;
+        for (int i : l->items) {
+            const Store* s = items[i].s;
+            ntq.push_back((int)((items[i].nq + scr::kBM - 1) / scr::kBM));
+            ntr.push_back((int)((std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN));
+            kb.push_back((int)(s->ldb / scr::kBK));
+        }
+        if (!fused_schedule(ntq, ntr, kb, units, epi_weight, l->P.sched, ms, &l->nctas)) {
+            delete p;
+            svdb_set_error("fused screen: the searches do not fit one launch's schedule");
+            return SVDB_EINVAL;
+        }
+        for (size_t j = 0; j < l->items.size(); ++j) p->maxsub[l->items[j]] = ms[j];
+    }
+    bytes->assign(n, 0);
+    p->qoff.assign(n, 0);
+    for (size_t i = 0; i < n; ++i) {
+        const Store* s = items[i].s;
+        p->qoff[i] = round_up(items[i].nq * s->ld * sizeof(double), 1024) + round_up(items[i].nq * sizeof(double), 1024);
+        (*bytes)[i] = p->qoff[i] + bf16_layout(s, items[i].nq, p->maxsub[i]).total;
+        Bf16Run* r = new (std::nothrow) Bf16Run();
+        if (!r) {
+            delete p;
+            svdb_set_error("fused screen: out of host memory");
+            return SVDB_ENOMEM;
+        }
+        p->runs.push_back(r);
+    }
+    p->bytes = *bytes;
+    *out = p;
+    return SVDB_OK;
+}
+
+void fused_set_scratch(FusedPlan* p, size_t i, void* scratch) { p->items[i].scratch = scratch; }
+
+size_t fused_launches(const FusedPlan* p) { return p->launches.size(); }
+
+int fused_begin(FusedPlan* p, size_t i) {
+    const FusedItem& it = p->items[i];
+    Store* s = it.s;
+    uint8_t* base = reinterpret_cast<uint8_t*>(it.scratch);
+    double* qbuf = reinterpret_cast<double*>(base);
+    double* qsq = reinterpret_cast<double*>(base + round_up(it.nq * s->ld * sizeof(double), 1024));
+    int rc = prep_queries_fp64(s, it.q, s->dim, it.nq, qbuf, qsq);
+    if (rc) return rc;
+    SearchArgs a;
+    a.q = qbuf;
+    a.qsq = qsq;
+    a.nq = it.nq;
+    a.k = it.k;
+    a.metric = p->metric;
+    a.seed = it.seed;
+    a.ids = it.ids;
+    a.dists = it.dists;
+    a.err = nullptr;
+    Bf16Run& R = *p->runs[i];
+    rc = bf16_begin(R, s, a, base + p->qoff[i], p->bytes[i] - p->qoff[i], false, p->maxsub[i]);
+    if (rc) return rc;
+    FusedPlan::Launch* l = p->launches[p->launch_of[i]];
+    l->P.map[p->slot_of[i]] = R.tmq;
+    l->P.grp[p->slot_of[i]] = R.P.g;
+    return SVDB_OK;
+}
+
+int fused_screen(FusedPlan* p, size_t li, cudaStream_t st) {
+    FusedPlan::Launch* l = p->launches[li];
+    if (l->nctas == 0) return SVDB_OK;
+    const bool norm = p->metric == SVDB_COSINE;
+    auto kern = l->kc == 0 ? (norm ? k_screen_bf16<16, true, false, false, false, true>
+                                   : k_screen_bf16<16, false, false, false, false, true>)
+              : l->kc == 1 ? (norm ? k_screen_bf16<32, true, false, false, false, true>
+                                   : k_screen_bf16<32, false, false, false, false, true>)
+                           : (norm ? k_screen_bf16<0, true, false, false, false, true>
+                                   : k_screen_bf16<0, false, false, false, false, true>);
+    static bool attr[6] = {};
+    const int v = 2 * l->kc + (norm ? 1 : 0);
+    const size_t smem = sizeof(scr::Smem) + 1024;
+    if (!attr[v]) {
+        SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr[v] = true;
+    }
+    const CUtensorMap& any = l->P.map[0];
+    kern<<<(unsigned)l->nctas, scr::kThreads, smem, st>>>(any, any, l->P);
+    SVDB_LAUNCH_CHECK();
+    return SVDB_OK;
+}
+
+int fused_end(FusedPlan* p, size_t i) { return bf16_end(*p->runs[i], nullptr); }
+
+void fused_destroy(FusedPlan* p) { delete p; }
 
 // ---------------------------------------------------------------------------
 // self-test of the bounded waits (no fault, no hang)
@@ -2638,19 +3020,19 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
     if (rc) return rc;
     ScreenParams P;
     std::memset(&P, 0, sizeof(P));
-    P.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
+    P.g.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
                                                  : norm ? (const void*)s->xbn : (const void*)s->xb);
-    P.qscale = qscale;
-    P.spar = reinterpret_cast<const float4*>(base + o_spar);
-    P.alpha = reinterpret_cast<const int*>(base + o_alpha);
-    P.nmax = s->d_count + (f8 ? 3 : 1);
-    P.qpar = qpar;
-    P.err = s->d_err;
-    P.dump = dump;
-    P.dump_ld = dld;
-    P.nq = (int)nq;
-    P.k = 1;
-    P.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
+    P.g.qscale = qscale;
+    P.g.spar = reinterpret_cast<const float4*>(base + o_spar);
+    P.g.alpha = reinterpret_cast<const int*>(base + o_alpha);
+    P.g.nmax = s->d_count + (f8 ? 3 : 1);
+    P.g.qpar = qpar;
+    P.g.err = s->d_err;
+    P.g.dump = dump;
+    P.g.dump_ld = dld;
+    P.g.nq = (int)nq;
+    P.g.k = 1;
+    P.g.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
     P.sched.direct = 1;
     P.sched.ntr = (int)ntiles;
     // more than 128 queries: the paired form (one cluster of two CTAs, M = 256)
@@ -2667,7 +3049,7 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
         CUtensorMap tmx;
         const size_t kbl = f8 ? s->ldb8 / (2 * scr::kBK) : s->ldb / scr::kBK;
         const size_t ntr_all = (std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN;
-        rc = make_map_tiles(gc, &tmx, P.xblk, ntr_all * kbl * scr::kBN);
+        rc = make_map_tiles(gc, &tmx, P.g.xblk, ntr_all * kbl * scr::kBN);
         if (!rc) rc = launch_screen(kern, true, 1, gc->screen_smem_pair, s->stream, tmq, tmx, P);
     }
     if (rc) return rc;
@@ -2676,7 +3058,7 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
     std::vector<uint8_t> hx;
     if (rops) {
         hx.resize(dld * ob);
-        SVDB_CUDA(cudaMemcpyAsync(hx.data(), P.xblk, hx.size(), cudaMemcpyDeviceToHost, s->stream));
+        SVDB_CUDA(cudaMemcpyAsync(hx.data(), P.g.xblk, hx.size(), cudaMemcpyDeviceToHost, s->stream));
     }
     if (qops) SVDB_CUDA(cudaMemcpyAsync(qops, qb, nq * ob, cudaMemcpyDeviceToHost, s->stream));
     SVDB_CUDA(cudaStreamSynchronize(s->stream));

@@ -20,7 +20,12 @@
 //                 at the same time (a screen fills the SMs another part's
 //                 screen leaves idle at its tail); 0: one part after another;
 //   screen     (cosine with a tensor-core precision) per store, the BF16 or
-//              the FP8 screen.
+//              the FP8 screen;
+//   fused      1: the BF16 searches' screens run as one tensor-core launch per
+//              k class over all stores (work split in proportion to each
+//              search's tiles, see dev_gemm.cu), their other phases on the
+//              stores' streams; 0: every search launches its own screen.  The
+//              autotuner also tries the fused schedule's epilogue weight.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -28,6 +33,7 @@
 #include <vector>
 
 #include "dev_common.cuh"
+#include "dev_search.cuh"
 #include "dev_store.cuh"
 
 namespace svdb {
@@ -72,6 +78,7 @@ struct Part {
 // one search of a run: `n` queries of part `part` with k = kg
 struct Group {
     int part = 0, n = 0, kg = 0;
+    int fidx = -1;  // its index in the fused plan (-1: screened by a launch of its own)
     int* d_idx = nullptr;   // rows of the part (nullptr: all of them, in order)
     double* d_q = nullptr;  // gathered queries (nullptr: the part's own buffer)
     int64_t* d_ids = nullptr;
@@ -95,11 +102,32 @@ struct Plan {
     float tuned_ms[4] = {0, 0, 0, 0};
     float swap_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint32_t captures = 0;
+    // fused screens
+    int fused = 0;
+    double epi_weight = 2.0;
+    FusedPlan* fp = nullptr;
+    std::vector<void*> fscratch;
+    std::vector<uint64_t> fepochs;  // store epochs the fused plan was made for
+    cudaEvent_t ev_screen = nullptr;
+    float fused_ms[2] = {0, 0};
+    float weight_ms[3] = {0, 0, 0};
+    int seed = -1;  // SearchArgs::seed of every search (the autotuner tries 1)
+    float seed_ms = 0;
 };
 
 int k_class(uint32_t k) { return k <= 16 ? 0 : (k <= 32 ? 1 : 2); }
 
+void free_fused(Plan* p) {
+    if (p->fp) fused_destroy(p->fp);
+    p->fp = nullptr;
+    for (void* b : p->fscratch) cudaFree(b);
+    p->fscratch.clear();
+    p->fepochs.clear();
+    for (Group& g : p->groups) g.fidx = -1;
+}
+
 void free_groups(Plan* p) {
+    free_fused(p);
     for (Group& g : p->groups) {
         cudaFree(g.d_idx);
         cudaFree(g.d_q);
@@ -153,12 +181,62 @@ int make_groups(Plan* p) {
     return SVDB_OK;
 }
 
+bool fused_current(const Plan* p) {
+    if (!p->fp || p->fepochs.size() != p->stores.size()) return false;
+    for (size_t i = 0; i < p->stores.size(); ++i)
+        if (p->stores[i]->epoch != p->fepochs[i]) return false;
+    return true;
+}
+
+// the fused plan over the searches that can take part (BF16 screen, a store
+// the screen certifies), with its scratch; made again when a store changes
+int build_fused(Plan* p) {
+    free_fused(p);
+    std::vector<FusedItem> items;
+    std::vector<int> gi;
+    for (size_t g = 0; g < p->groups.size(); ++g) {
+        const Group& G = p->groups[g];
+        const Part& P = p->parts[G.part];
+        const size_t si = std::find(p->stores.begin(), p->stores.end(), P.s) - p->stores.begin();
+        if (p->sprec[si] != SVDB_PREC_BF16 || !bf16_supported(P.s, (size_t)G.kg)) continue;
+        FusedItem it;
+        it.s = P.s;
+        it.seed = p->seed;
+        it.q = G.d_q ? G.d_q : P.q;
+        it.nq = (size_t)G.n;
+        it.k = (size_t)G.kg;
+        it.ids = G.d_ids;
+        it.dists = G.d_dists;
+        items.push_back(it);
+        gi.push_back((int)g);
+    }
+    if (items.empty()) return SVDB_OK;
+    std::vector<size_t> bytes;
+    int rc = fused_create(items, p->metric, p->epi_weight, &p->fp, &bytes);
+    if (rc) return rc;
+    for (size_t i = 0; i < items.size(); ++i) {
+        void* b = nullptr;
+        const cudaError_t e = cudaMalloc(&b, std::max<size_t>(bytes[i], 256));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            free_fused(p);
+            svdb_set_error("ragged plan: cannot allocate fused screen scratch: %s", cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? SVDB_ENOMEM : SVDB_ECUDA;
+        }
+        p->fscratch.push_back(b);
+        fused_set_scratch(p->fp, i, b);
+        p->groups[gi[i]].fidx = (int)i;
+    }
+    for (Store* s : p->stores) p->fepochs.push_back(s->epoch);
+    return SVDB_OK;
+}
+
 // the searches of one part's store (the plan's i-th), on that store's stream
 int enqueue_store(Plan* p, size_t si) {
     Store* s = p->stores[si];
     for (const Group& g : p->groups) {
         const Part& P = p->parts[g.part];
-        if (P.s != s) continue;
+        if (P.s != s || (p->fused && g.fidx >= 0)) continue;
         const double* q = P.q;
         if (g.d_idx) {
             const size_t total = (size_t)g.n * s->dim;
@@ -167,8 +245,8 @@ int enqueue_store(Plan* p, size_t si) {
             SVDB_LAUNCH_CHECK();
             q = g.d_q;
         }
-        int rc = svdbd_search(reinterpret_cast<svdbd_store*>(s), q, (size_t)g.n, (size_t)g.kg, p->metric,
-                              p->sprec[si], g.d_ids, g.d_dists, nullptr, 1, nullptr);
+        int rc = search_seeded(s, q, (size_t)g.n, (size_t)g.kg, p->metric, p->sprec[si], g.d_ids, g.d_dists,
+                               nullptr, 1, nullptr, p->seed);
         if (rc) return rc;
         const size_t total = (size_t)g.n * P.stride;
         k_ragged_scatter<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s->stream>>>(
@@ -178,8 +256,75 @@ int enqueue_store(Plan* p, size_t si) {
     return SVDB_OK;
 }
 
+// the fused searches' phases before (phase 0) or after (phase 1) their
+// screens, on store si's stream; phase 0 also runs the store's other searches
+int enqueue_fused_store(Plan* p, size_t si, int phase) {
+    Store* s = p->stores[si];
+    if (phase == 0) {
+        int rc = enqueue_store(p, si);
+        if (rc) return rc;
+    }
+    for (const Group& g : p->groups) {
+        const Part& P = p->parts[g.part];
+        if (P.s != s || g.fidx < 0) continue;
+        if (phase == 0) {
+            if (g.d_idx) {
+                const size_t total = (size_t)g.n * s->dim;
+                k_ragged_gather<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s->stream>>>(
+                    P.q, s->dim, g.d_idx, g.n, g.d_q);
+                SVDB_LAUNCH_CHECK();
+            }
+            int rc = fused_begin(p->fp, (size_t)g.fidx);
+            if (rc) return rc;
+        } else {
+            int rc = fused_end(p->fp, (size_t)g.fidx);
+            if (rc) return rc;
+            const size_t total = (size_t)g.n * P.stride;
+            k_ragged_scatter<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s->stream>>>(
+                g.d_ids, g.d_dists, g.kg, g.d_idx, g.n, P.d_k, P.stride, P.ids, P.dists);
+            SVDB_LAUNCH_CHECK();
+        }
+    }
+    return SVDB_OK;
+}
+
+// a run with fused screens: every store's first phase at once, the fused
+// launches on the origin stream, then every store's second phase
+int enqueue_fused(Plan* p) {
+    SVDB_CUDA(cudaEventRecord(p->ev_fork, p->origin));
+    for (size_t i = 0; i < p->stores.size(); ++i) {
+        Store* s = p->stores[i];
+        SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->ev_fork, 0));
+        int rc = enqueue_fused_store(p, i, 0);
+        if (rc) return rc;
+        SVDB_CUDA(cudaEventRecord(p->ev_store[i], s->stream));
+    }
+    for (size_t i = 0; i < p->stores.size(); ++i) SVDB_CUDA(cudaStreamWaitEvent(p->origin, p->ev_store[i], 0));
+    for (size_t l = 0; l < fused_launches(p->fp); ++l) {
+        int rc = fused_screen(p->fp, l, p->origin);
+        if (rc) return rc;
+    }
+    SVDB_CUDA(cudaEventRecord(p->ev_screen, p->origin));
+    for (size_t i = 0; i < p->stores.size(); ++i) {
+        Store* s = p->stores[i];
+        SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->ev_screen, 0));
+        int rc = enqueue_fused_store(p, i, 1);
+        if (rc) return rc;
+        SVDB_CUDA(cudaEventRecord(p->ev_store[i], s->stream));
+    }
+    for (size_t i = 0; i < p->stores.size(); ++i) SVDB_CUDA(cudaStreamWaitEvent(p->origin, p->ev_store[i], 0));
+    return SVDB_OK;
+}
+
 // one run, forked from and joined back to the origin stream (captured or not)
 int enqueue(Plan* p) {
+    if (p->fused) {
+        if (!fused_current(p)) {
+            int rc = build_fused(p);
+            if (rc) return rc;
+        }
+        if (p->fp) return enqueue_fused(p);
+    }
     SVDB_CUDA(cudaEventRecord(p->ev_fork, p->origin));
     cudaEvent_t prev = p->ev_fork;
     for (size_t i = 0; i < p->stores.size(); ++i) {
@@ -272,11 +417,13 @@ int run(Plan* p) {
     return SVDB_OK;
 }
 
-int configure(Plan* p, int grouping, int concurrent) {
+int configure(Plan* p, int grouping, int concurrent, int fused = 0) {
     drop_graph(p);
     const bool regroup = p->groups.empty() || grouping != p->grouping;
     p->grouping = grouping;
     p->concurrent = concurrent;
+    p->fused = fused;
+    if (!fused) free_fused(p);
     return regroup ? make_groups(p) : SVDB_OK;
 }
 
@@ -324,23 +471,64 @@ int autotune(Plan* p) {
     bool mixed = false;  // does any part hold queries of more than one k class?
     for (const Part& P : p->parts)
         for (size_t i = 1; i < P.nq && !mixed; ++i) mixed = k_class(P.hk[i]) != k_class(P.hk[0]);
-    const int cfg[4][2] = {{0, 1}, {1, 1}, {0, 0}, {1, 0}};
+    // (grouping, concurrent, fused); the fused screen runs every store's
+    // other phases concurrently
+    const int cfg[6][3] = {{0, 1, 0}, {1, 1, 0}, {0, 0, 0}, {1, 0, 0}, {0, 1, 1}, {1, 1, 1}};
+    const bool tc = p->precision != SVDB_PREC_FP64;
+    float ms[6] = {0, 0, 0, 0, 0, 0};
     int best = -1;
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < 6; ++c) {
         if (cfg[c][0] && !mixed) continue;
         if (!cfg[c][1] && p->stores.size() < 2) continue;
-        int rc = configure(p, cfg[c][0], cfg[c][1]);
-        if (!rc) rc = time_config(p, 3, best < 0 ? 1e30f : 1.5f * p->tuned_ms[best], &p->tuned_ms[c]);
+        if (cfg[c][2] && !tc) continue;
+        int rc = configure(p, cfg[c][0], cfg[c][1], cfg[c][2]);
+        if (!rc) rc = time_config(p, 3, best < 0 ? 1e30f : 1.5f * ms[best], &ms[c]);
         if (rc) return rc;
-        if (best < 0 || p->tuned_ms[c] < p->tuned_ms[best]) best = c;
+        if (best < 0 || ms[c] < ms[best]) best = c;
     }
-    int rc = configure(p, cfg[best][0], cfg[best][1]);
-    if (rc || p->metric != SVDB_COSINE || p->precision == SVDB_PREC_FP64) return rc;
-    float best_ms = p->tuned_ms[best];
+    for (int c = 0; c < 4; ++c) p->tuned_ms[c] = ms[c];
+    p->fused_ms[0] = ms[4];
+    p->fused_ms[1] = ms[5];
+    int rc = configure(p, cfg[best][0], cfg[best][1], cfg[best][2]);
+    if (rc) return rc;
+    float best_ms = ms[best];
+    if (p->fused) {  // the fused schedule's epilogue weight (work per tile beyond its k blocks)
+        const double w[3] = {1.0, 4.0, 8.0};
+        double keep = p->epi_weight;
+        for (int i = 0; i < 3; ++i) {
+            p->epi_weight = w[i];
+            drop_graph(p);
+            free_fused(p);
+            rc = time_config(p, 3, 1.5f * best_ms, &p->weight_ms[i]);
+            if (rc) return rc;
+            if (p->weight_ms[i] < best_ms) {
+                best_ms = p->weight_ms[i];
+                keep = w[i];
+            }
+        }
+        p->epi_weight = keep;
+        drop_graph(p);
+        free_fused(p);
+    }
+    if (tc) {  // thresholds seeded from a sample of each store (BF16 screens too)
+        p->seed = 1;
+        drop_graph(p);
+        free_fused(p);
+        rc = time_config(p, 3, 1.5f * best_ms, &p->seed_ms);
+        if (rc) return rc;
+        if (p->seed_ms < best_ms)
+            best_ms = p->seed_ms;
+        else
+            p->seed = -1;
+        drop_graph(p);
+        free_fused(p);
+    }
+    if (p->metric != SVDB_COSINE || p->precision == SVDB_PREC_FP64) return SVDB_OK;
     for (size_t i = 0; i < p->stores.size() && i < 8; ++i) {
         const int keep = p->sprec[i];
         p->sprec[i] = keep == SVDB_PREC_BF16 ? SVDB_PREC_FP8 : SVDB_PREC_BF16;
         drop_graph(p);
+        free_fused(p);
         rc = time_config(p, 3, 1.5f * best_ms, &p->swap_ms[i]);
         if (rc) return rc;
         if (p->swap_ms[i] < best_ms)
@@ -349,6 +537,7 @@ int autotune(Plan* p) {
             p->sprec[i] = keep;
     }
     drop_graph(p);
+    free_fused(p);
     return SVDB_OK;
 }
 
@@ -358,7 +547,7 @@ void destroy(Plan* p) {
     free_groups(p);
     for (Part& P : p->parts) cudaFree(P.d_k);
     for (cudaEvent_t e : p->ev_store) cudaEventDestroy(e);
-    for (cudaEvent_t e : {p->ev_fork, p->ev_done, p->ev_t0, p->ev_t1})
+    for (cudaEvent_t e : {p->ev_fork, p->ev_done, p->ev_t0, p->ev_t1, p->ev_screen})
         if (e) cudaEventDestroy(e);
     if (p->origin) cudaStreamDestroy(p->origin);
     delete p;
@@ -432,6 +621,7 @@ svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts,
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&p->ev_t0);
     if (e == cudaSuccess) e = cudaEventCreate(&p->ev_t1);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_screen, cudaEventDisableTiming);
     for (size_t i = 0; i < p->stores.size() && e == cudaSuccess; ++i) {
         cudaEvent_t ev = nullptr;
         e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -447,7 +637,11 @@ svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts,
         if (rc) return fail(rc);
     }
     p->sprec.assign(p->stores.size(), precision);
-    rc = (flags & SVDB_RAGGED_AUTOTUNE) ? svdb::autotune(p) : svdb::configure(p, 0, 1);
+    if (flags & SVDB_RAGGED_SEED) p->seed = 1;
+    rc = (flags & SVDB_RAGGED_AUTOTUNE)
+             ? svdb::autotune(p)
+             : svdb::configure(p, (flags & SVDB_RAGGED_BY_K_CLASS) ? 1 : 0, 1,
+                               (flags & SVDB_RAGGED_FUSED) && precision != SVDB_PREC_FP64 ? 1 : 0);
     if (rc) return fail(rc);
     return reinterpret_cast<svdbd_ragged*>(p);
 }
@@ -474,6 +668,13 @@ int svdbd_ragged_info(svdbd_ragged* hp, svdb_ragged_info* out) {
     for (size_t i = 0; i < p->stores.size() && i < 32; ++i)
         if (p->sprec[i] == SVDB_PREC_FP8) out->fp8_stores |= 1u << i;
     for (int i = 0; i < 8; ++i) out->swap_ms[i] = p->swap_ms[i];
+    out->fused = p->fused && p->fp ? 1 : 0;
+    out->fused_launches = p->fp ? (int32_t)svdb::fused_launches(p->fp) : 0;
+    for (int i = 0; i < 2; ++i) out->fused_ms[i] = p->fused_ms[i];
+    for (int i = 0; i < 3; ++i) out->weight_ms[i] = p->weight_ms[i];
+    out->epi_weight = (float)p->epi_weight;
+    out->seeded = p->seed > 0 ? 1 : 0;
+    out->seed_ms = p->seed_ms;
     return SVDB_OK;
 }
 

@@ -360,7 +360,12 @@ static bool host_pinned(const void* p) {
 
 extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t k, int metric, int precision,
                             int64_t* ids, double* dists, double* err, int on_device, svdb_search_stats* st) {
-    Store* s = reinterpret_cast<Store*>(hs);
+    return search_seeded(reinterpret_cast<Store*>(hs), q, nq, k, metric, precision, ids, dists, err, on_device, st,
+                         -1);
+}
+
+int svdb::search_seeded(Store* s, const double* q, size_t nq, size_t k, int metric, int precision, int64_t* ids,
+                        double* dists, double* err, int on_device, svdb_search_stats* st, int seed) {
     if (k == 0 || k > 128 || metric < 0 || metric > 2 ||
         (precision != SVDB_PREC_FP64 && precision != SVDB_PREC_BF16 && precision != SVDB_PREC_FP8)) {
         svdb_set_error("search: bad argument (k=%zu metric=%d precision=%d; k must be 1..128)", k, metric, precision);
@@ -417,6 +422,7 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
     a.nq = nq;
     a.k = k;
     a.metric = metric;
+    a.seed = seed >= 0 ? seed : s->seed_mode;
     if (on_device) {
         a.ids = ids;
         a.dists = dists;

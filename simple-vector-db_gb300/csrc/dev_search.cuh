@@ -2,6 +2,8 @@
 // (dev_search.cu) and the BF16 screen + re-rank (dev_gemm.cu).
 #pragma once
 
+#include <vector>
+
 #include "dev_common.cuh"
 #include "dev_store.cuh"
 
@@ -24,6 +26,9 @@ struct SearchArgs {
     double* dists;       // nq x k (device)
     double* err;         // nq x k (device) or null
     const int* nq_dev = nullptr;  // if set: only the first *nq_dev queries are answered (device-side count)
+    // tensor-core screens: start the running thresholds from the exact k-th
+    // best lower bound over a sample of the rows (-1: for the FP8 screen only)
+    int seed = -1;
 };
 
 // FP64 bound on |computed - exact| for one result (see dev_search.cu)
@@ -51,6 +56,34 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 size_t search_bf16_scratch(const Store* s, size_t nq, size_t k);
 // the screen certifies k <= 128 on stores without unscreenable rows
 bool bf16_supported(const Store* s, size_t k);
+
+// Fused screens (dev_gemm.cu): several BF16 searches, on one or more stores,
+// screened by one tensor-core launch per running top-k class (k <= 16, <= 32,
+// <= 128); each search's other phases run on its store's stream.
+struct FusedItem {
+    Store* s = nullptr;
+    int seed = -1;              // SearchArgs::seed
+    const double* q = nullptr;  // device queries, nq x s->dim
+    size_t nq = 0, k = 0;       // 1 <= k <= 128; the store holds no unscreenable rows
+    int64_t* ids = nullptr;     // device outputs, nq x k
+    double* dists = nullptr;
+    void* scratch = nullptr;    // device, the size fused_create gave (set with fused_set_scratch)
+};
+struct FusedPlan;
+// the launches and their schedules, and each search's scratch size;
+// epi_weight: the schedule's cost of a tile's epilogue, in k blocks
+int fused_create(const std::vector<FusedItem>& items, int metric, double epi_weight, FusedPlan** out,
+                 std::vector<size_t>* bytes);
+void fused_set_scratch(FusedPlan* p, size_t i, void* scratch);
+size_t fused_launches(const FusedPlan* p);
+int fused_begin(FusedPlan* p, size_t i);  // search i's queries and row terms, on its store's stream
+int fused_screen(FusedPlan* p, size_t launch, cudaStream_t st);  // after every search's begin
+int fused_end(FusedPlan* p, size_t i);    // search i's select ... redo, on its store's stream (after the screen)
+void fused_destroy(FusedPlan* p);
+
+// svdbd_search with SearchArgs::seed chosen by the caller
+int search_seeded(Store* s, const double* q, size_t nq, size_t k, int metric, int precision, int64_t* ids,
+                  double* dists, double* err, int on_device, svdb_search_stats* st, int seed);
 
 int num_sms();
 

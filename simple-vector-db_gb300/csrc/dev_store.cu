@@ -95,9 +95,7 @@ __global__ void k_derive_rows(const double* __restrict__ x64, size_t ld, __nv_bf
     // range only loses E4M3 precision, which its residual term accounts for)
     int f = 0;
     if (mx > 0.0 && isfinite(mx)) {
-        f = (int)floor(log2(448.0 / mx));
-        while (mx * ldexp(1.0, f) > 448.0) --f;
-        f = max(-120, min(120, f));
+        f = max(-120, min(120, e4m3_fit_exp(mx)));
     }
     const double sc8 = ldexp(1.0, f);
     // second pass: the unit-norm row for the cosine screen, its BF16 and FP8
@@ -899,6 +897,10 @@ int svdbd_store_read_row(svdbd_store* hs, int64_t slot, double* out) {
 
 int svdbd_store_sync(svdbd_store* hs) { return reinterpret_cast<Store*>(hs)->sync(); }
 
+int svdbd_store_set_seeding(svdbd_store* hs, int mode) {
+    reinterpret_cast<Store*>(hs)->seed_mode = mode < 0 ? -1 : (mode ? 1 : 0);
+    return SVDB_OK;
+}
 int svdbd_store_profile(svdbd_store* hs, int enable) { return reinterpret_cast<Store*>(hs)->prof_enable(enable != 0); }
 
 int svdbd_store_profile_read(svdbd_store* hs, double* ms, int reset) {

@@ -85,6 +85,7 @@ struct Store {
     static constexpr int kProfRing = 64;
     static constexpr int kProfMarks = SVDB_NSTAGES + 1;
     bool prof = false;
+    int seed_mode = -1;  // tensor-core screens' threshold seeding: -1 the default rule, 0 off, 1 on
     bool prof_events = false;
     cudaEvent_t pev[kProfRing][kProfMarks];
     int prof_head = 0, prof_pending = 0, prof_cur = -1;

@@ -64,7 +64,9 @@ class RaggedInfo(C.Structure):
     """svdb_ragged_info (include/svdb_gb300.h)."""
     _fields_ = [("grouping", C.c_int32), ("concurrent", C.c_int32), ("graph", C.c_int32), ("searches", C.c_int32),
                 ("tuned_ms", C.c_float * 4), ("captures", C.c_uint32), ("fp8_stores", C.c_uint32),
-                ("swap_ms", C.c_float * 8)]
+                ("swap_ms", C.c_float * 8), ("fused", C.c_int32), ("fused_launches", C.c_int32),
+                ("fused_ms", C.c_float * 2), ("weight_ms", C.c_float * 3), ("epi_weight", C.c_float),
+                ("seeded", C.c_int32), ("seed_ms", C.c_float)]
 
 
 class LoopConfig(C.Structure):
@@ -82,7 +84,7 @@ class LoopInfo(C.Structure):
 LOOP_NOT_STARTED, LOOP_RUNNING, LOOP_LEFT_IDLE, LOOP_STOPPED, LOOP_LEAVING = range(5)
 REQ_KD_NEAREST = 5
 
-RAGGED_AUTOTUNE, RAGGED_NO_GRAPH = 1, 2
+RAGGED_AUTOTUNE, RAGGED_NO_GRAPH, RAGGED_FUSED, RAGGED_BY_K_CLASS, RAGGED_SEED = 1, 2, 4, 8, 16
 SAVE_EXACT_COUNT = 1
 
 
@@ -126,6 +128,7 @@ def _load():
         "svdb_wait": (C.c_int, [vp]),
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
+        "svdb_set_screen_seeding": (C.c_int, [vp, C.c_int]),
         "svdb_selftest_bounded_wait": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_uint32)]),
         "svdb_save": (C.c_int, [vp, C.c_char_p, C.c_uint]),
         "svdb_format_compare": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32), sz,
@@ -369,6 +372,10 @@ class VectorDatabase:
     def reserve(self, rows: int, dim: int) -> None:
         _check(lib.svdb_reserve(self.ptr, rows, dim), "svdb_reserve")
 
+    def set_screen_seeding(self, mode: int) -> None:
+        """svdb_set_screen_seeding: -1 default (FP8 only), 0 never, 1 always."""
+        _check(lib.svdb_set_screen_seeding(self.ptr, int(mode)), "svdb_set_screen_seeding")
+
     def profile(self, enable: bool = True) -> None:
         _check(lib.svdb_profile(self.ptr, int(enable)), "svdb_profile")
 
@@ -539,7 +546,10 @@ class RaggedPlan:
         _check(lib.svdb_ragged_get_info(self.ptr, C.byref(inf)), "svdb_ragged_get_info")
         return {"grouping": inf.grouping, "concurrent": inf.concurrent, "graph": inf.graph,
                 "searches": inf.searches, "tuned_ms": [float(x) for x in inf.tuned_ms], "captures": inf.captures,
-                "fp8_stores": inf.fp8_stores, "swap_ms": [float(x) for x in inf.swap_ms]}
+                "fp8_stores": inf.fp8_stores, "swap_ms": [float(x) for x in inf.swap_ms], "fused": inf.fused,
+                "fused_launches": inf.fused_launches, "fused_ms": [float(x) for x in inf.fused_ms],
+                "weight_ms": [float(x) for x in inf.weight_ms], "epi_weight": float(inf.epi_weight),
+                "seeded": inf.seeded, "seed_ms": float(inf.seed_ms)}
 
     def close(self) -> None:
         if getattr(self, "ptr", None):

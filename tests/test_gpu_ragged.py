@@ -78,6 +78,8 @@ def test_ragged_plan_matches_oracle(S, oracle, metric, precision):
     assert sum(t > 0 for t in info["tuned_ms"]) == 4  # mixed k classes, 3 stores: every layout was timed
     # cosine: each store's screen was also tried the other way (BF16 <-> FP8)
     assert sum(t > 0 for t in info["swap_ms"]) == (3 if metric == 0 else 0)
+    # tensor-core precisions: the fused screen was timed for both groupings
+    assert sum(t > 0 for t in info["fused_ms"]) == (2 if precision != S.PREC_FP64 else 0)
     for b in bufs:  # the plan's results are rewritten by the runs below
         b[1].fill_(7)
     plan.run()
@@ -109,6 +111,80 @@ def test_ragged_plan_each_choice_and_no_graph(S, oracle):
     plan.run()
     plan.run()
     plan.wait()
+    _check(oracle, 0, cols, bufs)
+    plan.close()
+    for db in dbs:
+        db.close()
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+@pytest.mark.parametrize("flags", ["fused_by_class", "fused_per_part", "fused_no_graph", "fused_seeded"])
+def test_ragged_fused_screen_matches_oracle(S, oracle, metric, flags):
+    """The BF16 searches of every store screened by one fused launch per k
+    class (the schedule splits each launch's CTAs among the searches), with a
+    fourth part on the first store so one store serves two searches of a
+    class: exact answers for every query with its own k."""
+    import torch
+    rng = np.random.default_rng(900 + metric)
+    cols = _collections(rng)
+    X0 = cols[0][0]
+    Qx = X0[rng.integers(0, X0.shape[0], 70)] + 0.01 * rng.normal(size=(70, X0.shape[1]))
+    kx = rng.integers(1, 129, 70)
+    kx[:3] = (128, 17, 2)
+    dbs = []
+    for X, _, _ in cols:
+        db = S.VectorDatabase(0, 3)
+        db.insert_batch(X)
+        dbs.append(db)
+    cols4 = cols + [(X0, Qx, kx)]
+    parts, bufs = _bind(S, cols4, dbs + [dbs[0]])
+    f = {"fused_by_class": S.RAGGED_FUSED | S.RAGGED_BY_K_CLASS, "fused_per_part": S.RAGGED_FUSED,
+         "fused_no_graph": S.RAGGED_FUSED | S.RAGGED_BY_K_CLASS | S.RAGGED_NO_GRAPH,
+         "fused_seeded": S.RAGGED_FUSED | S.RAGGED_BY_K_CLASS | S.RAGGED_SEED}[flags]
+    plan = S.RaggedPlan(parts, metric, S.PREC_BF16, f)
+    for b in bufs:
+        b[1].fill_(7)
+    plan.run()
+    plan.run()
+    plan.wait()
+    info = plan.info()
+    assert info["fused"] == 1 and info["seeded"] == (flags == "fused_seeded")
+    # one launch per k class present: every part holds all three; one search
+    # per part takes the part's largest k (> 32 in every part)
+    assert info["fused_launches"] == (3 if flags != "fused_per_part" else 1)
+    _check(oracle, metric, cols4, bufs)
+    torch.cuda.synchronize()
+    plan.close()
+    for db in dbs:
+        db.close()
+
+
+def test_ragged_fused_screen_after_store_changes(S, oracle):
+    """A fused plan is rebuilt for the stores' new shapes (more rows, fewer
+    live rows) before the graph is captured again."""
+    rng = np.random.default_rng(6)
+    cols = _collections(rng)
+    dbs = []
+    for X, _, _ in cols:
+        db = S.VectorDatabase(0, 3)
+        db.insert_batch(X)
+        dbs.append(db)
+    parts, bufs = _bind(S, cols, dbs)
+    plan = S.RaggedPlan(parts, 0, S.PREC_BF16, S.RAGGED_FUSED | S.RAGGED_BY_K_CLASS)
+    plan.run()
+    plan.wait()
+    _check(oracle, 0, cols, bufs)
+    X0, Q0, k0 = cols[0]
+    extra = X0[:3000] + 1e-3 * rng.normal(size=(3000, X0.shape[1]))
+    dbs[0].insert_batch(extra)
+    cols[0] = (np.vstack([X0, extra]), Q0, k0)
+    X1, Q1, k1 = cols[1]
+    for i in (3, 40):
+        dbs[1].delete(i)
+    cols[1] = (np.delete(X1, [3, 41], axis=0), Q1, k1)
+    plan.run()
+    plan.wait()
+    assert plan.info()["fused"] == 1
     _check(oracle, 0, cols, bufs)
     plan.close()
     for db in dbs:
