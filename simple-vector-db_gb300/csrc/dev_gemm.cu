@@ -2330,7 +2330,7 @@ static int launch_select(Bf16Run& R, int nsub_, int subcap_, const float4* qp_, 
     const int nq = (int)R.a.nq, k = (int)R.a.k;
     // small batches carry many candidates per query: wider blocks
     const int sel_threads = nq >= 256 ? 256 : 1024;
-    const size_t sel_smem = k <= 32 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;
+    const size_t sel_smem = R.kc <= 1 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;  // the running top-k variants
     if (!gc->select_attr) {
         SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
         SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
@@ -2846,6 +2846,7 @@ int fused_create(const std::vector<FusedItem>& items, int metric, double epi_wei
 void fused_set_scratch(FusedPlan* p, size_t i, void* scratch) { p->items[i].scratch = scratch; }
 
 size_t fused_launches(const FusedPlan* p) { return p->launches.size(); }
+int fused_launch_of(const FusedPlan* p, size_t i) { return p->launch_of[i]; }
 
 int fused_begin(FusedPlan* p, size_t i) {
     const FusedItem& it = p->items[i];

@@ -108,7 +108,7 @@ struct Plan {
     FusedPlan* fp = nullptr;
     std::vector<void*> fscratch;
     std::vector<uint64_t> fepochs;  // store epochs the fused plan was made for
-    cudaEvent_t ev_screen = nullptr;
+    std::vector<cudaEvent_t> ev_launch;  // per fused launch: its screen is done
     float fused_ms[2] = {0, 0};
     float weight_ms[3] = {0, 0, 0};
     int seed = -1;  // SearchArgs::seed of every search (the autotuner tries 1)
@@ -227,6 +227,17 @@ int build_fused(Plan* p) {
         fused_set_scratch(p->fp, i, b);
         p->groups[gi[i]].fidx = (int)i;
     }
+    while (p->ev_launch.size() < fused_launches(p->fp)) {  // (events outlive the fused plan: created once)
+        cudaEvent_t ev = nullptr;
+        const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            free_fused(p);
+            svdb_set_error("ragged plan: cannot create events: %s", cudaGetErrorString(e));
+            return SVDB_ECUDA;
+        }
+        p->ev_launch.push_back(ev);
+    }
     for (Store* s : p->stores) p->fepochs.push_back(s->epoch);
     return SVDB_OK;
 }
@@ -256,9 +267,10 @@ int enqueue_store(Plan* p, size_t si) {
     return SVDB_OK;
 }
 
-// the fused searches' phases before (phase 0) or after (phase 1) their
-// screens, on store si's stream; phase 0 also runs the store's other searches
-int enqueue_fused_store(Plan* p, size_t si, int phase) {
+// the fused searches' phases before (phase 0) or after (phase 1: those of
+// fused launch `launch`) their screens, on store si's stream; phase 0 also
+// runs the store's other searches
+int enqueue_fused_store(Plan* p, size_t si, int phase, int launch = -1) {
     Store* s = p->stores[si];
     if (phase == 0) {
         int rc = enqueue_store(p, si);
@@ -267,6 +279,7 @@ int enqueue_fused_store(Plan* p, size_t si, int phase) {
     for (const Group& g : p->groups) {
         const Part& P = p->parts[g.part];
         if (P.s != s || g.fidx < 0) continue;
+        if (phase == 1 && fused_launch_of(p->fp, (size_t)g.fidx) != launch) continue;
         if (phase == 0) {
             if (g.d_idx) {
                 const size_t total = (size_t)g.n * s->dim;
@@ -300,16 +313,20 @@ int enqueue_fused(Plan* p) {
         SVDB_CUDA(cudaEventRecord(p->ev_store[i], s->stream));
     }
     for (size_t i = 0; i < p->stores.size(); ++i) SVDB_CUDA(cudaStreamWaitEvent(p->origin, p->ev_store[i], 0));
-    for (size_t l = 0; l < fused_launches(p->fp); ++l) {
+    // launch l's searches finish on their stores' streams while launch l + 1 screens
+    const size_t nl = fused_launches(p->fp);
+    for (size_t l = 0; l < nl; ++l) {
         int rc = fused_screen(p->fp, l, p->origin);
         if (rc) return rc;
+        SVDB_CUDA(cudaEventRecord(p->ev_launch[l], p->origin));
     }
-    SVDB_CUDA(cudaEventRecord(p->ev_screen, p->origin));
     for (size_t i = 0; i < p->stores.size(); ++i) {
         Store* s = p->stores[i];
-        SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->ev_screen, 0));
-        int rc = enqueue_fused_store(p, i, 1);
-        if (rc) return rc;
+        for (size_t l = 0; l < nl; ++l) {
+            SVDB_CUDA(cudaStreamWaitEvent(s->stream, p->ev_launch[l], 0));
+            int rc = enqueue_fused_store(p, i, 1, (int)l);
+            if (rc) return rc;
+        }
         SVDB_CUDA(cudaEventRecord(p->ev_store[i], s->stream));
     }
     for (size_t i = 0; i < p->stores.size(); ++i) SVDB_CUDA(cudaStreamWaitEvent(p->origin, p->ev_store[i], 0));
@@ -547,7 +564,8 @@ void destroy(Plan* p) {
     free_groups(p);
     for (Part& P : p->parts) cudaFree(P.d_k);
     for (cudaEvent_t e : p->ev_store) cudaEventDestroy(e);
-    for (cudaEvent_t e : {p->ev_fork, p->ev_done, p->ev_t0, p->ev_t1, p->ev_screen})
+    for (cudaEvent_t e : p->ev_launch) cudaEventDestroy(e);
+    for (cudaEvent_t e : {p->ev_fork, p->ev_done, p->ev_t0, p->ev_t1})
         if (e) cudaEventDestroy(e);
     if (p->origin) cudaStreamDestroy(p->origin);
     delete p;
@@ -621,7 +639,6 @@ svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts,
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&p->ev_t0);
     if (e == cudaSuccess) e = cudaEventCreate(&p->ev_t1);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_screen, cudaEventDisableTiming);
     for (size_t i = 0; i < p->stores.size() && e == cudaSuccess; ++i) {
         cudaEvent_t ev = nullptr;
         e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);

@@ -76,6 +76,7 @@ int fused_create(const std::vector<FusedItem>& items, int metric, double epi_wei
                  std::vector<size_t>* bytes);
 void fused_set_scratch(FusedPlan* p, size_t i, void* scratch);
 size_t fused_launches(const FusedPlan* p);
+int fused_launch_of(const FusedPlan* p, size_t i);  // the launch that screens search i
 int fused_begin(FusedPlan* p, size_t i);  // search i's queries and row terms, on its store's stream
 int fused_screen(FusedPlan* p, size_t launch, cudaStream_t st);  // after every search's begin
 int fused_end(FusedPlan* p, size_t i);    // search i's select ... redo, on its store's stream (after the screen)
