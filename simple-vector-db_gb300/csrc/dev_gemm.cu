@@ -10,10 +10,10 @@
 //               N=256, K=16, into two 256-column FP32 accumulators in TMEM
 //               (double buffered, so the epilogue of one row tile overlaps
 //               the MMAs of the next);
-//   warps 2-5   epilogue: tcgen05.ld of the accumulator (thread = query),
-//               screen key + certified error bound per (query, row), fused
-//               per-query running top-k of lower bounds, and emission of
-//               every row whose upper bound reaches the running threshold.
+//   warps 2-9   epilogue: tcgen05.ld of the accumulator (thread = query),
+//               screen key + certified error bound per (query, row), the
+//               per-query threshold from k shared bins of lower bounds, and
+//               emission of every row whose upper bound reaches it.
 // The distance matrix never reaches HBM: only candidates are written.
 // CTAs are grouped so that all query tiles of a group read the same store
 // tile at the same time (one HBM read, the rest L2 hits).
@@ -346,46 +346,6 @@ __device__ __forceinline__ float screen_bound(float4 p, float qn, float eqq, flo
     return __fmaf_ru(qn, p.y, __fmaf_ru(eqq, p.z, __fmaf_ru(scr::kC2, p.w, eq0)));
 }
 
-// running k best lower bounds of one query (k <= KL); `mn` is the k-th best
-template <int KL>
-struct TopL {
-    float v[KL];
-    float mn;
-    int am;
-    __device__ __forceinline__ void init(int k) {
-#pragma unroll
-        for (int i = 0; i < KL; ++i) v[i] = i < k ? -INFINITY : INFINITY;
-        mn = k > 0 ? -INFINITY : INFINITY;
-        am = 0;
-    }
-    __device__ __forceinline__ void push(float L) {
-#pragma unroll
-        for (int i = 0; i < KL; ++i)
-            if (i == am) v[i] = L;
-        mn = v[0];
-        am = 0;
-#pragma unroll
-        for (int i = 1; i < KL; ++i)
-            if (v[i] < mn) {
-                mn = v[i];
-                am = i;
-            }
-    }
-};
-
-// k > 32: no per-thread running top-k (it would not fit in registers); the
-// thresholds come from the shared bins and the published maxima alone
-template <>
-struct TopL<0> {
-    float v[1];
-    float mn;
-    __device__ __forceinline__ void init(int k) {
-        mn = k > 0 ? -INFINITY : INFINITY;
-        v[0] = mn;
-    }
-    __device__ __forceinline__ void push(float) {}
-};
-
 // Work of one CTA: up to kMaxSeg segments, each a range of store tiles
 // [lo, hi) against one query tile; `sub` numbers the segment among those of
 // its query tile (it selects the candidate sub-lists the segment writes).
@@ -442,8 +402,8 @@ struct ScreenParams {
     ScreenSched sched;
 };
 
-// A fused launch over several searches (of several stores, dimensions and
-// query batches, one running top-k class): their query tensor maps and
+// A fused launch over several searches (of several stores, dimensions, query
+// batches and k): their query tensor maps and
 // parameters travel in the launch's own parameter space, and the schedule's
 // units are CTAs of any of the searches.
 constexpr int kMaxGroups = 16;     // searches in one fused launch
@@ -510,7 +470,7 @@ using ScreenParamsT = std::conditional_t<MULTI, ScreenParamsMulti, ScreenParams>
 // and query batches): each segment carries its search (seg.grp), whose
 // parameters, shadow, K depth and query tensor map the three roles pick up at
 // the segment's start.
-template <int KL, bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false>
+template <bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false>
 __global__ void __launch_bounds__(scr::kThreads, 1)
     k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
                   const __grid_constant__ ScreenParamsT<MULTI> P) {
@@ -708,7 +668,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         // the even CTA's accumulator-free barrier, which both CTAs' epilogues arrive on
         const uint32_t accempty_c0 = PAIR ? cluster_addr(smem_u32(&S.accempty[0]), 0) : 0u;
         for (int sg = 0; sg < nseg && alive; ++sg) {
-        // every segment starts afresh: its query tile, running top-k, warm-up
+        // every segment starts afresh: its query tile, threshold, warm-up
         const ScreenSeg seg = sched_seg(P.sched, unit, sg);
         const GroupParams& GP = seg_params(P, seg);
         const int q = PAIR ? seg.qt * 2 * kBM + (int)rank * kBM + qi : seg.qt * kBM + qi;
@@ -731,10 +691,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             valid = qp.w != 0.f;
         }
-        TopL<KL> top;
-        top.init(valid ? GP.k : 0);  // invalid queries: threshold +inf, never emit, never push
         const int nsq = P.sched.direct ? 1 : (int)P.sched.nsq[seg.gq];
-        float tau_c = -INFINITY, published = -INFINITY;
+        float tau_c = -INFINITY;  // the query's threshold: shared bins and tau (seed)
         // this thread's own sub-list of the query's candidates: emission needs no
         // atomic, the count stays in a register and is stored once at the end
         const int sub = 2 * seg.sub + half;
@@ -804,13 +762,12 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 continue;
             }
             if (js == 0) {  // warp-uniform: lanes of invalid queries load and discard
-                // Warm-up on the segment's first tile, before anything is emitted: fold the
-                // lower bound of every row into the running k best (rows, not chunk
-                // maxima, so k values exist after one tile) and publish the chunk
-                // maxima to the bins (unit = the chunk's place among the warm-up
-                // chunks of the query tile's segments, so segments fill disjoint
-                // bins).  The emitting pass below then skips its pushes and its bin
-                // update for this tile, so no row is counted twice.
+                // Warm-up on the segment's first tile, before anything is emitted:
+                // publish the maxima of its 16-row chunks to the bins (unit = the
+                // chunk's place among the warm-up chunks of the query tile's
+                // segments, so segments fill disjoint bins), then read the bins
+                // back.  The emitting pass below skips its bin update for this
+                // tile, so no row is counted twice.
 #pragma unroll 1
                 for (int c = 0; c < kBN / 2 / kChunk; ++c) {
                     uint32_t v[kChunk];
@@ -827,7 +784,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                             // masked rows are NaN: every comparison with them is false
                             const float l = ((vb >> i) & 1u) ? __fsub_rd(F8 ? __uint_as_float(v[i]) * cs : __uint_as_float(v[i]), eq0) : __int_as_float(0x7fc00000);
                             maxl = fmaxf(maxl, l);
-                            if (valid && l > top.mn) top.push(l);
                         }
                     } else {
 #pragma unroll
@@ -836,7 +792,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                             const float key = __fmaf_rn(F8 ? __uint_as_float(v[i]) * cs : __uint_as_float(v[i]), p.x, -p.z);
                             const float l = __fsub_rd(__fsub_rd(key, __fmaf_ru(eq, p.y, p.w)), eq0);
                             maxl = fmaxf(maxl, l);
-                            if (valid && l > top.mn) top.push(l);
                         }
                     }
                     if (valid && maxl > -INFINITY)
@@ -855,7 +810,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 for (int t = 0; t < GP.k; ++t) bmin = min(bmin, __ldcg(bq + (size_t)t * GP.nq));
                 tau_c = fmaxf(tau_c, fmaxf(ord2f(__ldcg(GP.tau + q)), ord2f(bmin)));
             }
-            float thr = valid ? fmaxf(top.mn, tau_c) : INFINITY;
+            const float thr = valid ? tau_c : INFINITY;  // invalid queries never emit
             // the query's eq0 is folded into the threshold and the maxima
             // in accumulator units (cosine F8: exact rescale by a power of two)
             const float thr2 = ACCU ? __fsub_rd(thr, eq0) * ics : __fsub_rd(thr, eq0);
@@ -945,9 +900,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     }
                 }
             }
-            // Running threshold: the k-th best of per-tile maxima (distinct tiles
-            // are distinct rows, so it never exceeds the k-th best lower bound).
-            // The bins take the same maxima, one unit (tile half) per bin.  Units
+            // The tile half's best lower bound goes to one bin (its unit's).  Units
             // are numbered round by round over the query tile's segments, after
             // the warm-up's chunks (unit_id below), so the bins fill after about
             // k / (2 x segments) tiles of every segment whatever the segments'
@@ -959,7 +912,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 const int unit = 2 * kWarmUnits * nsq + (js - 1) * 2 * nsq + 2 * seg.sub + half;
                 atomicMax(&GP.bins[(size_t)(unit % GP.k) * GP.nq + q], f2ord(maxl));
             }
-            if (valid && js > 0 && maxl > top.mn) top.push(maxl);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -968,10 +920,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 else
                     mbar_arrive(&S.accempty[b]);
                 if (!NORM) mbar_arrive(&S.rp_empty[b]);
-            }
-            if (valid && top.mn > published) {
-                atomicMax(&GP.tau[q], f2ord(top.mn));
-                published = top.mn;
             }
         }
         if (!DUMP && q < GP.nq) GP.cnt[(size_t)q * GP.nsub + sub] = nemit;
@@ -1423,20 +1371,17 @@ __global__ void __launch_bounds__(256) k_stream_emit(const float* __restrict__ k
     }
 }
 
-// Pass 1: every thread keeps the k best lower bounds of its candidates
-// (registers); their union holds the k best overall, so a radix select over
-// it in shared memory gives the exact k-th largest.  Pass 2: survivors.
+// Pass 1: a radix select over the candidates' lower bounds gives the exact
+// k-th largest.  Pass 2: survivors.
 //
 // The query's candidates sit in nsub sub-lists (one per emitting thread of the
 // screen); candidate i of the concatenation is found by a binary search over
 // the exclusive prefix of the sub-list counts (shared memory).
-template <int KL>
 __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
                                                  int nsub, int subcap, const float4* __restrict__ rpar,
                                                  const float4* __restrict__ qpar, int k, int2* __restrict__ surv,
                                                  int* __restrict__ nsurv, int* __restrict__ sig,
                                                  uint8_t* __restrict__ flags, float* __restrict__ kth_out = nullptr) {
-    extern __shared__ uint32_t vals[];  // blockDim.x * k ordered lower bounds
     __shared__ int hist[256];
     __shared__ uint32_t s_sh[3];
     __shared__ int s_out, s_sig, s_over;
@@ -1502,23 +1447,8 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         s_sig = 0x7fffffff;
     }
     uint32_t thr_ord = 0;  // fewer than k candidates: every one survives
-    if constexpr (KL > 0) {
-        TopL<KL> top;
-        top.init(k);
-        for (int i = threadIdx.x; i < n; i += bd) {
-            const int2 c = at(i);
-            const float L = __fsub_rd(__int_as_float(c.y), screen_bound(__ldg(rpar + c.x), qp.x, qp.y, qp.z));
-            if (L > top.mn) top.push(L);
-        }
-#pragma unroll
-        for (int j = 0; j < KL; ++j)
-            if (j < k) vals[threadIdx.x * k + j] = f2u_ord(top.v[j]);
-        __syncthreads();
-        if (n >= k) thr_ord = block_kth_largest([&](int i) { return vals[i]; }, bd * k, k, hist, s_sh);
-    } else {
-        __syncthreads();
-        if (n >= k) thr_ord = block_kth_largest(lower, n, k, hist, s_sh);
-    }
+    __syncthreads();
+    if (n >= k) thr_ord = block_kth_largest(lower, n, k, hist, s_sh);
     if (kth_out) {  // seed mode: the exact k-th largest lower bound over these candidates, nothing else
         if (threadIdx.x == 0) {
             const uint32_t u = thr_ord;
@@ -1770,7 +1700,7 @@ __global__ void __launch_bounds__(kRefThreads) k_refine_keep(const int2* __restr
 // FP64 pipe is narrow; -0.0 is folded into +0.0 and NaN ranks as +inf, exactly
 // as double comparisons order them), ties to the lowest row.  Queries with
 // more rows are answered by the exact scan.
-constexpr int kSmallRerank = 512;
+constexpr int kSmallRerank = 2048;
 
 __device__ __forceinline__ long long rank_ord(int metric, double v) {
     double kk = metric == SVDB_EUCLIDEAN ? v : -v;
@@ -1942,15 +1872,14 @@ __global__ void k_scatter_results(const int64_t* __restrict__ ids_in, const doub
 // ---------------------------------------------------------------------------
 struct GemmPlanCache {
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    bool attr_set[16] = {};
-    bool select_attr = false;
+    bool attr_set[4] = {};  // per screen variant: 2 x E4M3 + cosine
     bool sort_attr = false;
     bool rerank_attr = false;
     bool refine_attr = false;
     bool stream_attr = false;
     size_t screen_smem = 0;
     size_t screen_smem_pair = 0;
-    bool attr_pair[16] = {};
+    bool attr_pair[4] = {};
 };
 
 static int gemm_cache(Store* s, GemmPlanCache** out) {
@@ -2041,7 +1970,7 @@ static int pair_units() {
     static int n = 0;
     if (!n) {
         n = std::max(1, num_sms() / 2);
-        auto kern = k_screen_bf16<16, true, false, false, true>;
+        auto kern = k_screen_bf16<true, false, false, true>;
         const int smem = (int)(sizeof(scr::SmemT<true>) + 1024);
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess) {
             cudaLaunchConfig_t cfg = {};
@@ -2274,7 +2203,6 @@ struct Bf16Run {
     Bf16Layout L;
     uint8_t* base = nullptr;
     bool f8 = false, norm = false, stream = false;
-    int kc = 0;  // running top-k variant of the screen and select: k <= 16, <= 32, <= 128
     int nsub_use = 0, subcap_use = 0;
     ScreenParams P;
     CUtensorMap tmq;
@@ -2285,16 +2213,10 @@ struct Bf16Run {
     }
 };
 
-static int k_class_of(size_t k) { return k <= 16 ? 0 : k <= 32 ? 1 : 2; }
-
 template <bool PR>
-static auto screen_kernel_of(bool e4m3, int kc, bool norm) {
-    return e4m3   ? (kc == 0 ? (norm ? k_screen_bf16<16, true, true, false, PR> : k_screen_bf16<16, false, true, false, PR>)
-                     : kc == 1 ? (norm ? k_screen_bf16<32, true, true, false, PR> : k_screen_bf16<32, false, true, false, PR>)
-                               : (norm ? k_screen_bf16<0, true, true, false, PR> : k_screen_bf16<0, false, true, false, PR>))
-           : kc == 0 ? (norm ? k_screen_bf16<16, true, false, false, PR> : k_screen_bf16<16, false, false, false, PR>)
-           : kc == 1 ? (norm ? k_screen_bf16<32, true, false, false, PR> : k_screen_bf16<32, false, false, false, PR>)
-                     : (norm ? k_screen_bf16<0, true, false, false, PR> : k_screen_bf16<0, false, false, false, PR>);
+static auto screen_kernel_of(bool e4m3, bool norm) {
+    return e4m3 ? (norm ? k_screen_bf16<true, true, false, PR> : k_screen_bf16<false, true, false, PR>)
+                : (norm ? k_screen_bf16<true, false, false, PR> : k_screen_bf16<false, false, false, PR>);
 }
 
 // one screen over nunits units (CTAs or pairs) with the query tensor map tmq_;
@@ -2302,16 +2224,16 @@ static auto screen_kernel_of(bool e4m3, int kc, bool norm) {
 static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtensorMap& tmq_, const ScreenParams& P_) {
     GemmPlanCache* gc = R.gc;
     Store* s = R.s;
-    const int v = e4m3 ? 6 + 2 * R.kc + (R.norm ? 1 : 0) : 2 * R.kc + (R.norm ? 1 : 0);
+    const int v = 2 * (e4m3 ? 1 : 0) + (R.norm ? 1 : 0);
     if (!pair) {
-        auto kern = screen_kernel_of<false>(e4m3, R.kc, R.norm);
+        auto kern = screen_kernel_of<false>(e4m3, R.norm);
         if (!gc->attr_set[v]) {
             SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
             gc->attr_set[v] = true;
         }
         return launch_screen(kern, false, nunits, gc->screen_smem, s->stream, tmq_, tmq_, P_);
     }
-    auto kern = screen_kernel_of<true>(e4m3, R.kc, R.norm);
+    auto kern = screen_kernel_of<true>(e4m3, R.norm);
     if (!gc->attr_pair[v]) {
         SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_pair));
         gc->attr_pair[v] = true;
@@ -2330,12 +2252,6 @@ static int launch_select(Bf16Run& R, int nsub_, int subcap_, const float4* qp_, 
     const int nq = (int)R.a.nq, k = (int)R.a.k;
     // small batches carry many candidates per query: wider blocks
     const int sel_threads = nq >= 256 ? 256 : 1024;
-    const size_t sel_smem = R.kc <= 1 ? (size_t)sel_threads * k * sizeof(uint32_t) : 0;  // the running top-k variants
-    if (!gc->select_attr) {
-        SVDB_CUDA(cudaFuncSetAttribute(k_select<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-        SVDB_CUDA(cudaFuncSetAttribute(k_select<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-        gc->select_attr = true;
-    }
     int2* cand = R.at<int2>(L.cand);
     int* cnt = R.at<int>(L.cnt);
     const float4* rpar = R.at<float4>(L.rpar);
@@ -2343,15 +2259,8 @@ static int launch_select(Bf16Run& R, int nsub_, int subcap_, const float4* qp_, 
     int* nsurv = R.at<int>(L.nsurv);
     int* sig = R.at<int>(L.sig);
     uint8_t* flags = R.at<uint8_t>(L.flags);
-    if (R.kc == 0)
-        k_select<16><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k,
-                                                                         surv, nsurv, sig, flags, kth);
-    else if (R.kc == 1)
-        k_select<32><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k,
-                                                                         surv, nsurv, sig, flags, kth);
-    else
-        k_select<0><<<(unsigned)nq, sel_threads, sel_smem, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k,
-                                                                        surv, nsurv, sig, flags, kth);
+    k_select<<<(unsigned)nq, sel_threads, 0, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k, surv, nsurv,
+                                                          sig, flags, kth);
     SVDB_LAUNCH_CHECK();
     return SVDB_OK;
 }
@@ -2392,7 +2301,6 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
     // f8: cosine screens the E4M3 unit-norm shadow, dot / Euclidean the E4M3
     // shadow with per-row power-of-two scales
     R.norm = a.metric == SVDB_COSINE;  // cosine screens the unit-norm shadow
-    R.kc = k_class_of(a.k);
     const bool norm = R.norm;
 
     // Seeding (the FP8 screen by default; BF16 when asked): start the running
@@ -2455,8 +2363,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         PS.g.nsub = nsub_s;
         PS.g.subcap = subcap_s;
         PS.g.kblocks = (int)(s->ldb / scr::kBK);
-        R.kc = k_class_of(a.k);
-        rc = run_screen(R, false, L.pair, nctas_s, tmq16, PS);
+            rc = run_screen(R, false, L.pair, nctas_s, tmq16, PS);
         if (rc) return rc;
         rc = launch_select(R, nsub_s, subcap_s, qpar16, seed);
         if (rc) return rc;
@@ -2691,14 +2598,13 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 }
 
 // ---------------------------------------------------------------------------
-// fused screens: several BF16 searches, screened by one launch per running
-// top-k class
+// fused screens: several BF16 searches (up to 16) screened by one launch
 // ---------------------------------------------------------------------------
 // A search's screen is one pass of tensor-core tiles over its store; a batch
 // spread over several stores (different dimensions, row counts and query
 // counts) screened one launch per search leaves SMs idle at the tail of each
 // launch and, for small searches, most of the launch.  A fused launch takes
-// the searches of one k class together: every search gets a share of the
+// up to 16 searches together: every search gets a share of the
 // launch's CTAs in proportion to its work (query tiles x store tiles x
 // (k blocks + epilogue weight)), given out greedily to the search with the
 // most work per CTA, and inside its share the single-search schedule
@@ -2706,7 +2612,6 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
 // parameters and query tensor map travel in the launch's parameter space.
 struct FusedPlan {
     struct Launch {
-        int kc = 0;
         std::vector<int> items;  // search of each group slot
         ScreenParamsMulti P;
         int nctas = 0;
@@ -2788,11 +2693,11 @@ int fused_create(const std::vector<FusedItem>& items, int metric, double epi_wei
     p->maxsub.assign(n, 1);
     p->launch_of.assign(n, -1);
     p->slot_of.assign(n, -1);
-    // launches: one per k class, at most kMaxGroups searches each
-    for (int kc = 0; kc < 3; ++kc) {
+    // launches of at most kMaxGroups searches each (any k: the screen's
+    // thresholds are each search's own bins)
+    {
         FusedPlan::Launch* cur = nullptr;
         for (size_t i = 0; i < n; ++i) {
-            if (k_class_of(items[i].k) != kc) continue;
             if (!cur || cur->items.size() == (size_t)kMaxGroups) {
                 cur = new (std::nothrow) FusedPlan::Launch();
                 if (!cur) {
@@ -2800,7 +2705,6 @@ int fused_create(const std::vector<FusedItem>& items, int metric, double epi_wei
                     svdb_set_error("fused screen: out of host memory");
                     return SVDB_ENOMEM;
                 }
-                cur->kc = kc;
                 p->launches.push_back(cur);
             }
             p->launch_of[i] = (int)p->launches.size() - 1;
@@ -2879,14 +2783,9 @@ int fused_screen(FusedPlan* p, size_t li, cudaStream_t st) {
     FusedPlan::Launch* l = p->launches[li];
     if (l->nctas == 0) return SVDB_OK;
     const bool norm = p->metric == SVDB_COSINE;
-    auto kern = l->kc == 0 ? (norm ? k_screen_bf16<16, true, false, false, false, true>
-                                   : k_screen_bf16<16, false, false, false, false, true>)
-              : l->kc == 1 ? (norm ? k_screen_bf16<32, true, false, false, false, true>
-                                   : k_screen_bf16<32, false, false, false, false, true>)
-                           : (norm ? k_screen_bf16<0, true, false, false, false, true>
-                                   : k_screen_bf16<0, false, false, false, false, true>);
-    static bool attr[6] = {};
-    const int v = 2 * l->kc + (norm ? 1 : 0);
+    auto kern = norm ? k_screen_bf16<true, false, false, false, true> : k_screen_bf16<false, false, false, false, true>;
+    static bool attr[2] = {};
+    const int v = norm ? 1 : 0;
     const size_t smem = sizeof(scr::Smem) + 1024;
     if (!attr[v]) {
         SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -3039,13 +2938,13 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
     // more than 128 queries: the paired form (one cluster of two CTAs, M = 256)
     const bool pair = nq > (size_t)scr::kBM;
     if (!pair) {
-        auto kern = f8 ? (norm ? k_screen_bf16<0, true, true, true> : k_screen_bf16<0, false, true, true>)
-                       : norm ? k_screen_bf16<0, true, false, true> : k_screen_bf16<0, false, false, true>;
+        auto kern = f8 ? (norm ? k_screen_bf16<true, true, true> : k_screen_bf16<false, true, true>)
+                       : norm ? k_screen_bf16<true, false, true> : k_screen_bf16<false, false, true>;
         SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem));
         rc = launch_screen(kern, false, 1, gc->screen_smem, s->stream, tmq, tmq, P);
     } else {
-        auto kern = f8 ? (norm ? k_screen_bf16<0, true, true, true, true> : k_screen_bf16<0, false, true, true, true>)
-                       : norm ? k_screen_bf16<0, true, false, true, true> : k_screen_bf16<0, false, false, true, true>;
+        auto kern = f8 ? (norm ? k_screen_bf16<true, true, true, true> : k_screen_bf16<false, true, true, true>)
+                       : norm ? k_screen_bf16<true, false, true, true> : k_screen_bf16<false, false, true, true>;
         SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_pair));
         CUtensorMap tmx;
         const size_t kbl = f8 ? s->ldb8 / (2 * scr::kBK) : s->ldb / scr::kBK;

@@ -10,22 +10,24 @@
 // graph and replayed with one launch; it is captured again when a store
 // changes in a way the graph bakes in (the store's epoch).
 //
-// Three choices change the speed but not the results, and the autotuner times
-// every combination on the plan's own inputs at creation:
+// Choices that change the speed but not the results, timed by the autotuner
+// on the plan's own inputs at creation:
 //   grouping   0: one search per part, k = the part's largest k;
-//              1: one search per k class (k <= 16, <= 32, <= 128: the screen's
-//                 register-resident running top-k, and the bins-only form),
-//                 so small-k queries do not pay for the part's largest k;
+//              1: one search per k class (k <= 16, <= 32, <= 128), so
+//                 small-k queries do not pay for the part's largest k (a
+//                 screen's threshold is the minimum of k shared bins: fewer
+//                 bins settle sooner);
 //   concurrent 1: the parts of different stores run on their stores' streams
 //                 at the same time (a screen fills the SMs another part's
 //                 screen leaves idle at its tail); 0: one part after another;
+//   fused      1: the BF16 searches' screens run as one tensor-core launch
+//              (up to 16 searches) over all stores (work split in proportion
+//              to each search's tiles, see dev_gemm.cu), their other phases
+//              on the stores' streams; 0: every search launches its own
+//              screen; with fused screens, also the schedule's epilogue weight;
+//   seed       thresholds seeded from a 1/16 sample of each store, or not;
 //   screen     (cosine with a tensor-core precision) per store, the BF16 or
-//              the FP8 screen;
-//   fused      1: the BF16 searches' screens run as one tensor-core launch per
-//              k class over all stores (work split in proportion to each
-//              search's tiles, see dev_gemm.cu), their other phases on the
-//              stores' streams; 0: every search launches its own screen.  The
-//              autotuner also tries the fused schedule's epilogue weight.
+//              the FP8 screen.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -448,6 +450,10 @@ int configure(Plan* p, int grouping, int concurrent, int fused = 0) {
 // stores' scratch; a configuration slower than `cutoff` ms stops there), then
 // the capture, then the best of `reps` timed runs
 int time_config(Plan* p, int reps, float cutoff, float* ms) {
+    if (p->fused && !fused_current(p)) {  // its scratch is allocated outside the timed runs
+        const int rb = build_fused(p);
+        if (rb) return rb;
+    }
     SVDB_CUDA(cudaEventRecord(p->ev_t0, p->origin));
     int rc = enqueue(p);
     if (rc) return rc;

@@ -57,9 +57,9 @@ size_t search_bf16_scratch(const Store* s, size_t nq, size_t k);
 // the screen certifies k <= 128 on stores without unscreenable rows
 bool bf16_supported(const Store* s, size_t k);
 
-// Fused screens (dev_gemm.cu): several BF16 searches, on one or more stores,
-// screened by one tensor-core launch per running top-k class (k <= 16, <= 32,
-// <= 128); each search's other phases run on its store's stream.
+// Fused screens (dev_gemm.cu): several BF16 searches, on one or more stores
+// and with any k, screened by one tensor-core launch (up to 16 searches per
+// launch); each search's other phases run on its store's stream.
 struct FusedItem {
     Store* s = nullptr;
     int seed = -1;              // SearchArgs::seed
