@@ -49,7 +49,7 @@ METRIC_NAME = "exact top-10 queries/s, 1Mx768: BF16+FP64-rerank vs plain FP64 GP
 # same 4096 cosine queries (the shadow is read once per launch, so the bytes
 # grow with the rows and a full launch is this times N).  None when no capture
 # of the current kernel exists.
-SCREEN_DRAM_BYTES_PER_ROW = (421.659648e6 + 19.84128e6) / 200_000
+SCREEN_DRAM_BYTES_PER_ROW = (419.859712e6 + 19.900160e6) / 200_000
 
 
 def log(*a):

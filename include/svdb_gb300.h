@@ -240,6 +240,13 @@ int svdb_ragged_wait(svdb_ragged* plan);
 /* the CUDA stream (cudaStream_t) runs are queued on */
 void* svdb_ragged_stream(svdb_ragged* plan);
 int svdb_ragged_get_info(svdb_ragged* plan, svdb_ragged_info* info);
+/* Per search of the plan's last run (info.searches of them), 12 values each:
+ * part, k, queries, fused (1: screened by a fused launch), then for fused
+ * searches candidates, survivors, re-ranked (over the search's queries),
+ * queries answered by the exact scan, bound failures, and of those queries
+ * how many overflowed the candidate lists, the survivor cap, the FP64
+ * re-rank (0 for searches with a screen of their own).  Waits for the run. */
+int svdb_ragged_get_search_stats(svdb_ragged* plan, uint64_t* out, size_t n);
 void svdb_ragged_destroy(svdb_ragged* plan);
 
 /* ---- serving: batches of mixed requests on a device-resident store -------

@@ -73,7 +73,15 @@ constexpr int kSurvCap = 8192;                    // survivors re-ranked per que
 constexpr size_t kCandBudget = size_t(16) << 30;  // bytes of candidate lists per search (HBM is plentiful)
 constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key and m, per unit of m
 // flags
-constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4;
+// per query: certified, or why the exact scan answers it (a candidate
+// sub-list overflowed, an invalid query, fewer than k finite results, a bound
+// that failed against the exact value, more survivors than the select keeps,
+// more rows than the FP64 re-rank holds)
+constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4, kSurvOverflow = 5,
+                  kRerankOverflow = 6;
+// per search: {candidates, survivors, re-ranked, widened, bound failures,
+// widened by candidate overflow, by survivor overflow, by re-rank overflow}
+constexpr int kStats = 8;
 
 // Shared memory of one CTA.  PAIR (a CTA pair on two SMs, cta_group::2):
 // each CTA holds its own 128 queries and half of the 256-row store tile, so
@@ -386,13 +394,16 @@ struct GroupParams {
     int* bins;           // k bins per query, bin-major (bin t of query q at t * nq + q, so a warp's 32
                          // queries read or raise one bin with one coalesced access): best chunk maximum
                          // of the chunks whose index % k is the bin
-    int* cnt;            // per (query, sub-list) candidate count (may exceed subcap: overflow)
-    int2* cand;          // per query: nsub sub-lists of subcap x {row slot, key bits}, stride cap
+    int* cnt;            // per (query, sub-list): candidates emitted, -1 when they overflowed its room
+    int* coff;           // per (query, sub-list): where its room starts in the query's list
+    int2* cand;          // per query (stride cap): {row slot, key bits} in the sub-lists' rooms (epilogue)
     int* err;            // set to 1 when a wait timed out
     float* dump;         // DUMP (diagnostics) only: raw accumulators, nq x dump_ld
     size_t dump_ld;
     int nq, k, cap;
-    int nsub, subcap;    // sub-list = (row group, column half): one emitting thread each
+    int nsub;            // width of cnt / coff: 2 x the most segments of any query tile
+                         // (sub-list = (segment, column half): one emitting thread each)
+    int ntr;             // store tiles the query tiles' segments cover
     int kblocks;  // ldb / 64
 };
 
@@ -692,11 +703,25 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             valid = qp.w != 0.f;
         }
         const int nsq = P.sched.direct ? 1 : (int)P.sched.nsq[seg.gq];
+        // warm-up tiles of each segment: enough that the warm-up chunks of the
+        // query tile's nsq segments reach all k bins (one tile when the segments
+        // are many; a query tile screened by one CTA at k = 100 takes 7)
+        const int nwarm = max(1, (GP.k + 2 * kWarmUnits * nsq - 1) / (2 * kWarmUnits * nsq));
         float tau_c = -INFINITY;  // the query's threshold: shared bins and tau (seed)
         // this thread's own sub-list of the query's candidates: emission needs no
         // atomic, the count stays in a register and is stored once at the end
         const int sub = 2 * seg.sub + half;
-        int2* cq = GP.cand + (size_t)(q < GP.nq ? q : 0) * GP.cap + (size_t)sub * GP.subcap;
+        // This sub-list's room in the query's list: half of the list is shared
+        // evenly among the query tile's 2 x nsq sub-lists, the other half in
+        // proportion to their segments' rows.  A query tile's segments cover
+        // its store tiles in `sub` order ([lo, hi) following one another), so
+        // the rooms follow one another too.
+        const int64_t ntr_all = max(GP.ntr, 1), half_cap = GP.cap / 2;
+        const int64_t even = half_cap / (2 * nsq);
+        const int64_t pa = half_cap * seg.lo / ntr_all, pb = half_cap * seg.hi / ntr_all, pm = pa + (pb - pa) / 2;
+        const int r0 = (int)(even * (2 * seg.sub + half) + (half ? pm : pa));
+        const int subcap = (int)(even + (half ? pb - pm : pm - pa));
+        int2* cq = GP.cand + (size_t)(q < GP.nq ? q : 0) * GP.cap + r0;
         int nemit = 0;
         for (int r = seg.lo, js = 0; r < seg.hi; ++r, ++j, ++js) {
             const int b = j & 1;
@@ -706,13 +731,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // of chunk c), loaded before the wait so their latency is hidden
             uint32_t vbl = 0;
             if (NORM && !DUMP && lane < kBN / 2 / 32) vbl = __ldg(GP.vbits + ((r * kBN + col0) >> 5) + lane);
-            // Threshold refresh from the shared bins and tau (tiles 1..7 of a
-            // segment, then every 8th): read BEFORE the accumulator wait, so the
-            // loads' latency overlaps it instead of stalling the epilogue.  Bins
-            // and tau only grow (atomicMax of valid lower bounds), so a value
+            // Threshold refresh from the shared bins and tau (the 7 tiles after
+            // the warm-up, then every 8th): read BEFORE the accumulator wait, so
+            // the loads' latency overlaps it instead of stalling the epilogue.
+            // Bins and tau only grow (atomicMax of valid lower bounds), so a value
             // read earlier is an older, smaller -- still valid -- threshold.
-            // (Tile 0 reads them after its warm-up, below.)
-            const bool refresh = !DUMP && valid && js > 0 && (js < 8 || (js & 7) == 0);
+            // (Warm-up tiles read them after their own contributions, below.)
+            const bool refresh = !DUMP && valid && js >= nwarm && (js < nwarm + 7 || (js & 7) == 0);
             int bmin_pre = 0x7fffffff, tau_pre = 0;
             if (refresh) {
                 const int* bq = GP.bins + q;
@@ -761,13 +786,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 }
                 continue;
             }
-            if (js == 0) {  // warp-uniform: lanes of invalid queries load and discard
-                // Warm-up on the segment's first tile, before anything is emitted:
-                // publish the maxima of its 16-row chunks to the bins (unit = the
-                // chunk's place among the warm-up chunks of the query tile's
-                // segments, so segments fill disjoint bins), then read the bins
-                // back.  The emitting pass below skips its bin update for this
-                // tile, so no row is counted twice.
+            if (js < nwarm) {  // warp-uniform: lanes of invalid queries load and discard
+                // Warm-up on the segment's first tiles, before they emit: publish
+                // the maxima of their 16-row chunks to the bins (unit = the chunk's
+                // place among the warm-up chunks of the query tile's segments,
+                // round by round, so segments fill disjoint bins), then read the
+                // bins back.  The emitting pass below skips its bin update for
+                // these tiles, so no row is counted twice.
 #pragma unroll 1
                 for (int c = 0; c < kBN / 2 / kChunk; ++c) {
                     uint32_t v[kChunk];
@@ -795,7 +820,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         }
                     }
                     if (valid && maxl > -INFINITY)
-                        atomicMax(&GP.bins[(size_t)(((2 * seg.sub + half) * kWarmUnits + c) % GP.k) * GP.nq + q],
+                        atomicMax(&GP.bins[(size_t)((((js * nsq + seg.sub) * 2 + half) * kWarmUnits + c) % GP.k) *
+                                               GP.nq + q],
                                   f2ord(maxl));
                 }
             }
@@ -804,7 +830,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // reflects what every CTA has seen of this query, not only this one.
             if (refresh) {
                 tau_c = fmaxf(tau_c, fmaxf(ord2f(tau_pre), ord2f(bmin_pre)));
-            } else if (valid && js == 0) {  // after the warm-up's own contributions
+            } else if (valid && js < nwarm) {  // after the warm-up's own contributions
                 const int* bq = GP.bins + q;
                 int bmin = 0x7fffffff;
                 for (int t = 0; t < GP.k; ++t) bmin = min(bmin, __ldcg(bq + (size_t)t * GP.nq));
@@ -874,8 +900,6 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     for (int g = 0; g < G; ++g) {
                         const bool wg = want && gm[g] >= thr2;
                         if (!__any_sync(0xffffffffu, wg)) continue;  // warp-uniform
-                        // lanes reserve their slots with one atomic each; the columns
-                        // any lane emits are stored with predicates
                         uint32_t mask = 0;
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
@@ -884,17 +908,26 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                                                              __fmaf_ru(eq, rc[8 * g + i].y, rc[8 * g + i].w));
                             mask |= (wg && u >= thr2 ? 1u : 0u) << i;
                         }
-                        const int base = nemit;
+                        // each lane stores its own columns, lowest first (the warp
+                        // loops as often as its busiest lane has columns); column i
+                        // of the group is picked by three selects on i's bits
+                        int slot = nemit;
                         nemit += __popc(mask);
-                        const uint32_t any = __reduce_or_sync(0xffffffffu, mask);
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            if ((any >> i) & 1u) {  // warp-uniform
-                                const int slot = base + __popc(mask & ((1u << i) - 1u));
-                                if (((mask >> i) & 1u) && slot < GP.subcap)
+                        while (__any_sync(0xffffffffu, mask != 0u)) {
+                            if (mask) {
+                                const int i = __ffs(mask) - 1;
+                                mask &= mask - 1u;
+                                const uint32_t a0 = (i & 1) ? v[8 * g + 1] : v[8 * g + 0];
+                                const uint32_t a1 = (i & 1) ? v[8 * g + 3] : v[8 * g + 2];
+                                const uint32_t a2 = (i & 1) ? v[8 * g + 5] : v[8 * g + 4];
+                                const uint32_t a3 = (i & 1) ? v[8 * g + 7] : v[8 * g + 6];
+                                const uint32_t b0 = (i & 2) ? a1 : a0;
+                                const uint32_t b1 = (i & 2) ? a3 : a2;
+                                const uint32_t val = (i & 4) ? b1 : b0;
+                                if (slot < subcap)
                                     cq[slot] = make_int2(rw + 8 * g + i,
-                                                         ACCU ? __float_as_int(__uint_as_float(v[8 * g + i]) * cs)
-                                                              : (int)v[8 * g + i]);
+                                                         ACCU ? __float_as_int(__uint_as_float(val) * cs) : (int)val);
+                                ++slot;
                             }
                         }
                     }
@@ -902,14 +935,13 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             // The tile half's best lower bound goes to one bin (its unit's).  Units
             // are numbered round by round over the query tile's segments, after
-            // the warm-up's chunks (unit_id below), so the bins fill after about
-            // k / (2 x segments) tiles of every segment whatever the segments'
-            // offsets; the warm-up tile's rows are already in the bins as chunks
-            // and are not published a second time (a row in two bins would make
-            // their minimum exceed the k-th best lower bound).
+            // the warm-up's chunks, whatever the segments' offsets; the warm-up
+            // tiles' rows are already in the bins as chunks and are not published
+            // a second time (a row in two bins would make their minimum exceed
+            // the k-th best lower bound).
             const float maxl = __fsub_rd(ACCU ? tmax * cs : tmax, eq0);
-            if (valid && js > 0 && maxl > thr) {
-                const int unit = 2 * kWarmUnits * nsq + (js - 1) * 2 * nsq + 2 * seg.sub + half;
+            if (valid && js >= nwarm && maxl > thr) {
+                const int unit = 2 * kWarmUnits * nsq * nwarm + (js - nwarm) * 2 * nsq + 2 * seg.sub + half;
                 atomicMax(&GP.bins[(size_t)(unit % GP.k) * GP.nq + q], f2ord(maxl));
             }
             tc_fence_before();
@@ -922,7 +954,10 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                 if (!NORM) mbar_arrive(&S.rp_empty[b]);
             }
         }
-        if (!DUMP && q < GP.nq) GP.cnt[(size_t)q * GP.nsub + sub] = nemit;
+        if (!DUMP && q < GP.nq) {
+            GP.cnt[(size_t)q * GP.nsub + sub] = nemit <= subcap ? nemit : -1;
+            GP.coff[(size_t)q * GP.nsub + sub] = r0;
+        }
         }
     }
 
@@ -1158,7 +1193,7 @@ __global__ void k_init_search(int* tau, int* bins, int* cnt, int nsub, uint8_t* 
         *alpha = 0;
         *redo_n = 0;
     }
-    if (i < 5) stats[i] = 0;
+    if (i < scr::kStats) stats[i] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1375,10 +1410,13 @@ __global__ void __launch_bounds__(256) k_stream_emit(const float* __restrict__ k
 // k-th largest.  Pass 2: survivors.
 //
 // The query's candidates sit in nsub sub-lists (one per emitting thread of the
-// screen); candidate i of the concatenation is found by a binary search over
-// the exclusive prefix of the sub-list counts (shared memory).
-__global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt, int cap,
-                                                 int nsub, int subcap, const float4* __restrict__ rpar,
+// screen, each at its own offset in the query's list); candidate i of the
+// concatenation is found by a binary search over the exclusive prefix of the
+// sub-list counts (shared memory).
+// coff null: one list (the streamed screen's), room cap.
+__global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, const int* __restrict__ cnt,
+                                                 const int* __restrict__ coff, int cap, int nsub,
+                                                 const float4* __restrict__ rpar,
                                                  const float4* __restrict__ qpar, int k, int2* __restrict__ surv,
                                                  int* __restrict__ nsurv, int* __restrict__ sig,
                                                  uint8_t* __restrict__ flags, float* __restrict__ kth_out = nullptr) {
@@ -1386,6 +1424,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     __shared__ uint32_t s_sh[3];
     __shared__ int s_out, s_sig, s_over;
     __shared__ int s_pre[scr::kMaxSub + 1];
+    __shared__ int s_off[scr::kMaxSub];
     const int q = blockIdx.x;
     const float4 qp = qpar[q];
     if (threadIdx.x < 32) {  // warp 0: prefix of the sub-list counts
@@ -1394,8 +1433,10 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
         bool over = false;
         for (int s0 = 0; s0 < nsub; s0 += 32) {
             const int s = s0 + lane;
-            const int c = s < nsub ? cnt[(size_t)q * nsub + s] : 0;
-            over = over || c > subcap;
+            int c = s < nsub ? cnt[(size_t)q * nsub + s] : 0;
+            over = over || (coff ? c < 0 : c > cap);
+            if (c < 0) c = 0;
+            if (s < nsub) s_off[s] = coff ? coff[(size_t)q * nsub + s] : 0;
             int incl = c;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -1435,7 +1476,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
             else
                 hi = mid - 1;
         }
-        return cbase[(size_t)lo * subcap + (i - s_pre[lo])];
+        return cbase[(size_t)s_off[lo] + (i - s_pre[lo])];
     };
     const int bd = blockDim.x;
     auto lower = [&](int i) {
@@ -1470,7 +1511,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     if (threadIdx.x == 0) {
         sig[q] = s_sig;
         nsurv[q] = s_out;
-        if (s_out > scr::kSurvCap) flags[q] = scr::kOverflow;
+        if (s_out > scr::kSurvCap) flags[q] = scr::kSurvOverflow;
     }
 }
 
@@ -1731,7 +1772,7 @@ __global__ void __launch_bounds__(256) k_rerank_small(const double* __restrict__
     if (flags[q] != scr::kOk) return;
     const int n = nsurv[q];
     if (n > kSmallRerank) {
-        if (threadIdx.x == 0) flags[q] = scr::kOverflow;  // the exact scan answers it
+        if (threadIdx.x == 0) flags[q] = scr::kRerankOverflow;  // the exact scan answers it
         return;
     }
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 2, s = lane & 3;
@@ -1818,24 +1859,27 @@ __global__ void __launch_bounds__(256) k_rerank_small(const double* __restrict__
 
 // gather query rows (padded FP64) of the queries to re-answer; scatter back
 // queries the screen could not certify, compacted on the device, with the
-// batch's statistics {candidates, survivors, re-ranked, widened, bound failures}
+// batch's statistics (scr::kStats)
 __global__ void k_collect_redo(const uint8_t* __restrict__ flags, const int* __restrict__ cnt, int nsub,
                                const int* __restrict__ nsurv, const int* __restrict__ nref, int nq,
                                int* __restrict__ list, int* __restrict__ count,
                                unsigned long long* __restrict__ stats) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long v[5] = {0, 0, 0, 0, 0};
+    unsigned long long v[scr::kStats] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (q < nq) {
         const uint8_t f = flags[q];
         if (f != scr::kOk) list[atomicAdd(count, 1)] = q;
-        for (int t = 0; t < nsub; ++t) v[0] += (unsigned)cnt[(size_t)q * nsub + t];
+        for (int t = 0; t < nsub; ++t) v[0] += (unsigned)max(cnt[(size_t)q * nsub + t], 0);
         v[1] = (unsigned)nsurv[q];
         v[2] = (unsigned)nref[q];
         v[3] = f != scr::kOk;
         v[4] = f == scr::kBoundFail;
+        v[5] = f == scr::kOverflow;
+        v[6] = f == scr::kSurvOverflow;
+        v[7] = f == scr::kRerankOverflow;
     }
 #pragma unroll
-    for (int t = 0; t < 5; ++t) {
+    for (int t = 0; t < scr::kStats; ++t) {
         unsigned long long x = v[t];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(stats + t, x);
@@ -2038,10 +2082,10 @@ static int launch_screen(K kern, bool pair, int units, size_t smem, cudaStream_t
 
 struct Bf16Layout {
     bool pair = false;  // the paired screen (query tiles of 256)
-    size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
+    size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, coff, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     size_t tmax = 0, cut = 0;  // the streamed screen of a single query (its keys reuse spar: npad floats)
     int ntr, cap;
-    int nctas, nsub, subcap;
+    int nctas, nsub;
     size_t npad;
     ScreenSched sched;
 };
@@ -2155,16 +2199,14 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
     }
     L.nsub = 2 * maxsub;
     L.cnt = take(nq * (size_t)L.nsub * sizeof(int));
+    L.coff = take(nq * (size_t)L.nsub * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
     // per query before the running thresholds settle), split into one
     // sub-list per emitting thread; at least the survivor cap in all, since
     // the refinement reuses the storage
     size_t cap = std::max<size_t>(scr::kCapMax, (size_t)L.nsub * scr::kSubMin);
     while (cap > (size_t)scr::kCapMin && nq * cap * sizeof(int2) > scr::kCandBudget) cap >>= 1;
-    size_t subcap = cap / L.nsub;
-    if (subcap * L.nsub < (size_t)scr::kSurvCap) subcap = (scr::kSurvCap + L.nsub - 1) / L.nsub;
-    L.subcap = (int)subcap;
-    L.cap = (int)(subcap * L.nsub);
+    L.cap = (int)cap;  // >= kCapMin = kSurvCap
     L.cand = take(nq * (size_t)L.cap * sizeof(int2));
     L.surv = take(nq * (size_t)scr::kSurvCap * sizeof(int2));
     L.nsurv = take(nq * sizeof(int));
@@ -2176,7 +2218,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
     // the exact-scan fallback, sized for the whole batch (its count is on the device)
     L.redo = take(nq * sizeof(int));
     L.redo_n = take(sizeof(int));
-    L.stats = take(5 * sizeof(unsigned long long));
+    L.stats = take(scr::kStats * sizeof(unsigned long long));
     L.rq = take(nq * s->ld * sizeof(double));
     L.rsq = take(nq * sizeof(double));
     L.rres = take(nq * (size_t)k_max_bf16 * (sizeof(int64_t) + 2 * sizeof(double)));
@@ -2203,7 +2245,7 @@ struct Bf16Run {
     Bf16Layout L;
     uint8_t* base = nullptr;
     bool f8 = false, norm = false, stream = false;
-    int nsub_use = 0, subcap_use = 0;
+    int nsub_use = 0;
     ScreenParams P;
     CUtensorMap tmq;
     uint32_t kernels = 0;
@@ -2245,9 +2287,9 @@ static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtens
     return launch_screen(kern, true, nunits, gc->screen_smem_pair, s->stream, tmq_, tmx, P_);
 }
 
-static int launch_select(Bf16Run& R, int nsub_, int subcap_, const float4* qp_, float* kth) {
+// one_list: the streamed screen's single list (no sub-list offsets)
+static int launch_select(Bf16Run& R, int nsub_, bool one_list, const float4* qp_, float* kth) {
     Store* s = R.s;
-    GemmPlanCache* gc = R.gc;
     const Bf16Layout& L = R.L;
     const int nq = (int)R.a.nq, k = (int)R.a.k;
     // small batches carry many candidates per query: wider blocks
@@ -2259,8 +2301,8 @@ static int launch_select(Bf16Run& R, int nsub_, int subcap_, const float4* qp_, 
     int* nsurv = R.at<int>(L.nsurv);
     int* sig = R.at<int>(L.sig);
     uint8_t* flags = R.at<uint8_t>(L.flags);
-    k_select<<<(unsigned)nq, sel_threads, 0, s->stream>>>(cand, cnt, L.cap, nsub_, subcap_, rpar, qp_, k, surv, nsurv,
-                                                          sig, flags, kth);
+    k_select<<<(unsigned)nq, sel_threads, 0, s->stream>>>(cand, cnt, one_list ? nullptr : R.at<int>(L.coff), L.cap,
+                                                          nsub_, rpar, qp_, k, surv, nsurv, sig, flags, kth);
     SVDB_LAUNCH_CHECK();
     return SVDB_OK;
 }
@@ -2328,7 +2370,6 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         int maxsub_s = 1;
         const int nctas_s = screen_schedule(ntq, ntr_seed, PS.sched, &maxsub_s, screen_units(L.pair));
         const int nsub_s = 2 * maxsub_s;
-        const int subcap_s = L.cap / nsub_s;
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
                                                                               qb16, q32, qpar16);
         SVDB_LAUNCH_CHECK();
@@ -2353,6 +2394,8 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         PS.g.tau = tau;
         PS.g.bins = bins;
         PS.g.cnt = cnt;
+        PS.g.coff = R.at<int>(L.coff);
+        PS.g.ntr = ntr_seed;
         PS.g.cand = cand;
         PS.g.err = s->d_err;
         PS.g.dump = nullptr;
@@ -2361,11 +2404,10 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         PS.g.k = k;
         PS.g.cap = L.cap;
         PS.g.nsub = nsub_s;
-        PS.g.subcap = subcap_s;
         PS.g.kblocks = (int)(s->ldb / scr::kBK);
             rc = run_screen(R, false, L.pair, nctas_s, tmq16, PS);
         if (rc) return rc;
-        rc = launch_select(R, nsub_s, subcap_s, qpar16, seed);
+        rc = launch_select(R, nsub_s, false, qpar16, seed);
         if (rc) return rc;
         R.kernels += 5;
     }
@@ -2381,7 +2423,6 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
     R.stream = maxsub_ext <= 0 && norm && !f8 && nq <= kStreamQ &&
                (size_t)nq * s->ldb * sizeof(float) <= (size_t)kStreamQBytes;
     R.nsub_use = R.stream ? 1 : L.nsub;
-    R.subcap_use = R.stream ? L.cap : L.subcap;
     k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, R.nsub_use, flags, nq, k,
                                                                          alpha, redo_n, dstats, seed);
     SVDB_LAUNCH_CHECK();
@@ -2407,6 +2448,8 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
     g.tau = tau;
     g.bins = bins;
     g.cnt = cnt;
+    g.coff = R.at<int>(L.coff);
+    g.ntr = L.ntr;
     g.cand = cand;
     g.err = s->d_err;  // persistent: read at the next synchronous point
     g.dump = nullptr;
@@ -2415,7 +2458,6 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
     g.k = k;
     g.cap = L.cap;
     g.nsub = L.nsub;
-    g.subcap = L.subcap;
     g.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
     R.P.sched = L.sched;
     return SVDB_OK;
@@ -2477,7 +2519,7 @@ static int bf16_end(Bf16Run& R, svdb_search_stats* st) {
     unsigned long long* dstats = R.at<unsigned long long>(L.stats);
     float* q32 = R.at<float>(L.q32);
 
-    int rc = launch_select(R, R.nsub_use, R.subcap_use, qpar, nullptr);
+    int rc = launch_select(R, R.nsub_use, R.stream, qpar, nullptr);
     if (rc) return rc;
     s->prof_mark(3);
     const size_t ref_smem = s->ld * sizeof(float);
@@ -2619,6 +2661,7 @@ struct FusedPlan {
     std::vector<FusedItem> items;
     int metric = 0;
     std::vector<int> maxsub;     // per item
+    std::vector<int> tbase;      // per item: its first query tile in its launch's schedule
     std::vector<size_t> qoff;    // per item: offset of the screen's scratch after the padded queries
     std::vector<size_t> bytes;   // per item
     std::vector<int> launch_of, slot_of;
@@ -2633,7 +2676,8 @@ struct FusedPlan {
 // CTAs of the fused launch for each job, then the jobs' segments; false when
 // the launch's tables cannot hold the schedule
 static bool fused_schedule(const std::vector<int>& ntq, const std::vector<int>& ntr, const std::vector<int>& kb,
-                           int units, double epi_weight, ScreenSchedMulti& S, std::vector<int>& maxsub, int* nctas) {
+                           int units, double epi_weight, ScreenSchedMulti& S, std::vector<int>& maxsub,
+                           std::vector<int>& tbase, int* nctas) {
     const size_t n = ntq.size();
     std::memset(&S, 0, sizeof(S));
     if ((int)n > units) return false;
@@ -2648,6 +2692,7 @@ static bool fused_schedule(const std::vector<int>& ntq, const std::vector<int>& 
     }
     int c = 0, gq = 0;
     maxsub.assign(n, 1);
+    tbase.assign(n, 0);
     ScreenSched* one = new (std::nothrow) ScreenSched();
     if (!one) return false;
     bool ok = true;
@@ -2670,6 +2715,7 @@ static bool fused_schedule(const std::vector<int>& ntq, const std::vector<int>& 
         }
         for (int q = 0; q < ntq[i]; ++q) S.nsq[gq + q] = one->direct ? 1 : one->nsq[q];
         maxsub[i] = ms;
+        tbase[i] = gq;
         c += cg;
         gq += ntq[i];
     }
@@ -2691,6 +2737,7 @@ int fused_create(const std::vector<FusedItem>& items, int metric, double epi_wei
     p->metric = metric;
     const size_t n = items.size();
     p->maxsub.assign(n, 1);
+    p->tbase.assign(n, 0);
     p->launch_of.assign(n, -1);
     p->slot_of.assign(n, -1);
     // launches of at most kMaxGroups searches each (any k: the screen's
@@ -2714,19 +2761,22 @@ int fused_create(const std::vector<FusedItem>& items, int metric, double epi_wei
     }
     const int units = num_sms();
     for (FusedPlan::Launch* l : p->launches) {
-        std::vector<int> ntq, ntr, kb, ms;
+        std::vector<int> ntq, ntr, kb, ms, tb;
         for (int i : l->items) {
             const Store* s = items[i].s;
             ntq.push_back((int)((items[i].nq + scr::kBM - 1) / scr::kBM));
             ntr.push_back((int)((std::max<size_t>(s->slots, 1) + scr::kBN - 1) / scr::kBN));
             kb.push_back((int)(s->ldb / scr::kBK));
         }
-        if (!fused_schedule(ntq, ntr, kb, units, epi_weight, l->P.sched, ms, &l->nctas)) {
+        if (!fused_schedule(ntq, ntr, kb, units, epi_weight, l->P.sched, ms, tb, &l->nctas)) {
             delete p;
             svdb_set_error("fused screen: the searches do not fit one launch's schedule");
             return SVDB_EINVAL;
         }
-        for (size_t j = 0; j < l->items.size(); ++j) p->maxsub[l->items[j]] = ms[j];
+        for (size_t j = 0; j < l->items.size(); ++j) {
+            p->maxsub[l->items[j]] = ms[j];
+            p->tbase[l->items[j]] = tb[j];
+        }
     }
     bytes->assign(n, 0);
     p->qoff.assign(n, 0);
@@ -2776,6 +2826,7 @@ int fused_begin(FusedPlan* p, size_t i) {
     FusedPlan::Launch* l = p->launches[p->launch_of[i]];
     l->P.map[p->slot_of[i]] = R.tmq;
     l->P.grp[p->slot_of[i]] = R.P.g;
+
     return SVDB_OK;
 }
 
@@ -2798,6 +2849,18 @@ int fused_screen(FusedPlan* p, size_t li, cudaStream_t st) {
 }
 
 int fused_end(FusedPlan* p, size_t i) { return bf16_end(*p->runs[i], nullptr); }
+
+int fused_stats(FusedPlan* p, size_t i, unsigned long long* out) {
+    const Bf16Run& R = *p->runs[i];
+    if (!R.base) {
+        std::memset(out, 0, scr::kStats * sizeof(unsigned long long));
+        return SVDB_OK;
+    }
+    SVDB_CUDA(cudaStreamSynchronize(R.s->stream));
+    SVDB_CUDA(cudaMemcpy(out, R.at<unsigned long long>(R.L.stats), scr::kStats * sizeof(unsigned long long),
+                         cudaMemcpyDeviceToHost));
+    return SVDB_OK;
+}
 
 void fused_destroy(FusedPlan* p) { delete p; }
 
@@ -2935,6 +2998,7 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
     P.g.kblocks = f8 ? (int)(s->ldb8 / (2 * scr::kBK)) : (int)(s->ldb / scr::kBK);
     P.sched.direct = 1;
     P.sched.ntr = (int)ntiles;
+    P.g.ntr = (int)ntiles;
     // more than 128 queries: the paired form (one cluster of two CTAs, M = 256)
     const bool pair = nq > (size_t)scr::kBM;
     if (!pair) {

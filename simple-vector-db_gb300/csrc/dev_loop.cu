@@ -56,7 +56,8 @@ namespace {
 
 constexpr int kLoopThreads = 256;
 constexpr int kLoopMaxKd = 32;  // KD dimensions the loop's descent keeps in registers
-constexpr uint32_t kStateIdle = 0, kStateRunning = 1, kStateLeftIdle = 2, kStateStopped = 3, kStateLeaving = 4;
+// loop states (LoopCtl::state); 0 is "not started", set by the host only
+constexpr uint32_t kStateRunning = 1, kStateLeftIdle = 2, kStateStopped = 3, kStateLeaving = 4;
 
 // one request slot of the ring (host memory, mapped)
 struct __align__(64) LoopSlot {

@@ -701,6 +701,30 @@ int svdbd_ragged_info(svdbd_ragged* hp, svdb_ragged_info* out) {
     return SVDB_OK;
 }
 
+// per search of the last run: {part, k, queries, fused, candidates, survivors,
+// re-ranked, widened, bound failures, widened by candidate / survivor /
+// re-rank overflow}; the counters are those of fused searches (0 otherwise)
+int svdbd_ragged_search_stats(svdbd_ragged* hp, uint64_t* out, size_t n) {
+    Plan* p = reinterpret_cast<Plan*>(hp);
+    SVDB_CUDA(cudaStreamSynchronize(p->origin));
+    for (size_t i = 0; i < n && i < p->groups.size(); ++i) {
+        const svdb::Group& g = p->groups[i];
+        uint64_t* o = out + i * 12;
+        std::memset(o, 0, 12 * sizeof(uint64_t));
+        o[0] = (uint64_t)g.part;
+        o[1] = (uint64_t)g.kg;
+        o[2] = (uint64_t)g.n;
+        if (p->fused && p->fp && g.fidx >= 0) {
+            o[3] = 1;
+            unsigned long long st[8];
+            int rc = svdb::fused_stats(p->fp, (size_t)g.fidx, st);
+            if (rc) return rc;
+            for (int t = 0; t < 8; ++t) o[4 + t] = st[t];
+        }
+    }
+    return SVDB_OK;
+}
+
 void svdbd_ragged_destroy(svdbd_ragged* hp) {
     if (hp) svdb::destroy(reinterpret_cast<Plan*>(hp));
 }

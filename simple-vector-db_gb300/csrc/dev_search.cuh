@@ -80,6 +80,8 @@ int fused_launch_of(const FusedPlan* p, size_t i);  // the launch that screens s
 int fused_begin(FusedPlan* p, size_t i);  // search i's queries and row terms, on its store's stream
 int fused_screen(FusedPlan* p, size_t launch, cudaStream_t st);  // after every search's begin
 int fused_end(FusedPlan* p, size_t i);    // search i's select ... redo, on its store's stream (after the screen)
+// search i's statistics of its last run (8 counters, see scr::kStats); waits for its store's stream
+int fused_stats(FusedPlan* p, size_t i, unsigned long long* out);
 void fused_destroy(FusedPlan* p);
 
 // svdbd_search with SearchArgs::seed chosen by the caller

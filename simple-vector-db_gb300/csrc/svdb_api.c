@@ -621,6 +621,17 @@ SVDB_API int svdb_ragged_wait(svdb_ragged* r) {
 
 SVDB_API void* svdb_ragged_stream(svdb_ragged* r) { return r ? svdbd_ragged_stream(r->dev) : NULL; }
 
+SVDB_API int svdb_ragged_get_search_stats(svdb_ragged* r, uint64_t* out, size_t n) {
+    if (!r || (n && !out)) {
+        svdb_set_error("svdb_ragged_get_search_stats: NULL argument");
+        return SVDB_EINVAL;
+    }
+    ragged_lock(r, 1);
+    int rc = svdbd_ragged_search_stats(r->dev, out, n);
+    ragged_lock(r, 0);
+    return rc;
+}
+
 SVDB_API int svdb_ragged_get_info(svdb_ragged* r, svdb_ragged_info* info) {
     if (!r || !info) {
         svdb_set_error("svdb_ragged_get_info: NULL argument");

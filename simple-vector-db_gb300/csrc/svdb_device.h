@@ -151,6 +151,7 @@ int svdbd_ragged_run(svdbd_ragged* p);
 int svdbd_ragged_wait(svdbd_ragged* p);
 void* svdbd_ragged_stream(svdbd_ragged* p);
 int svdbd_ragged_info(svdbd_ragged* p, svdb_ragged_info* out);
+int svdbd_ragged_search_stats(svdbd_ragged* p, uint64_t* out, size_t n);
 void svdbd_ragged_destroy(svdbd_ragged* p);
 
 /* ---- KD tree mirror ------------------------------------------------------ */

@@ -165,6 +165,7 @@ def _load():
         "svdb_ragged_wait": (C.c_int, [vp]),
         "svdb_ragged_stream": (vp, [vp]),
         "svdb_ragged_get_info": (C.c_int, [vp, C.POINTER(RaggedInfo)]),
+        "svdb_ragged_get_search_stats": (C.c_int, [vp, C.POINTER(C.c_uint64), C.c_size_t]),
         "svdb_ragged_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
@@ -550,6 +551,16 @@ class RaggedPlan:
                 "fused_launches": inf.fused_launches, "fused_ms": [float(x) for x in inf.fused_ms],
                 "weight_ms": [float(x) for x in inf.weight_ms], "epi_weight": float(inf.epi_weight),
                 "seeded": inf.seeded, "seed_ms": float(inf.seed_ms)}
+
+    def search_stats(self) -> np.ndarray:
+        """svdb_ragged_get_search_stats: [searches, 12] uint64 (part, k, queries,
+        fused, candidates, survivors, re-ranked, widened, bound failures,
+        widened by candidate / survivor / re-rank overflow)."""
+        n = self.info()["searches"]
+        out = np.zeros((n, 12), np.uint64)
+        _check(lib.svdb_ragged_get_search_stats(self.ptr, out.ctypes.data_as(C.POINTER(C.c_uint64)), n),
+               "svdb_ragged_get_search_stats")
+        return out
 
     def close(self) -> None:
         if getattr(self, "ptr", None):
