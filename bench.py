@@ -594,6 +594,23 @@ def run_ragged(args, ws, rank, local):
             if not (np.array_equal(gi[i, :k], wi[0]) and np.array_equal(gd[i, :k], wv[0])):
                 raise SystemExit("bench: ragged plan results differ from the oracle")
 
+    # CPU baseline: the oracle's FP64 brute force on all host cores over a
+    # sample of each collection's queries (each with its own k), weighted by
+    # the collections' query shares
+    cpu = None
+    if args.cpu_sample > 0:
+        threads = os.cpu_count() or 1
+        per_q_s = 0.0
+        nq_all = sum(Q.shape[0] for _, Q, _ in cols)
+        for X, Q, ks in cols:
+            m = min(max(1, args.cpu_sample // 16), Q.shape[0])
+            t = time.perf_counter()
+            for i in range(m):
+                oracle_topk(X, Q[i:i + 1], S.COSINE, int(ks[i]))
+            per_q_s += (time.perf_counter() - t) / m * (Q.shape[0] / nq_all)
+        cpu = {"value": 1.0 / per_q_s, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": f"{min(max(1, args.cpu_sample // 16), 1 << 30)} queries per collection (their own k), "
+                         f"the oracle's FP64 brute force, weighted by the collections' query shares"}
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stream = torch.cuda.ExternalStream(plan.stream())
     for _ in range(args.warmup):
@@ -631,7 +648,7 @@ def run_ragged(args, ws, rank, local):
                      "seeded_thresholds": info["seeded"], "autotune_ms_seeded": info["seed_ms"],
                      "autotune_ms_with_store_screen_swapped": info["swap_ms"][:5],
                      "autotune_s": tune_s, "captures": info["captures"]},
-            "clocks": clocks}
+            "cpu_baseline": cpu, "clocks": clocks}
     print(json.dumps(line), flush=True)
     plan.close()
     for db in dbs:

@@ -370,6 +370,7 @@ struct ScreenSched {
     ScreenSeg seg[kMaxCtas][kMaxSeg];
     uint8_t nseg[kMaxCtas];
     uint16_t nsq[kMaxCtas];  // segments of query tile gq (the `sub` values 0..nsq-1)
+    uint16_t nst[kMaxCtas];  // of those, the ones that start with their CTA (the first nst subs)
     int direct;  // 1: no table; CTA i takes query tile i against every store tile
     int ntr;
 };
@@ -424,6 +425,7 @@ struct ScreenSchedMulti {
     ScreenSeg seg[kMaxUnitsM][kMaxSeg];
     uint8_t nseg[kMaxUnitsM];
     uint16_t nsq[kMaxQTilesM];
+    uint16_t nst[kMaxQTilesM];
     int direct;  // always 0 (every unit has its table row)
     int ntr;
 };
@@ -703,10 +705,15 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             valid = qp.w != 0.f;
         }
         const int nsq = P.sched.direct ? 1 : (int)P.sched.nsq[seg.gq];
-        // warm-up tiles of each segment: enough that the warm-up chunks of the
-        // query tile's nsq segments reach all k bins (one tile when the segments
-        // are many; a query tile screened by one CTA at k = 100 takes 7)
-        const int nwarm = max(1, (GP.k + 2 * kWarmUnits * nsq - 1) / (2 * kWarmUnits * nsq));
+        // The query tile's segments that start with their CTAs (nst, subs
+        // 0..nst-1) warm up: enough tiles that their warm-up chunks together
+        // reach all k bins.  A segment that starts later (a tail a CTA takes
+        // after its first segment) finds the bins filled and does not.  Every
+        // segment's units cycle through all k bins from its own offset.
+        const int nst = P.sched.direct ? 1 : (int)P.sched.nst[seg.gq];
+        const bool starter = sg == 0;
+        const int nwarm = starter ? max(1, (GP.k + 2 * kWarmUnits * nst - 1) / (2 * kWarmUnits * nst)) : 0;
+        const int boff = (int)(((int64_t)seg.sub * GP.k) / (starter ? nst : nsq));
         float tau_c = -INFINITY;  // the query's threshold: shared bins and tau (seed)
         // this thread's own sub-list of the query's candidates: emission needs no
         // atomic, the count stays in a register and is stored once at the end
@@ -788,9 +795,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             }
             if (js < nwarm) {  // warp-uniform: lanes of invalid queries load and discard
                 // Warm-up on the segment's first tiles, before they emit: publish
-                // the maxima of their 16-row chunks to the bins (unit = the chunk's
-                // place among the warm-up chunks of the query tile's segments,
-                // round by round, so segments fill disjoint bins), then read the
+                // the maxima of their 16-row chunks to the bins (one bin per
+                // chunk, consecutive from the segment's offset), then read the
                 // bins back.  The emitting pass below skips its bin update for
                 // these tiles, so no row is counted twice.
 #pragma unroll 1
@@ -820,8 +826,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         }
                     }
                     if (valid && maxl > -INFINITY)
-                        atomicMax(&GP.bins[(size_t)((((js * nsq + seg.sub) * 2 + half) * kWarmUnits + c) % GP.k) *
-                                               GP.nq + q],
+                        atomicMax(&GP.bins[(size_t)((boff + (js * 2 + half) * kWarmUnits + c) % GP.k) * GP.nq + q],
                                   f2ord(maxl));
                 }
             }
@@ -933,15 +938,15 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     }
                 }
             }
-            // The tile half's best lower bound goes to one bin (its unit's).  Units
-            // are numbered round by round over the query tile's segments, after
-            // the warm-up's chunks, whatever the segments' offsets; the warm-up
-            // tiles' rows are already in the bins as chunks and are not published
-            // a second time (a row in two bins would make their minimum exceed
-            // the k-th best lower bound).
+            // The tile half's best lower bound goes to one bin (its unit's: the
+            // segment's sequence continues after its warm-up chunks).  Any
+            // assignment is valid as long as every row unit goes to one bin: the
+            // warm-up tiles' rows are already in the bins as chunks and are not
+            // published a second time (a row in two bins would make their
+            // minimum exceed the k-th best lower bound).
             const float maxl = __fsub_rd(ACCU ? tmax * cs : tmax, eq0);
             if (valid && js >= nwarm && maxl > thr) {
-                const int unit = 2 * kWarmUnits * nsq * nwarm + (js - nwarm) * 2 * nsq + 2 * seg.sub + half;
+                const int unit = boff + 2 * kWarmUnits * nwarm + (js - nwarm) * 2 + half;
                 atomicMax(&GP.bins[(size_t)(unit % GP.k) * GP.nq + q], f2ord(maxl));
             }
             tc_fence_before();
@@ -2086,6 +2091,7 @@ struct Bf16Layout {
     size_t tmax = 0, cut = 0;  // the streamed screen of a single query (its keys reuse spar: npad floats)
     int ntr, cap;
     int nctas, nsub;
+    int nsub_seed_max;  // sub-lists per query cnt / coff hold (>= nsub and the seeding screen's)
     size_t npad;
     ScreenSched sched;
 };
@@ -2110,12 +2116,14 @@ static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub, int un
     }
     std::vector<int> ord(ntq, 0);
     bool fits = true;
+    std::vector<int> starters(ntq, 0);
     auto add = [&](int c, int qt, int lo, int hi) {
         if (hi <= lo) return;
         if (S.nseg[c] >= kMaxSeg) {
             fits = false;
             return;
         }
+        if (S.nseg[c] == 0) ++starters[qt];
         S.seg[c][S.nseg[c]++] = ScreenSeg{lo, hi, (uint16_t)qt, (uint16_t)ord[qt]++, 0, (uint16_t)qt};
     };
     const int base = G / ntq, ea = G % ntq;
@@ -2150,7 +2158,11 @@ static int screen_schedule(int ntq, int ntr, ScreenSched& S, int* maxsub, int un
                 S.seg[c][S.nseg[c]++] = ScreenSeg{(int)((int64_t)g * ntr / base), (int)((int64_t)(g + 1) * ntr / base),
                                                   (uint16_t)qt, (uint16_t)ord[qt]++, 0, (uint16_t)qt};
     }
-    for (int qt = 0; qt < ntq; ++qt) S.nsq[qt] = (uint16_t)std::max(1, ord[qt]);
+    if (!fits) starters = ord;  // (row groups: one segment per CTA)
+    for (int qt = 0; qt < ntq; ++qt) {
+        S.nsq[qt] = (uint16_t)std::max(1, ord[qt]);
+        S.nst[qt] = (uint16_t)std::max(1, starters[qt]);
+    }
     *maxsub = std::max(1, *std::max_element(ord.begin(), ord.end()));
     return c;
 }
@@ -2198,8 +2210,23 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
         L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair));
     }
     L.nsub = 2 * maxsub;
-    L.cnt = take(nq * (size_t)L.nsub * sizeof(int));
-    L.coff = take(nq * (size_t)L.nsub * sizeof(int));
+    // the threshold seeding's screen (a 1/16 sample of the store) has its own
+    // schedule, whose query tiles may have more segments: cnt / coff hold
+    // either search's sub-lists
+    int nsub_cnt = L.nsub;
+    if (L.ntr >= 32 && nq >= 32) {
+        ScreenSched* ss = new (std::nothrow) ScreenSched();
+        const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
+        int maxsub_s = scr::kMaxSub / 2;  // (the largest any schedule uses, if the sizing cannot be done here)
+        if (ss) {
+            screen_schedule((int)((nq + tq - 1) / tq), L.ntr / 16, *ss, &maxsub_s, screen_units(L.pair));
+            delete ss;
+        }
+        nsub_cnt = std::max(nsub_cnt, 2 * maxsub_s);
+    }
+    L.nsub_seed_max = nsub_cnt;
+    L.cnt = take(nq * (size_t)nsub_cnt * sizeof(int));
+    L.coff = take(nq * (size_t)nsub_cnt * sizeof(int));
     // candidate lists: as long as the budget allows (small batches emit more
     // per query before the running thresholds settle), split into one
     // sub-list per emitting thread; at least the survivor cap in all, since
@@ -2370,6 +2397,10 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         int maxsub_s = 1;
         const int nctas_s = screen_schedule(ntq, ntr_seed, PS.sched, &maxsub_s, screen_units(L.pair));
         const int nsub_s = 2 * maxsub_s;
+        if (nsub_s > L.nsub_seed_max) {  // (the layout sized cnt / coff for this schedule)
+            svdb_set_error("search_bf16: the seeding schedule does not fit its layout");
+            return SVDB_EINVAL;
+        }
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
                                                                               qb16, q32, qpar16);
         SVDB_LAUNCH_CHECK();
@@ -2713,7 +2744,10 @@ static bool fused_schedule(const std::vector<int>& ntq, const std::vector<int>& 
             }
             S.nseg[c + j] = (uint8_t)ns;
         }
-        for (int q = 0; q < ntq[i]; ++q) S.nsq[gq + q] = one->direct ? 1 : one->nsq[q];
+        for (int q = 0; q < ntq[i]; ++q) {
+            S.nsq[gq + q] = one->direct ? 1 : one->nsq[q];
+            S.nst[gq + q] = one->direct ? 1 : one->nst[q];
+        }
         maxsub[i] = ms;
         tbase[i] = gq;
         c += cg;

@@ -546,7 +546,7 @@ int autotune(Plan* p) {
         drop_graph(p);
         free_fused(p);
     }
-    if (p->metric != SVDB_COSINE || p->precision == SVDB_PREC_FP64) return SVDB_OK;
+    if (p->metric != SVDB_COSINE || p->precision == SVDB_PREC_FP64) return p->fused ? build_fused(p) : SVDB_OK;
     for (size_t i = 0; i < p->stores.size() && i < 8; ++i) {
         const int keep = p->sprec[i];
         p->sprec[i] = keep == SVDB_PREC_BF16 ? SVDB_PREC_FP8 : SVDB_PREC_BF16;
@@ -561,7 +561,7 @@ int autotune(Plan* p) {
     }
     drop_graph(p);
     free_fused(p);
-    return SVDB_OK;
+    return p->fused ? build_fused(p) : SVDB_OK;  // the kept choice, ready for the first run
 }
 
 void destroy(Plan* p) {
@@ -691,7 +691,7 @@ int svdbd_ragged_info(svdbd_ragged* hp, svdb_ragged_info* out) {
     for (size_t i = 0; i < p->stores.size() && i < 32; ++i)
         if (p->sprec[i] == SVDB_PREC_FP8) out->fp8_stores |= 1u << i;
     for (int i = 0; i < 8; ++i) out->swap_ms[i] = p->swap_ms[i];
-    out->fused = p->fused && p->fp ? 1 : 0;
+    out->fused = p->fused && p->fp ? 1 : 0;  // (a fused plan over no searches is no fused plan)
     out->fused_launches = p->fp ? (int32_t)svdb::fused_launches(p->fp) : 0;
     for (int i = 0; i < 2; ++i) out->fused_ms[i] = p->fused_ms[i];
     for (int i = 0; i < 3; ++i) out->weight_ms[i] = p->weight_ms[i];
