@@ -361,3 +361,29 @@ print("paired ok")
     env = dict(os.environ, SVDB_SCREEN_PAIR="1")
     r = subprocess.run([sys.executable, "-c", code, *paths], env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "paired ok" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_bf16_seeded_thresholds(S, oracle, metric):
+    """svdb_set_screen_seeding: the BF16 screen's thresholds start from the
+    exact k-th best lower bound of a 1/16 sample of the store; the answers
+    are the oracle's either way, and the sample prunes candidates."""
+    rng = np.random.default_rng(700 + metric)
+    X = rng.uniform(-1, 1, (60_000, 64))  # uniform rows: many near-ties for large k
+    Q = rng.uniform(-1, 1, (300, 64))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    wid, wval = oracle.topk(metric, X, Q, 100)
+    cands = []
+    for mode in (0, 1):
+        db.set_screen_seeding(mode)
+        for k in (16, 100):
+            st = S.SearchStats()
+            ids, vals = db.search(Q, k, metric, S.PREC_BF16, stats=st)
+            assert np.array_equal(ids, wid[:, :k]), (mode, k)
+            assert np.array_equal(vals, wval[:, :k]), (mode, k)
+            assert st.bound_failures == 0 and st.widened == 0
+            if k == 100:
+                cands.append(st.candidates)
+    assert cands[1] < cands[0]  # seeded thresholds emit fewer candidates
+    db.close()

@@ -152,6 +152,10 @@ def test_ragged_fused_screen_matches_oracle(S, oracle, metric, flags):
     # one launch holds up to 16 searches of any k: 12 searches (4 parts x 3
     # k classes) or 4 (one per part)
     assert info["fused_launches"] == 1
+    st = plan.search_stats()  # per search: part, k, queries, fused, funnel of the last run
+    assert st.shape == (info["searches"], 12) and (st[:, 3] == 1).all()
+    assert (st[:, 2] > 0).all() and (st[:, 4] > 0).all() and (st[:, 8] == 0).all()
+    assert sorted(set(st[:, 0].tolist())) == [0, 1, 2, 3]
     _check(oracle, metric, cols4, bufs)
     torch.cuda.synchronize()
     plan.close()
