@@ -558,7 +558,7 @@ def run_ragged(args, ws, rank, local):
     torch.cuda.set_device(local)
     prec = S.PREC_BF16 if args.precision == "bf16" else S.PREC_FP64
     cols = W.config4(8192)
-    tune = S.RAGGED_AUTOTUNE
+    tune = {"auto": S.RAGGED_AUTOTUNE, "fused": S.RAGGED_FUSED, "per-store": 0}[args.ragged_plan]
     if args.ragged_part:  # one collection's queries of one k class, default choices (small ncu captures)
         c, kc = (int(x) for x in args.ragged_part.split(":"))
         X, Q, ks = cols[c]
@@ -633,7 +633,7 @@ def run_ragged(args, ws, rank, local):
             "config": {"workload": "5 collections (D,N) = (64,2M) (128,1M) (384,500k) (768,200k) (1536,50k), "
                                    "uniform[-1,1] seed 4, 8192 queries split 40/25/15/12/8 %, k ~ U[1,100], cosine",
                        "precision": args.precision, "l2": "stores (5.4 GB FP64) larger than L2; no flush needed",
-                       "part": args.ragged_part or "all"},
+                       "part": args.ragged_part or "all", "plan": args.ragged_plan},
             "plan": {"grouping": info["grouping"], "concurrent": info["concurrent"], "graph": info["graph"],
                      "searches_per_run": info["searches"], "graph_launches_per_step": 1,
                      "fp8_screen_stores": [i for i in range(5) if info["fp8_stores"] >> i & 1],
@@ -1269,6 +1269,9 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: trace length per store size")
     ap.add_argument("--fp64-seconds", type=float, default=2.0, help="serve: cut-off of the plain FP64 trace")
     ap.add_argument("--loop-rows", type=int, default=1_000_000, help="loop: initial rows of the loop's store")
+    ap.add_argument("--ragged-plan", default="auto", choices=["auto", "fused", "per-store"],
+                    help="ragged: autotuned plan, or fixed choices (one search per part, stores concurrent; "
+                         "screens fused into one launch, or one per search)")
     ap.add_argument("--ragged-part", default="", help="ragged: only collection C's queries of k class K "
                     "(C:K, K = 0 for k <= 16, 1 for <= 32, 2 above), default plan choices")
     ap.add_argument("--percall-threads", type=int, default=16, help="percall: concurrent caller threads")

@@ -78,7 +78,7 @@ constexpr float kC2 = 1.9073486328125e-06f;       // 2^-19: FP32 rounding of key
 // that failed against the exact value, more survivors than the select keeps,
 // more rows than the FP64 re-rank holds)
 constexpr uint8_t kOk = 0, kOverflow = 1, kInvalidQuery = 2, kTooFew = 3, kBoundFail = 4, kSurvOverflow = 5,
-                  kRerankOverflow = 6;
+                  kRerankOverflow = 6, kRerankLarge = 7;  // (7: between the re-rank's two passes only)
 // per search: {candidates, survivors, re-ranked, widened, bound failures,
 // widened by candidate overflow, by survivor overflow, by re-rank overflow}
 constexpr int kStats = 8;
@@ -1740,13 +1740,15 @@ __global__ void __launch_bounds__(kRefThreads) k_refine_keep(const int2* __restr
 // ---------------------------------------------------------------------------
 // stage 3: FP64 re-rank of what the refinement keeps
 // ---------------------------------------------------------------------------
-// The common case: at most kSmallRerank rows left per query.  One block per
-// query scores them (4 lanes per row, canonical order) and ranks them by
-// counting, on order-preserving 64-bit integer images of the ranking key (the
-// FP64 pipe is narrow; -0.0 is folded into +0.0 and NaN ranks as +inf, exactly
-// as double comparisons order them), ties to the lowest row.  Queries with
-// more rows are answered by the exact scan.
-constexpr int kSmallRerank = 2048;
+// One block per query scores the rows left (4 lanes per row, canonical
+// order) and ranks them by counting, on order-preserving 64-bit integer
+// images of the ranking key (the FP64 pipe is narrow; -0.0 is folded into
+// +0.0 and NaN ranks as +inf, exactly as double comparisons order them), ties
+// to the lowest row.  Two passes: up to kSmallRerank rows (the common case,
+// small shared memory, many blocks per SM), then up to kLargeRerank rows for
+// the queries the first pass handed on; queries with more rows are answered
+// by the exact scan.
+constexpr int kSmallRerank = 512, kLargeRerank = 2048;
 
 __device__ __forceinline__ long long rank_ord(int metric, double v) {
     double kk = metric == SVDB_EUCLIDEAN ? v : -v;
@@ -1756,7 +1758,7 @@ __device__ __forceinline__ long long rank_ord(int metric, double v) {
     return b >= 0 ? b : b ^ 0x7fffffffffffffffll;
 }
 
-template <bool EUC>
+template <bool EUC, int CAP>
 __global__ void __launch_bounds__(256) k_rerank_small(const double* __restrict__ x64, size_t ld,
                                                       const double* __restrict__ qbuf, const double* __restrict__ qsq,
                                                       const double* __restrict__ sq64, const int2* __restrict__ surv,
@@ -1769,15 +1771,17 @@ __global__ void __launch_bounds__(256) k_rerank_small(const double* __restrict__
     extern __shared__ __align__(16) uint8_t sm[];
     double* qs = reinterpret_cast<double*>(sm);
     long long* skey = reinterpret_cast<long long*>(qs + ld);
-    double* sval = reinterpret_cast<double*>(skey + kSmallRerank);
-    int* srow = reinterpret_cast<int*>(sval + kSmallRerank);
-    int* spos = srow + kSmallRerank;  // candidate index at each output position
+    double* sval = reinterpret_cast<double*>(skey + CAP);
+    int* srow = reinterpret_cast<int*>(sval + CAP);
+    int* spos = srow + CAP;  // candidate index at each output position
     __shared__ int s_bad;
     const int q = blockIdx.x;
-    if (flags[q] != scr::kOk) return;
+    // the first pass takes certified queries, the second the ones it handed on
+    if (flags[q] != (CAP == kSmallRerank ? scr::kOk : scr::kRerankLarge)) return;
     const int n = nsurv[q];
-    if (n > kSmallRerank) {
-        if (threadIdx.x == 0) flags[q] = scr::kRerankOverflow;  // the exact scan answers it
+    if (n > CAP) {
+        if (threadIdx.x == 0)  // the second pass, or else the exact scan, answers it
+            flags[q] = CAP == kSmallRerank ? scr::kRerankLarge : scr::kRerankOverflow;
         return;
     }
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 2, s = lane & 3;
@@ -2591,24 +2595,31 @@ static int bf16_end(Bf16Run& R, svdb_search_stats* st) {
     s->prof_mark(4);
 
     {
-        const size_t rr_smem = s->ld * sizeof(double) + (size_t)kSmallRerank * (8 + 8 + 4 + 4);
         if (!gc->rerank_attr) {
-            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           200 * 1024));
-            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           200 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<true, kSmallRerank>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<false, kSmallRerank>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<true, kLargeRerank>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            SVDB_CUDA(cudaFuncSetAttribute(k_rerank_small<false, kLargeRerank>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
             gc->rerank_attr = true;
         }
-        if (a.metric == SVDB_EUCLIDEAN)
-            k_rerank_small<true><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
-                s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k, a.metric, (int)s->dim, rpar, qpar,
-                s->logical, a.ids, a.dists, a.err, flags);
-        else
-            k_rerank_small<false><<<(unsigned)nq, 256, rr_smem, s->stream>>>(
-                s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k, a.metric, (int)s->dim, rpar, qpar,
-                s->logical, a.ids, a.dists, a.err, flags);
+        const bool euc = a.metric == SVDB_EUCLIDEAN;
+        const size_t sm_small = s->ld * sizeof(double) + (size_t)kSmallRerank * (8 + 8 + 4 + 4);
+        const size_t sm_large = s->ld * sizeof(double) + (size_t)kLargeRerank * (8 + 8 + 4 + 4);
+        auto rr_small = euc ? k_rerank_small<true, kSmallRerank> : k_rerank_small<false, kSmallRerank>;
+        auto rr_large = euc ? k_rerank_small<true, kLargeRerank> : k_rerank_small<false, kLargeRerank>;
+        rr_small<<<(unsigned)nq, 256, sm_small, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k,
+                                                             a.metric, (int)s->dim, rpar, qpar, s->logical, a.ids,
+                                                             a.dists, a.err, flags);
         SVDB_LAUNCH_CHECK();
-        ++R.kernels;
+        rr_large<<<(unsigned)nq, 256, sm_large, s->stream>>>(s->x64, s->ld, a.q, a.qsq, s->sq64, cand, L.cap, nref, k,
+                                                             a.metric, (int)s->dim, rpar, qpar, s->logical, a.ids,
+                                                             a.dists, a.err, flags);
+        SVDB_LAUNCH_CHECK();
+        R.kernels += 2;
     }
 
     // queries the screen could not certify: exact FP64 scan, entirely on the

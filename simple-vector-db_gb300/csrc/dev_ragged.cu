@@ -665,6 +665,7 @@ svdbd_ragged* svdbd_ragged_create(const svdbd_ragged_part* parts, size_t nparts,
              ? svdb::autotune(p)
              : svdb::configure(p, (flags & SVDB_RAGGED_BY_K_CLASS) ? 1 : 0, 1,
                                (flags & SVDB_RAGGED_FUSED) && precision != SVDB_PREC_FP64 ? 1 : 0);
+    if (!rc && p->fused && !p->fp) rc = svdb::build_fused(p);  // ready for the first run (and reported)
     if (rc) return fail(rc);
     return reinterpret_cast<svdbd_ragged*>(p);
 }
