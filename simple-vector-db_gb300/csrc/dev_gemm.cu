@@ -85,10 +85,11 @@ constexpr int kStats = 8;
 
 // Shared memory of one CTA.  PAIR (a CTA pair on two SMs, cta_group::2):
 // each CTA holds its own 128 queries and half of the 256-row store tile, so
-// a stage is 32 KB instead of 48 KB and the ring is 6 deep.
-template <bool PAIR>
+// a stage is 32 KB instead of 48 KB and the ring is 6 deep.  DUO (two CTAs
+// on each SM): a 2-deep ring, so that two CTAs' shared memory fits one SM.
+template <bool PAIR, bool DUO = false>
 struct SmemT {
-    static constexpr int ST = PAIR ? 6 : kStages;
+    static constexpr int ST = PAIR ? 6 : (DUO ? 2 : kStages);
     static constexpr uint32_t SA = kStageA;
     static constexpr uint32_t SB = PAIR ? kStageB / 2 : kStageB;
     // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
@@ -106,6 +107,11 @@ struct SmemT {
     int abort;
 };
 using Smem = SmemT<false>;
+// DUO: accumulators per CTA (TMEM columns / 256); one, so two CTAs share an SM's 512 columns
+template <bool DUO>
+constexpr uint32_t tmem_cols() {
+    return DUO ? (uint32_t)kBN : kTmemCols;
+}
 }  // namespace scr
 
 // ---------------------------------------------------------------------------
@@ -357,7 +363,7 @@ __device__ __forceinline__ float screen_bound(float4 p, float qn, float eqq, flo
 // Work of one CTA: up to kMaxSeg segments, each a range of store tiles
 // [lo, hi) against one query tile; `sub` numbers the segment among those of
 // its query tile (it selects the candidate sub-lists the segment writes).
-constexpr int kMaxCtas = 160;
+constexpr int kMaxCtas = 320;  // (two CTAs per SM in the DUO form)
 constexpr int kMaxSeg = 4;
 // grp: the search the segment belongs to (a fused launch screens several at
 // once; 0 otherwise); gq: the query tile's index among all the launch's query
@@ -483,13 +489,18 @@ using ScreenParamsT = std::conditional_t<MULTI, ScreenParamsMulti, ScreenParams>
 // and query batches): each segment carries its search (seg.grp), whose
 // parameters, shadow, K depth and query tensor map the three roles pick up at
 // the segment's start.
-template <bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false>
-__global__ void __launch_bounds__(scr::kThreads, 1)
+// DUO: two CTAs per SM, each with one accumulator (the other CTA's MMAs run
+// while this one's epilogue drains it) and a 2-deep ring; twice the epilogue
+// warps per SM, for stores whose tiles are a few k blocks deep.
+template <bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false, bool DUO = false>
+__global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
     k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
                   const __grid_constant__ ScreenParamsT<MULTI> P) {
     static_assert(!(MULTI && (PAIR || DUMP)), "a fused launch is single-CTA and screens");
+    static_assert(!(DUO && (PAIR || DUMP || MULTI)), "the two-CTA form is a plain screen");
     using namespace scr;
-    using SM = SmemT<PAIR>;
+    using SM = SmemT<PAIR, DUO>;
+    constexpr uint32_t TC = tmem_cols<DUO>();
     constexpr int ST = SM::ST;
     // cosine FP8 works in accumulator units (thresholds scaled in, keys out);
     // dot / Euclidean FP8 scales each accumulator into key units at once
@@ -531,7 +542,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         if constexpr (PAIR)
             tmem_alloc_pair(&S.tmem_base, kTmemCols);  // one warp of each CTA, collectively
         else
-            tmem_alloc(&S.tmem_base, kTmemCols);
+            tmem_alloc(&S.tmem_base, TC);
     }
     tc_fence_before();
     __syncthreads();
@@ -619,8 +630,8 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             const ScreenSeg sgm = sched_seg(P.sched, unit, sg);
             const int KB = seg_params(P, sgm).kblocks;
             for (int r = sgm.lo, rh = sgm.hi; r < rh && ok; ++r, ++j) {
-                const int b = j & 1;
-                const uint32_t use = (uint32_t)j >> 1;
+                const int b = DUO ? 0 : (j & 1);  // accumulator
+                const uint32_t use = DUO ? (uint32_t)j : (uint32_t)j >> 1;
                 if (!mbar_wait(&S.accempty[b], (use & 1u) ^ 1u, abort, kWaitLimitNs)) break;
                 tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(b * kBN);
@@ -731,9 +742,11 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         int2* cq = GP.cand + (size_t)(q < GP.nq ? q : 0) * GP.cap + r0;
         int nemit = 0;
         for (int r = seg.lo, js = 0; r < seg.hi; ++r, ++j, ++js) {
-            const int b = j & 1;
-            const uint32_t use = (uint32_t)j >> 1;
-            const float4* rps = S.rp[b] + col0;  // this warp's 128 rows, staged by the producer
+            const int b = DUO ? 0 : (j & 1);  // accumulator
+            const uint32_t use = DUO ? (uint32_t)j : (uint32_t)j >> 1;
+            const int rb = j & 1;  // slot of the row-parameter ring (two deep whatever the accumulators)
+            const uint32_t ruse = (uint32_t)j >> 1;
+            const float4* rps = S.rp[rb] + col0;  // this warp's 128 rows, staged by the producer
             // cosine: validity words of this warp's 128 rows (lane c holds the word
             // of chunk c), loaded before the wait so their latency is hidden
             uint32_t vbl = 0;
@@ -761,7 +774,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
             // tcgen05.ld is warp-collective (.sync.aligned): every branch that
             // leads to one must be taken by the whole warp, including this wait
             bool got = mbar_wait(&S.accfull[b], use & 1u, abort, kWaitLimitNs);
-            if (!NORM) got = got && mbar_wait(&S.rp_full[b], use & 1u, abort, kWaitLimitNs);
+            if (!NORM) got = got && mbar_wait(&S.rp_full[rb], ruse & 1u, abort, kWaitLimitNs);
             if (!__all_sync(0xffffffffu, got)) {
                 alive = false;
                 break;
@@ -789,7 +802,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                         mbar_arrive_cluster(accempty_c0 + (uint32_t)(b * sizeof(uint64_t)));
                     else
                         mbar_arrive(&S.accempty[b]);
-                    if (!NORM) mbar_arrive(&S.rp_empty[b]);
+                    if (!NORM) mbar_arrive(&S.rp_empty[rb]);
                 }
                 continue;
             }
@@ -956,7 +969,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
                     mbar_arrive_cluster(accempty_c0 + (uint32_t)(b * sizeof(uint64_t)));
                 else
                     mbar_arrive(&S.accempty[b]);
-                if (!NORM) mbar_arrive(&S.rp_empty[b]);
+                if (!NORM) mbar_arrive(&S.rp_empty[rb]);
             }
         }
         if (!DUMP && q < GP.nq) {
@@ -977,7 +990,7 @@ __global__ void __launch_bounds__(scr::kThreads, 1)
         if constexpr (PAIR)
             tmem_dealloc_pair(tmem, kTmemCols);
         else
-            tmem_dealloc(tmem, kTmemCols);
+            tmem_dealloc(tmem, TC);
     }
 }
 
@@ -1933,6 +1946,8 @@ struct GemmPlanCache {
     size_t screen_smem = 0;
     size_t screen_smem_pair = 0;
     bool attr_pair[4] = {};
+    bool attr_duo[4] = {};
+    size_t screen_smem_duo = 0;
 };
 
 static int gemm_cache(Store* s, GemmPlanCache** out) {
@@ -1954,6 +1969,7 @@ static int gemm_cache(Store* s, GemmPlanCache** out) {
         }
         c->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
         c->screen_smem = sizeof(scr::Smem) + 1024;
+        c->screen_smem_duo = sizeof(scr::SmemT<false, true>) + 1024;
         c->screen_smem_pair = sizeof(scr::SmemT<true>) + 1024;
         s->gemm = c;
     }
@@ -2045,7 +2061,14 @@ static int pair_units() {
     return n;
 }
 
-static int screen_units(bool pair) { return pair ? pair_units() : std::min(num_sms(), kMaxCtas); }
+// Stores whose tiles are at most this many k blocks deep (D <= 128) screen
+// with two CTAs per SM: there the epilogue, not the MMAs, sets the pace.
+constexpr int kDuoMaxKb = 2;
+static bool screen_duo(const Store* s, bool pair) { return !pair && (int)(s->ldb / scr::kBK) <= kDuoMaxKb; }
+
+static int screen_units(bool pair, bool duo = false) {
+    return pair ? pair_units() : std::min((duo ? 2 : 1) * num_sms(), kMaxCtas);
+}
 
 // tensor map over a shadow's swizzled tiles as rows of 128 bytes (256 rows per
 // tile and k block), copied as they are (the paired screen loads half a tile)
@@ -2091,6 +2114,7 @@ static int launch_screen(K kern, bool pair, int units, size_t smem, cudaStream_t
 
 struct Bf16Layout {
     bool pair = false;  // the paired screen (query tiles of 256)
+    bool duo = false;   // two CTAs per SM (shallow tiles)
     size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, coff, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     size_t tmax = 0, cut = 0;  // the streamed screen of a single query (its keys reuse spar: npad floats)
     int ntr, cap;
@@ -2210,8 +2234,9 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
         maxsub = maxsub_ext;
     } else {
         L.pair = screen_pair(nq);
+        L.duo = screen_duo(s, L.pair);
         const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
-        L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair));
+        L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair, L.duo));
     }
     L.nsub = 2 * maxsub;
     // the threshold seeding's screen (a 1/16 sample of the store) has its own
@@ -2223,7 +2248,7 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
         const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
         int maxsub_s = scr::kMaxSub / 2;  // (the largest any schedule uses, if the sizing cannot be done here)
         if (ss) {
-            screen_schedule((int)((nq + tq - 1) / tq), L.ntr / 16, *ss, &maxsub_s, screen_units(L.pair));
+            screen_schedule((int)((nq + tq - 1) / tq), L.ntr / 16, *ss, &maxsub_s, screen_units(L.pair, L.duo));
             delete ss;
         }
         nsub_cnt = std::max(nsub_cnt, 2 * maxsub_s);
@@ -2298,6 +2323,19 @@ static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtens
     GemmPlanCache* gc = R.gc;
     Store* s = R.s;
     const int v = 2 * (e4m3 ? 1 : 0) + (R.norm ? 1 : 0);
+    if (!pair && R.L.duo) {
+        auto kern = e4m3 ? (R.norm ? k_screen_bf16<true, true, false, false, false, true>
+                                   : k_screen_bf16<false, true, false, false, false, true>)
+                         : (R.norm ? k_screen_bf16<true, false, false, false, false, true>
+                                   : k_screen_bf16<false, false, false, false, false, true>);
+        if (!gc->attr_duo[v]) {
+            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_duo));
+            gc->attr_duo[v] = true;
+        }
+        kern<<<(unsigned)nunits, scr::kThreads, gc->screen_smem_duo, s->stream>>>(tmq_, tmq_, P_);
+        SVDB_LAUNCH_CHECK();
+        return SVDB_OK;
+    }
     if (!pair) {
         auto kern = screen_kernel_of<false>(e4m3, R.norm);
         if (!gc->attr_set[v]) {
@@ -2399,7 +2437,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         const int64_t npad_seed = (int64_t)ntr_seed * scr::kBN;
         ScreenParams PS;
         int maxsub_s = 1;
-        const int nctas_s = screen_schedule(ntq, ntr_seed, PS.sched, &maxsub_s, screen_units(L.pair));
+        const int nctas_s = screen_schedule(ntq, ntr_seed, PS.sched, &maxsub_s, screen_units(L.pair, L.duo));
         const int nsub_s = 2 * maxsub_s;
         if (nsub_s > L.nsub_seed_max) {  // (the layout sized cnt / coff for this schedule)
             svdb_set_error("search_bf16: the seeding schedule does not fit its layout");
