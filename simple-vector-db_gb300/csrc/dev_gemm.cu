@@ -117,34 +117,8 @@ constexpr uint32_t tmem_cols() {
 // ---------------------------------------------------------------------------
 // PTX wrappers (sm_100a family: tcgen05, TMA, mbarrier)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t gtimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
 }
 // Bounded wait: false when the limit ran out or another role raised `abort`.
 __device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, uint64_t limit_ns) {
@@ -168,13 +142,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
             smem_u32(dst)),
         "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
         : "memory");
-}
-// plain bulk copy global -> shared (16-byte aligned, size a multiple of 16)
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
 }
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
@@ -311,6 +278,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// The wait, tied to the registers of the load it completes: the compiler sees
+// it redefine them, so no use of them moves above it.
+template <int N>
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[N]) {
+    tmem_ld_wait();
+#pragma unroll
+    for (int i = 0; i < N; ++i) asm volatile("" : "+r"(r[i]));
+}
 
 // UMMA shared-memory descriptor: K-major, 128-byte swizzle, rows 128 B apart,
 // 8-row swizzle atoms 1024 B apart (SBO); LBO unused for this layout.
@@ -788,7 +763,7 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
                     uint32_t v[32];
                     __syncwarp();  // converged warp for the collective load
                     tmem_ld32(tbase + (uint32_t)(c * 32), v);
-                    tmem_ld_wait();
+                    tmem_ld_wait(v);
                     if (q < GP.nq) {
                         float* o = GP.dump + (size_t)q * GP.dump_ld + row0 + c * 32;
 #pragma unroll
@@ -817,7 +792,7 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
                     uint32_t v[kChunk];
                     __syncwarp();  // converged warp for the collective load
                     tmem_ld16(tbase + (uint32_t)(c * kChunk), v);
-                    tmem_ld_wait();
+                    tmem_ld_wait(v);
                     const float4* rc = rps + c * kChunk;
                     float maxl = -INFINITY;
                     if (NORM) {
@@ -859,17 +834,17 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
             // in accumulator units (cosine F8: exact rescale by a power of two)
             const float thr2 = ACCU ? __fsub_rd(thr, eq0) * ics : __fsub_rd(thr, eq0);
             constexpr int C = NORM ? 32 : 16;  // accumulator columns per collective load
+            constexpr int NC = kBN / 2 / C;    // chunks of this warp's 128 columns
             float tmax = -INFINITY;            // best lower bound (less eq0) of this warp's 128 rows
-#pragma unroll 1
-            for (int c = 0; c < kBN / 2 / C; ++c) {
-                uint32_t v[C];
-                const int rw = row0 + c * C;
+            auto ld_chunk = [&](int c, uint32_t (&v)[C]) {
                 __syncwarp();  // converged warp for the collective load
                 if constexpr (C == 32)
                     tmem_ld32(tbase + (uint32_t)(c * C), v);
                 else
                     tmem_ld16(tbase + (uint32_t)(c * C), v);
-                tmem_ld_wait();
+            };
+            auto screen_chunk = [&](int c, uint32_t (&v)[C]) {
+                const int rw = row0 + c * C;
                 const float4* rc = rps + c * C;
                 // per 8-column group: best upper bound (less eq0); emission is
                 // handled group by group, only where some lane reaches the threshold
@@ -950,6 +925,13 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
                         }
                     }
                 }
+            };
+#pragma unroll 1
+            for (int c = 0; c < NC; ++c) {
+                uint32_t v[C];
+                ld_chunk(c, v);
+                tmem_ld_wait(v);
+                screen_chunk(c, v);
             }
             // The tile half's best lower bound goes to one bin (its unit's: the
             // segment's sequence continues after its warm-up chunks).  Any

@@ -67,18 +67,38 @@ __global__ void __launch_bounds__(256) k_scan_fp64(const double* __restrict__ x6
                                                    int64_t rows_per_slice, const double* __restrict__ qbuf,
                                                    const double* __restrict__ qsq, int nq, int metric, int k,
                                                    Entry* __restrict__ part, int nslices,
-                                                   const int* __restrict__ nq_dev) {
+                                                   const int* __restrict__ nq_dev, int* __restrict__ err_flag) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t qbar;
     if (nq_dev) nq = min(nq, *nq_dev);
     if ((int)blockIdx.y * QB >= nq) return;  // whole block beyond the answered queries
     double* qs = reinterpret_cast<double*>(smem_raw);
     const int qb0 = blockIdx.y * QB;
     const int slice = blockIdx.x;
-    for (size_t i = threadIdx.x; i < (size_t)QB * ld; i += blockDim.x) {
-        const int qi = (int)(i / ld);
-        qs[i] = qb0 + qi < nq ? qbuf[(size_t)(qb0 + qi) * ld + (i % ld)] : 0.0;
+    // The query tile: one bulk copy per query row (rows are ld doubles, a
+    // multiple of 128 bytes, from a 16-byte aligned buffer) completing on
+    // qbar; rows past the last query are zero-filled with plain stores.
+    const int nrow = min(QB, nq - qb0);
+    if (threadIdx.x == 0) {
+        mbar_init(&qbar, 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&qbar, (uint32_t)((size_t)nrow * ld * sizeof(double)));
+        for (int qi = 0; qi < nrow; ++qi)
+            bulk_load(qs + (size_t)qi * ld, qbuf + (size_t)(qb0 + qi) * ld, (uint32_t)(ld * sizeof(double)), &qbar);
     }
-    __syncthreads();
+    for (size_t i = (size_t)nrow * ld + threadIdx.x; i < (size_t)QB * ld; i += blockDim.x) qs[i] = 0.0;
+    __syncthreads();  // qbar initialised before anyone waits on it
+    const bool got = mbar_wait_for(&qbar, 0, 2000000000ull);
+    if (__syncthreads_or(!got)) {
+        // the copy did not complete within 2 s: report it, give the copies in
+        // flight one more bounded wait, and leave without results
+        if (threadIdx.x == 0) {
+            if (err_flag) atomicExch(err_flag, 1);
+            mbar_wait_for(&qbar, 0, 2000000000ull);
+        }
+        __syncthreads();
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, s = lane & 3;
     double qn[QB];
 #pragma unroll
@@ -252,12 +272,16 @@ struct ScanPlan {
     size_t smem;
 };
 
+// dynamic shared memory of a scan CTA at most: the opt-in limit (227 KB)
+// less the static mbarrier of the query tile
+constexpr size_t kScanSmemMax = 227 * 1024 - 64;
+
 static ScanPlan plan_scan(const Store* s, size_t nq, size_t k) {
     ScanPlan p;
     p.ks = k <= 32 ? 1 : (k <= 64 ? 2 : 4);
     const int qbmax = p.ks == 1 ? 8 : (p.ks == 2 ? 4 : 2);
     p.qb = 1;
-    while (p.qb < qbmax && (size_t)p.qb * 2 <= nq) p.qb *= 2;
+    while (p.qb < qbmax && (size_t)p.qb * 2 <= nq && (size_t)p.qb * 2 * s->ld * sizeof(double) <= kScanSmemMax) p.qb *= 2;
     p.nqb = (int)((nq + p.qb - 1) / p.qb);
     const int target = num_sms() * 4;
     int ns = std::max(1, (target + p.nqb - 1) / p.nqb);
@@ -278,10 +302,19 @@ size_t search_fp64_scratch(const Store* s, size_t nq, size_t k) {
 template <int QB, int KS, bool EUC>
 static int launch_scan(Store* s, const ScanPlan& p, const SearchArgs& a, Entry* part) {
     auto kern = k_scan_fp64<QB, KS, EUC>;
-    if (p.smem > 48 * 1024) SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
+    if (p.smem > kScanSmemMax) {  // one query row of more than ~29,000 doubles
+        svdb_set_error("search_fp64: dimension %zu too large for the scan's query tile", s->dim);
+        return SVDB_EINVAL;
+    }
+    if (p.smem > 48 * 1024 - 64)  // with the static mbarrier, beyond the default 48 KB
+        SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
+    if (reinterpret_cast<uintptr_t>(a.q) % 16 != 0) {  // the query tile is bulk-copied
+        svdb_set_error("search_fp64: query buffer not 16-byte aligned");
+        return SVDB_EINVAL;
+    }
     dim3 grid((unsigned)p.nslices, (unsigned)p.nqb);
     kern<<<grid, 256, p.smem, s->stream>>>(s->x64, s->ld, s->live, s->sq64, (int64_t)s->slots, p.rows_per_slice, a.q,
-                                          a.qsq, (int)a.nq, a.metric, (int)a.k, part, p.nslices, a.nq_dev);
+                                          a.qsq, (int)a.nq, a.metric, (int)a.k, part, p.nslices, a.nq_dev, s->d_err);
     SVDB_LAUNCH_CHECK();
     return SVDB_OK;
 }
