@@ -1206,8 +1206,11 @@ __device__ __forceinline__ uint32_t f2u_ord(float f) {
 }
 
 // k-th largest of m ordered values get(i) (every thread of the block calls
-// it): four 8-bit radix passes with a shared histogram
-template <class Get>
+// it): four 8-bit radix passes with a shared histogram.  Each thread keeps
+// U loads in flight; warp 0 finds each pass's digit with a scan over the
+// lanes (lane l holds the counts of digits 255 - 8l .. 248 - 8l, largest
+// first), so no thread walks the 256 bins alone.
+template <int U = 4, class Get>
 __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t* sh) {
     if (threadIdx.x == 0) {
         sh[0] = 0;  // prefix
@@ -1215,27 +1218,58 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
         sh[2] = (uint32_t)k;
     }
     __syncthreads();
+    const int nt = blockDim.x;
     for (int shift = 24; shift >= 0; shift -= 8) {
-        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+        for (int i = threadIdx.x; i < 256; i += nt) hist[i] = 0;
         __syncthreads();
         const uint32_t pre = sh[0], msk = sh[1];
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        int i = threadIdx.x;
+        for (; i + (U - 1) * nt < m; i += U * nt) {
+            uint32_t v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = get(i + u * nt);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if ((v[u] & msk) == pre) atomicAdd(&hist[(v[u] >> shift) & 255u], 1);
+        }
+        for (; i < m; i += nt) {
             const uint32_t v = get(i);
             if ((v & msk) == pre) atomicAdd(&hist[(v >> shift) & 255u], 1);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            int cum = 0, need = (int)sh[2], dsel = 0;
-            for (int dgt = 255; dgt >= 0; --dgt) {
-                if (cum + hist[dgt] >= need) {
-                    dsel = dgt;
-                    break;
-                }
-                cum += hist[dgt];
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            const int need = (int)sh[2];
+            int c[8], sum = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                c[j] = hist[255 - 8 * lane - j];
+                sum += c[j];
             }
-            sh[2] = (uint32_t)(need - cum);
-            sh[0] = pre | ((uint32_t)dsel << shift);
-            sh[1] = msk | (255u << shift);
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int excl = incl - sum;
+            // the lane whose digits take the running count from below `need` to it
+            const unsigned hit = __ballot_sync(0xffffffffu, excl < need && incl >= need);
+            if (lane == (hit ? __ffs(hit) - 1 : 0)) {
+                int cum = total, dsel = 0;  // fewer than `need` values: digit 0, as a full walk ends
+                if (hit) {
+                    cum = excl;
+                    for (int j = 0; j < 8; ++j) {
+                        dsel = 255 - 8 * lane - j;
+                        if (cum + c[j] >= need) break;
+                        cum += c[j];
+                    }
+                }
+                sh[2] = (uint32_t)(need - cum);
+                sh[0] = pre | ((uint32_t)dsel << shift);
+                sh[1] = msk | (255u << shift);
+            }
         }
         __syncthreads();
     }
@@ -1489,7 +1523,7 @@ __global__ void __launch_bounds__(1024) k_select(const int2* __restrict__ cand, 
     }
     uint32_t thr_ord = 0;  // fewer than k candidates: every one survives
     __syncthreads();
-    if (n >= k) thr_ord = block_kth_largest(lower, n, k, hist, s_sh);
+    if (n >= k) thr_ord = block_kth_largest<2>(lower, n, k, hist, s_sh);  // a binary search per value: two in flight
     if (kth_out) {  // seed mode: the exact k-th largest lower bound over these candidates, nothing else
         if (threadIdx.x == 0) {
             const uint32_t u = thr_ord;
