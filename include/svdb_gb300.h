@@ -525,6 +525,15 @@ int svdb_profile_read(VectorDatabase* db, double* ms, int reset);
  * batches of at least 32 queries). */
 int svdb_set_screen_seeding(VectorDatabase* db, int mode);
 
+/* Which screen an SVDB_PREC_FP8 search runs (the results are the same: both
+ * screens are certified and followed by the same exact refinement).  mode
+ * -1: the default rule -- the E4M3 screen for batches of at least 1,024
+ * queries with k <= 32, where it was measured to be the faster one (its
+ * seed sample of 1/16 of the rows settles the looser E4M3 thresholds), the
+ * BF16 screen otherwise; 0: always the BF16 screen; 1: always the E4M3
+ * screen. */
+int svdb_set_fp8_screen(VectorDatabase* db, int mode);
+
 /* The CUDA stream (cudaStream_t) the database's kernels run on. */
 void* svdb_stream(VectorDatabase* db);
 

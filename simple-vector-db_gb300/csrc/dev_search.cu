@@ -397,6 +397,19 @@ extern "C" int svdbd_search(svdbd_store* hs, const double* q, size_t nq, size_t 
                          -1);
 }
 
+// An SVDB_PREC_FP8 search runs the E4M3 screen where it was measured to pay
+// (1M x 768 mixture, cosine): batches of at least 1,024 queries, whose BF16
+// seed pass over 1/16 of the rows settles the E4M3 screen's looser
+// thresholds, and k <= 32.  At k = 48 .. 100 the seed sample held fewer than
+// k rows of a query's neighbourhood, the candidate lists overflowed and the
+// queries fell back to the FP64 scan; at 64 queries and fewer the BF16
+// screen (or the streamed one) was faster.  Elsewhere the BF16 screen runs:
+// its results are identical.
+static bool fp8_screen_pays(const Store* s, size_t nq, size_t k) {
+    if (s->fp8_mode >= 0) return s->fp8_mode == 1;
+    return nq >= 1024 && k <= 32;
+}
+
 int svdb::search_seeded(Store* s, const double* q, size_t nq, size_t k, int metric, int precision, int64_t* ids,
                         double* dists, double* err, int on_device, svdb_search_stats* st, int seed) {
     if (k == 0 || k > 128 || metric < 0 || metric > 2 ||
@@ -483,7 +496,7 @@ int svdb::search_seeded(Store* s, const double* q, size_t nq, size_t k, int metr
             st->reranked += (uint64_t)nq * s->nlive;
         }
     } else {
-        rc = search_bf16(s, a, kscr, kbytes, st, precision == SVDB_PREC_FP8);
+        rc = search_bf16(s, a, kscr, kbytes, st, precision == SVDB_PREC_FP8 && fp8_screen_pays(s, nq, k));
     }
     s->prof_mark(SVDB_NSTAGES);
     s->prof_end();

@@ -901,6 +901,10 @@ int svdbd_store_set_seeding(svdbd_store* hs, int mode) {
     reinterpret_cast<Store*>(hs)->seed_mode = mode < 0 ? -1 : (mode ? 1 : 0);
     return SVDB_OK;
 }
+int svdbd_store_set_fp8(svdbd_store* hs, int mode) {
+    reinterpret_cast<Store*>(hs)->fp8_mode = mode < 0 ? -1 : (mode ? 1 : 0);
+    return SVDB_OK;
+}
 int svdbd_store_profile(svdbd_store* hs, int enable) { return reinterpret_cast<Store*>(hs)->prof_enable(enable != 0); }
 
 int svdbd_store_profile_read(svdbd_store* hs, double* ms, int reset) {

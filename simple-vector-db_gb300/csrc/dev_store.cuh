@@ -86,6 +86,7 @@ struct Store {
     static constexpr int kProfMarks = SVDB_NSTAGES + 1;
     bool prof = false;
     int seed_mode = -1;  // tensor-core screens' threshold seeding: -1 the default rule, 0 off, 1 on
+    int fp8_mode = -1;   // SVDB_PREC_FP8 searches: -1 the default rule, 0 BF16 screens, 1 E4M3 screens
     bool prof_events = false;
     cudaEvent_t pev[kProfRing][kProfMarks];
     int prof_head = 0, prof_pending = 0, prof_cur = -1;

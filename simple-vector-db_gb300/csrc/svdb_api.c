@@ -409,6 +409,16 @@ SVDB_API int svdb_wait(VectorDatabase* db) {
     return d->dev ? svdbd_store_wait(d->dev) : SVDB_OK;
 }
 
+SVDB_API int svdb_set_fp8_screen(VectorDatabase* db, int mode) {
+    if (!db) return SVDB_EINVAL;
+    svdb_db* d = svdb_of(db);
+    pthread_mutex_lock(&db->mutex);
+    int rc = d->dev ? svdbd_store_set_fp8(d->dev, mode) : SVDB_EINVAL;
+    if (!d->dev) svdb_set_error("svdb_set_fp8_screen: the store holds no rows");
+    pthread_mutex_unlock(&db->mutex);
+    return rc;
+}
+
 SVDB_API int svdb_set_screen_seeding(VectorDatabase* db, int mode) {
     if (!db) return SVDB_EINVAL;
     svdb_db* d = svdb_of(db);

@@ -60,6 +60,7 @@ int svdbd_store_wait(svdbd_store* s);
 /* stage timing (svdb_profile / svdb_profile_read) */
 int svdbd_store_profile(svdbd_store* s, int enable);
 int svdbd_store_set_seeding(svdbd_store* s, int mode);
+int svdbd_store_set_fp8(svdbd_store* s, int mode);
 int svdbd_store_profile_read(svdbd_store* s, double* ms, int reset);
 
 /* reference-exact /compare for n slot pairs (host arrays in/out) */

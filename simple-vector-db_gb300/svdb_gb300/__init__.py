@@ -129,6 +129,7 @@ def _load():
         "svdb_last_error": (C.c_char_p, []),
         "svdb_profile": (C.c_int, [vp, C.c_int]),
         "svdb_set_screen_seeding": (C.c_int, [vp, C.c_int]),
+        "svdb_set_fp8_screen": (C.c_int, [vp, C.c_int]),
         "svdb_selftest_bounded_wait": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_uint32)]),
         "svdb_save": (C.c_int, [vp, C.c_char_p, C.c_uint]),
         "svdb_format_compare": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32), sz,
@@ -372,6 +373,11 @@ class VectorDatabase:
 
     def reserve(self, rows: int, dim: int) -> None:
         _check(lib.svdb_reserve(self.ptr, rows, dim), "svdb_reserve")
+
+    def set_fp8_screen(self, mode: int) -> None:
+        """svdb_set_fp8_screen: which screen PREC_FP8 searches run; -1 the
+        default rule (E4M3 for >= 1,024 queries and k <= 32), 0 BF16, 1 E4M3."""
+        _check(lib.svdb_set_fp8_screen(self.ptr, int(mode)), "svdb_set_fp8_screen")
 
     def set_screen_seeding(self, mode: int) -> None:
         """svdb_set_screen_seeding: -1 default (FP8 only), 0 never, 1 always."""

@@ -345,6 +345,7 @@ C = rng.normal(size=(40, 256))
 X = C[rng.integers(0, 40, 60000)] + 0.05 * rng.normal(size=(60000, 256))
 db = S.VectorDatabase(0, 3)
 db.insert_batch(X)
+db.set_fp8_screen(1)
 for nq in (300, 1024):
     Q = C[rng.integers(0, 40, nq)] + 0.05 * rng.normal(size=(nq, 256))
     for metric in (0, 1):

@@ -61,6 +61,7 @@ def mixture_1m(S, W):
     db.reserve(1_000_000, 768)
     db.insert_batch(X)
     db.sync()
+    db.set_fp8_screen(1)  # FP8 cases run the E4M3 screen at every batch size
     yield X, Q, db
     db.close()
 

@@ -32,6 +32,7 @@ def _mixture(rng, n, d, centres, sigma=0.05):
 
 
 def _search(S, db, Q, k, metric=0):
+    db.set_fp8_screen(1)  # the E4M3 screen at every batch size and k (the default rule picks by both)
     st = S.SearchStats()
     ids, vals = db.search(Q, k, metric, PREC_FP8, stats=st)
     return ids, vals, st
@@ -117,4 +118,35 @@ def test_fp8_unseparable_data_falls_back_exact(S, oracle, metric):
     wid, wval = oracle.topk(metric, U, Qu, 10)
     assert np.array_equal(ids, wid) and np.array_equal(vals, wval)
     assert st.bound_failures == 0
+    db.close()
+
+
+def test_fp8_default_rule_picks_the_screen(S, oracle):
+    """svdb_set_fp8_screen(-1), the default: an FP8 search runs the E4M3
+    screen only for batches of at least 1,024 queries with k <= 32, and the
+    BF16 screen otherwise -- the same survivors and kernels as a BF16 search,
+    and the same answers.  Mode 0 always takes the BF16 screen, mode 1 the E4M3 one."""
+    rng = np.random.default_rng(90)
+    C, X = _mixture(rng, 60_000, 128, 48)
+    Q = C[rng.integers(0, 48, 1024)] + 0.05 * rng.normal(size=(1024, 128))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+
+    def run(q, k, prec, mode):
+        db.set_fp8_screen(mode)
+        st = S.SearchStats()
+        ids, vals = db.search(q, k, 0, prec, stats=st)
+        return ids, vals, (st.survivors, st.kernels)  # (candidates depend on the running thresholds' timing)
+
+    for nq, k, e4m3 in ((1024, 10, True), (1024, 32, True), (1024, 33, False), (300, 10, False), (1, 10, False)):
+        wid, wval = oracle.topk(0, X, Q[:nq], k)
+        bi, bv, bst = run(Q[:nq], k, S.PREC_BF16, -1)
+        di, dv, dst = run(Q[:nq], k, PREC_FP8, -1)
+        fi, fv, fst = run(Q[:nq], k, PREC_FP8, 1)
+        zi, zv, zst = run(Q[:nq], k, PREC_FP8, 0)
+        for ids, vals in ((bi, bv), (di, dv), (fi, fv), (zi, zv)):
+            assert np.array_equal(ids, wid) and np.array_equal(vals, wval), (nq, k)
+        assert zst == bst, (nq, k)                   # mode 0: the BF16 screen
+        assert (dst == fst) if e4m3 else (dst == bst), (nq, k, dst, fst, bst)
+        assert fst != bst, (nq, k)                   # mode 1: the E4M3 screen (another funnel)
     db.close()
