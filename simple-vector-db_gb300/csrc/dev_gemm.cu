@@ -67,7 +67,7 @@ constexpr uint32_t kStageB = kBN * kBK * 2;  // 32 KB
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far beyond any legitimate wait
 constexpr int kCapMin = 8192, kCapMax = 65536;   // candidates kept per query (adaptive)
 constexpr int kSubMin = 4096;                     // slots per sub-list when the budget allows
-constexpr int kMaxSub = 512;                      // sub-lists per query: 2 per segment of its query tile
+constexpr int kMaxSub = 1024;                     // sub-lists per query: 2 per segment of its query tile
 constexpr int kWarmUnits = kBN / 2 / kChunk;       // chunks one epilogue thread publishes in a warm-up
 constexpr int kSurvCap = 8192;                    // survivors re-ranked per query
 constexpr size_t kCandBudget = size_t(16) << 30;  // bytes of candidate lists per search (HBM is plentiful)
@@ -339,6 +339,7 @@ __device__ __forceinline__ float screen_bound(float4 p, float qn, float eqq, flo
 // [lo, hi) against one query tile; `sub` numbers the segment among those of
 // its query tile (it selects the candidate sub-lists the segment writes).
 constexpr int kMaxCtas = 320;  // (two CTAs per SM in the DUO form)
+static_assert(2 * kMaxCtas <= scr::kMaxSub, "a query tile split over every CTA has 2 sub-lists per CTA");
 constexpr int kMaxSeg = 4;
 // grp: the search the segment belongs to (a fused launch screens several at
 // once; 0 otherwise); gq: the query tile's index among all the launch's query
@@ -2375,6 +2376,10 @@ static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtens
 // one_list: the streamed screen's single list (no sub-list offsets)
 static int launch_select(Bf16Run& R, int nsub_, bool one_list, const float4* qp_, float* kth) {
     Store* s = R.s;
+    if (nsub_ > scr::kMaxSub) {  // (k_select's prefix of the sub-list counts is in shared memory)
+        svdb_set_error("search_bf16: %d candidate sub-lists per query, more than %d", nsub_, scr::kMaxSub);
+        return SVDB_EINVAL;
+    }
     const Bf16Layout& L = R.L;
     const int nq = (int)R.a.nq, k = (int)R.a.k;
     // small batches carry many candidates per query: wider blocks

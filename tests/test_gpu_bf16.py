@@ -388,3 +388,24 @@ def test_bf16_seeded_thresholds(S, oracle, metric):
                 cands.append(st.candidates)
     assert cands[1] < cands[0]  # seeded thresholds emit fewer candidates
     db.close()
+
+
+@pytest.mark.parametrize("metric", [0, 1, 2])
+def test_bf16_shallow_store_one_query_tile_on_every_cta(S, oracle, metric):
+    """A D = 64 store of 100,000 rows (391 tiles of 256) and a batch of one
+    query tile: the two-CTA-per-SM screen splits the tile over ~300 CTAs,
+    each writing two candidate sub-lists, so the select's prefix over the
+    sub-lists holds ~600 counts.  Answers equal the oracle's."""
+    rng = np.random.default_rng(720 + metric)
+    C = rng.normal(size=(64, 64))
+    X = C[rng.integers(0, 64, 100_000)] + 0.05 * rng.normal(size=(100_000, 64))
+    Q = C[rng.integers(0, 64, 5)] + 0.05 * rng.normal(size=(5, 64))
+    db = S.VectorDatabase(0, 3)
+    db.insert_batch(X)
+    for k in (1, 10, 100):
+        wid, wval = oracle.topk(metric, X, Q, k)
+        st = S.SearchStats()
+        ids, vals = db.search(Q, k, metric, S.PREC_BF16, stats=st)
+        assert np.array_equal(ids, wid) and np.array_equal(vals, wval), k
+        assert st.bound_failures == 0
+    db.close()
