@@ -1278,11 +1278,12 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
 }
 
 // ---------------------------------------------------------------------------
-// stage 1 for a single cosine query: CUDA cores stream the unit-norm BF16
-// shadow (a 128-query tensor tile would be 1/128 used).  Measured on 1M x 768:
-// one query 0.51 ms per search against 0.579 ms through the tensor-core
-// screen; at four queries the FMAs made it slower (screen stage 0.53 ms
-// against ~0.42 ms), so batches of two or more take the tensor cores.
+// stage 1 for one or two cosine queries: CUDA cores stream the unit-norm
+// BF16 shadow (a 128-query tensor tile would be 1/128 used).  Measured on
+// 1M x 768: one query 0.47 ms per search, two 0.486 ms, against 0.58 ms
+// through the tensor-core screen; at four queries the FMAs made it slower
+// (screen stage 0.53 ms against ~0.42 ms), so batches of three or more take
+// the tensor cores.
 // ---------------------------------------------------------------------------
 // The key is the same BF16 dot product bq . bxn as the tensor-core screen's,
 // summed in FP32 by FMAs: the products of BF16 values are exact, and each
@@ -1294,7 +1295,7 @@ __device__ uint32_t block_kth_largest(Get get, int m, int k, int* hist, uint32_t
 // tile maximum (tiles are disjoint, so k tile maxima are keys of k distinct
 // rows: a valid lower bound of the k-th best key); then every row whose upper
 // bound reaches the k-th lower bound is a candidate.
-constexpr int kStreamQ = 1;               // queries per streamed search
+constexpr int kStreamQ = 2;               // queries per streamed search, at most
 constexpr int kStreamWarps = 8;           // warps per store tile (rows 32w .. 32w+31)
 constexpr int kStreamQBytes = 32 * 1024;  // query values (FP32) in shared memory
 
@@ -1309,6 +1310,7 @@ size_t stream_smem(size_t nq, size_t ldb) { return nq * ldb * sizeof(float); }
 // one CTA per SM keeping six 32 KB bulk copies in flight.  Keys go
 // to keys[q][slot]; each warp's maximum over its 32 rows of a tile to
 // wmax[q][tile * 8 + warp] (disjoint rows: k of them bound the k-th best key).
+template <int QN>
 __global__ void __launch_bounds__(32 * kStreamWarps)
     k_stream_keys(const uint8_t* __restrict__ xbn, int KB, const __nv_bfloat16* __restrict__ qb, size_t ldb, int nq,
                   const uint32_t* __restrict__ vbits, size_t npad, int ntr, float* __restrict__ keys,
@@ -1326,14 +1328,14 @@ __global__ void __launch_bounds__(32 * kStreamWarps)
     // rows of step s are 32 warp + 4 s + rsub, so r & 7 = rsub (even s) or rsub + 4
     const int ce = g8 ^ rsub, co = g8 ^ (rsub + 4);
     const uint8_t* src = xbn + ((size_t)t * KB * 256 + warp * 32 + rsub) * 128 + g8 * 16;
-    float acc[8][kStreamQ];
+    float acc[8][QN];
 #pragma unroll
     for (int s = 0; s < 8; ++s)
 #pragma unroll
-        for (int qi = 0; qi < kStreamQ; ++qi) acc[s][qi] = 0.f;
+        for (int qi = 0; qi < QN; ++qi) acc[s][qi] = 0.f;
     auto fold = [&](const uint4 (&v)[8], int kb) {
 #pragma unroll
-        for (int qi = 0; qi < kStreamQ; ++qi) {
+        for (int qi = 0; qi < QN; ++qi) {
             if (qi < nq) {
                 const float* qq = s_q + (size_t)qi * K + kb * 64;
                 const float4 e0 = *reinterpret_cast<const float4*>(qq + ce * 8);
@@ -1375,16 +1377,16 @@ __global__ void __launch_bounds__(32 * kStreamWarps)
         fold(v0, kb);
     }
     const uint32_t vw = __ldg(vbits + (((size_t)t * 256 + warp * 32) >> 5));  // this warp's 32 rows
-    float m[kStreamQ];
+    float m[QN];
 #pragma unroll
-    for (int qi = 0; qi < kStreamQ; ++qi) m[qi] = -INFINITY;
+    for (int qi = 0; qi < QN; ++qi) m[qi] = -INFINITY;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int rw = s * 4 + rsub;  // row within the warp's 32
         const bool valid = (vw >> rw) & 1u;
         const size_t slot = (size_t)t * 256 + warp * 32 + rw;
 #pragma unroll
-        for (int qi = 0; qi < kStreamQ; ++qi) {
+        for (int qi = 0; qi < QN; ++qi) {
             float a = acc[s][qi];
             a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 1));
             a = __fadd_rn(a, __shfl_xor_sync(0xffffffffu, a, 2));
@@ -1396,7 +1398,7 @@ __global__ void __launch_bounds__(32 * kStreamWarps)
         }
     }
 #pragma unroll
-    for (int qi = 0; qi < kStreamQ; ++qi) {
+    for (int qi = 0; qi < QN; ++qi) {
         float x = m[qi];
         for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
         if (lane == 0 && qi < nq) wmax[(size_t)qi * ntr * kStreamWarps + (size_t)t * kStreamWarps + warp] = x;
@@ -2513,7 +2515,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
         k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
                                                                               a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
-    // a single cosine query: the streamed screen, one candidate list
+    // one or two cosine queries: the streamed screen, one candidate list per query
     R.stream = maxsub_ext <= 0 && norm && !f8 && nq <= kStreamQ &&
                (size_t)nq * s->ldb * sizeof(float) <= (size_t)kStreamQBytes;
     R.nsub_use = R.stream ? 1 : L.nsub;
@@ -2574,10 +2576,12 @@ static int bf16_screen(Bf16Run& R) {
     const int KB = (int)(s->ldb / scr::kBK);
     const size_t smem = stream_smem((size_t)nq, s->ldb);
     if (!R.gc->stream_attr) {
-        SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamQBytes));
+        SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamQBytes));
+        SVDB_CUDA(cudaFuncSetAttribute(k_stream_keys<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamQBytes));
         R.gc->stream_attr = true;
     }
-    k_stream_keys<<<(unsigned)L.ntr, 32 * kStreamWarps, smem, s->stream>>>(
+    static_assert(kStreamQ == 2, "one instantiation per query count");
+    (nq == 1 ? k_stream_keys<1> : k_stream_keys<2>)<<<(unsigned)L.ntr, 32 * kStreamWarps, smem, s->stream>>>(
         reinterpret_cast<const uint8_t*>(s->xbn), KB, R.at<__nv_bfloat16>(L.qb), s->ldb, nq, R.at<uint32_t>(L.vbits),
         L.npad, L.ntr, keys, tmax);
     SVDB_LAUNCH_CHECK();
