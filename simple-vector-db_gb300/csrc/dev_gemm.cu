@@ -58,6 +58,9 @@ constexpr int kBM = 128;  // queries per tile (TMEM lanes)
 constexpr int kBN = 256;  // store rows per tile (accumulator columns)
 constexpr int kBK = 64;   // K per stage: one 128-byte swizzle row of BF16
 constexpr int kStages = 4;
+// Small batches: a query tile of at most 32 (64) queries stages only those
+// rows, and the ring is 6 (5) deep instead of 4.
+constexpr int stages_for_rows(int qr) { return qr <= 32 ? 6 : (qr <= 64 ? 5 : kStages); }
 constexpr int kEpiWarps = 8;  // two per TMEM lane quadrant, each owning half of the columns
 constexpr int kChunk = 16;    // accumulator columns per tcgen05.ld in the epilogue
 constexpr int kThreads = 32 * (2 + kEpiWarps);
@@ -87,10 +90,16 @@ constexpr int kStats = 8;
 // each CTA holds its own 128 queries and half of the 256-row store tile, so
 // a stage is 32 KB instead of 48 KB and the ring is 6 deep.  DUO (two CTAs
 // on each SM): a 2-deep ring, so that two CTAs' shared memory fits one SM.
-template <bool PAIR, bool DUO = false>
+// QR < 128 (a batch of at most QR queries): a stage holds those query rows
+// only (4 or 8 KB) and the ring is deeper, so more of the store is in
+// flight.  The M = 128 MMA still reads 128 rows from the stage's address:
+// rows past QR are whatever follows in shared memory (the next stages), and
+// only the accumulator lanes of absent queries, which the epilogue ignores,
+// depend on them.
+template <bool PAIR, bool DUO = false, int QR = kBM>
 struct SmemT {
-    static constexpr int ST = PAIR ? 6 : (DUO ? 2 : kStages);
-    static constexpr uint32_t SA = kStageA;
+    static constexpr int ST = PAIR ? 6 : (DUO ? 2 : stages_for_rows(QR));
+    static constexpr uint32_t SA = (uint32_t)QR * kBK * 2;
     static constexpr uint32_t SB = PAIR ? kStageB / 2 : kStageB;
     // 1024-byte aligned stage buffers first (SW128 atoms need 1024 B alignment)
     uint8_t a[ST][SA];
@@ -107,6 +116,9 @@ struct SmemT {
     int abort;
 };
 using Smem = SmemT<false>;
+static_assert(sizeof(SmemT<false, false, 32>) + 1024 <= 232448 && sizeof(SmemT<false, false, 64>) + 1024 <= 232448,
+              "the small-batch rings fit the opt-in shared memory");
+static_assert(32 * kBK * 2 % 1024 == 0, "SW128 stages start on 1024-byte boundaries");
 // DUO: accumulators per CTA (TMEM columns / 256); one, so two CTAs share an SM's 512 columns
 template <bool DUO>
 constexpr uint32_t tmem_cols() {
@@ -468,14 +480,16 @@ using ScreenParamsT = std::conditional_t<MULTI, ScreenParamsMulti, ScreenParams>
 // DUO: two CTAs per SM, each with one accumulator (the other CTA's MMAs run
 // while this one's epilogue drains it) and a 2-deep ring; twice the epilogue
 // warps per SM, for stores whose tiles are a few k blocks deep.
-template <bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false, bool DUO = false>
+template <bool NORM, bool F8 = false, bool DUMP = false, bool PAIR = false, bool MULTI = false, bool DUO = false,
+          int QR = scr::kBM>
 __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
     k_screen_bf16(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmx,
                   const __grid_constant__ ScreenParamsT<MULTI> P) {
     static_assert(!(MULTI && (PAIR || DUMP)), "a fused launch is single-CTA and screens");
     static_assert(!(DUO && (PAIR || DUMP || MULTI)), "the two-CTA form is a plain screen");
+    static_assert(QR == scr::kBM || !(PAIR || DUMP || MULTI || DUO), "the small-batch forms are plain screens");
     using namespace scr;
-    using SM = SmemT<PAIR, DUO>;
+    using SM = SmemT<PAIR, DUO, QR>;
     constexpr uint32_t TC = tmem_cols<DUO>();
     constexpr int ST = SM::ST;
     // cosine FP8 works in accumulator units (thresholds scaled in, keys out);
@@ -565,7 +579,7 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
                                          qt * 2 * kBM + (int)rank * kBM);
                         tma_load_2d_pair(S.b[stage], &tmx, fb, 0, (r * KB + kb) * kBN + (int)rank * (kBN / 2));
                     } else {
-                        mbar_expect_tx(&S.full[stage], kStageA + kStageB);
+                        mbar_expect_tx(&S.full[stage], SM::SA + kStageB);  // (QR < 128: a query map of QR-row boxes)
                         tma_load_2d(S.a[stage], tm, &S.full[stage], kb * (F8 ? 2 * kBK : kBK), qt * kBM);
                         // the store tile: one contiguous 32 KB block, already swizzled
                         bulk_load(S.b[stage], GP.xblk + ((size_t)r * KB + kb) * kStageB, kStageB, &S.full[stage]);
@@ -1966,6 +1980,8 @@ struct GemmPlanCache {
     size_t screen_smem_pair = 0;
     bool attr_pair[4] = {};
     bool attr_duo[4] = {};
+    bool attr_sq[2][4] = {};       // the small-batch forms: 32 and 64 query rows
+    size_t screen_smem_sq[2] = {};
     size_t screen_smem_duo = 0;
 };
 
@@ -1989,6 +2005,8 @@ static int gemm_cache(Store* s, GemmPlanCache** out) {
         c->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
         c->screen_smem = sizeof(scr::Smem) + 1024;
         c->screen_smem_duo = sizeof(scr::SmemT<false, true>) + 1024;
+        c->screen_smem_sq[0] = sizeof(scr::SmemT<false, false, 32>) + 1024;
+        c->screen_smem_sq[1] = sizeof(scr::SmemT<false, false, 64>) + 1024;
         c->screen_smem_pair = sizeof(scr::SmemT<true>) + 1024;
         s->gemm = c;
     }
@@ -2134,6 +2152,7 @@ static int launch_screen(K kern, bool pair, int units, size_t smem, cudaStream_t
 struct Bf16Layout {
     bool pair = false;  // the paired screen (query tiles of 256)
     bool duo = false;   // two CTAs per SM (shallow tiles)
+    int qr = scr::kBM;  // query rows per stage: 32 / 64 for batches that small (deeper rings)
     size_t qb, qscale, qb16, qpar16, seed, q32, qpar, rpar, spar, vbits, tau, bins, cnt, coff, cand, surv, nsurv, nref, sig, perm, flags, alpha, redo, redo_n, stats, rq, rsq, rres, rscr, total;
     size_t tmax = 0, cut = 0;  // the streamed screen of a single query (its keys reuse spar: npad floats)
     int ntr, cap;
@@ -2254,6 +2273,10 @@ static Bf16Layout bf16_layout(const Store* s, size_t nq, int maxsub_ext = 0) {
     } else {
         L.pair = screen_pair(nq);
         L.duo = screen_duo(s, L.pair);
+        // measured on 1M x 768: screen 0.38-0.40 -> 0.32-0.34 ms at 3-32 queries (32 rows,
+        // 6 stages), ~0.37 -> 0.355 ms at 48 (64 rows, 5 stages); at 64 queries the
+        // 5-deep ring was no faster (0.382 against 0.377 ms)
+        if (!L.pair && !L.duo) L.qr = nq <= 32 ? 32 : (nq <= 48 ? 64 : scr::kBM);
         const size_t tq = L.pair ? 2 * scr::kBM : scr::kBM;
         L.nctas = screen_schedule((int)((nq + tq - 1) / tq), L.ntr, L.sched, &maxsub, screen_units(L.pair, L.duo));
     }
@@ -2336,6 +2359,14 @@ static auto screen_kernel_of(bool e4m3, bool norm) {
                 : (norm ? k_screen_bf16<true, false, false, PR> : k_screen_bf16<false, false, false, PR>);
 }
 
+template <int QR>
+static auto small_batch_kernel_of(bool e4m3, bool norm) {
+    return e4m3 ? (norm ? k_screen_bf16<true, true, false, false, false, false, QR>
+                        : k_screen_bf16<false, true, false, false, false, false, QR>)
+                : (norm ? k_screen_bf16<true, false, false, false, false, false, QR>
+                        : k_screen_bf16<false, false, false, false, false, false, QR>);
+}
+
 // one screen over nunits units (CTAs or pairs) with the query tensor map tmq_;
 // the paired form also gets the tensor map of the shadow's tiles
 static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtensorMap& tmq_, const ScreenParams& P_) {
@@ -2354,6 +2385,15 @@ static int run_screen(Bf16Run& R, bool e4m3, bool pair, int nunits, const CUtens
         kern<<<(unsigned)nunits, scr::kThreads, gc->screen_smem_duo, s->stream>>>(tmq_, tmq_, P_);
         SVDB_LAUNCH_CHECK();
         return SVDB_OK;
+    }
+    if (!pair && R.L.qr < scr::kBM) {  // a small batch: the deeper ring (tmq_ has boxes of qr rows)
+        const int f = R.L.qr == 32 ? 0 : 1;
+        auto kern = f == 0 ? small_batch_kernel_of<32>(e4m3, R.norm) : small_batch_kernel_of<64>(e4m3, R.norm);
+        if (!gc->attr_sq[f][v]) {
+            SVDB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc->screen_smem_sq[f]));
+            gc->attr_sq[f][v] = true;
+        }
+        return launch_screen(kern, false, nunits, gc->screen_smem_sq[f], s->stream, tmq_, tmq_, P_);
     }
     if (!pair) {
         auto kern = screen_kernel_of<false>(e4m3, R.norm);
@@ -2477,7 +2517,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
             nullptr, rpar, spar, alpha, vbits);
         SVDB_LAUNCH_CHECK();
         CUtensorMap tmq16;
-        rc = make_map(gc, &tmq16, qb16, a.nq, s->ldb, scr::kBM);
+        rc = make_map(gc, &tmq16, qb16, a.nq, s->ldb, L.qr);
         if (rc) return rc;
         PS.g.xblk = reinterpret_cast<const uint8_t*>(norm ? (const void*)s->xbn : (const void*)s->xb);
         PS.g.qscale = qscale;
@@ -2529,7 +2569,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
     R.kernels += 3;
     if (R.stream) return SVDB_OK;
 
-    rc = f8 ? make_map8(gc, &R.tmq, qb, a.nq, s->ldb8, scr::kBM) : make_map(gc, &R.tmq, qb, a.nq, s->ldb, scr::kBM);
+    rc = f8 ? make_map8(gc, &R.tmq, qb, a.nq, s->ldb8, L.qr) : make_map(gc, &R.tmq, qb, a.nq, s->ldb, L.qr);
     if (rc) return rc;
     GroupParams& g = R.P.g;
     g.xblk = reinterpret_cast<const uint8_t*>(f8 ? (norm ? (const void*)s->xbn8 : (const void*)s->xb8)
