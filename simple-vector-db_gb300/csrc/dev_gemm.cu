@@ -995,20 +995,24 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
 // per-search preparation
 // ---------------------------------------------------------------------------
 // BF16 copies of the (already padded FP64) queries + per-query bound terms.
-// 4 lanes per query, canonical FP64 reductions.
+// One warp per query: the FP64 pipe is narrow, and with fewer lanes a small
+// batch waits on each lane's long chain of dependent FP64 operations.  The
+// two sums of squares feed only the bounds, whose 1 + 2^-30 factor covers
+// their FP64 rounding in any order.
+constexpr int kPrepLanes = 32;
 __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
                             size_t ldb, int metric, __nv_bfloat16* __restrict__ qb, float* __restrict__ q32,
                             float4* __restrict__ qpar) {
-    const int lane = threadIdx.x & 31, s = lane & 3;
-    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
-    const bool active = qi < nq;
+    const int lane = threadIdx.x & 31, s = lane;
+    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const bool active = qi < nq;  // warp-uniform
     double res = 0.0, bsq = 0.0;
     bool finite = true;
     if (active) {
         const double* src = qbuf + (size_t)qi * ld;
         __nv_bfloat16* dst = qb + (size_t)qi * ldb;
         float* dst32 = q32 + (size_t)qi * ld;
-        for (size_t j = 2 * s; j < ld; j += 8) {
+        for (size_t j = 2 * s; j < ld; j += 2 * kPrepLanes) {
             const double a = src[j], c = src[j + 1];
             const __nv_bfloat16 ha = __double2bfloat16(a), hc = __double2bfloat16(c);
             const double fa = (double)__bfloat162float(ha), fc = (double)__bfloat162float(hc);
@@ -1021,14 +1025,16 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
             dst[j + 1] = hc;
             *reinterpret_cast<float2*>(dst32 + j) = make_float2(__double2float_rn(a), __double2float_rn(c));
         }
-        for (size_t j = ld + 2 * s; j < ldb; j += 8) {
+        for (size_t j = ld + 2 * s; j < ldb; j += 2 * kPrepLanes) {
             dst[j] = __float2bfloat16(0.0f);
             dst[j + 1] = __float2bfloat16(0.0f);
         }
     }
-    res = group4_sum(res);
-    bsq = group4_sum(bsq);
-    const unsigned all_finite = __all_sync(0xffffffffu, finite);  // conservative: any lane of the warp
+    for (int o = 16; o > 0; o >>= 1) {
+        res += __shfl_xor_sync(0xffffffffu, res, o);
+        bsq += __shfl_xor_sync(0xffffffffu, bsq, o);
+    }
+    const unsigned all_finite = __all_sync(0xffffffffu, finite);  // the warp is the query
     if (active && s == 0) {
         const double sq = qsq[qi];
         const double up = 1.0 + 9.313225746154785e-10;  // 1 + 2^-30: FP64 rounding of the sums
@@ -1067,20 +1073,19 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
 __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
                           size_t ldb8, int metric, uint8_t* __restrict__ q8, float* __restrict__ q32,
                           float4* __restrict__ qpar, float* __restrict__ qscale) {
-    const int lane = threadIdx.x & 31, s = lane & 3;
-    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
-    const bool active = qi < nq;
+    const int lane = threadIdx.x & 31, s = lane;  // one warp per query, as k_prep_bf16
+    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const bool active = qi < nq;  // warp-uniform
     const double* src = qbuf + (size_t)(active ? qi : 0) * ld;
     double m = 0.0;
     bool finite = true;
     if (active)
-        for (size_t j = s; j < ld; j += 4) {
+        for (size_t j = s; j < ld; j += kPrepLanes) {
             const double a = src[j];
             finite = finite && isfinite(a);
             m = fmax(m, fabs(a));
         }
-    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
-    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 1));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     int e = 0;
     if (m > 0.0 && isfinite(m)) {
         e = max(-126, min(126, e4m3_fit_exp(m)));  // |e| >= 100 marks the query invalid below
@@ -1090,7 +1095,7 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
     if (active) {
         uint8_t* dst = q8 + (size_t)qi * ldb8;
         float* dst32 = q32 + (size_t)qi * ld;
-        for (size_t j = 2 * s; j < ld; j += 8) {
+        for (size_t j = 2 * s; j < ld; j += 2 * kPrepLanes) {
             const double a = src[j], c = src[j + 1];
             const __nv_fp8_storage_t ea = __nv_cvt_double_to_fp8(a * sc, __NV_SATFINITE, __NV_E4M3);
             const __nv_fp8_storage_t ec = __nv_cvt_double_to_fp8(c * sc, __NV_SATFINITE, __NV_E4M3);
@@ -1104,13 +1109,15 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
             dst[j + 1] = ec;
             *reinterpret_cast<float2*>(dst32 + j) = make_float2(__double2float_rn(a), __double2float_rn(c));
         }
-        for (size_t j = ld + 2 * s; j < ldb8; j += 8) {
+        for (size_t j = ld + 2 * s; j < ldb8; j += 2 * kPrepLanes) {
             dst[j] = 0;
             dst[j + 1] = 0;
         }
     }
-    res = group4_sum(res);
-    bsq = group4_sum(bsq);
+    for (int o = 16; o > 0; o >>= 1) {
+        res += __shfl_xor_sync(0xffffffffu, res, o);
+        bsq += __shfl_xor_sync(0xffffffffu, bsq, o);
+    }
     const unsigned all_finite = __all_sync(0xffffffffu, finite);
     if (active && s == 0) {
         const double sq = qsq[qi];
@@ -2506,7 +2513,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
             svdb_set_error("search_bf16: the seeding schedule does not fit its layout");
             return SVDB_EINVAL;
         }
-        k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
+        k_prep_bf16<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
                                                                               qb16, q32, qpar16);
         SVDB_LAUNCH_CHECK();
         k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, nsub_s, flags, nq, k, alpha,
@@ -2549,10 +2556,10 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
     }
 
     if (f8)
-        k_prep_f8<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(
+        k_prep_f8<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(
             a.q, a.qsq, nq, s->ld, s->ldb8, a.metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
     else
-        k_prep_bf16<<<(unsigned)((a.nq * 4 + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
+        k_prep_bf16<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
                                                                               a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
     // one or two cosine queries: the streamed screen, one candidate list per query
@@ -3120,10 +3127,10 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
     rc = prep_queries_fp64(s, qraw, s->dim, nq, qbuf, qsq);
     if (rc) return rc;
     if (f8)
-        k_prep_f8<<<(unsigned)((nq * 4 + 255) / 256), 256, 0, s->stream>>>(
+        k_prep_f8<<<(unsigned)((nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(
             qbuf, qsq, (int)nq, s->ld, s->ldb8, metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
     else
-        k_prep_bf16<<<(unsigned)((nq * 4 + 255) / 256), 256, 0, s->stream>>>(
+        k_prep_bf16<<<(unsigned)((nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(
             qbuf, qsq, (int)nq, s->ld, s->ldb, metric, reinterpret_cast<__nv_bfloat16*>(qb), q32, qpar);
     SVDB_LAUNCH_CHECK();
     CUtensorMap tmq;
