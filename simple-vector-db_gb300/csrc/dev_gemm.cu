@@ -116,6 +116,7 @@ struct SmemT {
     int abort;
 };
 using Smem = SmemT<false>;
+static_assert(Smem::SA == kStageA, "the default stage holds a full 128-query tile");
 static_assert(sizeof(SmemT<false, false, 32>) + 1024 <= 232448 && sizeof(SmemT<false, false, 64>) + 1024 <= 232448,
               "the small-batch rings fit the opt-in shared memory");
 static_assert(32 * kBK * 2 % 1024 == 0, "SW128 stages start on 1024-byte boundaries");
@@ -1000,13 +1001,13 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
 // two sums of squares feed only the bounds, whose 1 + 2^-30 factor covers
 // their FP64 rounding in any order.
 constexpr int kPrepLanes = 32;
-__global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
+__global__ void k_prep_bf16(const double* __restrict__ qbuf, int nq, size_t ld,
                             size_t ldb, int metric, __nv_bfloat16* __restrict__ qb, float* __restrict__ q32,
                             float4* __restrict__ qpar) {
     const int lane = threadIdx.x & 31, s = lane;
     const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const bool active = qi < nq;  // warp-uniform
-    double res = 0.0, bsq = 0.0;
+    double res = 0.0, bsq = 0.0, sqw = 0.0;  // sqw: |q|^2 in this warp's order (bounds only)
     bool finite = true;
     if (active) {
         const double* src = qbuf + (size_t)qi * ld;
@@ -1019,6 +1020,8 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
             finite = finite && isfinite(fa) && isfinite(fc);
             bsq = fma(fa, fa, bsq);
             bsq = fma(fc, fc, bsq);
+            sqw = fma(a, a, sqw);
+            sqw = fma(c, c, sqw);
             res = fma(a - fa, a - fa, res);
             res = fma(c - fc, c - fc, res);
             dst[j] = ha;
@@ -1033,11 +1036,14 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
     for (int o = 16; o > 0; o >>= 1) {
         res += __shfl_xor_sync(0xffffffffu, res, o);
         bsq += __shfl_xor_sync(0xffffffffu, bsq, o);
+        sqw += __shfl_xor_sync(0xffffffffu, sqw, o);
     }
     const unsigned all_finite = __all_sync(0xffffffffu, finite);  // the warp is the query
     if (active && s == 0) {
-        const double sq = qsq[qi];
+        // an upper bound of |q|^2 (the canonical |q|^2 of the reported values
+        // may still be in flight on another stream)
         const double up = 1.0 + 9.313225746154785e-10;  // 1 + 2^-30: FP64 rounding of the sums
+        const double sq = sqw * up;
         const double qn = sqrt(sq) * up;
         const double eq = sqrt(res) * up;
         const double bqn = sqrt(bsq) * up;
@@ -1070,7 +1076,7 @@ __global__ void k_prep_bf16(const double* __restrict__ qbuf, const double* __res
 // accumulation of E4M3 products is modelled pessimistically, as if each K=32
 // step kept only 13 bits: c_acc = (ldb8/32 + 1) x 40 x 2^-13 of |bq| |bx|
 // (for D = 768 about 0.12; the E4M3 rounding itself is ~0.04 per vector).
-__global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restrict__ qsq, int nq, size_t ld,
+__global__ void k_prep_f8(const double* __restrict__ qbuf, int nq, size_t ld,
                           size_t ldb8, int metric, uint8_t* __restrict__ q8, float* __restrict__ q32,
                           float4* __restrict__ qpar, float* __restrict__ qscale) {
     const int lane = threadIdx.x & 31, s = lane;  // one warp per query, as k_prep_bf16
@@ -1091,7 +1097,7 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
         e = max(-126, min(126, e4m3_fit_exp(m)));  // |e| >= 100 marks the query invalid below
     }
     const double sc = ldexp(1.0, e);
-    double res = 0.0, bsq = 0.0;
+    double res = 0.0, bsq = 0.0, sqw = 0.0;  // sqw: |q|^2 in this warp's order (bounds only)
     if (active) {
         uint8_t* dst = q8 + (size_t)qi * ldb8;
         float* dst32 = q32 + (size_t)qi * ld;
@@ -1103,6 +1109,8 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
             const double fc = (double)__half2float(__half(__nv_cvt_fp8_to_halfraw(ec, __NV_E4M3))) / sc;
             bsq = fma(fa, fa, bsq);
             bsq = fma(fc, fc, bsq);
+            sqw = fma(a, a, sqw);
+            sqw = fma(c, c, sqw);
             res = fma(a - fa, a - fa, res);
             res = fma(c - fc, c - fc, res);
             dst[j] = ea;
@@ -1117,11 +1125,12 @@ __global__ void k_prep_f8(const double* __restrict__ qbuf, const double* __restr
     for (int o = 16; o > 0; o >>= 1) {
         res += __shfl_xor_sync(0xffffffffu, res, o);
         bsq += __shfl_xor_sync(0xffffffffu, bsq, o);
+        sqw += __shfl_xor_sync(0xffffffffu, sqw, o);
     }
     const unsigned all_finite = __all_sync(0xffffffffu, finite);
     if (active && s == 0) {
-        const double sq = qsq[qi];
         const double up = 1.0 + 9.313225746154785e-10;
+        const double sq = sqw * up;  // an upper bound of |q|^2, as in k_prep_bf16
         const double qn = sqrt(sq) * up;
         const double eq = sqrt(res) * up;
         const double bqn = sqrt(bsq) * up;
@@ -2513,7 +2522,7 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
             svdb_set_error("search_bf16: the seeding schedule does not fit its layout");
             return SVDB_EINVAL;
         }
-        k_prep_bf16<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb, a.metric,
+        k_prep_bf16<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(a.q, nq, s->ld, s->ldb, a.metric,
                                                                               qb16, q32, qpar16);
         SVDB_LAUNCH_CHECK();
         k_init_search<<<(unsigned)((a.nq + 255) / 256), 256, 0, s->stream>>>(tau, bins, cnt, nsub_s, flags, nq, k, alpha,
@@ -2557,9 +2566,9 @@ static int bf16_begin(Bf16Run& R, Store* s, const SearchArgs& a, void* scratch, 
 
     if (f8)
         k_prep_f8<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(
-            a.q, a.qsq, nq, s->ld, s->ldb8, a.metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
+            a.q, nq, s->ld, s->ldb8, a.metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
     else
-        k_prep_bf16<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(a.q, a.qsq, nq, s->ld, s->ldb,
+        k_prep_bf16<<<(unsigned)((a.nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(a.q, nq, s->ld, s->ldb,
                                                                               a.metric, qb, q32, qpar);
     SVDB_LAUNCH_CHECK();
     // one or two cosine queries: the streamed screen, one candidate list per query
@@ -2783,6 +2792,11 @@ int search_bf16(Store* s, const SearchArgs& a, void* scratch, size_t scratch_byt
     }
     int rc = bf16_begin(*R, s, a, scratch, scratch_bytes, f8, 0);
     if (!rc) rc = bf16_screen(*R);
+    // the refinement and re-rank read the canonical |q|^2 (the screen did not)
+    if (!rc && a.qsq_ready && cudaStreamWaitEvent(s->stream, a.qsq_ready, 0) != cudaSuccess) {
+        svdb_set_error("search_bf16: cudaStreamWaitEvent: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = SVDB_ECUDA;
+    }
     if (!rc) {
         s->prof_mark(2);
         rc = bf16_end(*R, st);
@@ -3128,10 +3142,10 @@ int debug_screen_acc(Store* s, const double* hq, size_t nq, int metric, bool f8,
     if (rc) return rc;
     if (f8)
         k_prep_f8<<<(unsigned)((nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(
-            qbuf, qsq, (int)nq, s->ld, s->ldb8, metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
+            qbuf, (int)nq, s->ld, s->ldb8, metric, reinterpret_cast<uint8_t*>(qb), q32, qpar, qscale);
     else
         k_prep_bf16<<<(unsigned)((nq * kPrepLanes + 255) / 256), 256, 0, s->stream>>>(
-            qbuf, qsq, (int)nq, s->ld, s->ldb, metric, reinterpret_cast<__nv_bfloat16*>(qb), q32, qpar);
+            qbuf, (int)nq, s->ld, s->ldb, metric, reinterpret_cast<__nv_bfloat16*>(qb), q32, qpar);
     SVDB_LAUNCH_CHECK();
     CUtensorMap tmq;
     rc = f8 ? make_map8(gc, &tmq, qb, nq, s->ldb8, scr::kBM) : make_map(gc, &tmq, qb, nq, s->ldb, scr::kBM);

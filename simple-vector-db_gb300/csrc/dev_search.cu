@@ -49,6 +49,59 @@ __global__ void k_prep_queries(const double* __restrict__ q, size_t qs, int nq, 
     if (active && s == 0) qsq[qi] = p;
 }
 
+// The canonical sums of squares alone, with exactly k_prep_queries'
+// arithmetic (so the values are identical), and the padded copy alone, one
+// thread per element.  A search whose screen needs no canonical |q|^2 runs the
+// first beside its screen on the store's side stream.
+__global__ void k_query_sq(const double* __restrict__ q, size_t qs, int nq, int d, size_t ld,
+                           double* __restrict__ qsq) {
+    const int lane = threadIdx.x & 31, s = lane & 3;
+    const int qi = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2);
+    const bool active = qi < nq;
+    double p = 0.0;
+    if (active) {
+        const double* src = q + (size_t)qi * qs;
+        for (size_t j = 2 * s; j < ld; j += 8) {
+            const double a = j < (size_t)d ? src[j] : 0.0;
+            const double b = j + 1 < (size_t)d ? src[j + 1] : 0.0;
+            p = fma(a, a, p);
+            p = fma(b, b, p);
+        }
+    }
+    p = group4_sum(p);
+    if (active && s == 0) qsq[qi] = p;
+}
+
+__global__ void k_pad_queries(const double* __restrict__ q, size_t qs, int64_t n, int d, size_t ld,
+                              double* __restrict__ qbuf) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // element of the nq x ld buffer
+    if (i >= n) return;
+    const int64_t qi = i / (int64_t)ld;
+    const size_t j = (size_t)(i - qi * (int64_t)ld);
+    qbuf[i] = j < (size_t)d ? q[(size_t)qi * qs + j] : 0.0;
+}
+
+int prep_queries_split(Store* s, const double* q_dev, size_t qs, size_t nq, double* qbuf, double* qsq,
+                       cudaEvent_t* ready) {
+    *ready = nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        cs = cudaStreamCaptureStatusActive;
+    }
+    if (cs != cudaStreamCaptureStatusNone || s->side_ready() != SVDB_OK) return prep_queries_fp64(s, q_dev, qs, nq, qbuf, qsq);
+    SVDB_CUDA(cudaEventRecord(s->ev_fork, s->stream));  // the queries are in place (their upload is on the stream)
+    SVDB_CUDA(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+    k_query_sq<<<(unsigned)((nq * 4 + 255) / 256), 256, 0, s->side>>>(q_dev, qs, (int)nq, (int)s->dim, s->ld, qsq);
+    SVDB_LAUNCH_CHECK();
+    SVDB_CUDA(cudaEventRecord(s->ev_side, s->side));
+    const int64_t n = (int64_t)nq * (int64_t)s->ld;
+    k_pad_queries<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(q_dev, qs, n, (int)s->dim, s->ld, qbuf);
+    SVDB_LAUNCH_CHECK();
+    *ready = s->ev_side;
+    return SVDB_OK;
+}
+
 int prep_queries_fp64(Store* s, const double* q_dev, size_t qs, size_t nq, double* qbuf, double* qsq) {
     k_prep_queries<<<(unsigned)((nq * 4 + 255) / 256), 256, 0, s->stream>>>(q_dev, qs, (int)nq, (int)s->dim, s->ld,
                                                                          qbuf, qsq);
@@ -479,9 +532,15 @@ int svdb::search_seeded(Store* s, const double* q, size_t nq, size_t k, int metr
         a.err = (double*)(outp + out_n * (sizeof(int64_t) + sizeof(double)));
     }
     uint32_t kernels = 0;
-    rc = prep_queries_fp64(s, qsrc, s->dim, nq, qbuf, qsq);
+    // the tensor-core screens need no canonical |q|^2: it is summed beside them
+    cudaEvent_t qsq_ready = nullptr;
+    if (s->nlive && use_bf16)
+        rc = prep_queries_split(s, qsrc, s->dim, nq, qbuf, qsq, &qsq_ready);
+    else
+        rc = prep_queries_fp64(s, qsrc, s->dim, nq, qbuf, qsq);
     if (rc) return rc;
-    ++kernels;
+    kernels += qsq_ready ? 2 : 1;
+    a.qsq_ready = qsq_ready;
     s->prof_mark(1);
     if (s->nlive == 0) {
         k_fill_empty<<<(unsigned)((out_n + 255) / 256), 256, 0, s->stream>>>(a.ids, a.dists, a.err, out_n);
@@ -497,6 +556,8 @@ int svdb::search_seeded(Store* s, const double* q, size_t nq, size_t k, int metr
         }
     } else {
         rc = search_bf16(s, a, kscr, kbytes, st, precision == SVDB_PREC_FP8 && fp8_screen_pays(s, nq, k));
+        // joined whatever happened: nothing later on the stream may outrun the side stream's writes
+        if (qsq_ready && cudaStreamWaitEvent(s->stream, qsq_ready, 0) != cudaSuccess) cudaGetLastError();
     }
     s->prof_mark(SVDB_NSTAGES);
     s->prof_end();

@@ -29,6 +29,8 @@ struct SearchArgs {
     // tensor-core screens: start the running thresholds from the exact k-th
     // best lower bound over a sample of the rows (-1: for the FP8 screen only)
     int seed = -1;
+    // set: qsq is written on another stream; wait on this event before reading it
+    cudaEvent_t qsq_ready = nullptr;
 };
 
 // FP64 bound on |computed - exact| for one result (see dev_search.cu)
@@ -42,6 +44,12 @@ __device__ __forceinline__ double result_err_bound(int metric, int d, double val
 
 // queries (nq rows, stride qs) -> padded buffer (stride ld) + sums of squares
 int prep_queries_fp64(Store* s, const double* q_dev, size_t qs, size_t nq, double* qbuf, double* qsq);
+// the same, with the canonical sums of squares on the store's side stream
+// (they are read only after the screen): *ready is the event that marks them
+// written, or null when they were computed on the store's stream (a stream
+// being captured into a graph keeps the one-stream form)
+int prep_queries_split(Store* s, const double* q_dev, size_t qs, size_t nq, double* qbuf, double* qsq,
+                       cudaEvent_t* ready);
 
 // exact FP64 scan + merge over all live slots, writing SearchArgs outputs
 // marks=false: called as the fallback of another stage (no profiling marks)

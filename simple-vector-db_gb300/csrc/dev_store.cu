@@ -551,6 +551,7 @@ int Store::scratch_reserve(size_t bytes) {
     if (erc) return erc;
     if (bytes <= scratch_bytes) return SVDB_OK;
     SVDB_CUDA(cudaStreamSynchronize(stream));
+    if (side) SVDB_CUDA(cudaStreamSynchronize(side));  // (a search's |q|^2 may be written there)
     cudaFree(scratch);
     scratch = nullptr;
     scratch_bytes = 0;
@@ -568,6 +569,25 @@ int Store::scratch_reserve(size_t bytes) {
 
 // After the stream is idle: a device kernel's bounded wait that ran out shows
 // here as SVDB_ETIMEOUT (once; the word is cleared).
+int Store::side_ready() {
+    if (side) return SVDB_OK;
+    cudaStream_t st = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&a, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (st) cudaStreamDestroy(st);
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+        return SVDB_ECUDA;
+    }
+    side = st;
+    ev_fork = a;
+    ev_side = b;
+    return SVDB_OK;
+}
+
 int Store::check_error() {
     if (!d_err) return SVDB_OK;
     int h = 0;
@@ -725,6 +745,7 @@ void svdbd_store_destroy(svdbd_store* hs) {
         return;
     }
     cudaStreamSynchronize(s->stream);
+    if (s->side) cudaStreamSynchronize(s->side);
     cudaFree(s->x64);
     cudaFree(s->xb);
     cudaFree(s->x32);
@@ -752,6 +773,9 @@ void svdbd_store_destroy(svdbd_store* hs) {
     s->release_extra();
     s->uuid_free();
     s->kdm_free();
+    if (s->side) cudaStreamDestroy(s->side);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_side) cudaEventDestroy(s->ev_side);
     cudaStreamDestroy(s->stream);
     delete s;
 }

@@ -22,6 +22,9 @@ struct Store {
     size_t slots = 0;  // slots on the device
     size_t nlive = 0;  // live slots as of the last sync
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;      // work beside a search's screen (created on first use)
+    cudaEvent_t ev_fork = nullptr, ev_side = nullptr;
+    int side_ready();
 
     double* x64 = nullptr;
     __nv_bfloat16* xb = nullptr;
