@@ -998,8 +998,9 @@ __global__ void __launch_bounds__(scr::kThreads, DUO ? 2 : 1)
 // BF16 copies of the (already padded FP64) queries + per-query bound terms.
 // One warp per query: the FP64 pipe is narrow, and with fewer lanes a small
 // batch waits on each lane's long chain of dependent FP64 operations.  The
-// two sums of squares feed only the bounds, whose 1 + 2^-30 factor covers
-// their FP64 rounding in any order.
+// sums of squares (of the query, of its BF16 copy and of the difference) feed
+// only the bounds, whose 1 + 2^-30 factor covers their FP64 rounding in any
+// order; the canonical |q|^2 of the reported values is not read here.
 constexpr int kPrepLanes = 32;
 __global__ void k_prep_bf16(const double* __restrict__ qbuf, int nq, size_t ld,
                             size_t ldb, int metric, __nv_bfloat16* __restrict__ qb, float* __restrict__ q32,
